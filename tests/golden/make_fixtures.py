@@ -1,0 +1,75 @@
+"""Generate the committed test fixtures from the reference's own test data.
+
+Run once in a checkout where the reference tree is available:
+
+    python tests/golden/make_fixtures.py /path/to/CellListMap.jl
+
+It reads
+  * test/applications/gromacs/argon/cubic.pdb  (the reference's ``argon_pdb_file``,
+    src/CellListMap.jl:61): 100 argon atoms, fixed-column PDB coordinates parsed as
+    Float64, as PDBTools does;
+  * test/applications/namd/{o1..o6,t1,t2}.dcd: one frame each of a Neon system,
+    CHARMM DCD with float32 coordinates (read by Chemfiles in
+    test/applications/namd/ParticleSystem_vs_NAMD.jl:21-26);
+and writes
+  * tests/golden/argon_cubic.npy   (100 x 3 float64)
+  * tests/golden/namd_frames.npz   (one (n, 3) float32 array per frame)
+Only coordinates are extracted.  The expected values these fixtures are checked
+against are quoted, with their source lines, in tests/test_oracle_kat.py.
+"""
+import os
+import struct
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def read_pdb_coords(path):
+    xyz = []
+    with open(path) as f:
+        for line in f:
+            if line.startswith("ATOM") or line.startswith("HETATM"):
+                xyz.append([float(line[30:38]), float(line[38:46]), float(line[46:54])])
+    return np.array(xyz, dtype=np.float64)
+
+
+def read_dcd_first_frame(path):
+    """Minimal CHARMM/NAMD DCD reader (Fortran unformatted records, little endian)."""
+    data = open(path, "rb").read()
+    pos = 0
+    recs = []
+    while pos < len(data):
+        (n,) = struct.unpack_from("<i", data, pos)
+        recs.append(data[pos + 4:pos + 4 + n])
+        (n2,) = struct.unpack_from("<i", data, pos + 4 + n)
+        assert n == n2, "corrupt DCD record"
+        pos += 8 + n
+    hdr = recs[0]
+    assert hdr[:4] == b"CORD"
+    icntrl = struct.unpack_from("<20i", hdr, 4)
+    has_cell = icntrl[10] != 0
+    natoms = struct.unpack_from("<i", recs[2])[0]
+    k = 3
+    if has_cell:
+        k += 1  # unit-cell record (6 doubles) precedes the coordinates
+    x = np.frombuffer(recs[k], dtype="<f4")
+    y = np.frombuffer(recs[k + 1], dtype="<f4")
+    z = np.frombuffer(recs[k + 2], dtype="<f4")
+    assert x.size == natoms == y.size == z.size
+    return np.stack([x, y, z], axis=1).astype(np.float32)
+
+
+def main(ref_root):
+    pdb = os.path.join(ref_root, "test", "applications", "gromacs", "argon", "cubic.pdb")
+    np.save(os.path.join(HERE, "argon_cubic.npy"), read_pdb_coords(pdb))
+    frames = {}
+    for name in ["o1", "o2", "o3", "o4", "o5", "o6", "t1", "t2"]:
+        frames[name] = read_dcd_first_frame(os.path.join(ref_root, "test", "applications", "namd", name + ".dcd"))
+    np.savez_compressed(os.path.join(HERE, "namd_frames.npz"), **frames)
+    print("wrote fixtures:", sorted(frames), "argon", read_pdb_coords(pdb).shape)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
