@@ -1,0 +1,316 @@
+#!/usr/bin/env python
+"""Benchmark of the cutoff-pair engine on GB300: within-cutoff pairs per second.
+
+Workload (one "step" = cell-list build + pair map over the whole system):
+  1,048,576 Float32 particles, fcc lattice (64^3 cells x 4) at density 0.8 mapped through the triclinic
+  cell a=(L,0,0), b=(0.2L,L,0), c=(0.1L,0.15L,L), Gaussian jitter sigma=0.05, Lennard-Jones
+  (sigma=1, eps=1) energy + forces with cutoff 2.5.  Seeded synthetic data (seed 2).
+Forms: exact (input-dtype arithmetic, bit-exact pair set) is `value`; the FP32-split form is reported
+beside it.  `e2e` goes through the C ABI with host buffers (H2D of positions and D2H of energy+forces
+inside the timed region).  `--impl reference` times the CPU restatement of the reference algorithm
+(OpenMP over all host cores) on the same workload.
+
+Multi-GPU: the path is run as independent replicas (one per rank); value = pairs of all ranks / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "within-cutoff pairs/s (cell-list build + pair map, LJ energy+forces)"
+WORKLOAD = "fcc1M_f32_triclinic_lj_rc2.5"
+CUTOFF = 2.5
+
+
+def make_workload(ncell=64, rho=0.8, jitter=0.05, seed=2):
+    """fcc lattice in fractional coordinates mapped through the triclinic cell matrix, plus jitter."""
+    n = 4 * ncell ** 3
+    L = (n / rho) ** (1.0 / 3.0)
+    g = np.stack(np.meshgrid(np.arange(ncell), np.arange(ncell), np.arange(ncell), indexing="ij"), -1).reshape(-1, 3)
+    basis = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    frac = ((g[:, None, :] + basis[None, :, :]).reshape(-1, 3)) / ncell
+    M = np.array([[L, 0.2 * L, 0.1 * L], [0.0, L, 0.15 * L], [0.0, 0.0, L]])  # columns a, b, c
+    rng = np.random.default_rng(seed)
+    x = frac @ M.T + rng.normal(0.0, jitter, (n, 3))
+    return x.astype(np.float32), M
+
+
+def flops_per_pair(cell_size, cutoff, f_op=20.0):
+    """Algorithmic flops per within-cutoff pair: 8*R + F_op, R = 27 h^3 / ((4/3) pi rc^3)."""
+    R = 27.0 * float(np.prod(cell_size)) / (4.0 / 3.0 * math.pi * cutoff ** 3)
+    return 8.0 * R + f_op, R
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [v.strip() for v in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_reference(x, M, steps, warmup, threads):
+    """The reference algorithm on the host cores: the oracle's cell-list build + threaded map."""
+    from oracle import oracle as orc
+    kw = dict(kind="tri", unitcell=M, cutoff=CUTOFF, dtype=np.float32, nthreads=threads, compensated=False,
+              params=[1.0, 1.0, 4.0, 4.0])
+    pairs = orc.run("count", x, **{k: v for k, v in kw.items() if k != "params"})["count"]
+    for _ in range(warmup):
+        orc.run("lj_forces", x, **kw)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        orc.run("lj_forces", x, **kw)
+    dt = time.perf_counter() - t0
+    return pairs, dt
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--ncell", type=int, default=64, help="fcc cells per side (64 -> 1,048,576 particles)")
+    ap.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU baseline sample")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    threads = os.cpu_count() or 1
+
+    x_host, M = make_workload(args.ncell)
+    n = x_host.shape[0]
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        pairs, dt = cpu_reference(x_host, M, args.steps, max(0, min(args.warmup, 1)), threads)
+        v = pairs * args.steps / dt
+        line = {"metric": METRIC, "value": v, "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "impl": "reference",
+                "config": {"workload": WORKLOAD, "n_particles": n, "pairs_per_step": int(pairs), "cutoff": CUTOFF,
+                           "cell": "triclinic", "op": "lj_energy_forces"},
+                "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": threads, "kind": "port",
+                                 "sample": f"full workload, {args.steps} steps (serial build + OpenMP map)"},
+                "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    pkg.build()
+    L = pkg._abi.load()
+    A = pkg._abi
+
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    x_dev = torch.from_numpy(x_host).to(dev)
+    f_dev = torch.zeros((n, 3), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (129 MB)
+
+    h = C.c_void_p()
+    assert L.clm_create(A.CLM_F32, 3, 1, C.byref(h)) == 0
+    assert L.clm_set_stream(h, C.c_void_p(stream.cuda_stream)) == 0
+    Mf = np.ascontiguousarray(M.flatten(order="F"))
+    assert L.clm_set_box(h, Mf.ctypes.data_as(C.POINTER(C.c_double)), A.CLM_TRICLINIC, CUTOFF, 1) == 0
+
+    p = A.OpParams()
+    p.p[0], p.p[1], p.p[2], p.p[3] = 1.0, 1.0, 4.0, 4.0
+    o_dev = A.Outputs()
+    o_dev.forces_x = f_dev.data_ptr()
+    o_dev.out_on_device = 1
+
+    def step_device():
+        st = L.clm_set_positions(h, 0, C.c_void_p(x_dev.data_ptr()), n, 1)
+        st = st or L.clm_build(h)
+        st = st or L.clm_run(h, A.OP["lj_forces"], C.byref(p), C.byref(o_dev))
+        if st:
+            buf = C.create_string_buffer(512)
+            L.clm_last_error(h, buf, 512)
+            raise RuntimeError(f"clm status {st}: {buf.value.decode()}")
+
+    # pairs per step (untimed)
+    L.clm_set_positions(h, 0, C.c_void_p(x_dev.data_ptr()), n, 1)
+    oc = A.Outputs()
+    assert L.clm_run(h, A.OP["count"], C.byref(A.OpParams()), C.byref(oc)) == 0
+    pairs = int(oc.count)
+
+    def timed(form):
+        L.clm_set_precision(h, form)
+        for _ in range(args.warmup):
+            step_device()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        l0 = C.c_int64()
+        L.clm_stats(h, C.byref(l0))
+        tot_ms, kern_ms = 0.0, []
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.add_(1.0)  # evict L2 between timed steps (outside the events)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step_device()
+            e1.record(stream)
+            e1.synchronize()
+            tot_ms += e0.elapsed_time(e1)
+            bm, mm = C.c_float(), C.c_float()
+            L.clm_last_timings(h, C.byref(bm), C.byref(mm))
+            kern_ms.append(mm.value)
+        torch.cuda.synchronize()
+        l1 = C.c_int64()
+        L.clm_stats(h, C.byref(l1))
+        if world > 1:
+            t = torch.tensor([tot_ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            tot_ms = float(t.item())
+        return tot_ms, statistics.mean(kern_ms), (l1.value - l0.value)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    t_exact, k_exact, launches = timed(A.CLM_PREC_EXACT)
+    clk = clocks.stop()
+    t_split, k_split, _ = timed(A.CLM_PREC_SPLIT)
+    value = pairs * args.steps * world / (t_exact * 1e-3)
+    split_value = pairs * args.steps * world / (t_split * 1e-3)
+
+    # e2e: public C ABI with host buffers (pinned), copies inside the timed region
+    L.clm_set_precision(h, A.CLM_PREC_EXACT)
+    x_pin = torch.from_numpy(x_host).pin_memory()
+    f_pin = torch.empty((n, 3), dtype=torch.float32).pin_memory()
+    o_host = A.Outputs()
+    o_host.forces_x = f_pin.data_ptr()
+    o_host.out_on_device = 0
+    for _ in range(args.warmup):
+        L.clm_set_positions(h, 0, C.c_void_p(x_pin.data_ptr()), n, 0)
+        L.clm_run(h, A.OP["lj_forces"], C.byref(p), C.byref(o_host))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        L.clm_set_positions(h, 0, C.c_void_p(x_pin.data_ptr()), n, 0)
+        st = L.clm_run(h, A.OP["lj_forces"], C.byref(p), C.byref(o_host))
+        assert st == 0
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+    e2e = pairs * args.steps * world / t_e2e
+    energy = o_host.scalar
+
+    # roofline of the pair kernel (FP32 pipe): algorithmic flops per launch / kernel time
+    box = np.zeros(3)
+    cs = np.zeros(3)
+    L.clm_get_box(h, None, cs.ctypes.data, None, None, None, None, None, None)
+    fpp, R = flops_per_pair(cs, CUTOFF)
+    peaks = C.CDLL(os.path.join(ge.PKG_DIR, "_build", "libclm_peaks.so"))
+    peaks.clm_peak_fp32_gflops.restype = C.c_double
+    peaks.clm_peak_fp32_gflops.argtypes = [C.c_int]
+    fp32_peak = peaks.clm_peak_fp32_gflops(1 << 16) / 1e3  # TFLOP/s
+    achieved = pairs * fpp / (k_exact * 1e-3) / 1e12
+    traffic = None
+    tj = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tj):
+        traffic = json.load(open(tj)).get("k_pairs_lj_forces_f32_per_launch_bytes")
+
+    cpu = None
+    if rank == 0:
+        try:
+            cpairs, cdt = cpu_reference(x_host, M, args.cpu_steps, 0, threads)
+            cpu = {"value": cpairs * args.cpu_steps / cdt, "unit": "pairs/s", "cores": threads, "kind": "port",
+                   "sample": f"full workload, {args.cpu_steps} step(s), serial build + OpenMP map on {threads} threads"}
+        except Exception as ex:  # pragma: no cover
+            cpu = {"value": None, "unit": "pairs/s", "cores": threads, "kind": "port", "sample": f"failed: {ex}"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_exact / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fcc + Gaussian jitter)",
+        "config": {"workload": WORKLOAD, "n_particles": n, "pairs_per_step": pairs, "cutoff": CUTOFF,
+                   "cell": "triclinic", "op": "lj_energy_forces", "l2": "flushed between steps (256 MiB write)",
+                   "parallelism": f"replicas x{world}", "energy": energy},
+        "forms": {"exact": {"value": value, "kernel_ms": k_exact},
+                  "split": {"value": split_value, "kernel_ms": k_split, "ms_per_step": t_split / args.steps}},
+        "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": int(x_pin.numel() * 4),
+                "d2h_bytes_per_step": int(f_pin.numel() * 4 + 8)},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak if fp32_peak > 0 else None, "traffic": traffic,
+                     "kernel": "k_pairs<float,3,FORCES,exact>", "flops_per_pair": fpp, "candidates_per_hit": R,
+                     "peak_source": "measured FP32 FMA throughput (libclm_peaks.so, same run)"},
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "gpu_launches": launches,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    L.clm_destroy(h)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,610 @@
+// Cell-list construction on the GPU (K1-K4).
+//
+// Replaces UpdateCellList! (src/internals/CellLists.jl:727-927, serial order
+// of add_particles! 940-950 and add_particle_to_celllist! 983-1057) and the
+// non-periodic build (src/internals/NonPeriodicCells.jl:93-251):
+//
+//   K1 k_wrap_count  wrap into the first cell (wrap_to_first, CellOperations.jl:91-94),
+//                    rotate, test the 3^N-1 translation images against the computing
+//                    box (replicate_particle!, Box.jl:556-566) -> copies per particle
+//   scan             exclusive prefix sum of copies per particle
+//   K2 k_emit        one (cell, particle<<5|image) key/value per copy, cell histogram,
+//                    real-cell flags (particle_cell + real_particle_border_case)
+//   K3 radix sort    stable LSD radix sort of the keys by cell: inside a cell the
+//                    copies keep particle-index order, which is the reference's serial
+//                    order (a particle has at most one copy per cell)
+//   K4 k_gather      coordinates of each copy in cell order (SoA), particle codes,
+//                    FP32 cell-relative offsets for the pair prefilter
+//   compaction       list of cells that contain real particles, in linear order
+//
+// Every kernel bounds-checks its indices; inconsistencies set bits of the
+// handle's device error word instead of faulting.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "clm_internal.hpp"
+
+namespace clm {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+// ------------------------------------------------------------------ scan
+constexpr int SCAN_IPT = 8;
+constexpr int SCAN_TILE = kBlock * SCAN_IPT;
+
+__global__ void __launch_bounds__(kBlock) k_scan_tiles(const int* __restrict__ in, int* __restrict__ out, int64_t m,
+                                                       int* __restrict__ tile_sums) {
+  __shared__ int wsum[kBlock / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_IPT;
+  int v[SCAN_IPT];
+  int s = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_IPT; k++) {
+    int64_t idx = base + k;
+    int t = (idx < m) ? in[idx] : 0;
+    v[k] = s;
+    s += t;
+  }
+  int incl = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int w = (lane < kBlock / 32) ? wsum[lane] : 0;
+    int wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    if (lane < kBlock / 32) wsum[lane] = wi - w;
+  }
+  __syncthreads();
+  const int off = (incl - s) + wsum[warp];
+#pragma unroll
+  for (int k = 0; k < SCAN_IPT; k++) {
+    int64_t idx = base + k;
+    if (idx < m) out[idx] = v[k] + off;
+  }
+  if (threadIdx.x == kBlock - 1) tile_sums[blockIdx.x] = off + s;
+}
+
+__global__ void __launch_bounds__(kBlock) k_scan_add(int* __restrict__ out, int64_t m, const int* __restrict__ offs) {
+  const int add = offs[blockIdx.x];
+  const int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
+#pragma unroll
+  for (int k = 0; k < SCAN_IPT; k++) {
+    int64_t idx = base + (int64_t)k * kBlock + threadIdx.x;
+    if (idx < m) out[idx] += add;
+  }
+}
+
+// ------------------------------------------------------------------ radix sort (8-bit digits)
+constexpr int RS_IPT = 8;
+constexpr int RS_TILE = kBlock * RS_IPT;  // 2048 keys per tile
+constexpr int RS_WARPS = kBlock / 32;
+
+__global__ void __launch_bounds__(kBlock) k_rs_hist(const uint32_t* __restrict__ keys, int n, int shift,
+                                                    int* __restrict__ hist, int ntiles) {
+  __shared__ int h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * RS_TILE;
+#pragma unroll
+  for (int k = 0; k < RS_IPT; k++) {
+    int64_t idx = base + (int64_t)k * kBlock + threadIdx.x;
+    if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1);
+  }
+  __syncthreads();
+  hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// Stable scatter: items of a tile are ranked in tile order (warp, then item
+// slot, then lane) with warp-level match_any, then placed at the scanned
+// digit offset of the tile.
+__global__ void __launch_bounds__(kBlock) k_rs_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                                       uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, int n,
+                                                       int shift, const int* __restrict__ offs, int ntiles) {
+  __shared__ int wcnt[RS_WARPS][257];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int d = threadIdx.x; d < RS_WARPS * 257; d += kBlock) (&wcnt[0][0])[d] = 0;
+  __syncthreads();
+  const int64_t wbase = (int64_t)blockIdx.x * RS_TILE + (int64_t)warp * (32 * RS_IPT);
+  uint32_t kk[RS_IPT], vv[RS_IPT];
+  int rank[RS_IPT], dig[RS_IPT];
+  const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int k = 0; k < RS_IPT; k++) {
+    int64_t idx = wbase + k * 32 + lane;
+    bool valid = idx < n;
+    kk[k] = valid ? kin[idx] : 0u;
+    vv[k] = valid ? vin[idx] : 0u;
+    int d = valid ? (int)((kk[k] >> shift) & 255u) : 256;
+    dig[k] = d;
+    unsigned peers = __match_any_sync(0xffffffffu, d);
+    int leader = __ffs(peers) - 1;
+    int cur = wcnt[warp][d];
+    __syncwarp();
+    if (lane == leader) wcnt[warp][d] = cur + __popc(peers);
+    __syncwarp();
+    rank[k] = cur + __popc(peers & lt);
+  }
+  __syncthreads();
+  {
+    int d = threadIdx.x;  // one digit per thread (kBlock == 256)
+    int run = offs[(int64_t)d * ntiles + blockIdx.x];
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; w++) {
+      int t = wcnt[w][d];
+      wcnt[w][d] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < RS_IPT; k++) {
+    if (dig[k] < 256) {
+      int pos = wcnt[warp][dig[k]] + rank[k];
+      if (pos >= 0 && pos < n) {
+        kout[pos] = kk[k];
+        vout[pos] = vv[k];
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ K1: wrap, images, copy count
+template <class T, int N>
+__global__ void __launch_bounds__(kBlock) k_wrap_count(DevGeom<T> g, const T* __restrict__ x, int n,
+                                                       T* __restrict__ wrapped, uint32_t* __restrict__ mask,
+                                                       int* __restrict__ ncopy, int* __restrict__ err) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T xi[N];
+  bool bad = false;
+#pragma unroll
+  for (int k = 0; k < N; k++) {
+    xi[k] = x[(int64_t)i * N + k];
+    bad = bad || isnan(xi[k]);
+  }
+  if (bad) {
+    atomicOr(err, DERR_NAN);
+#pragma unroll
+    for (int k = 0; k < N; k++) wrapped[(int64_t)i * N + k] = T(0);
+    mask[i] = 0;
+    ncopy[i] = 0;
+    return;
+  }
+  T p[N];
+  if (g.kind == NONPERIODIC) {
+#pragma unroll
+    for (int k = 0; k < N; k++) p[k] = xi[k];
+  } else {
+    wrap_point<T, N>(g, xi, p);
+  }
+#pragma unroll
+  for (int k = 0; k < N; k++) wrapped[(int64_t)i * N + k] = p[k];
+  uint32_t m = 0;
+  int cnt = 1;
+  if (g.kind != NONPERIODIC) {
+    for (int k = 0; k < g.nimg; k++) {
+      if (k == g.zero_code) continue;
+      T q[N];
+#pragma unroll
+      for (int d = 0; d < N; d++) q[d] = xadd(p[d], g.shift[k][d]);
+      if (in_box<T, N>(g, q)) {
+        m |= 1u << k;
+        cnt++;
+      }
+    }
+  }
+  mask[i] = m;
+  ncopy[i] = cnt;
+}
+
+// ------------------------------------------------------------------ K2: keys, histogram, real flags
+template <class T, int N>
+__global__ void __launch_bounds__(kBlock) k_emit(DevGeom<T> g, const T* __restrict__ wrapped,
+                                                 const uint32_t* __restrict__ mask, const int* __restrict__ ncopy,
+                                                 const int* __restrict__ copy_off, int n, int cap,
+                                                 uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                                 int* __restrict__ cell_count, int* __restrict__ cell_flags,
+                                                 int* __restrict__ err) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (ncopy[i] == 0) return;
+  int base = copy_off[i];
+  if (base < 0 || base + ncopy[i] > cap) {
+    atomicOr(err, DERR_COPY_OVERFLOW);
+    return;
+  }
+  T p[N];
+#pragma unroll
+  for (int k = 0; k < N; k++) p[k] = wrapped[(int64_t)i * N + k];
+  int li = cell_of<T, N>(g, p, true);
+  if (li < 0) {
+    atomicOr(err, DERR_CELL_RANGE);
+    li = 0;
+  }
+  keys[base] = (uint32_t)li;
+  vals[base] = ((uint32_t)i << 5) | (uint32_t)g.zero_code;
+  atomicAdd(&cell_count[li], 1);
+  cell_flags[li] = 1;
+  int t = 1;
+  uint32_t m = mask[i];
+  while (m) {
+    int k = __ffs(m) - 1;
+    m &= m - 1;
+    T q[N];
+#pragma unroll
+    for (int d = 0; d < N; d++) q[d] = xadd(p[d], g.shift[k][d]);
+    int lk = cell_of<T, N>(g, q, false);
+    if (lk < 0) {
+      atomicOr(err, DERR_CELL_RANGE);
+      lk = 0;
+    }
+    keys[base + t] = (uint32_t)lk;
+    vals[base + t] = ((uint32_t)i << 5) | (uint32_t)k;
+    atomicAdd(&cell_count[lk], 1);
+    t++;
+  }
+}
+
+// ------------------------------------------------------------------ K4: gather in cell order
+template <class T, int N>
+__global__ void __launch_bounds__(kBlock) k_gather(DevGeom<T> g, const T* __restrict__ wrapped,
+                                                   const uint32_t* __restrict__ skeys,
+                                                   const uint32_t* __restrict__ svals, int ncopies, int n,
+                                                   T* __restrict__ px, T* __restrict__ py, T* __restrict__ pz,
+                                                   float4* __restrict__ off, int* __restrict__ code,
+                                                   int* __restrict__ err) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncopies) return;
+  uint32_t v = svals[t];
+  int p = (int)(v >> 5);
+  int k = (int)(v & 31u);
+  if (p >= n || k >= g.nimg) {
+    atomicOr(err, DERR_CELL_RANGE);
+    p = 0;
+    k = g.zero_code;
+  }
+  T q[N];
+#pragma unroll
+  for (int d = 0; d < N; d++) {
+    T w = wrapped[(int64_t)p * N + d];
+    q[d] = (k == g.zero_code) ? w : xadd(w, g.shift[k][d]);
+  }
+  int li = (int)skeys[t];
+  int c[3];
+  cart_of(li, g.nc, N, c);
+  float o[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int d = 0; d < N; d++) {
+    double origin = (double)g.cbmin[d] + (double)g.cs[d] * (double)(c[d] - 1);
+    o[d] = (float)((double)q[d] - origin);
+  }
+  px[t] = q[0];
+  py[t] = q[1];
+  if (N == 3) pz[t] = q[N - 1];
+  off[t] = make_float4(o[0], o[1], o[2], 0.f);
+  code[t] = (k == g.zero_code) ? p : -(p + 1);
+}
+
+__global__ void k_compact(const int* __restrict__ flags, const int* __restrict__ scanned, int ncells,
+                          int* __restrict__ list) {
+  int li = blockIdx.x * blockDim.x + threadIdx.x;
+  if (li >= ncells) return;
+  if (flags[li]) list[scanned[li]] = li;
+}
+
+template <class T, int N>
+__global__ void __launch_bounds__(kBlock) k_minmax(const T* __restrict__ x, int n, T* __restrict__ part) {
+  __shared__ T smin[N][kBlock], smax[N][kBlock];
+  T lo[N], hi[N];
+#pragma unroll
+  for (int d = 0; d < N; d++) {
+    lo[d] = INFINITY;
+    hi[d] = -INFINITY;
+  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int d = 0; d < N; d++) {
+      T v = x[(int64_t)i * N + d];
+      lo[d] = fmin(lo[d], v);
+      hi[d] = fmax(hi[d], v);
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < N; d++) {
+    smin[d][threadIdx.x] = lo[d];
+    smax[d][threadIdx.x] = hi[d];
+  }
+  __syncthreads();
+  for (int s = kBlock / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) {
+#pragma unroll
+      for (int d = 0; d < N; d++) {
+        smin[d][threadIdx.x] = fmin(smin[d][threadIdx.x], smin[d][threadIdx.x + s]);
+        smax[d][threadIdx.x] = fmax(smax[d][threadIdx.x], smax[d][threadIdx.x + s]);
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int d = 0; d < N; d++) {
+      part[(int64_t)blockIdx.x * 2 * N + d] = smin[d][0];
+      part[(int64_t)blockIdx.x * 2 * N + N + d] = smax[d][0];
+    }
+  }
+}
+
+inline int grid_for(int64_t n, int block = kBlock) { return (int)std::max<int64_t>(1, (n + block - 1) / block); }
+
+}  // namespace
+
+// ------------------------------------------------------------------ host side
+int scan_exclusive(Handle& h, const int* in, int* out, int64_t m, int* total, int depth) {
+  if (m <= 0) {
+    if (total) CLM_CUDA_TRY(h, cudaMemsetAsync(total, 0, sizeof(int), h.stream));
+    return OK;
+  }
+  if (depth >= 4) {
+    h.last_error = "scan too deep";
+    return ERR_INTERNAL;
+  }
+  int64_t ntiles = (m + SCAN_TILE - 1) / SCAN_TILE;
+  if (ntiles == 1) {
+    k_scan_tiles<<<1, kBlock, 0, h.stream>>>(in, out, m, total);
+    CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+    return OK;
+  }
+  DevBuf& lv = h.scan.level[depth];
+  if (!lv.reserve((size_t)(ntiles + 1) * sizeof(int) * 2)) return ERR_NOMEM;
+  int* sums = lv.as<int>();
+  int* sums_scan = sums + ntiles;
+  k_scan_tiles<<<(unsigned)ntiles, kBlock, 0, h.stream>>>(in, out, m, sums);
+  CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+  int st = scan_exclusive(h, sums, sums_scan, ntiles, total, depth + 1);
+  if (st) return st;
+  k_scan_add<<<(unsigned)ntiles, kBlock, 0, h.stream>>>(out, m, sums_scan);
+  CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+  return OK;
+}
+
+template <class T> void fill_devgeom(const Geometry<T>& g, int precision, DevGeom<T>& d) {
+  std::memset(&d, 0, sizeof(d));
+  (void)precision;
+  d.dim = g.dim;
+  d.kind = g.kind;
+  d.lcell = g.lcell;
+  d.ncells = (int)g.ncells();
+  for (int i = 0; i < 3; i++) {
+    d.nc[i] = (int)g.nc[i];
+    d.cbmin[i] = g.cbmin[i];
+    d.cbmax[i] = g.cbmax[i];
+    d.cs[i] = g.cs[i];
+    d.csf[i] = (float)g.cs[i];
+    for (int j = 0; j < 3; j++) {
+      d.Min[i][j] = g.Min[i][j];
+      d.R[i][j] = g.R[i][j];
+      d.Rinv[i][j] = g.Rinv[i][j];
+    }
+  }
+  d.det_in = g.det_in;
+  d.cutoff = g.cutoff;
+  d.cutoff_sqr = g.cutoff_sqr;
+  d.margin_wide = (double)g.cutoff * (1.0 + std::sqrt((double)g.dim) / 2.0);
+  d.nimg = (g.dim == 3) ? 27 : 9;
+  d.zero_code = (g.dim == 3) ? 13 : 4;
+  // translation_image: x + Mal * s, s in {-1,0,1}^N with the first index fastest
+  for (int k = 0; k < d.nimg; k++) {
+    int s[3], kk = k;
+    for (int i = 0; i < g.dim; i++) {
+      s[i] = kk % 3 - 1;
+      kk /= 3;
+    }
+    for (int i = 0; i < g.dim; i++) {
+      T acc = g.Mal[i][0] * T(s[0]);
+      for (int j = 1; j < g.dim; j++) acc = acc + g.Mal[i][j] * T(s[j]);
+      d.shift[k][i] = acc;
+    }
+  }
+  // FP32 prefilter band around cutoff^2 (relative 2^-13, far above the FP32
+  // error of d2 computed from cell-relative offsets, ~2^-18 relative).
+  double c2 = (double)g.cutoff_sqr;
+  d.thr_hi = std::nextafter((float)(c2 * (1.0 + std::ldexp(1.0, -13))), INFINITY);
+  d.thr_lo = std::nextafter((float)(c2 * (1.0 - std::ldexp(1.0, -13))), 0.0f);
+}
+
+template <class T> int set_limits(Handle& h, T* lo, T* hi) {
+  // limits over x (and y for two sets): src/internals/CellOperations.jl:262-324
+  const int N = h.dim;
+  bool any = false;
+  T glo[3], ghi[3];
+  for (int s = 0; s < h.nsets; s++) {
+    SetData& S = h.sets[s];
+    T slo[3] = {0, 0, 0}, shi[3] = {0, 0, 0};
+    if (S.n > 0) {
+      int nb = std::min<int64_t>(1024, (S.n + kBlock - 1) / kBlock);
+      if (!S.minmax.reserve(sizeof(T) * 2 * N * nb)) return ERR_NOMEM;
+      if (N == 3) k_minmax<T, 3><<<nb, kBlock, 0, h.stream>>>(S.x.as<T>(), (int)S.n, S.minmax.as<T>());
+      else k_minmax<T, 2><<<nb, kBlock, 0, h.stream>>>(S.x.as<T>(), (int)S.n, S.minmax.as<T>());
+      CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+      std::vector<T> part((size_t)(2 * N * nb));
+      CLM_CUDA_TRY(h, cudaMemcpyAsync(part.data(), S.minmax.p, part.size() * sizeof(T), cudaMemcpyDeviceToHost, h.stream));
+      CLM_CUDA_TRY(h, cudaStreamSynchronize(h.stream));
+      for (int d = 0; d < N; d++) {
+        slo[d] = part[d];
+        shi[d] = part[N + d];
+      }
+      for (int b = 1; b < nb; b++)
+        for (int d = 0; d < N; d++) {
+          slo[d] = geo::jmin(slo[d], part[(size_t)b * 2 * N + d]);
+          shi[d] = geo::jmax(shi[d], part[(size_t)b * 2 * N + N + d]);
+        }
+    }
+    for (int d = 0; d < N; d++) {
+      glo[d] = any ? geo::jmin(glo[d], slo[d]) : slo[d];
+      ghi[d] = any ? geo::jmax(ghi[d], shi[d]) : shi[d];
+    }
+    any = true;
+  }
+  for (int d = 0; d < N; d++) {
+    lo[d] = glo[d];
+    hi[d] = ghi[d];
+  }
+  return OK;
+}
+
+template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
+  SetData& S = h.sets[set];
+  const int N = g.dim;
+  const int64_t n = S.n;
+  const int64_t ncells = g.ncells();
+  if (ncells > (int64_t)1 << 30) {
+    h.last_error = "too many cells for the cell grid (reduce lcell or enlarge cutoff)";
+    return ERR_ARG;
+  }
+  S.ncells = ncells;
+  DevGeom<T> dg;
+  fill_devgeom(g, h.precision, dg);
+  int* err = h.err.as<int>();
+  if (!S.cell_count.reserve(sizeof(int) * (ncells + 1)) || !S.cell_start.reserve(sizeof(int) * (ncells + 1)) ||
+      !S.cell_flags.reserve(sizeof(int) * (ncells + 1)) || !S.real_scan.reserve(sizeof(int) * (ncells + 1)) ||
+      !S.real_list.reserve(sizeof(int) * (ncells + 1)))
+    return ERR_NOMEM;
+  CLM_CUDA_TRY(h, cudaMemsetAsync(S.cell_count.p, 0, sizeof(int) * (ncells + 1), h.stream));
+  CLM_CUDA_TRY(h, cudaMemsetAsync(S.cell_flags.p, 0, sizeof(int) * (ncells + 1), h.stream));
+  if (n == 0) {
+    CLM_CUDA_TRY(h, cudaMemsetAsync(S.cell_start.p, 0, sizeof(int) * (ncells + 1), h.stream));
+    S.n_copies = 0;
+    S.n_real_cells = 0;
+    S.built = true;
+    S.dirty = false;
+    return OK;
+  }
+  if (!S.wrapped.reserve(sizeof(T) * N * n) || !S.mask.reserve(sizeof(uint32_t) * n) ||
+      !S.ncopy.reserve(sizeof(int) * (n + 1)) || !S.copy_off.reserve(sizeof(int) * (n + 1)))
+    return ERR_NOMEM;
+  const int gn = grid_for(n);
+  if (N == 3)
+    k_wrap_count<T, 3><<<gn, kBlock, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
+                                                   S.ncopy.as<int>(), err);
+  else
+    k_wrap_count<T, 2><<<gn, kBlock, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
+                                                   S.ncopy.as<int>(), err);
+  CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+  int* d_total = S.copy_off.as<int>() + n;
+  int st = scan_exclusive(h, S.ncopy.as<int>(), S.copy_off.as<int>(), n, d_total);
+  if (st) return st;
+  // one host sync: number of copies and the error word
+  CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned, d_total, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+  CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 1, err, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+  CLM_CUDA_TRY(h, cudaStreamSynchronize(h.stream));
+  if (h.pinned[1] & DERR_NAN) {
+    h.last_error = "Invalid coordinates found (NaN) in the particle positions.";
+    return ERR_NAN;
+  }
+  const int64_t nc = h.pinned[0];
+  if (nc < n || nc > (int64_t)INT32_MAX - 1) {
+    h.last_error = "copy count out of range";
+    return ERR_INTERNAL;
+  }
+  S.n_copies = nc;
+  for (int b = 0; b < 2; b++)
+    if (!S.keys[b].reserve(sizeof(uint32_t) * nc) || !S.vals[b].reserve(sizeof(uint32_t) * nc)) return ERR_NOMEM;
+  if (N == 3)
+    k_emit<T, 3><<<gn, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(),
+                                             S.copy_off.as<int>(), (int)n, (int)nc, S.keys[0].as<uint32_t>(),
+                                             S.vals[0].as<uint32_t>(), S.cell_count.as<int>(), S.cell_flags.as<int>(), err);
+  else
+    k_emit<T, 2><<<gn, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(),
+                                             S.copy_off.as<int>(), (int)n, (int)nc, S.keys[0].as<uint32_t>(),
+                                             S.vals[0].as<uint32_t>(), S.cell_count.as<int>(), S.cell_flags.as<int>(), err);
+  CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+  // stable LSD radix sort by cell
+  int bits = 1;
+  while (((int64_t)1 << bits) < ncells) bits++;
+  const int passes = (bits + 7) / 8;
+  const int ntiles = (int)((nc + RS_TILE - 1) / RS_TILE);
+  if (!S.rs_hist.reserve(sizeof(int) * (256 * (int64_t)ntiles + 1))) return ERR_NOMEM;
+  int cur = 0;
+  for (int pss = 0; pss < passes; pss++) {
+    int shift = 8 * pss;
+    k_rs_hist<<<ntiles, kBlock, 0, h.stream>>>(S.keys[cur].as<uint32_t>(), (int)nc, shift, S.rs_hist.as<int>(), ntiles);
+    CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+    st = scan_exclusive(h, S.rs_hist.as<int>(), S.rs_hist.as<int>(), 256 * (int64_t)ntiles, S.rs_hist.as<int>() + 256 * (int64_t)ntiles);
+    if (st) return st;
+    k_rs_scatter<<<ntiles, kBlock, 0, h.stream>>>(S.keys[cur].as<uint32_t>(), S.vals[cur].as<uint32_t>(),
+                                                  S.keys[1 - cur].as<uint32_t>(), S.vals[1 - cur].as<uint32_t>(),
+                                                  (int)nc, shift, S.rs_hist.as<int>(), ntiles);
+    CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+    cur = 1 - cur;
+  }
+  // cell offsets
+  st = scan_exclusive(h, S.cell_count.as<int>(), S.cell_start.as<int>(), ncells, S.cell_start.as<int>() + ncells);
+  if (st) return st;
+  // gather coordinates in cell order
+  if (!S.px.reserve(sizeof(T) * nc) || !S.py.reserve(sizeof(T) * nc) || !S.pz.reserve(sizeof(T) * nc) ||
+      !S.off.reserve(sizeof(float4) * nc) || !S.code.reserve(sizeof(int) * nc))
+    return ERR_NOMEM;
+  const int gc = grid_for(nc);
+  if (N == 3)
+    k_gather<T, 3><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
+                                               S.vals[cur].as<uint32_t>(), (int)nc, (int)n, S.px.as<T>(), S.py.as<T>(),
+                                               S.pz.as<T>(), S.off.as<float4>(), S.code.as<int>(), err);
+  else
+    k_gather<T, 2><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
+                                               S.vals[cur].as<uint32_t>(), (int)nc, (int)n, S.px.as<T>(), S.py.as<T>(),
+                                               S.pz.as<T>(), S.off.as<float4>(), S.code.as<int>(), err);
+  CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+  // cells with real particles, in linear order
+  st = scan_exclusive(h, S.cell_flags.as<int>(), S.real_scan.as<int>(), ncells, S.real_scan.as<int>() + ncells);
+  if (st) return st;
+  k_compact<<<grid_for(ncells), kBlock, 0, h.stream>>>(S.cell_flags.as<int>(), S.real_scan.as<int>(), (int)ncells,
+                                                       S.real_list.as<int>());
+  CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+  CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 2, S.real_scan.as<int>() + ncells, sizeof(int), cudaMemcpyDeviceToHost,
+                                  h.stream));
+  CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 3, err, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+  CLM_CUDA_TRY(h, cudaStreamSynchronize(h.stream));
+  if (h.pinned[3] & (DERR_CELL_RANGE | DERR_COPY_OVERFLOW)) {
+    h.last_error = "cell-list build consistency check failed (particle outside the computing box)";
+    return ERR_INTERNAL;
+  }
+  S.n_real_cells = h.pinned[2];
+  S.built = true;
+  S.dirty = false;
+  return OK;
+}
+
+template void fill_devgeom<float>(const Geometry<float>&, int, DevGeom<float>&);
+template void fill_devgeom<double>(const Geometry<double>&, int, DevGeom<double>&);
+template int build_set<float>(Handle&, int, const Geometry<float>&);
+template int build_set<double>(Handle&, int, const Geometry<double>&);
+template int set_limits<float>(Handle&, float*, float*);
+template int set_limits<double>(Handle&, double*, double*);
+
+}  // namespace clm

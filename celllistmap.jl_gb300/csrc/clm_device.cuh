@@ -1,0 +1,148 @@
+// Device-side definitions shared by the build and pair kernels.
+//
+// Bit-exactness: every multiply/add/divide/sqrt on the exact path goes through
+// the *_rn intrinsics below, which the compiler never fuses into FMAs, so the
+// device reproduces the reference's separately rounded Julia arithmetic
+// (Julia does not contract a*b+c).  The FP32 prefilter in the pair kernels is
+// free to use FMAs: it only decides which pairs get an exact re-test.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace clm {
+
+// ---------------------------------------------------------------- exact arithmetic
+__device__ __forceinline__ double xadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double xsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double xmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double xdiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double xsqrt(double a) { return __dsqrt_rn(a); }
+__device__ __forceinline__ float xadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float xsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float xmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float xdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float xsqrt(float a) { return __fsqrt_rn(a); }
+
+// ---------------------------------------------------------------- geometry on device
+constexpr int kMaxDim = 3;
+
+template <class T> struct DevGeom {
+  int dim, kind, lcell;
+  int nc[3];
+  int ncells;
+  T Min[3][3];    // input unit cell (wrap solve / product)
+  T det_in;
+  T R[3][3];      // rotation after wrapping (identity unless triclinic)
+  T Rinv[3][3];   // rotation back for pair coordinates
+  T shift[27][3]; // aligned-cell translation of image code k (first index fastest)
+  T cbmin[3], cbmax[3], cs[3];
+  T cutoff, cutoff_sqr;
+  double margin_wide;   // projection margin when lcell > 1 (computed in double, as the reference does)
+  float csf[3];         // cell sizes in FP32 for the prefilter
+  float thr_hi, thr_lo; // FP32 prefilter bounds on d2 (maybe-inside / surely-inside)
+  int zero_code;        // image code of the zero shift (13 in 3D, 4 in 2D)
+  int nimg;             // 3^dim
+};
+
+// StaticArrays solve (Cramer form), then fastmod1, boundary -> 0, then M*p and R*(.)
+template <class T, int N>
+__device__ __forceinline__ void wrap_point(const DevGeom<T>& g, const T* x, T* out) {
+  T p[N];
+  const auto& a = g.Min;
+  if constexpr (N == 3) {
+    p[0] = xdiv(xadd(xadd(xmul(xsub(xmul(a[1][1], a[2][2]), xmul(a[1][2], a[2][1])), x[0]),
+                          xmul(xsub(xmul(a[0][2], a[2][1]), xmul(a[0][1], a[2][2])), x[1])),
+                     xmul(xsub(xmul(a[0][1], a[1][2]), xmul(a[0][2], a[1][1])), x[2])),
+                g.det_in);
+    p[1] = xdiv(xadd(xadd(xmul(xsub(xmul(a[1][2], a[2][0]), xmul(a[1][0], a[2][2])), x[0]),
+                          xmul(xsub(xmul(a[0][0], a[2][2]), xmul(a[0][2], a[2][0])), x[1])),
+                     xmul(xsub(xmul(a[0][2], a[1][0]), xmul(a[0][0], a[1][2])), x[2])),
+                g.det_in);
+    p[2] = xdiv(xadd(xadd(xmul(xsub(xmul(a[1][0], a[2][1]), xmul(a[1][1], a[2][0])), x[0]),
+                          xmul(xsub(xmul(a[0][1], a[2][0]), xmul(a[0][0], a[2][1])), x[1])),
+                     xmul(xsub(xmul(a[0][0], a[1][1]), xmul(a[0][1], a[1][0])), x[2])),
+                g.det_in);
+  } else {
+    p[0] = xdiv(xsub(xmul(a[1][1], x[0]), xmul(a[0][1], x[1])), g.det_in);
+    p[1] = xdiv(xsub(xmul(a[0][0], x[1]), xmul(a[1][0], x[0])), g.det_in);
+  }
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    p[i] = xsub(p[i], floor(p[i]));
+    if (p[i] == T(1)) p[i] = T(0);
+  }
+  T w[N];
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    T s = xmul(a[i][0], p[0]);
+#pragma unroll
+    for (int k = 1; k < N; k++) s = xadd(s, xmul(a[i][k], p[k]));
+    w[i] = s;
+  }
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    T s = xmul(g.R[i][0], w[0]);
+#pragma unroll
+    for (int k = 1; k < N; k++) s = xadd(s, xmul(g.R[i][k], w[k]));
+    out[i] = s;
+  }
+}
+
+template <class T, int N>
+__device__ __forceinline__ bool in_box(const DevGeom<T>& g, const T* x) {
+  bool ok = true;
+#pragma unroll
+  for (int i = 0; i < N; i++) ok = ok && (g.cbmin[i] <= x[i]) && (x[i] < g.cbmax[i]);
+  return ok;
+}
+
+// floor((x - xmin)/cell_size) + 1 with the border-case shift for real particles
+// (src/internals/Box.jl:499-508, src/internals/CellLists.jl:956-967).  Returns
+// the 0-based linear cell index, or -1 if the cell is outside the grid.
+template <class T, int N>
+__device__ __forceinline__ int cell_of(const DevGeom<T>& g, const T* x, bool real) {
+  int li = 0;
+#pragma unroll
+  for (int i = N - 1; i >= 0; i--) {
+    T q = xdiv(xsub(x[i], g.cbmin[i]), g.cs[i]);
+    double fq = floor((double)q);
+    if (!(fq >= -1.0 && fq < (double)g.nc[i])) return -1;
+    int c = (int)fq + 1;
+    if (real) {
+      if (c == g.lcell) c += 1;
+      if (c == g.nc[i] - g.lcell + 1) c -= 1;
+    }
+    if (c < 1 || c > g.nc[i]) return -1;
+    li = li * g.nc[i] + (c - 1);
+  }
+  return li;
+}
+
+__device__ __forceinline__ void cart_of(int li, const int* nc, int dim, int* c) {
+  c[0] = li % nc[0] + 1;
+  int r = li / nc[0];
+  if (dim == 3) {
+    c[1] = r % nc[1] + 1;
+    c[2] = r / nc[1] + 1;
+  } else {
+    c[1] = r + 1;
+    c[2] = 1;
+  }
+}
+
+// cell_center (src/internals/Box.jl:517-525)
+template <class T, int N>
+__device__ __forceinline__ void cell_center(const DevGeom<T>& g, const int* c, T* ctr) {
+#pragma unroll
+  for (int i = 0; i < N; i++) ctr[i] = xsub(xadd(g.cbmin[i], xmul(g.cs[i], (T)c[i])), xdiv(g.cs[i], T(2)));
+}
+
+// Device error bits (OR-ed into the handle's error word).
+enum DevError : int {
+  DERR_NAN = 1,
+  DERR_CELL_RANGE = 2,
+  DERR_COPY_OVERFLOW = 4,
+  DERR_NL_OVERFLOW = 8,
+};
+
+}  // namespace clm

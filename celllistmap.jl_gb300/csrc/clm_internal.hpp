@@ -1,0 +1,121 @@
+// Host-side state of a library handle (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "clm_device.cuh"
+#include "clm_geometry.hpp"
+
+namespace clm {
+
+enum Status {
+  OK = 0, ERR_ARG = 1, ERR_CELL_TOO_SMALL = 2, ERR_NAN = 3, ERR_DIM = 4, ERR_CUDA = 5, ERR_CAPACITY = 6,
+  ERR_STATE = 7, ERR_TIMEOUT = 8, ERR_NOMEM = 9, ERR_LCELL = 10, ERR_NONPERIODIC_CELL = 11, ERR_INTERNAL = 12
+};
+
+// Grow-only device buffer.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  // Ensures capacity for `nbytes`; returns false on allocation failure.
+  bool reserve(size_t nbytes) {
+    if (nbytes <= bytes && p) return true;
+    size_t want = nbytes + nbytes / 4 + 256;
+    void* q = nullptr;
+    if (cudaMalloc(&q, want) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    if (p) cudaFree(p);
+    p = q;
+    bytes = want;
+    return true;
+  }
+  template <class U> U* as() const { return static_cast<U*>(p); }
+};
+
+// One particle set and its cell list on the device.
+struct SetData {
+  int64_t n = 0;
+  bool dirty = true;
+  bool built = false;
+  DevBuf x;                 // positions as given (n x dim, column-major dim x n)
+  DevBuf wrapped;           // wrapped (and rotated) positions, n x dim
+  DevBuf mask;              // per particle: bit k set if image k lies in the computing box
+  DevBuf ncopy, copy_off;   // copies per particle and their exclusive scan
+  DevBuf keys[2], vals[2];  // (cell, particle<<5 | image) pairs for the radix sort
+  DevBuf cell_count, cell_start, cell_flags;
+  DevBuf real_list, real_scan;
+  DevBuf px, py, pz;        // copies in cell order (SoA), handle dtype
+  DevBuf off;               // FP32 cell-relative offsets (float4) for the prefilter
+  DevBuf code;              // particle index (>= 0 real copy, -(index+1) image)
+  DevBuf rs_hist;
+  DevBuf minmax;            // non-periodic limits scratch
+  int64_t n_copies = 0;
+  int64_t n_real_cells = 0;
+  int64_t n_cells_with_particles = 0;
+  int64_t ncells = 0;
+};
+
+struct ScanTemp {
+  DevBuf level[4];
+};
+
+struct Handle {
+  int dtype = 1, dim = 3, nsets = 1;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  bool box_set = false;
+  int kind = 0, lcell = 1;
+  double M[9] = {};
+  double cutoff = 0;
+  int precision = 0;
+  Geometry<double> gd;
+  Geometry<float> gf;
+  SetData sets[2];
+  ScanTemp scan;
+  DevBuf err;        // device error word
+  DevBuf counters;   // device counters (NL count, etc.)
+  DevBuf nl_i, nl_j, nl_d;
+  int64_t nl_cap = 0, nl_n = 0;
+  bool nl_valid = false;
+  DevBuf partial;    // per-block partial reductions
+  DevBuf opbuf;      // operator parameter staging (types, tables, velocities, bins)
+  DevBuf outbuf;     // device outputs staged before copying to the caller
+  int* pinned = nullptr;       // small pinned host staging area (256 bytes)
+  cudaEvent_t ev[4] = {};
+  float build_ms = 0, map_ms = 0;
+  int64_t launches = 0;        // kernels launched by this handle (cumulative)
+  std::string last_error;
+};
+
+// Status helpers
+#define CLM_CUDA_TRY(h, call)                                                            \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess) {                                                             \
+      (h).last_error = std::string("CUDA error: ") + cudaGetErrorString(e_) + " at " #call; \
+      return ERR_CUDA;                                                                   \
+    }                                                                                    \
+  } while (0)
+
+// Build (clm_build.cu)
+int scan_exclusive(Handle& h, const int* in, int* out, int64_t m, int* total, int depth = 0);
+template <class T> int build_set(Handle& h, int set, const Geometry<T>& g);
+template <class T> int set_limits(Handle& h, T* lo, T* hi);
+template <class T> void fill_devgeom(const Geometry<T>& g, int precision, DevGeom<T>& d);
+
+// Map (clm_pairs.cu)
+struct OpRequest;
+template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const void* params, void* outputs);
+
+}  // namespace clm

@@ -1,0 +1,1051 @@
+// Cell-pair map on the GPU (K5 self, K6 cross, K7 operator epilogues).
+//
+// Replaces _pairwise! and its inner loops:
+//   self  src/internals/self.jl:106-184      cross src/internals/cross.jl:265-313
+//   vicinal cells with projection culling    src/internals/vicinal_cells.jl:4-75,
+//                                            src/internals/auxiliary_functions.jl:166-186
+//   non-periodic inner loops                 src/internals/NonPeriodicCells.jl:281-352
+// and the per-batch output copies + reduce_output! with on-chip reductions.
+//
+// Work decomposition: one warp per cell that contains real particles (the
+// reference's batches of `cell_indices_real`).  The warp's lanes hold the
+// particles of that cell (split into 1, 2 or 4 lane groups for small cells so
+// that each group takes every G-th neighbour); the particles of each cell of
+// the stencil are staged 32 at a time in shared memory and broadcast.
+//
+// Pair rules are the reference's: orthorhombic self = same cell (later slot,
+// at least one real) + forward half stencil (at least one real); triclinic self
+// = full stencil, real i, index(i) < index(j); cross = full stencil, real i in
+// the same cell, (real i or real j) in vicinal orthorhombic cells; non-periodic
+// = forward stencil, no realness rules.  Vicinal cells apply the projection
+// filter |(x_j - c_i).u| <= margin and |proj_j - proj_i| <= cutoff with the
+// reference's arithmetic.
+//
+// Exact form (CLM_PREC_EXACT): FP32 distances from cell-relative offsets
+// discard pairs that are certainly outside the cutoff (a band of 2^-13 relative
+// covers the FP32 error); every remaining candidate is re-tested with the
+// reference's arithmetic in the input dtype, so the pair set and d are bit-exact.
+// Split form (CLM_PREC_SPLIT): pairs certainly inside are accepted from the
+// FP32 test and evaluated in FP32; only the band is re-tested in the input
+// dtype.  Sums are accumulated in FP64 (Kahan-compensated FP32 per lane).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <type_traits>
+#include <vector>
+
+#include "clm_internal.hpp"
+#include "celllistmap_gb300.h"
+
+namespace clm {
+
+namespace {
+
+constexpr int kWarps = 4;
+constexpr int kThreads = kWarps * 32;
+constexpr int kJC = 32;  // staged neighbours per round
+
+template <class T> struct SetView {
+  const T* px;
+  const T* py;
+  const T* pz;
+  const float4* off;
+  const int* code;
+  const int* cell_start;
+};
+
+template <class T> struct PairArgs {
+  DevGeom<T> g;
+  SetView<T> X, Y;
+  const int* real_list;
+  int n_real;
+  int self;
+  int split;
+  int op;
+  int* err;
+  // operator parameters
+  double p[4];
+  int ntypes;
+  const int* tx;
+  const int* ty;
+  const double* eps_t;
+  const double* sig_t;
+  const T* vx;
+  const T* vy;
+  const T* bins;
+  int nbins;
+  // outputs
+  int* nl_i;
+  int* nl_j;
+  T* nl_d;
+  unsigned long long* nl_count;
+  long long nl_cap;
+  double* fx;       // forces accumulators (double), n_x * dim
+  double* fy;       // n_y * dim (cross)
+  double* part_e;   // per-block energy
+  unsigned long long* part_c;  // per-block count
+  T* part_min_d2;
+  int* part_min_ij;
+  unsigned long long* part_hc;  // nbins per block
+  double* part_hs;              // nbins per block
+};
+
+__device__ __forceinline__ void stencil_offset(bool forward, int l, int dim, int k, int* o) {
+  const int w = 2 * l + 1;
+  o[2] = 0;
+  if (forward) {
+    if (dim == 3) {
+      const int nA = l * w * w, nB = l * w;
+      if (k < nA) {
+        o[0] = 1 + k % l;
+        int r = k / l;
+        o[1] = r % w - l;
+        o[2] = r / w - l;
+      } else if (k < nA + nB) {
+        int k2 = k - nA;
+        o[0] = 0;
+        o[1] = 1 + k2 % l;
+        o[2] = k2 / l - l;
+      } else {
+        o[0] = 0;
+        o[1] = 0;
+        o[2] = 1 + (k - nA - nB);
+      }
+    } else {
+      const int nA = l * w;
+      if (k < nA) {
+        o[0] = 1 + k % l;
+        o[1] = k / l - l;
+      } else {
+        o[0] = 0;
+        o[1] = 1 + (k - nA);
+      }
+    }
+  } else {
+    int total = (dim == 3) ? w * w * w : w * w;
+    int center = (total - 1) / 2;
+    int kk = (k < center) ? k : k + 1;
+    o[0] = kk % w - l;
+    o[1] = (kk / w) % w - l;
+    if (dim == 3) o[2] = kk / (w * w) - l;
+  }
+}
+
+template <class T> __device__ __forceinline__ T pos_of(const SetView<T>& S, int d, int t) {
+  return d == 0 ? S.px[t] : (d == 1 ? S.py[t] : S.pz[t]);
+}
+
+// Kahan-compensated accumulator (FP32) or plain FP64
+template <class A> struct Acc {
+  A s = 0, c = 0;
+  __device__ __forceinline__ void add(A v) {
+    if (std::is_same<A, float>::value) {
+      A y = v - c;
+      A t = s + y;
+      c = (t - s) - y;
+      s = t;
+    } else {
+      s += v;
+    }
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+enum OpKind { OPK_NL = 0, OPK_SCALAR = 1, OPK_FORCES = 2, OPK_MIN = 3, OPK_HIST = 4 };
+
+// Per-pair energy u and g = (du/dr)/r (force contribution df = g*(x_i - x_j)).
+template <class V, class T>
+__device__ __forceinline__ void pair_value(const PairArgs<T>& A, int op, V d2, int i, int j, V& u, V& g) {
+  switch (op) {
+    case 2:  // COUNT
+      u = V(1);
+      g = V(0);
+      break;
+    case 3:  // SUM_D2
+      u = d2;
+      g = V(0);
+      break;
+    case 4:  // SUM_D
+      u = sqrt(d2);
+      g = V(0);
+      break;
+    case 5:  // SUM_INV_D
+      u = V(1) / sqrt(d2);
+      g = V(0);
+      break;
+    case 6:
+    case 7: {  // SOFT (c - d)^2
+      V d = sqrt(d2);
+      V c = (V)A.p[0];
+      u = (c - d) * (c - d);
+      g = V(-2) * (c - d) / d;
+      break;
+    }
+    case 8:
+    case 9: {  // LJ eps*(c12 (s/d)^12 - c6 (s/d)^6)
+      V eps = (V)A.p[0], sig = (V)A.p[1];
+      if (A.ntypes > 0) {
+        int ti = A.tx[i];
+        int tj = A.self ? A.tx[j] : A.ty[j];
+        eps = (V)A.eps_t[ti * A.ntypes + tj];
+        sig = (V)A.sig_t[ti * A.ntypes + tj];
+      }
+      V c12 = (V)A.p[2], c6 = (V)A.p[3];
+      V sr2 = (sig * sig) / d2;
+      V sr6 = sr2 * sr2 * sr2;
+      V sr12 = sr6 * sr6;
+      u = eps * (c12 * sr12 - c6 * sr6);
+      g = eps * (V(-12) * c12 * sr12 + V(6) * c6 * sr6) / d2;
+      break;
+    }
+    case 12: {  // 1/d with gradient accumulation
+      V d = sqrt(d2);
+      u = V(1) / d;
+      g = u / d2;
+      break;
+    }
+    default:
+      u = V(0);
+      g = V(0);
+  }
+}
+
+template <class T, int N, int OPK, bool SPLIT>
+__global__ void __launch_bounds__(kThreads) k_pairs(const PairArgs<T> A) {
+  using V = T;  // exact-form value type
+  // accumulation type: FP64 for the exact FP64 form, Kahan-compensated FP32 otherwise
+  using FA = typename std::conditional<std::is_same<T, double>::value && !SPLIT, double, float>::type;
+  const DevGeom<T>& g = A.g;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const unsigned FULL = 0xffffffffu;
+
+  __shared__ float4 s_off[kWarps][kJC];
+  __shared__ int s_code[kWarps][kJC];
+  __shared__ T s_x[kWarps][3][kJC];
+  __shared__ T s_proj[kWarps][kJC];
+  __shared__ unsigned int s_hc[(OPK == OPK_HIST) ? kWarps : 1][(OPK == OPK_HIST) ? 256 : 1];
+  __shared__ double s_hs[(OPK == OPK_HIST) ? kWarps : 1][(OPK == OPK_HIST) ? 256 : 1];
+  __shared__ double s_red[kWarps];
+  __shared__ unsigned long long s_redc[kWarps];
+
+  const bool tri = (g.kind == TRICLINIC);
+  const bool nonper = (g.kind == NONPERIODIC);
+  const bool self = A.self != 0;
+  const bool forward = self && !tri;
+  const int l = g.lcell;
+  const int w = 2 * l + 1;
+  const int nsten = forward ? (((N == 3) ? w * w * w : w * w) - 1) / 2 : ((N == 3) ? w * w * w : w * w) - 1;
+  const bool fp64 = std::is_same<T, double>::value;
+  const bool use_prefilter = fp64 || SPLIT;
+
+  if constexpr (OPK == OPK_HIST) {
+    for (int b = lane; b < A.nbins; b += 32) {
+      s_hc[warp][b] = 0u;
+      s_hs[warp][b] = 0.0;
+    }
+    __syncwarp();
+  }
+
+  // per-lane accumulators
+  Acc<FA> e_acc;
+  unsigned long long c_acc = 0;
+  T best_d2 = INFINITY;
+  int best_i = 0x7fffffff, best_j = 0x7fffffff;
+
+  const int gw = blockIdx.x * kWarps + warp;
+  const int nw = gridDim.x * kWarps;
+  for (int r = gw; r < A.n_real; r += nw) {
+    const int li = A.real_list[r];
+    int ci[3];
+    cart_of(li, g.nc, N, ci);
+    const int si = A.X.cell_start[li];
+    const int ni = A.X.cell_start[li + 1] - si;
+    const int G = (ni <= 8) ? 4 : ((ni <= 16) ? 2 : 1);
+    const int LP = 32 / G;
+    const int grp = lane / LP;
+    const int il = lane % LP;
+    const unsigned gmask = ((LP == 32) ? FULL : ((1u << LP) - 1u)) << (grp * LP);
+
+    for (int ib = 0; ib < ni; ib += LP) {
+      const int ii = ib + il;
+      const bool vi = ii < ni;
+      const int ti = si + (vi ? ii : 0);
+      T xi[3] = {0, 0, 0};
+      float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
+      int code_i = 0;
+      if (vi) {
+#pragma unroll
+        for (int d = 0; d < N; d++) xi[d] = pos_of(A.X, d, ti);
+        oi = A.X.off[ti];
+        code_i = A.X.code[ti];
+      }
+      const bool real_i = code_i >= 0;
+      const int idx_i = real_i ? code_i : -code_i - 1;
+      bool act_i = vi;
+      if (!nonper && (tri || !self) && !real_i) act_i = false;  // i must be real except ortho self/cross-vicinal
+      if (!self && !nonper && !tri) act_i = vi;                 // ortho cross: ghosts of x may pair in vicinal cells
+      // force accumulators for i (rotated frame)
+      FA fi[3] = {0, 0, 0};
+
+      for (int o = 0; o <= nsten; o++) {
+        int oc[3] = {0, 0, 0};
+        if (o > 0) stencil_offset(forward, l, N, o - 1, oc);
+        int cj[3];
+        bool inr = true;
+#pragma unroll
+        for (int d = 0; d < N; d++) {
+          cj[d] = ci[d] + oc[d];
+          inr = inr && cj[d] >= 1 && cj[d] <= g.nc[d];
+        }
+        if (!inr) {
+          if (lane == 0) atomicOr(A.err, DERR_CELL_RANGE);
+          continue;
+        }
+        int lj = cj[0] - 1;
+        if (N == 3) lj += g.nc[0] * ((cj[1] - 1) + g.nc[1] * (cj[2] - 1));
+        else lj += g.nc[0] * (cj[1] - 1);
+        const int sj = A.Y.cell_start[lj];
+        const int nj = A.Y.cell_start[lj + 1] - sj;
+        if (nj == 0) continue;
+        const bool same = (o == 0);
+        // projection direction (vicinal cells only)
+        T ctr_i[3] = {0, 0, 0}, u[3] = {0, 0, 0};
+        T margin = 0;
+        T proj_i = 0;
+        if (!same) {
+          T ctr_j[3];
+          cell_center<T, N>(g, ci, ctr_i);
+          cell_center<T, N>(g, cj, ctr_j);
+          T dc[3] = {0, 0, 0};
+#pragma unroll
+          for (int d = 0; d < N; d++) dc[d] = xsub(ctr_j[d], ctr_i[d]);
+          T s2 = xmul(dc[0], dc[0]);
+#pragma unroll
+          for (int d = 1; d < N; d++) s2 = xadd(s2, xmul(dc[d], dc[d]));
+          T dcn = xsqrt(s2);
+#pragma unroll
+          for (int d = 0; d < N; d++) u[d] = xdiv(dc[d], dcn);
+          margin = xadd(g.cutoff, xdiv(dcn, T(2)));
+          if (act_i) {
+            T pv = xmul(xsub(xi[0], ctr_i[0]), u[0]);
+#pragma unroll
+            for (int d = 1; d < N; d++) pv = xadd(pv, xmul(xsub(xi[d], ctr_i[d]), u[d]));
+            proj_i = pv;
+          }
+        }
+        // FP32 displacement between cell origins: x_i - x_j = (off_i - off_j) - cs*(cj - ci)
+        float dcf[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int d = 0; d < N; d++) dcf[d] = g.csf[d] * (float)(cj[d] - ci[d]);
+
+        for (int jb = 0; jb < nj; jb += kJC) {
+          const int cnt = min(kJC, nj - jb);
+          // stage
+          if (lane < cnt) {
+            const int tj = sj + jb + lane;
+            s_off[warp][lane] = A.Y.off[tj];
+            s_code[warp][lane] = A.Y.code[tj];
+            T xj[3] = {0, 0, 0};
+#pragma unroll
+            for (int d = 0; d < N; d++) {
+              xj[d] = pos_of(A.Y, d, tj);
+              s_x[warp][d][lane] = xj[d];
+            }
+            if (!same) {
+              T pv = xmul(xsub(xj[0], ctr_i[0]), u[0]);
+#pragma unroll
+              for (int d = 1; d < N; d++) pv = xadd(pv, xmul(xsub(xj[d], ctr_i[d]), u[d]));
+              bool keep = (l == 1) ? (fabs(pv) <= margin) : ((double)fabs(pv) <= g.margin_wide);
+              s_proj[warp][lane] = keep ? pv : (T)NAN;
+            }
+          }
+          __syncwarp();
+          for (int jq = 0; jq < cnt; jq += G) {
+            const int j = jq + grp;
+            const bool vj = j < cnt;
+            bool cand = act_i && vj;
+            int code_j = vj ? s_code[warp][j] : 0;
+            const bool real_j = code_j >= 0;
+            const int idx_j = real_j ? code_j : -code_j - 1;
+            if (cand) {
+              if (nonper) {
+                if (self && same) cand = (jb + j) > ii;
+              } else if (self) {
+                if (tri) cand = idx_i < idx_j;
+                else if (same) cand = ((jb + j) > ii) && (real_i || real_j);
+                else cand = real_i || real_j;
+              } else {
+                if (!tri && !same) cand = real_i || real_j;
+                else cand = real_i;
+              }
+            }
+            bool hit = false;
+            bool sure = false;
+            float d2f = 0.f;
+            float dvf[3] = {0.f, 0.f, 0.f};
+            if (cand && use_prefilter) {
+              float4 oj = s_off[warp][j];
+              dvf[0] = (oi.x - oj.x) - dcf[0];
+              dvf[1] = (oi.y - oj.y) - dcf[1];
+              dvf[2] = (N == 3) ? ((oi.z - oj.z) - dcf[2]) : 0.f;
+              d2f = fmaf(dvf[2], dvf[2], fmaf(dvf[1], dvf[1], dvf[0] * dvf[0]));
+              if (!(d2f <= g.thr_hi)) cand = false;
+              else if (SPLIT && d2f <= g.thr_lo) {
+                // certainly inside; the projection filter never removes such pairs
+                sure = same || (s_proj[warp][j] == s_proj[warp][j]);
+                if (sure) hit = true;
+                cand = false;
+              }
+            }
+            T d2 = 0;
+            if (cand) {
+              // exact re-test with the reference's arithmetic
+              bool pass = true;
+              if (!same) pass = fabs(xsub(s_proj[warp][j], proj_i)) <= g.cutoff;
+              if (pass) {
+                T dx = xsub(xi[0], s_x[warp][0][j]);
+                d2 = xmul(dx, dx);
+#pragma unroll
+                for (int d = 1; d < N; d++) {
+                  T dd = xsub(xi[d], s_x[warp][d][j]);
+                  d2 = xadd(d2, xmul(dd, dd));
+                }
+                hit = d2 <= g.cutoff_sqr;
+              }
+            }
+            // ---------------- operator epilogues
+            if constexpr (OPK == OPK_NL) {
+              unsigned bal = __ballot_sync(FULL, hit);
+              if (bal) {
+                unsigned long long base = 0;
+                int leader = __ffs(bal) - 1;
+                if (lane == leader) base = atomicAdd(A.nl_count, (unsigned long long)__popc(bal));
+                base = __shfl_sync(FULL, base, leader);
+                if (hit) {
+                  unsigned long long pos = base + __popc(bal & ((1u << lane) - 1u));
+                  if ((long long)pos < A.nl_cap) {
+                    A.nl_i[pos] = idx_i;
+                    A.nl_j[pos] = idx_j;
+                    A.nl_d[pos] = sure ? (T)sqrtf(d2f) : xsqrt(d2);
+                  }
+                }
+              }
+            } else if constexpr (OPK == OPK_SCALAR) {
+              if (hit) {
+                if (A.op == 2) {
+                  c_acc++;
+                } else if (sure) {
+                  float uu, gg;
+                  pair_value<float, T>(A, A.op, d2f, idx_i, idx_j, uu, gg);
+                  e_acc.add((FA)uu);
+                } else {
+                  V uu, gg;
+                  pair_value<V, T>(A, A.op, (V)d2, idx_i, idx_j, uu, gg);
+                  e_acc.add((FA)uu);
+                }
+              }
+            } else if constexpr (OPK == OPK_FORCES) {
+              FA df[3] = {0, 0, 0};
+              if (hit) {
+                FA uu, gg;
+                if (sure) {
+                  float uf, gf;
+                  pair_value<float, T>(A, A.op, d2f, idx_i, idx_j, uf, gf);
+                  uu = (FA)uf;
+                  gg = (FA)gf;
+#pragma unroll
+                  for (int d = 0; d < N; d++) df[d] = gg * (FA)dvf[d];
+                } else {
+                  V uv, gv;
+                  pair_value<V, T>(A, A.op, (V)d2, idx_i, idx_j, uv, gv);
+                  uu = (FA)uv;
+                  gg = (FA)gv;
+#pragma unroll
+                  for (int d = 0; d < N; d++) df[d] = gg * (FA)xsub(xi[d], s_x[warp][d][j]);
+                }
+                e_acc.add(uu);
+#pragma unroll
+                for (int d = 0; d < N; d++) fi[d] -= df[d];
+              }
+              unsigned bal = __ballot_sync(FULL, hit) & gmask;
+              if (__ballot_sync(FULL, bal != 0u)) {
+                // reduce df over the lanes of each group (they share the same j)
+#pragma unroll
+                for (int d = 0; d < N; d++) {
+                  FA v = df[d];
+                  for (int s = LP / 2; s > 0; s >>= 1) v += __shfl_xor_sync(FULL, v, s);
+                  df[d] = v;
+                }
+                if (il == 0 && bal != 0u) {
+                  double* F = self ? A.fx : A.fy;
+#pragma unroll
+                  for (int d = 0; d < N; d++) atomicAdd(&F[(int64_t)idx_j * N + d], (double)df[d]);
+                }
+              }
+            } else if constexpr (OPK == OPK_MIN) {
+              if (hit) {
+                T dd2 = d2;
+                if (sure) dd2 = (T)d2f;  // split form: FP32 estimate
+                if (dd2 < best_d2 || (dd2 == best_d2 && (idx_i < best_i || (idx_i == best_i && idx_j < best_j)))) {
+                  best_d2 = dd2;
+                  best_i = idx_i;
+                  best_j = idx_j;
+                }
+              }
+            } else if constexpr (OPK == OPK_HIST) {
+              if (hit) {
+                // searchsortedfirst(bins, r) - 1 with r = sqrt(d2)
+                bool exact_r = !sure;
+                T r = 0;
+                int b = -1;
+                if (sure) {
+                  float rf = sqrtf(d2f);
+                  int lo = 0, hi = A.nbins + 1;
+                  while (lo < hi) {
+                    int mid = (lo + hi) >> 1;
+                    if ((float)A.bins[mid] >= rf) hi = mid;
+                    else lo = mid + 1;
+                  }
+                  b = lo - 1;
+                  // an edge within 2^-12 relative of r: decide with the exact distance
+                  const float tol = rf * 2.44140625e-4f;
+                  if ((lo <= A.nbins && fabsf((float)A.bins[lo] - rf) <= tol) ||
+                      (lo >= 1 && fabsf((float)A.bins[lo - 1] - rf) <= tol))
+                    exact_r = true;
+                  r = (T)rf;
+                }
+                if (exact_r) {
+                  T dx = xsub(xi[0], s_x[warp][0][j]);
+                  T e2 = xmul(dx, dx);
+#pragma unroll
+                  for (int d = 1; d < N; d++) {
+                    T dd = xsub(xi[d], s_x[warp][d][j]);
+                    e2 = xadd(e2, xmul(dd, dd));
+                  }
+                  r = xsqrt(e2);
+                  int lo = 0, hi = A.nbins + 1;
+                  while (lo < hi) {
+                    int mid = (lo + hi) >> 1;
+                    if (A.bins[mid] >= r) hi = mid;
+                    else lo = mid + 1;
+                  }
+                  b = lo - 1;
+                }
+                if (b >= 0 && b < A.nbins) {
+                  FA dv[3] = {0, 0, 0};
+                  if (sure) {
+#pragma unroll
+                    for (int d = 0; d < N; d++) dv[d] = (FA)dvf[d];
+                  } else {
+#pragma unroll
+                    for (int d = 0; d < N; d++) dv[d] = (FA)xsub(xi[d], s_x[warp][d][j]);
+                  }
+                  if (tri) {
+                    FA rv[3];
+#pragma unroll
+                    for (int a = 0; a < N; a++) {
+                      FA s = 0;
+#pragma unroll
+                      for (int k = 0; k < N; k++) s += (FA)g.Rinv[a][k] * dv[k];
+                      rv[a] = s;
+                    }
+#pragma unroll
+                    for (int a = 0; a < N; a++) dv[a] = rv[a];
+                  }
+                  const T* vy = self ? A.vx : A.vy;
+                  FA dot = 0;
+#pragma unroll
+                  for (int d = 0; d < N; d++)
+                    dot += ((FA)A.vx[(int64_t)idx_i * N + d] - (FA)vy[(int64_t)idx_j * N + d]) * dv[d];
+                  atomicAdd(&s_hc[warp][b], 1u);
+                  atomicAdd(&s_hs[warp][b], (double)(dot / (FA)r));
+                }
+              }
+            }
+          }
+          __syncwarp();
+        }
+      }
+      if constexpr (OPK == OPK_FORCES) {
+        // combine the groups' partial forces on i, then one atomic per component
+#pragma unroll
+        for (int d = 0; d < N; d++) {
+          FA v = fi[d];
+          for (int s = LP; s < 32; s <<= 1) v += __shfl_xor_sync(FULL, v, s);
+          fi[d] = v;
+        }
+        if (vi && grp == 0 && (fi[0] != FA(0) || fi[1] != FA(0) || fi[2] != FA(0))) {
+#pragma unroll
+          for (int d = 0; d < N; d++) atomicAdd(&A.fx[(int64_t)idx_i * N + d], (double)fi[d]);
+        }
+      }
+    }
+  }
+
+  // ---------------- block reductions to per-block partials
+  if constexpr (OPK == OPK_SCALAR || OPK == OPK_FORCES) {
+    double e = e_acc.value();
+    unsigned long long c = c_acc;
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+      e += __shfl_xor_sync(FULL, e, s);
+      c += __shfl_xor_sync(FULL, c, s);
+    }
+    if (lane == 0) {
+      s_red[warp] = e;
+      s_redc[warp] = c;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double es = 0;
+      unsigned long long cs = 0;
+      for (int k = 0; k < kWarps; k++) {
+        es += s_red[k];
+        cs += s_redc[k];
+      }
+      A.part_e[blockIdx.x] = es;
+      A.part_c[blockIdx.x] = cs;
+    }
+  } else if constexpr (OPK == OPK_MIN) {
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+      T od = __shfl_xor_sync(FULL, best_d2, s);
+      int oi_ = __shfl_xor_sync(FULL, best_i, s);
+      int oj_ = __shfl_xor_sync(FULL, best_j, s);
+      if (od < best_d2 || (od == best_d2 && (oi_ < best_i || (oi_ == best_i && oj_ < best_j)))) {
+        best_d2 = od;
+        best_i = oi_;
+        best_j = oj_;
+      }
+    }
+    __shared__ T s_md[kWarps];
+    __shared__ int s_mi[kWarps], s_mj[kWarps];
+    if (lane == 0) {
+      s_md[warp] = best_d2;
+      s_mi[warp] = best_i;
+      s_mj[warp] = best_j;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      T bd = s_md[0];
+      int bi = s_mi[0], bj = s_mj[0];
+      for (int k = 1; k < kWarps; k++) {
+        if (s_md[k] < bd || (s_md[k] == bd && (s_mi[k] < bi || (s_mi[k] == bi && s_mj[k] < bj)))) {
+          bd = s_md[k];
+          bi = s_mi[k];
+          bj = s_mj[k];
+        }
+      }
+      A.part_min_d2[blockIdx.x] = bd;
+      A.part_min_ij[2 * blockIdx.x] = bi;
+      A.part_min_ij[2 * blockIdx.x + 1] = bj;
+    }
+  } else if constexpr (OPK == OPK_HIST) {
+    __syncthreads();
+    for (int b = threadIdx.x; b < A.nbins; b += kThreads) {
+      unsigned long long c = 0;
+      double s = 0;
+      for (int k = 0; k < kWarps; k++) {
+        c += s_hc[k][b];
+        s += s_hs[k][b];
+      }
+      A.part_hc[(int64_t)blockIdx.x * A.nbins + b] = c;
+      A.part_hs[(int64_t)blockIdx.x * A.nbins + b] = s;
+    }
+  }
+}
+
+// Fixed-order reductions of the per-block partials (deterministic results).
+__global__ void k_reduce_scalar(const double* __restrict__ pe, const unsigned long long* __restrict__ pc, int nb,
+                                double* __restrict__ out_e, unsigned long long* __restrict__ out_c) {
+  __shared__ double se[256];
+  __shared__ unsigned long long sc[256];
+  double e = 0;
+  unsigned long long c = 0;
+  for (int b = threadIdx.x; b < nb; b += 256) {
+    e += pe[b];
+    c += pc[b];
+  }
+  se[threadIdx.x] = e;
+  sc[threadIdx.x] = c;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) {
+      se[threadIdx.x] += se[threadIdx.x + s];
+      sc[threadIdx.x] += sc[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    *out_e = se[0];
+    *out_c = sc[0];
+  }
+}
+
+template <class T>
+__global__ void k_reduce_min(const T* __restrict__ pd, const int* __restrict__ pij, int nb, T* out_d, int* out_ij) {
+  if (threadIdx.x != 0) return;
+  T bd = INFINITY;
+  int bi = 0x7fffffff, bj = 0x7fffffff;
+  for (int b = 0; b < nb; b++) {
+    T d = pd[b];
+    int i = pij[2 * b], j = pij[2 * b + 1];
+    if (d < bd || (d == bd && (i < bi || (i == bi && j < bj)))) {
+      bd = d;
+      bi = i;
+      bj = j;
+    }
+  }
+  *out_d = bd;
+  out_ij[0] = bi;
+  out_ij[1] = bj;
+}
+
+__global__ void k_reduce_hist(const unsigned long long* __restrict__ pc, const double* __restrict__ ps, int nb,
+                              int nbins, unsigned long long* oc, double* os) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbins) return;
+  unsigned long long c = 0;
+  double s = 0;
+  for (int k = 0; k < nb; k++) {
+    c += pc[(int64_t)k * nbins + b];
+    s += ps[(int64_t)k * nbins + b];
+  }
+  oc[b] = c;
+  os[b] = s;
+}
+
+// forces: accumulators (rotated frame, double) -> output dtype in the original frame
+template <class T, int N>
+__global__ void k_forces_out(const double* __restrict__ facc, int64_t n, DevGeom<T> g, int rotate, T* __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double f[N];
+#pragma unroll
+  for (int d = 0; d < N; d++) f[d] = facc[i * N + d];
+  if (rotate) {
+    double r[N];
+#pragma unroll
+    for (int a = 0; a < N; a++) {
+      double s = 0;
+#pragma unroll
+      for (int k = 0; k < N; k++) s += (double)g.Rinv[a][k] * f[k];
+      r[a] = s;
+    }
+#pragma unroll
+    for (int d = 0; d < N; d++) f[d] = r[d];
+  }
+#pragma unroll
+  for (int d = 0; d < N; d++) out[i * N + d] = (T)f[d];
+}
+
+template <class T> SetView<T> view_of(const SetData& S) {
+  SetView<T> v;
+  v.px = S.px.as<T>();
+  v.py = S.py.as<T>();
+  v.pz = S.pz.as<T>();
+  v.off = S.off.as<float4>();
+  v.code = S.code.as<int>();
+  v.cell_start = S.cell_start.as<int>();
+  return v;
+}
+
+inline int opkind_of(int op) {
+  switch (op) {
+    case 1: return OPK_NL;
+    case 2: case 3: case 4: case 5: case 6: case 8: return OPK_SCALAR;
+    case 7: case 9: case 12: return OPK_FORCES;
+    case 10: return OPK_MIN;
+    case 11: return OPK_HIST;
+    default: return -1;
+  }
+}
+
+template <class T, int N, bool SPLIT>
+cudaError_t launch_s(int opk, int grid, cudaStream_t st, const PairArgs<T>& A) {
+  switch (opk) {
+    case OPK_NL: k_pairs<T, N, OPK_NL, SPLIT><<<grid, kThreads, 0, st>>>(A); break;
+    case OPK_SCALAR: k_pairs<T, N, OPK_SCALAR, SPLIT><<<grid, kThreads, 0, st>>>(A); break;
+    case OPK_FORCES: k_pairs<T, N, OPK_FORCES, SPLIT><<<grid, kThreads, 0, st>>>(A); break;
+    case OPK_MIN: k_pairs<T, N, OPK_MIN, SPLIT><<<grid, kThreads, 0, st>>>(A); break;
+    case OPK_HIST: k_pairs<T, N, OPK_HIST, SPLIT><<<grid, kThreads, 0, st>>>(A); break;
+  }
+  return cudaGetLastError();
+}
+
+template <class T, int N>
+cudaError_t launch(int opk, int grid, cudaStream_t st, const PairArgs<T>& A) {
+  return A.split ? launch_s<T, N, true>(opk, grid, st, A) : launch_s<T, N, false>(opk, grid, st, A);
+}
+
+}  // namespace
+
+// Estimated number of pairs assuming uniform density (src/internals/neighborlist.jl:229-241)
+static double estimated_pairs(const Handle& h, double vol) {
+  const double pi = 3.14159265358979323846;
+  double sph = (h.dim == 2 ? pi : 4.0 * pi / 3.0) * std::pow(h.cutoff, h.dim);
+  double nx = (double)h.sets[0].n;
+  if (h.nsets == 1) return std::max(0.0, nx * (nx - 1) / 2 * sph / vol);
+  return std::max(0.0, nx * (double)h.sets[1].n * sph / vol);
+}
+
+template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const void* vparams, void* vout) {
+  const clm_op_params* P = static_cast<const clm_op_params*>(vparams);
+  clm_outputs* O = static_cast<clm_outputs*>(vout);
+  const int opk = opkind_of(op);
+  if (opk < 0) {
+    h.last_error = "unknown operator id";
+    return ERR_ARG;
+  }
+  const int N = g.dim;
+  SetData& X = h.sets[0];
+  SetData& Y = (h.nsets == 2) ? h.sets[1] : h.sets[0];
+  PairArgs<T> A;
+  std::memset(&A, 0, sizeof(A));
+  fill_devgeom(g, h.precision, A.g);
+  A.X = view_of<T>(X);
+  A.Y = view_of<T>(Y);
+  A.real_list = X.real_list.as<int>();
+  A.n_real = (int)X.n_real_cells;
+  A.self = (h.nsets == 1);
+  A.split = (h.precision == 1);
+  A.op = op;
+  A.err = h.err.as<int>();
+  const double c_default = (double)g.cutoff;
+  for (int k = 0; k < 4; k++) A.p[k] = P ? P->p[k] : 0.0;
+  if ((op == 6 || op == 7) && A.p[0] == 0.0) A.p[0] = c_default;
+  // operator tables staged on the device
+  size_t need = 0;
+  auto align = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  const int64_t nx = X.n, ny = (h.nsets == 2) ? Y.n : 0;
+  const bool types = P && (op == 8 || op == 9) && P->ntypes > 0;
+  const bool hist = (op == 11);
+  if (types) {
+    if (!P->types_x || !P->eps_table || !P->sig_table || (h.nsets == 2 && !P->types_y)) {
+      h.last_error = "LJ with types needs types_x (types_y), eps_table and sig_table";
+      return ERR_ARG;
+    }
+    need += align(sizeof(int) * nx) + align(sizeof(int) * ny) + 2 * align(sizeof(double) * P->ntypes * P->ntypes);
+  }
+  if (hist) {
+    if (!P || P->nbins < 1 || P->nbins > 256 || !P->bins || !P->vel_x || (h.nsets == 2 && !P->vel_y)) {
+      h.last_error = "RHIST needs 1..256 bins, bin edges and velocities";
+      return ERR_ARG;
+    }
+    need += align(sizeof(T) * (P->nbins + 1)) + align(sizeof(T) * nx * N) + align(sizeof(T) * ny * N);
+  }
+  if (need && !h.opbuf.reserve(need)) return ERR_NOMEM;
+  char* ob = h.opbuf.as<char>();
+  size_t at = 0;
+  const cudaMemcpyKind k_in = (P && P->params_on_device) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  if (types) {
+    A.ntypes = P->ntypes;
+    int* tx = (int*)(ob + at);
+    at += align(sizeof(int) * nx);
+    int* ty = (int*)(ob + at);
+    at += align(sizeof(int) * ny);
+    double* et = (double*)(ob + at);
+    at += align(sizeof(double) * P->ntypes * P->ntypes);
+    double* stb = (double*)(ob + at);
+    at += align(sizeof(double) * P->ntypes * P->ntypes);
+    CLM_CUDA_TRY(h, cudaMemcpyAsync(tx, P->types_x, sizeof(int) * nx, k_in, h.stream));
+    if (ny) CLM_CUDA_TRY(h, cudaMemcpyAsync(ty, P->types_y, sizeof(int) * ny, k_in, h.stream));
+    CLM_CUDA_TRY(h, cudaMemcpyAsync(et, P->eps_table, sizeof(double) * P->ntypes * P->ntypes, k_in, h.stream));
+    CLM_CUDA_TRY(h, cudaMemcpyAsync(stb, P->sig_table, sizeof(double) * P->ntypes * P->ntypes, k_in, h.stream));
+    A.tx = tx;
+    A.ty = ty;
+    A.eps_t = et;
+    A.sig_t = stb;
+  }
+  if (hist) {
+    A.nbins = P->nbins;
+    T* bins = (T*)(ob + at);
+    at += align(sizeof(T) * (P->nbins + 1));
+    T* vx = (T*)(ob + at);
+    at += align(sizeof(T) * nx * N);
+    T* vy = (T*)(ob + at);
+    at += align(sizeof(T) * ny * N);
+    // bin edges are given in double; compare in the handle dtype as the reference does
+    std::vector<T> b((size_t)P->nbins + 1);
+    if (P->params_on_device) {
+      std::vector<double> bd((size_t)P->nbins + 1);
+      CLM_CUDA_TRY(h, cudaMemcpy(bd.data(), P->bins, sizeof(double) * bd.size(), cudaMemcpyDeviceToHost));
+      for (size_t k = 0; k < b.size(); k++) b[k] = (T)bd[k];
+    } else {
+      for (size_t k = 0; k < b.size(); k++) b[k] = (T)P->bins[k];
+    }
+    CLM_CUDA_TRY(h, cudaMemcpyAsync(bins, b.data(), sizeof(T) * b.size(), cudaMemcpyHostToDevice, h.stream));
+    CLM_CUDA_TRY(h, cudaMemcpyAsync(vx, P->vel_x, sizeof(T) * nx * N, k_in, h.stream));
+    if (ny) CLM_CUDA_TRY(h, cudaMemcpyAsync(vy, P->vel_y, sizeof(T) * ny * N, k_in, h.stream));
+    A.bins = bins;
+    A.vx = vx;
+    A.vy = vy;
+    CLM_CUDA_TRY(h, cudaStreamSynchronize(h.stream));  // the host vector b goes out of scope
+  }
+  // grid: static round-robin of real cells over warps (deterministic)
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((A.n_real + kWarps - 1) / kWarps, 152 * 16));
+  // partials
+  const size_t part_bytes = align(sizeof(double) * grid) + align(sizeof(unsigned long long) * grid) +
+                            align(sizeof(T) * grid) + align(sizeof(int) * 2 * grid) +
+                            (hist ? align(sizeof(unsigned long long) * grid * A.nbins) + align(sizeof(double) * grid * A.nbins) : 0) +
+                            4 * align(sizeof(double) * 512);
+  if (!h.partial.reserve(part_bytes)) return ERR_NOMEM;
+  char* pb = h.partial.as<char>();
+  at = 0;
+  A.part_e = (double*)(pb + at);
+  at += align(sizeof(double) * grid);
+  A.part_c = (unsigned long long*)(pb + at);
+  at += align(sizeof(unsigned long long) * grid);
+  A.part_min_d2 = (T*)(pb + at);
+  at += align(sizeof(T) * grid);
+  A.part_min_ij = (int*)(pb + at);
+  at += align(sizeof(int) * 2 * grid);
+  if (hist) {
+    A.part_hc = (unsigned long long*)(pb + at);
+    at += align(sizeof(unsigned long long) * grid * A.nbins);
+    A.part_hs = (double*)(pb + at);
+    at += align(sizeof(double) * grid * A.nbins);
+  }
+  char* res = pb + at;  // final results
+  double* r_e = (double*)res;
+  unsigned long long* r_c = (unsigned long long*)(res + 8);
+  T* r_md = (T*)(res + 16);
+  int* r_mij = (int*)(res + 24);
+  unsigned long long* r_hc = (unsigned long long*)(res + 256);
+  double* r_hs = (double*)(res + 256 + 8 * 256);
+  // outputs
+  const bool forces = (opk == OPK_FORCES);
+  if (forces) {
+    size_t fb = sizeof(double) * (nx + ny) * N;
+    if (!h.outbuf.reserve(fb + sizeof(T) * (nx + ny) * N + 256)) return ERR_NOMEM;
+    A.fx = h.outbuf.as<double>();
+    A.fy = A.fx + nx * N;
+    CLM_CUDA_TRY(h, cudaMemsetAsync(A.fx, 0, fb, h.stream));
+  }
+  if (opk == OPK_NL) {
+    double vol = std::fabs((double)g.det_in);
+    int64_t est = (int64_t)(estimated_pairs(h, vol) * 1.15) + 4096;
+    if (h.nl_cap < est) h.nl_cap = est;
+    if (!h.counters.reserve(64)) return ERR_NOMEM;
+    A.nl_count = h.counters.as<unsigned long long>();
+  }
+  for (int attempt = 0; attempt < 2; attempt++) {
+    if (opk == OPK_NL) {
+      if (!h.nl_i.reserve(sizeof(int) * h.nl_cap) || !h.nl_j.reserve(sizeof(int) * h.nl_cap) ||
+          !h.nl_d.reserve(sizeof(T) * h.nl_cap))
+        return ERR_NOMEM;
+      A.nl_i = h.nl_i.as<int>();
+      A.nl_j = h.nl_j.as<int>();
+      A.nl_d = h.nl_d.as<T>();
+      A.nl_cap = h.nl_cap;
+      CLM_CUDA_TRY(h, cudaMemsetAsync(A.nl_count, 0, sizeof(unsigned long long), h.stream));
+    }
+    cudaEventRecord(h.ev[2], h.stream);  // brackets the pair kernel alone
+    cudaError_t e = (N == 3) ? launch<T, 3>(opk, grid, h.stream, A) : launch<T, 2>(opk, grid, h.stream, A);
+    cudaEventRecord(h.ev[3], h.stream);
+    if (e != cudaSuccess) {
+      h.last_error = std::string("pair kernel launch failed: ") + cudaGetErrorString(e);
+      return ERR_CUDA;
+    }
+    h.launches++;
+    if (opk != OPK_NL) break;
+    unsigned long long n_pairs = 0;
+    CLM_CUDA_TRY(h, cudaMemcpyAsync(&n_pairs, A.nl_count, sizeof(n_pairs), cudaMemcpyDeviceToHost, h.stream));
+    CLM_CUDA_TRY(h, cudaStreamSynchronize(h.stream));
+    h.nl_n = (int64_t)n_pairs;
+    if ((int64_t)n_pairs <= h.nl_cap) break;
+    h.nl_cap = (int64_t)n_pairs + n_pairs / 16 + 1024;  // retry once with the exact size
+  }
+  if (opk == OPK_SCALAR || opk == OPK_FORCES) {
+    k_reduce_scalar<<<1, 256, 0, h.stream>>>(A.part_e, A.part_c, grid, r_e, r_c);
+  } else if (opk == OPK_MIN) {
+    k_reduce_min<T><<<1, 32, 0, h.stream>>>(A.part_min_d2, A.part_min_ij, grid, r_md, r_mij);
+  } else if (opk == OPK_HIST) {
+    k_reduce_hist<<<(A.nbins + 63) / 64, 64, 0, h.stream>>>(A.part_hc, A.part_hs, grid, A.nbins, r_hc, r_hs);
+  }
+  CLM_CUDA_TRY(h, cudaGetLastError());
+  if (opk != OPK_NL) h.launches++;
+  if (forces) {
+    const int rot = (g.kind == TRICLINIC) ? 1 : 0;
+    DevGeom<T>& dg = A.g;
+    T* dst_x = nullptr;
+    T* dst_y = nullptr;
+    // stage into outbuf after the accumulators when the caller gave host pointers
+    size_t acc_bytes = sizeof(double) * (nx + ny) * N;
+    if (!O->out_on_device) {
+      dst_x = (T*)(h.outbuf.as<char>() + acc_bytes);
+      dst_y = dst_x + nx * N;
+    } else {
+      dst_x = (T*)O->forces_x;
+      dst_y = (T*)O->forces_y;
+    }
+    h.launches += (nx && dst_x) + (ny && dst_y);
+    if (nx && dst_x) {
+      if (N == 3) k_forces_out<T, 3><<<(unsigned)((nx + 255) / 256), 256, 0, h.stream>>>(A.fx, nx, dg, rot, dst_x);
+      else k_forces_out<T, 2><<<(unsigned)((nx + 255) / 256), 256, 0, h.stream>>>(A.fx, nx, dg, rot, dst_x);
+    }
+    if (ny && dst_y) {
+      if (N == 3) k_forces_out<T, 3><<<(unsigned)((ny + 255) / 256), 256, 0, h.stream>>>(A.fx + nx * N, ny, dg, rot, dst_y);
+      else k_forces_out<T, 2><<<(unsigned)((ny + 255) / 256), 256, 0, h.stream>>>(A.fx + nx * N, ny, dg, rot, dst_y);
+    }
+    CLM_CUDA_TRY(h, cudaGetLastError());
+    if (!O->out_on_device) {
+      if (O->forces_x && nx)
+        CLM_CUDA_TRY(h, cudaMemcpyAsync(O->forces_x, dst_x, sizeof(T) * nx * N, cudaMemcpyDeviceToHost, h.stream));
+      if (O->forces_y && ny)
+        CLM_CUDA_TRY(h, cudaMemcpyAsync(O->forces_y, dst_y, sizeof(T) * ny * N, cudaMemcpyDeviceToHost, h.stream));
+    }
+  }
+  // scalar results
+  char hostres[256 + 16 * 256];
+  CLM_CUDA_TRY(h, cudaMemcpyAsync(hostres, res, sizeof(hostres), cudaMemcpyDeviceToHost, h.stream));
+  CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 4, h.err.p, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+  CLM_CUDA_TRY(h, cudaStreamSynchronize(h.stream));
+  cudaEventElapsedTime(&h.map_ms, h.ev[2], h.ev[3]);
+  if (h.pinned[4] & DERR_CELL_RANGE) {
+    h.last_error = "pair map consistency check failed (stencil cell outside the grid)";
+    return ERR_INTERNAL;
+  }
+  std::memcpy(&O->scalar, hostres, 8);
+  unsigned long long cnt;
+  std::memcpy(&cnt, hostres + 8, 8);
+  O->count = (int64_t)cnt;
+  if (opk == OPK_NL) {
+    O->count = h.nl_n;
+    h.nl_valid = true;
+  }
+  if (op == 2) O->scalar = (double)cnt;
+  if (opk == OPK_MIN) {
+    T md;
+    int mij[2];
+    std::memcpy(&md, hostres + 16, sizeof(T));
+    std::memcpy(mij, hostres + 24, 8);
+    if (std::isinf((double)md)) {
+      O->min_d = INFINITY;
+      O->min_i = -1;
+      O->min_j = -1;
+    } else {
+      O->min_d = (double)std::sqrt(md);
+      O->min_i = mij[0] + O->index_base;
+      O->min_j = mij[1] + O->index_base;
+    }
+  }
+  if (opk == OPK_HIST) {
+    if (O->out_on_device) {
+      CLM_CUDA_TRY(h, cudaMemcpyAsync(O->hist_count, r_hc, 8 * A.nbins, cudaMemcpyDeviceToDevice, h.stream));
+      CLM_CUDA_TRY(h, cudaMemcpyAsync(O->hist_sum, r_hs, 8 * A.nbins, cudaMemcpyDeviceToDevice, h.stream));
+    } else {
+      if (O->hist_count) std::memcpy(O->hist_count, hostres + 256, 8 * A.nbins);
+      if (O->hist_sum) std::memcpy(O->hist_sum, hostres + 256 + 8 * 256, 8 * A.nbins);
+    }
+  }
+  return OK;
+}
+
+template int run_pairs<float>(Handle&, const Geometry<float>&, int, const void*, void*);
+template int run_pairs<double>(Handle&, const Geometry<double>&, int, const void*, void*);
+
+}  // namespace clm

@@ -1,0 +1,183 @@
+/*
+ * celllistmap_gb300.h — C ABI of libcelllist_cuda.so, the GB300 (sm_103a)
+ * cutoff-pair engine: cell-list construction and the cell-pair map with a
+ * registry of built-in pair operators.
+ *
+ * Every function returns an int32 status (CLM_OK = 0).  A handle owns all the
+ * device buffers it uses; host pointers passed in are read during the call and
+ * not retained.  One handle = one CUDA stream = one host thread at a time;
+ * different handles are independent.
+ *
+ * The entry points replace these calls of CellListMap.jl (paths are relative to
+ * the CellListMap.jl source tree):
+ *   Box(unitcell, cutoff; lcell)          src/internals/Box.jl:191-203, 330-335, 374-377
+ *   CellList / UpdateCellList!            src/internals/CellLists.jl:511-521, 590-605, 644-927, 1094-1204
+ *   _pairwise!(f, output, box, cl)        src/internals/self.jl:28-45, src/internals/cross.jl:8-25
+ *   pairwise!(f, sys)                     src/API/pairwise.jl:48-63
+ *   neighborlist / neighborlist!          src/API/neighborlist.jl:217-231, 314-340
+ * with `f` restricted to the built-in operators enumerated by clm_op_id.
+ */
+#ifndef CELLLISTMAP_GB300_H
+#define CELLLISTMAP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct clm_handle_s* clm_handle;
+
+/* Status codes.  The Julia/Python front ends map them back to the reference's
+ * exception types (ArgumentError, DimensionMismatch). */
+enum clm_status {
+  CLM_OK = 0,
+  CLM_ERR_ARG = 1,             /* invalid argument (ArgumentError) */
+  CLM_ERR_CELL_TOO_SMALL = 2,  /* unit cell check failed, src/internals/Box.jl:243,597-607 */
+  CLM_ERR_NAN = 3,             /* NaN coordinates, src/internals/CellOperations.jl:6-21 */
+  CLM_ERR_DIM = 4,             /* dimension mismatch, src/internals/CellLists.jl:740-751 */
+  CLM_ERR_CUDA = 5,            /* a CUDA runtime call failed */
+  CLM_ERR_CAPACITY = 6,        /* output buffer too small; the required size is reported */
+  CLM_ERR_STATE = 7,           /* call out of order (e.g. run before build) */
+  CLM_ERR_TIMEOUT = 8,         /* a bounded device-side wait gave up */
+  CLM_ERR_NOMEM = 9,           /* device allocation failed */
+  CLM_ERR_LCELL = 10,          /* lcell < 1, src/internals/Box.jl:192 */
+  CLM_ERR_NONPERIODIC_CELL = 11, /* unit-cell update on a non-periodic system, src/API/updating.jl:30-45 */
+  CLM_ERR_INTERNAL = 12        /* a device-side consistency check failed */
+};
+
+enum clm_dtype { CLM_F32 = 0, CLM_F64 = 1 };
+
+/* Box kinds: OrthorhombicCell, TriclinicCell, NonPeriodicCell (src/internals/Box.jl:5-9) */
+enum clm_cell_kind { CLM_ORTHO = 0, CLM_TRICLINIC = 1, CLM_NONPERIODIC = 2 };
+
+/* Built-in pair operators.  Each reproduces one closure pattern of the
+ * reference (file:line of the pattern in the comments). */
+enum clm_op_id {
+  CLM_OP_NL = 1,             /* push_pair!: (i, j, d), src/internals/neighborlist.jl:253-262 */
+  CLM_OP_COUNT = 2,          /* number of pairs, test/modules/Testing.jl:135-141 */
+  CLM_OP_SUM_D2 = 3,         /* output += d2, src/API/ParticleSystem.jl:110-118 */
+  CLM_OP_SUM_D = 4,          /* output += d, test/modules/Testing.jl:22 */
+  CLM_OP_SUM_INV_D = 5,      /* output += 1/d */
+  CLM_OP_SOFT_ENERGY = 6,    /* u += (c - d)^2, test/examples/packmol.jl:49-55 */
+  CLM_OP_SOFT_FORCES = 7,    /* energy and forces of (c - d)^2 */
+  CLM_OP_LJ_ENERGY = 8,      /* u += eps*(c12 (s/d)^12 - c6 (s/d)^6), test/applications/namd/ParticleSystem_vs_NAMD.jl:15-18 */
+  CLM_OP_LJ_FORCES = 9,      /* energy and forces of the same, per-type eps/sigma tables optional */
+  CLM_OP_MINDIST = 10,       /* argmin d, test/examples/nearest_neighbor.jl:9-16,43 */
+  CLM_OP_RHIST = 11,         /* radial histogram with per-bin velocity accumulator, test/examples/pairwise_velocities.jl:17-24 */
+  CLM_OP_INV_D_FORCES = 12   /* energy 1/d with gradient accumulation, docs/src/ParticleSystem/single_set_compound.md:79-86 */
+};
+
+/* Precision forms of the map (see clm_set_precision). */
+enum clm_precision {
+  CLM_PREC_EXACT = 0,  /* input dtype end to end; results bit-exact with the reference's arithmetic */
+  CLM_PREC_SPLIT = 1   /* FP32 pair arithmetic on cell-relative offsets, FP64 re-test of pairs near the cutoff */
+};
+
+/* Operator parameters (clm_run's op_params).  Unused fields are ignored. */
+typedef struct {
+  double p[8];               /* SOFT: p[0] = c (0 => cutoff).  LJ: p[0] = eps, p[1] = sigma, p[2] = c12, p[3] = c6 */
+  int32_t ntypes;            /* LJ: number of particle types (0 => single eps/sigma) */
+  int32_t nbins;             /* RHIST: number of bins */
+  const int32_t* types_x;    /* LJ: type of each x particle (host or device, see params_on_device) */
+  const int32_t* types_y;    /* LJ cross: type of each y particle */
+  const double* eps_table;   /* LJ: ntypes x ntypes row-major */
+  const double* sig_table;   /* LJ: ntypes x ntypes row-major */
+  const double* vel_x;       /* RHIST: velocities of x, n x dim, in the handle's dtype */
+  const double* vel_y;       /* RHIST cross: velocities of y */
+  const double* bins;        /* RHIST: nbins+1 ascending edges */
+  int32_t params_on_device;  /* 1 if the pointers above are device pointers */
+  int32_t reserved;
+} clm_op_params;
+
+/* Outputs of clm_run.  Pointers may be host or device (out_on_device).  Only
+ * the fields the operator produces are written. */
+typedef struct {
+  double scalar;             /* energies / sums (host, always written when produced) */
+  int64_t count;             /* pair count (COUNT, NL) */
+  int64_t min_i, min_j;      /* MINDIST: pair with the smallest distance (index_base applied) */
+  double min_d;
+  void* forces_x;            /* n_x x dim in the handle's dtype */
+  void* forces_y;            /* n_y x dim (cross) */
+  int64_t* hist_count;       /* nbins */
+  double* hist_sum;          /* nbins */
+  int32_t out_on_device;
+  int32_t index_base;        /* 0 or 1 for MINDIST indices */
+} clm_outputs;
+
+/* Handle lifecycle.  nsets = 1 (self pairs) or 2 (x-y cross pairs).
+ * Replaces ParticleSystem(...) state: src/API/ParticleSystem.jl:142-202. */
+int32_t clm_create(int32_t dtype, int32_t dim, int32_t nsets, clm_handle* h);
+int32_t clm_destroy(clm_handle h);
+
+/* Bind the handle to a CUDA stream (cudaStream_t passed as void*; NULL = the
+ * handle's own stream). */
+int32_t clm_set_stream(clm_handle h, void* stream);
+
+/* Box(unitcell, cutoff; lcell) — src/internals/Box.jl:191-270, update_box 395-423.
+ * M: column-major dim x dim unit cell (columns are lattice vectors); for
+ * CLM_ORTHO only the diagonal is used; ignored for CLM_NONPERIODIC (the box is
+ * derived from the positions at each build, src/internals/ParticleSystem.jl:158-164). */
+int32_t clm_set_box(clm_handle h, const double* M, int32_t cell_kind, double cutoff, int32_t lcell);
+
+/* Positions of set `set` (0 = x, 1 = y): n points, dim x n column-major (the
+ * memory layout of a Julia Vector{SVector} / Matrix(dim, n)), in the handle's
+ * dtype.  is_device = 1 if xyz is a device pointer.  Marks the set dirty
+ * (ParticleSystemPositions.updated, src/API/ParticleSystemPositions.jl:14-22). */
+int32_t clm_set_positions(clm_handle h, int32_t set, const void* xyz, int64_t n, int32_t is_device);
+
+/* UpdateCellList! for every dirty set — src/internals/CellLists.jl:727-927,
+ * 1180-1204; non-periodic: src/internals/NonPeriodicCells.jl:93-251. */
+int32_t clm_build(clm_handle h);
+
+/* Select the precision form of clm_run (CLM_PREC_EXACT or CLM_PREC_SPLIT). */
+int32_t clm_set_precision(clm_handle h, int32_t precision);
+
+/* _pairwise!(op, output, box, cl) — src/internals/self.jl:28-184,
+ * src/internals/cross.jl:8-129 — for one built-in operator.  Builds first if a
+ * set is dirty (UpdateParticleSystem!, src/internals/ParticleSystem.jl:379-445). */
+int32_t clm_run(clm_handle h, int32_t op_id, const clm_op_params* params, clm_outputs* out);
+
+/* Neighbour list of the last CLM_OP_NL run: the number of pairs, then the
+ * pairs (unordered, as in src/API/neighborlist.jl:229-230).  d has the
+ * handle's dtype.  index_base 1 gives Julia indices. */
+int32_t clm_nl_count(clm_handle h, int64_t* n);
+int32_t clm_nl_fetch(clm_handle h, int64_t* i, int64_t* j, void* d, int64_t cap, int32_t index_base,
+                     int32_t out_on_device);
+
+/* Box fields as computed by the library (for Box mirrors and parity checks):
+ * nc[dim], cell_size[dim], computing box min/max[dim], aligned unit cell,
+ * rotation and inverse rotation (column-major dim x dim), cutoff. */
+int32_t clm_get_box(clm_handle h, int64_t* nc, double* cell_size, double* cbmin, double* cbmax, double* aligned,
+                    double* rotation, double* inv_rotation, double* cutoff);
+
+/* CellList summary of set `set` after a build: real particles, particles in the
+ * computing box including images, cells with particles, cells with real
+ * particles (src/internals/CellLists.jl:115-137). */
+int32_t clm_get_celllist_info(clm_handle h, int32_t set, int64_t* n_real, int64_t* n_particles,
+                              int64_t* n_cells_with_particles, int64_t* n_cells_with_real);
+
+/* The built cell list of set `set`, copies in cell order: linear cell index
+ * (0-based, x fastest), particle index (index_base applied), real flag and
+ * coordinates (n_particles x dim, handle dtype).  Host buffers. */
+int32_t clm_fetch_celllist(clm_handle h, int32_t set, int64_t cap, int64_t* cell, int64_t* index, int8_t* real,
+                           void* coords, int32_t index_base);
+
+/* Timing of the last build and run (device milliseconds, CUDA events). */
+int32_t clm_last_timings(clm_handle h, float* build_ms, float* map_ms);
+
+/* Number of CUDA kernels this handle has launched so far (cumulative). */
+int32_t clm_stats(clm_handle h, int64_t* kernel_launches);
+
+/* Human-readable description of the last error on this handle. */
+int32_t clm_last_error(clm_handle h, char* buf, size_t n);
+
+/* Library version string. */
+const char* clm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CELLLISTMAP_GB300_H */

@@ -608,7 +608,8 @@ template <class T, int N> struct OpCtx {
 };
 
 template <class T, int N>
-inline void apply_op(const OpCtx<T, N>& ctx, Local& L, int64_t i, int64_t j, const T* xi, const T* xj, T d2) {
+inline void apply_op(const OpCtx<T, N>& ctx, Local& L, int64_t i, int64_t j, const T* xi, const T* xj, T d2,
+                     const Mat<T, N>* rinv = nullptr) {
   const orc_op* op = ctx.op;
   const int code = op->op;
   if (code == OP_COUNT) { L.count++; return; }
@@ -621,6 +622,15 @@ inline void apply_op(const OpCtx<T, N>& ctx, Local& L, int64_t i, int64_t j, con
   double dd2;
   if (sizeof(T) == sizeof(double)) dd2 = (double)d2;
   else { dd2 = dv[0] * dv[0]; for (int k = 1; k < N; k++) dd2 = dd2 + dv[k] * dv[k]; }
+  if (rinv) {
+    double r[N];
+    for (int a = 0; a < N; a++) {
+      double acc = 0;
+      for (int k = 0; k < N; k++) acc += (double)rinv->a[a][k] * dv[k];
+      r[a] = acc;
+    }
+    for (int a = 0; a < N; a++) dv[a] = r[a];
+  }
   double dd = std::sqrt(dd2);
   switch (code) {
     case OP_SUM_D2: L.energy.add(dd2); break;
@@ -716,15 +726,12 @@ template <class T, int N> struct Mapper {
     nonper = (B.kind == KIND_NONPER);
   }
 
+  // Pair values are evaluated in double: for triclinic cells the difference of the
+  // (rotated) copies is rotated back with the inverse rotation in double, so that
+  // Float32 inputs are checked against an FP64 evaluation rather than against the
+  // Float32 rotation of pair.x/pair.y (self.jl:178).
   inline void emit(Local& L, const Particle<T, N>& pi, const Particle<T, N>& pj, T d2) const {
-    if (tri) {
-      T xr[N], yr[N];
-      matvec(B.Rinv, pi.x, xr);
-      matvec(B.Rinv, pj.x, yr);
-      apply_op(ctx, L, pi.index, pj.index, xr, yr, d2);
-    } else {
-      apply_op(ctx, L, pi.index, pj.index, pi.x, pj.x, d2);
-    }
+    apply_op(ctx, L, pi.index, pj.index, pi.x, pj.x, d2, tri ? &B.Rinv : nullptr);
   }
 
   static inline T dist2(const T* a, const T* b) {

@@ -1,0 +1,61 @@
+"""CPU tests of the C-ABI boundary: the library builds for sm_103a, loads, and exports every
+symbol declared in include/celllistmap_gb300.h.  No compute call is made (no GPU here)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from tests.conftest import ROOT
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "celllistmap_gb300.h")).read()
+    return sorted(set(re.findall(r"\b(clm_[a-z_]+)\s*\(", src)))
+
+
+def test_header_declares_the_python_binding_table(clm):
+    assert declared_symbols() == sorted(clm._abi.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(clm):
+    path = clm._abi.lib_path()
+    assert os.path.exists(path)
+    lib = ctypes.CDLL(path)
+    for name in declared_symbols():
+        assert hasattr(lib, name), name
+
+
+def test_version_string(clm):
+    lib = clm._abi.load()
+    assert b"sm_103a" in lib.clm_version()
+
+
+def test_create_rejects_bad_arguments_without_touching_the_gpu(clm):
+    lib = clm._abi.load()
+    h = ctypes.c_void_p()
+    assert lib.clm_create(7, 3, 1, ctypes.byref(h)) == 1   # bad dtype
+    assert lib.clm_create(1, 4, 1, ctypes.byref(h)) == 1   # bad dim
+    assert lib.clm_create(1, 3, 3, ctypes.byref(h)) == 1   # bad nsets
+    assert lib.clm_destroy(None) == 1
+
+
+def test_python_front_end_reports_missing_library(tmp_path, clm):
+    saved = clm._abi._lib
+    clm._abi._lib = None
+    try:
+        with pytest.raises(ImportError):
+            clm._abi.load(str(tmp_path / "missing.so"))
+    finally:
+        clm._abi._lib = saved
+
+
+def test_dimension_and_argument_checks_happen_on_the_host(clm):
+    api = clm._api if hasattr(clm, "_api") else clm.api
+    with pytest.raises(clm.ArgumentError):
+        api._get_dim([1.0, 1.0, 1.0, 1.0], [[0.0, 0.0, 0.0, 0.0]])
+    with pytest.raises(clm.ArgumentError):
+        api._get_dim([1.0, 1.0, 1.0], [[0.0, 0.0]])
+    assert api._promote_dtype([1, 1, 1], 2, None) == "float64"
+    import numpy as np
+    assert api._promote_dtype(np.array([1.0, 1.0], np.float32), np.float32(0.1), None) == np.float32

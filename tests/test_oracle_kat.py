@@ -1,0 +1,230 @@
+"""CPU tests: the oracle against the reference's known-answer values and its naive O(N^2) check.
+
+Expected values are quoted from the reference (file:line beside each).
+"""
+import os
+
+import numpy as np
+import pytest
+
+ARGON_SIDES = [21.0, 21.0, 21.0]
+
+
+@pytest.fixture(scope="module")
+def argon(golden_dir):
+    return np.load(os.path.join(golden_dir, "argon_cubic.npy"))
+
+
+@pytest.fixture(scope="module")
+def namd(golden_dir):
+    return np.load(os.path.join(golden_dir, "namd_frames.npz"))
+
+
+def test_argon_sum_d2(orc, argon):
+    # src/API/ParticleSystem.jl:110-118
+    r = orc.run("sum_d2", argon, unitcell=ARGON_SIDES, cutoff=8.0)
+    assert r["scalar"] == pytest.approx(43774.54367600001, rel=1e-12)
+
+
+def test_argon_two_sets_sum_d2(orc, argon):
+    # src/API/ParticleSystem.jl:122-139
+    r = orc.run("sum_d2", argon[:50], argon[50:], unitcell=ARGON_SIDES, cutoff=8.0)
+    assert r["scalar"] == pytest.approx(21886.196785000004, rel=1e-12)
+
+
+def test_argon_neighborlists(orc, argon):
+    # src/API/neighborlist.jl:262-311.  These docstrings were produced with PDBTools returning Float32
+    # coordinates (promoted to Float64 by the Float64 cutoff): with them every quoted distance is bit-exact.
+    x32 = argon.astype(np.float32).astype(np.float64)
+    nl = orc.run("nl", x32, kind="nonperiodic", cutoff=8.0)
+    assert len(nl["i"]) == 857
+    a, b, d = orc.canonical_pairs(nl["i"], nl["j"], nl["d"])
+    for (i, j), dist in {(0, 19): 3.163779526466901, (0, 60): 4.08865164675529, (0, 66): 5.939772435456664,
+                         (77, 87): 7.0061163797598445, (53, 87): 7.933654063435482}.items():
+        assert d[(a == i) & (b == j)][0] == dist
+    nl = orc.run("nl", x32, unitcell=ARGON_SIDES, cutoff=8.0)
+    assert len(nl["i"]) == 1143
+    a, b, d = orc.canonical_pairs(nl["i"], nl["j"], nl["d"])
+    for (i, j), dist in {(0, 6): 3.3638756414119397, (0, 19): 3.163779526466901, (0, 46): 6.243868666689442,
+                         (37, 67): 7.409287768713663, (67, 89): 7.8758006026725464}.items():
+        assert d[(a == i) & (b == j)][0] == dist
+    nl = orc.run("nl", x32[:50], x32[50:], kind="nonperiodic", cutoff=8.0)
+    assert len(nl["i"]) == 439
+    for (i, j), dist in {(0, 10): 4.08865164675529, (0, 16): 5.939772435456664, (0, 29): 2.4572288423012236,
+                         (45, 47): 4.9269093987894745, (45, 0): 7.99947286297016}.items():
+        assert nl["d"][(nl["i"] == i) & (nl["j"] == j)][0] == dist
+
+
+def test_argon_min_distance(orc, argon):
+    # src/API/parallel_custom.jl:279-289
+    r = orc.run("mindist", argon, unitcell=ARGON_SIDES, cutoff=8.0)
+    assert r["min"][2] == 2.1991993997816563  # bit-exact with Float64 coordinates
+
+
+def test_argon_inverse_distance_and_gradient(orc, argon):
+    # docs/src/ParticleSystem/single_set_compound.md:103-117
+    r = orc.run("inv_d_forces", argon, unitcell=ARGON_SIDES, cutoff=8.0)
+    assert r["scalar"] == pytest.approx(207.37593043370862, rel=1e-13)
+    np.testing.assert_allclose(r["forces_x"][0], [0.02649383330735732, 0.18454277989323772, -0.012253902366284958],
+                               rtol=1e-10)
+    np.testing.assert_allclose(r["forces_x"][-1], [-0.031012009183076745, 0.03543655648545698, 0.03184912163097636],
+                               rtol=1e-10)
+
+
+def test_argon_nonperiodic_box(orc, argon):
+    # test/API/ParticleSystem.jl:214-223 (sides of the non-periodic box, 2 decimals)
+    b8 = orc.box_info(argon, kind="nonperiodic", cutoff=8.0)
+    np.testing.assert_allclose(np.diag(b8["input_unit_cell"]), [35.63, 35.76, 35.79], atol=6e-3)
+    b10 = orc.box_info(argon, kind="nonperiodic", cutoff=10.0)
+    np.testing.assert_allclose(np.diag(b10["input_unit_cell"]), [39.83, 39.96, 39.99], atol=6e-3)
+
+
+NAMD_CASES = [
+    # test/applications/namd/ParticleSystem_vs_NAMD.jl:55-116
+    ("o1", [50.0, 50.0, 50.0], 32230.01699504111),
+    ("o2", [80.0, 70.0, 50.0], 1093.7225407797744),
+    ("o3", [[50.0, 0.0, 50.0], [50.0, 50.0, 0.0], [0.0, 50.0, 50.0]], 1724.3195067566828),
+    ("o4", np.array([[70.7107, 0.0, 0.0], [35.3553, 61.2372, 0.0], [35.3553, 20.4124, 57.735]]).T, 1754.0802503953591),
+    ("o5", np.array([[70.7107, 0.0, 0.0], [35.3553, 61.2372, 0.0], [35.3553, 20.4124, 57.735]]).T, 1765.1389457850137),
+    ("o6", [80.0, 80.0, 80.0], -158.04751357760088),
+    ("t1", [[80.0, 0.0, 30.0], [30.0, 80.0, 0.0], [0.0, 40.0, 80.0]], -116.53213607052128),
+    ("t2", [[50.0, 0.0, 0.0], [50.0, 50.0, 0.0], [0.0, 50.0, 50.0]], 32096.48839031735),
+]
+NAMD_EPS, NAMD_SIG = 0.0441795, 2 * 1.64009
+
+
+@pytest.mark.parametrize("lcell", [1, 3])
+@pytest.mark.parametrize("name,uc,expected", NAMD_CASES)
+def test_namd_lj_energies(orc, namd, name, uc, expected, lcell):
+    uc = np.asarray(uc, float)
+    kind = "ortho" if uc.ndim == 1 else "tri"
+    r = orc.run("lj_energy", namd[name].astype(np.float64), kind=kind, unitcell=uc, cutoff=10.0, lcell=lcell,
+                params=[NAMD_EPS, NAMD_SIG, 1.0, 2.0])
+    assert r["scalar"] == pytest.approx(expected, rel=1e-12)
+
+
+def test_small_exact_cases(orc):
+    # test/API/neighborlists.jl:183-193
+    def nl(x, **kw):
+        x = np.asarray(x, float)
+        r = orc.run("nl", x, dim=x.shape[1], **kw)
+        return list(zip(r["i"], r["j"], r["d"]))
+
+    assert nl([[0.0, 0.0, 1.0], [0.0, 0.0, 10.0], [0.0, 0.0, 7.0]], kind="nonperiodic", cutoff=2.0) == []
+    assert nl([[0.0, 1.0], [0.0, 10.0]], kind="nonperiodic", cutoff=2.0) == []
+    side = 2.0 + np.nextafter(1.0, 2.0)
+    assert nl([[0.0, 0.0]], unitcell=[side, side], cutoff=1.0) == []
+    got = nl([[0.0, 0.0], [0.0, 1.0]], unitcell=[side, side], cutoff=1.0)
+    assert [(min(a, b), max(a, b), d) for a, b, d in got] == [(0, 1, 1.0)]
+    assert nl([[0.0, 0.0], [0.0, 1.0]], unitcell=[2.0, 2.0], cutoff=np.nextafter(1.0, 0.0)) == []
+    got = nl([[0.0, 0.0], np.array([0.0, 1.0]) + np.nextafter(1.0, 2.0)], unitcell=[2.0, 2.0], cutoff=np.nextafter(1.0, 0.0))
+    assert [(min(a, b), max(a, b), d) for a, b, d in got] == [(0, 1, 0.9999999999999998)]
+
+
+def test_cutoff_ties_unit_square(orc):
+    # test/API/neighborlists.jl:244-266
+    for x in [np.nextafter(0.1, 1.0), np.nextafter(0.9, 0.0)]:
+        r = orc.run("nl", np.array([[0.0, 0.0], [x, 0.0]]), dim=2, unitcell=[1.0, 1.0], cutoff=0.1)
+        assert len(r["i"]) == 0
+    for x in [-0.1, 0.1, 0.9]:
+        r = orc.run("nl", np.array([[0.0, 0.0], [x, 0.0]]), dim=2, unitcell=[1.0, 1.0], cutoff=0.1)
+        assert len(r["i"]) == 1
+
+
+def test_computing_box(orc):
+    # test/API/ParticleSystem.jl:228-234: unit cube, cutoff 0.1 -> computing box (-0.1, 1.1)
+    b = orc.box_info(unitcell=[1.0, 1.0, 1.0], cutoff=0.1)
+    np.testing.assert_allclose(b["computing_box"][0], [-0.1] * 3, atol=1e-15)
+    np.testing.assert_allclose(b["computing_box"][1], [1.1] * 3, atol=1e-15)
+
+
+def test_box_docstring_examples(orc):
+    # jldoctests of src/internals/Box.jl:159-188 and 320-327
+    assert list(orc.box_info(unitcell=[[100, 50, 0], [0, 120, 0], [0, 0, 130]], kind="tri", cutoff=10.0)["nc"]) == [20, 13, 16]
+    assert list(orc.box_info(unitcell=[100, 120, 150], cutoff=10.0)["nc"]) == [13, 15, 18]
+    assert list(orc.box_info(unitcell=[120, 150, 100], cutoff=10.0)["nc"]) == [15, 18, 13]
+
+
+def test_cell_too_small_and_lcell(orc):
+    # src/internals/Box.jl:192, 243
+    with pytest.raises(orc.OracleError) as e:
+        orc.box_info(unitcell=[10.0, 10.0, 10.0], cutoff=5.0)
+    assert e.value.code == 2
+    with pytest.raises(orc.OracleError) as e:
+        orc.box_info(unitcell=[10.0, 10.0, 10.0], cutoff=1.0, lcell=0)
+    assert e.value.code == 10
+
+
+def test_nan_coordinates(orc):
+    # src/internals/CellOperations.jl:6-21
+    x = np.random.default_rng(0).random((10, 3))
+    x[3, 1] = np.nan
+    with pytest.raises(orc.OracleError) as e:
+        orc.run("count", x, unitcell=[1.0, 1.0, 1.0], cutoff=0.1)
+    assert e.value.code == 3
+
+
+CASES = [
+    # (dim, kind, unitcell, cutoff, lcell, n)
+    (3, "ortho", [10.0, 12.0, 11.0], 1.5, 1, 800),
+    (3, "ortho", [10.0, 12.0, 11.0], 1.5, 2, 800),
+    (3, "tri", [[10.0, 2.0, 1.0], [0.0, 11.0, 1.5], [0.0, 0.0, 12.0]], 1.5, 1, 800),
+    (3, "tri", [[10.0, 2.0, 1.0], [0.0, 11.0, 1.5], [0.0, 0.0, 12.0]], 1.5, 3, 600),
+    (3, "nonperiodic", None, 1.5, 1, 800),
+    (2, "ortho", [10.0, 12.0], 1.2, 1, 600),
+    (2, "tri", [[10.0, 3.0], [0.0, 11.0]], 1.2, 2, 600),
+    (2, "nonperiodic", None, 1.2, 1, 600),
+]
+
+
+@pytest.mark.parametrize("cross", [False, True])
+@pytest.mark.parametrize("dim,kind,uc,cut,lcell,n", CASES)
+def test_celllist_matches_naive(orc, dim, kind, uc, cut, lcell, n, cross):
+    """The cell-list restatement finds the same pairs as the naive minimum-image loop
+    (the reference's own correctness strategy, test/internals/tests.jl:181-299)."""
+    rng = np.random.default_rng(dim * 100 + lcell + (7 if cross else 0))
+    span = 12.0
+    x = rng.random((n, dim)) * span - 1.0
+    y = rng.random((n // 2, dim)) * span - 1.0 if cross else None
+    kw = dict(dim=dim, kind=kind, unitcell=uc, cutoff=cut, lcell=lcell)
+    cl = orc.run("nl", x, y, **kw)
+    nv = orc.run("nl", x, y, naive=True, **kw)
+    if cross:
+        a = np.lexsort((cl["j"], cl["i"]))
+        b = np.lexsort((nv["j"], nv["i"]))
+        np.testing.assert_array_equal(cl["i"][a], nv["i"][b])
+        np.testing.assert_array_equal(cl["j"][a], nv["j"][b])
+        np.testing.assert_allclose(cl["d"][a], nv["d"][b], rtol=1e-12)
+    else:
+        A = orc.canonical_pairs(cl["i"], cl["j"], cl["d"])
+        B = orc.canonical_pairs(nv["i"], nv["j"], nv["d"])
+        np.testing.assert_array_equal(A[0], B[0])
+        np.testing.assert_array_equal(A[1], B[1])
+        np.testing.assert_allclose(A[2], B[2], rtol=1e-12)
+    e1 = orc.run("soft_forces", x, y, **kw)
+    e2 = orc.run("soft_forces", x, y, naive=True, **kw)
+    assert e1["scalar"] == pytest.approx(e2["scalar"], rel=1e-12)
+    np.testing.assert_allclose(e1["forces_x"], e2["forces_x"], atol=1e-11 * max(1.0, np.abs(e2["forces_x"]).max()))
+
+
+def test_pathological_coordinates(orc):
+    """test/modules/Testing.jl:36-60: points on faces, +-nextfloat(0), outside the box."""
+    rng = np.random.default_rng(5)
+    sides = np.array([250.0, 250.0, 250.0])
+    x = sides * rng.random((200, 3))
+    x[0] = -sides / 2
+    x[1] = -sides / 2 + [np.nextafter(0, 1), np.nextafter(0, 1), sides[2] * rng.random()]
+    x[2] = -sides / 2 + [np.nextafter(0, -1), np.nextafter(0, -1), sides[2] * rng.random()]
+    x[3] = sides / 2 + [np.nextafter(0, 1), np.nextafter(0, 1), sides[2] * rng.random()]
+    x[4] = sides / 2 + [np.nextafter(0, -1), np.nextafter(0, -1), sides[2] * rng.random()]
+    x[9] = sides
+    x[10] = sides + [np.nextafter(0, 1), np.nextafter(0, 1), sides[2] * rng.random()]
+    x[11] = sides + [np.nextafter(0, -1), np.nextafter(0, -1), sides[2] * rng.random()]
+    x[12] = [np.nextafter(0, 1), np.nextafter(0, 1), sides[2] * rng.random()]
+    x[13] = [np.nextafter(0, -1), np.nextafter(0, -1), sides[2] * rng.random()]
+    x[14] = 0.0
+    x[99] = [sides[0] / 2, -sides[1] / 2, 2 * sides[2]]
+    for lcell in (1, 2):
+        cl = orc.run("count", x, unitcell=sides, cutoff=10.0, lcell=lcell)
+        nv = orc.run("count", x, unitcell=sides, cutoff=10.0, naive=True)
+        assert cl["count"] == nv["count"]
