@@ -45,7 +45,7 @@ namespace {
 
 constexpr int kWarps = 4;
 constexpr int kThreads = kWarps * 32;
-constexpr int kJC = 32;  // staged neighbours per round
+
 
 template <class T> struct SetView {
   const T* px;
@@ -60,6 +60,7 @@ template <class T> struct PairArgs {
   DevGeom<T> g;
   SetView<T> X, Y;
   const int* real_list;
+  const int* xflags;  // per cell of set x: contains real particles
   int n_real;
   int self;
   int split;
@@ -155,6 +156,36 @@ template <class A> struct Acc {
 
 enum OpKind { OPK_NL = 0, OPK_SCALAR = 1, OPK_FORCES = 2, OPK_MIN = 3, OPK_HIST = 4 };
 
+// Reciprocal and reciprocal square root for pair VALUES (energies, forces), which are checked against
+// tolerances, never used for pair membership or neighbour-list distances.
+//  FP32: hardware approximations (rcp.approx / rsqrt.approx, a couple of ulp).
+//  FP64: the hardware FP64 estimate refined by two Newton-Raphson steps, each of which squares the
+//        relative error (y <- y + y(1 - x y) for 1/x; y <- y + y/2 (1 - x y^2) for 1/sqrt(x)).
+__device__ __forceinline__ float vrcp(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float vrsqrt(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double vrcp(double x) {
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  double e = fma(-x, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-x, y, 1.0);
+  return fma(y, e, y);
+}
+__device__ __forceinline__ double vrsqrt(double x) {
+  double y;
+  asm("rsqrt.approx.f64 %0, %1;" : "=d"(y) : "d"(x));
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    double e = fma(-x, y * y, 1.0);
+    y = fma(0.5 * y, e, y);
+  }
+  return y;
+}
+
 // Per-pair energy u and g = (du/dr)/r (force contribution df = g*(x_i - x_j)).
 template <class V, class T>
 __device__ __forceinline__ void pair_value(const PairArgs<T>& A, int op, V d2, int i, int j, V& u, V& g) {
@@ -168,19 +199,20 @@ __device__ __forceinline__ void pair_value(const PairArgs<T>& A, int op, V d2, i
       g = V(0);
       break;
     case 4:  // SUM_D
-      u = sqrt(d2);
+      u = d2 * vrsqrt(d2);
       g = V(0);
       break;
     case 5:  // SUM_INV_D
-      u = V(1) / sqrt(d2);
+      u = vrsqrt(d2);
       g = V(0);
       break;
     case 6:
     case 7: {  // SOFT (c - d)^2
-      V d = sqrt(d2);
+      V ri = vrsqrt(d2);
+      V d = d2 * ri;
       V c = (V)A.p[0];
       u = (c - d) * (c - d);
-      g = V(-2) * (c - d) / d;
+      g = V(-2) * (c - d) * ri;
       break;
     }
     case 8:
@@ -193,17 +225,18 @@ __device__ __forceinline__ void pair_value(const PairArgs<T>& A, int op, V d2, i
         sig = (V)A.sig_t[ti * A.ntypes + tj];
       }
       V c12 = (V)A.p[2], c6 = (V)A.p[3];
-      V sr2 = (sig * sig) / d2;
+      V r2i = vrcp(d2);
+      V sr2 = (sig * sig) * r2i;
       V sr6 = sr2 * sr2 * sr2;
       V sr12 = sr6 * sr6;
       u = eps * (c12 * sr12 - c6 * sr6);
-      g = eps * (V(-12) * c12 * sr12 + V(6) * c6 * sr6) / d2;
+      g = eps * (V(-12) * c12 * sr12 + V(6) * c6 * sr6) * r2i;
       break;
     }
     case 12: {  // 1/d with gradient accumulation
-      V d = sqrt(d2);
-      u = V(1) / d;
-      g = u / d2;
+      V ri = vrsqrt(d2);
+      u = ri;
+      g = ri * ri * ri;
       break;
     }
     default:
@@ -212,34 +245,91 @@ __device__ __forceinline__ void pair_value(const PairArgs<T>& A, int op, V d2, i
   }
 }
 
-template <class T, int N, int OPK, bool SPLIT>
-__global__ void __launch_bounds__(kThreads) k_pairs(const PairArgs<T> A) {
-  using V = T;  // exact-form value type
-  // accumulation type: FP64 for the exact FP64 form, Kahan-compensated FP32 otherwise
+__device__ __forceinline__ bool is_forward(const int* o) {
+  // neighbor_cells_forward (src/internals/Box.jl:436-457): lexicographically positive in (x, y, z)
+  return o[0] > 0 || (o[0] == 0 && (o[1] > 0 || (o[1] == 0 && o[2] > 0)));
+}
+
+template <class T, int N>
+__device__ __forceinline__ T exact_dot_rel(const T* x, const T* c, const T* u) {
+  T s = xmul(xsub(x[0], c[0]), u[0]);
+#pragma unroll
+  for (int d = 1; d < N; d++) s = xadd(s, xmul(xsub(x[d], c[d]), u[d]));
+  return s;
+}
+
+// The reference's projection filter for a pair seen from cell `from` (center cf) towards cell `to`
+// (center ct): the particle of `to` must satisfy |proj| <= margin and |proj_to - proj_from| <= cutoff
+// (src/internals/vicinal_cells.jl:4-75, auxiliary_functions.jl:166-186).
+template <class T, int N>
+__device__ bool projection_pass(const DevGeom<T>& g, const T* cf, const T* ct, const T* x_from, const T* x_to) {
+  T dc[3] = {0, 0, 0};
+#pragma unroll
+  for (int d = 0; d < N; d++) dc[d] = xsub(ct[d], cf[d]);
+  T s2 = xmul(dc[0], dc[0]);
+#pragma unroll
+  for (int d = 1; d < N; d++) s2 = xadd(s2, xmul(dc[d], dc[d]));
+  T dcn = xsqrt(s2);
+  T u[3] = {0, 0, 0};
+#pragma unroll
+  for (int d = 0; d < N; d++) u[d] = xdiv(dc[d], dcn);
+  T pt = exact_dot_rel<T, N>(x_to, cf, u);
+  bool keep = (g.lcell == 1) ? (fabs(pt) <= xadd(g.cutoff, xdiv(dcn, T(2)))) : ((double)fabs(pt) <= g.margin_wide);
+  if (!keep) return false;
+  T pf = exact_dot_rel<T, N>(x_from, cf, u);
+  return fabs(xsub(pt, pf)) <= g.cutoff;
+}
+
+// Pair map kernel.  CROSS: x-y pairs; otherwise self pairs.  For OPK_FORCES on a single set each real
+// particle owns its force ("owner computes": full stencil, no atomics on the partner) and the energy is
+// counted only on the side from which the reference visits the pair.
+//
+// Each warp takes one cell; the cells of its stencil are concatenated into one candidate stream,
+// staged 64 at a time.  Phase A: every lane tests its particle against its share of the staged
+// candidates with an FP32 distance (FMA) and records the candidates inside cutoff^2 (1 + 2^-13) in a
+// bit mask.  Phase B: the lanes walk their masks, apply the reference's pair rules, re-test in the input
+// dtype where needed, and run the operator epilogue.  The projection filter of the reference is
+// evaluated only for pairs with d2 > cutoff^2 (1 - 2^-13): any pair further inside passes it (the
+// projection of the separation on a unit vector cannot exceed the separation, and the margin covers the
+// half cell), so skipping it elsewhere leaves the pair set unchanged.
+template <class T, int N, int OPK, bool SPLIT, bool CROSS>
+__global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(const PairArgs<T> A) {
+  using V = T;
   using FA = typename std::conditional<std::is_same<T, double>::value && !SPLIT, double, float>::type;
+  constexpr bool OWNER = (OPK == OPK_FORCES) && !CROSS;
+  constexpr bool FP64 = std::is_same<T, double>::value;
+  constexpr bool ABS_PF = !FP64 && !SPLIT;  // FP32 exact form: the prefilter uses the coordinates themselves
+  constexpr int JC = 128;                   // staging capacity: 32 candidates per lane group (G <= 4)
   const DevGeom<T>& g = A.g;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const unsigned FULL = 0xffffffffu;
 
-  __shared__ float4 s_off[kWarps][kJC];
-  __shared__ int s_code[kWarps][kJC];
-  __shared__ T s_x[kWarps][3][kJC];
-  __shared__ T s_proj[kWarps][kJC];
+  __shared__ int s_st_start[kWarps][32];
+  __shared__ int s_st_pref[kWarps][33];
+  __shared__ int s_st_meta[kWarps][32];
+  __shared__ float4 s_pf[kWarps][JC];       // prefilter coordinates; .w carries the particle code
+  __shared__ int s_meta[kWarps][JC];        // stencil offset and flags of the candidate's cell
+  __shared__ T s_x[kWarps][3][ABS_PF ? 1 : JC];
+  __shared__ unsigned short s_q[kWarps][1024];  // compacted candidates: (particle slot << 8) | staged index
+  __shared__ T s_ix[kWarps][3][32];              // particles of the current chunk of the cell
+  __shared__ float s_ipf[kWarps][3][32];
+  __shared__ int s_icode[kWarps][32];
+  __shared__ FA s_if[kWarps][3][(OPK == OPK_FORCES) ? 32 : 1];  // force sums of those particles
   __shared__ unsigned int s_hc[(OPK == OPK_HIST) ? kWarps : 1][(OPK == OPK_HIST) ? 256 : 1];
   __shared__ double s_hs[(OPK == OPK_HIST) ? kWarps : 1][(OPK == OPK_HIST) ? 256 : 1];
   __shared__ double s_red[kWarps];
   __shared__ unsigned long long s_redc[kWarps];
 
+  constexpr int F_SAME = 1 << 24, F_BACK = 1 << 25, F_REALCELL = 1 << 26;
   const bool tri = (g.kind == TRICLINIC);
   const bool nonper = (g.kind == NONPERIODIC);
-  const bool self = A.self != 0;
-  const bool forward = self && !tri;
+  const bool full = tri || CROSS || OWNER;
   const int l = g.lcell;
   const int w = 2 * l + 1;
-  const int nsten = forward ? (((N == 3) ? w * w * w : w * w) - 1) / 2 : ((N == 3) ? w * w * w : w * w) - 1;
-  const bool fp64 = std::is_same<T, double>::value;
-  const bool use_prefilter = fp64 || SPLIT;
+  const int wN = (N == 3) ? w * w * w : w * w;
+  const int nent = (full ? wN - 1 : (wN - 1) / 2) + 1;  // entry 0 is the cell itself
+  const T band = (T)g.thr_lo;                           // d2 above this: projection filter applies
 
   if constexpr (OPK == OPK_HIST) {
     for (int b = lane; b < A.nbins; b += 32) {
@@ -249,8 +339,8 @@ __global__ void __launch_bounds__(kThreads) k_pairs(const PairArgs<T> A) {
     __syncwarp();
   }
 
-  // per-lane accumulators
-  Acc<FA> e_acc;
+  double e_tot = 0.0;  // per-lane energy (FP64); FP32 partial sums are folded in per particle chunk
+  FA e_part = 0;
   unsigned long long c_acc = 0;
   T best_d2 = INFINITY;
   int best_i = 0x7fffffff, best_j = 0x7fffffff;
@@ -261,159 +351,255 @@ __global__ void __launch_bounds__(kThreads) k_pairs(const PairArgs<T> A) {
     const int li = A.real_list[r];
     int ci[3];
     cart_of(li, g.nc, N, ci);
+    T ctr_i[3] = {0, 0, 0};
+    cell_center<T, N>(g, ci, ctr_i);
     const int si = A.X.cell_start[li];
     const int ni = A.X.cell_start[li + 1] - si;
     const int G = (ni <= 8) ? 4 : ((ni <= 16) ? 2 : 1);
     const int LP = 32 / G;
     const int grp = lane / LP;
     const int il = lane % LP;
-    const unsigned gmask = ((LP == 32) ? FULL : ((1u << LP) - 1u)) << (grp * LP);
 
     for (int ib = 0; ib < ni; ib += LP) {
       const int ii = ib + il;
       const bool vi = ii < ni;
       const int ti = si + (vi ? ii : 0);
       T xi[3] = {0, 0, 0};
-      float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
+      float pi[3] = {0.f, 0.f, 0.f};
       int code_i = 0;
       if (vi) {
 #pragma unroll
         for (int d = 0; d < N; d++) xi[d] = pos_of(A.X, d, ti);
-        oi = A.X.off[ti];
         code_i = A.X.code[ti];
+        if (ABS_PF) {
+#pragma unroll
+          for (int d = 0; d < N; d++) pi[d] = (float)xi[d];
+        } else {
+          float4 oi = A.X.off[ti];
+          pi[0] = oi.x;
+          pi[1] = oi.y;
+          pi[2] = oi.z;
+        }
       }
       const bool real_i = code_i >= 0;
       const int idx_i = real_i ? code_i : -code_i - 1;
-      bool act_i = vi;
-      if (!nonper && (tri || !self) && !real_i) act_i = false;  // i must be real except ortho self/cross-vicinal
-      if (!self && !nonper && !tri) act_i = vi;                 // ortho cross: ghosts of x may pair in vicinal cells
-      // force accumulators for i (rotated frame)
-      FA fi[3] = {0, 0, 0};
+      const bool act_i = (OWNER || tri) ? (vi && real_i) : vi;
+      if (grp == 0) {
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          s_ix[warp][d][il] = xi[d];
+          s_ipf[warp][d][il] = pi[d];
+          if constexpr (OPK == OPK_FORCES) s_if[warp][d][il] = FA(0);
+        }
+        s_icode[warp][il] = code_i;
+      }
+      __syncwarp();
 
-      for (int o = 0; o <= nsten; o++) {
-        int oc[3] = {0, 0, 0};
-        if (o > 0) stencil_offset(forward, l, N, o - 1, oc);
-        int cj[3];
-        bool inr = true;
-#pragma unroll
-        for (int d = 0; d < N; d++) {
-          cj[d] = ci[d] + oc[d];
-          inr = inr && cj[d] >= 1 && cj[d] <= g.nc[d];
-        }
-        if (!inr) {
-          if (lane == 0) atomicOr(A.err, DERR_CELL_RANGE);
-          continue;
-        }
-        int lj = cj[0] - 1;
-        if (N == 3) lj += g.nc[0] * ((cj[1] - 1) + g.nc[1] * (cj[2] - 1));
-        else lj += g.nc[0] * (cj[1] - 1);
-        const int sj = A.Y.cell_start[lj];
-        const int nj = A.Y.cell_start[lj + 1] - sj;
-        if (nj == 0) continue;
-        const bool same = (o == 0);
-        // projection direction (vicinal cells only)
-        T ctr_i[3] = {0, 0, 0}, u[3] = {0, 0, 0};
-        T margin = 0;
-        T proj_i = 0;
-        if (!same) {
-          T ctr_j[3];
-          cell_center<T, N>(g, ci, ctr_i);
-          cell_center<T, N>(g, cj, ctr_j);
-          T dc[3] = {0, 0, 0};
-#pragma unroll
-          for (int d = 0; d < N; d++) dc[d] = xsub(ctr_j[d], ctr_i[d]);
-          T s2 = xmul(dc[0], dc[0]);
-#pragma unroll
-          for (int d = 1; d < N; d++) s2 = xadd(s2, xmul(dc[d], dc[d]));
-          T dcn = xsqrt(s2);
-#pragma unroll
-          for (int d = 0; d < N; d++) u[d] = xdiv(dc[d], dcn);
-          margin = xadd(g.cutoff, xdiv(dcn, T(2)));
-          if (act_i) {
-            T pv = xmul(xsub(xi[0], ctr_i[0]), u[0]);
-#pragma unroll
-            for (int d = 1; d < N; d++) pv = xadd(pv, xmul(xsub(xi[d], ctr_i[d]), u[d]));
-            proj_i = pv;
-          }
-        }
-        // FP32 displacement between cell origins: x_i - x_j = (off_i - off_j) - cs*(cj - ci)
-        float dcf[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-        for (int d = 0; d < N; d++) dcf[d] = g.csf[d] * (float)(cj[d] - ci[d]);
-
-        for (int jb = 0; jb < nj; jb += kJC) {
-          const int cnt = min(kJC, nj - jb);
-          // stage
-          if (lane < cnt) {
-            const int tj = sj + jb + lane;
-            s_off[warp][lane] = A.Y.off[tj];
-            s_code[warp][lane] = A.Y.code[tj];
-            T xj[3] = {0, 0, 0};
+      for (int k0 = 0; k0 < nent; k0 += 32) {
+        // ---- stencil table for entries k0 .. k0+31
+        {
+          const int kk = k0 + lane;
+          int cnt = 0, start = 0, meta = 0;
+          if (kk < nent) {
+            int o[3] = {0, 0, 0};
+            if (kk > 0) stencil_offset(!full, l, N, kk - 1, o);
+            int cj[3] = {1, 1, 1};
+            bool inr = true;
 #pragma unroll
             for (int d = 0; d < N; d++) {
-              xj[d] = pos_of(A.Y, d, tj);
-              s_x[warp][d][lane] = xj[d];
+              cj[d] = ci[d] + o[d];
+              inr = inr && cj[d] >= 1 && cj[d] <= g.nc[d];
             }
-            if (!same) {
-              T pv = xmul(xsub(xj[0], ctr_i[0]), u[0]);
+            if (!inr) {
+              atomicOr(A.err, DERR_CELL_RANGE);
+            } else {
+              int lj = cj[0] - 1;
+              if (N == 3) lj += g.nc[0] * ((cj[1] - 1) + g.nc[1] * (cj[2] - 1));
+              else lj += g.nc[0] * (cj[1] - 1);
+              start = A.Y.cell_start[lj];
+              cnt = A.Y.cell_start[lj + 1] - start;
+              meta = (o[0] + 128) | ((o[1] + 128) << 8) | ((o[2] + 128) << 16);
+              if (kk == 0) meta |= F_SAME;
+              if (kk > 0 && full && !is_forward(o)) meta |= F_BACK;
+              if (OWNER && A.xflags[lj]) meta |= F_REALCELL;
+            }
+          }
+          int incl = cnt;
 #pragma unroll
-              for (int d = 1; d < N; d++) pv = xadd(pv, xmul(xsub(xj[d], ctr_i[d]), u[d]));
-              bool keep = (l == 1) ? (fabs(pv) <= margin) : ((double)fabs(pv) <= g.margin_wide);
-              s_proj[warp][lane] = keep ? pv : (T)NAN;
+          for (int o2 = 1; o2 < 32; o2 <<= 1) {
+            int y = __shfl_up_sync(FULL, incl, o2);
+            if (lane >= o2) incl += y;
+          }
+          s_st_pref[warp][lane + 1] = incl;
+          if (lane == 0) s_st_pref[warp][0] = 0;
+          s_st_start[warp][lane] = start;
+          s_st_meta[warp][lane] = meta;
+        }
+        __syncwarp();
+        const int total = s_st_pref[warp][32];
+
+        const int JR = 32 * G;  // candidates per round: each lane tests exactly 32
+        for (int rb = 0; rb < total; rb += JR) {
+          const int cntr = min(JR, total - rb);
+          // ---- stage candidates rb .. rb+JR-1 (positions past the stream are padded with NaN)
+          for (int q = lane; q < JR; q += 32) {
+            if (q < cntr) {
+              const int e = rb + q;
+              int lo = 0, hi = 31;
+              while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (s_st_pref[warp][mid] <= e) lo = mid;
+                else hi = mid - 1;
+              }
+              const int tj = s_st_start[warp][lo] + (e - s_st_pref[warp][lo]);
+              const int meta = s_st_meta[warp][lo];
+              const int code = A.Y.code[tj];
+              s_meta[warp][q] = meta;
+              if (ABS_PF) {
+                s_pf[warp][q] = make_float4((float)pos_of(A.Y, 0, tj), (float)pos_of(A.Y, 1, tj),
+                                            N == 3 ? (float)pos_of(A.Y, N - 1, tj) : 0.f, __int_as_float(code));
+              } else {
+                const float4 oj = A.Y.off[tj];
+                // shift the offset by the cell displacement so that x_i - x_j ~ off_i - pf
+                s_pf[warp][q] = make_float4(oj.x + g.csf[0] * (float)((meta & 255) - 128),
+                                            oj.y + g.csf[1] * (float)(((meta >> 8) & 255) - 128),
+                                            oj.z + g.csf[2] * (float)(((meta >> 16) & 255) - 128),
+                                            __int_as_float(code));
+#pragma unroll
+                for (int d = 0; d < N; d++) s_x[warp][d][ABS_PF ? 0 : q] = pos_of(A.Y, d, tj);
+              }
+            } else {
+              s_pf[warp][q] = make_float4(NAN, NAN, NAN, 0.f);
             }
           }
           __syncwarp();
-          for (int jq = 0; jq < cnt; jq += G) {
-            const int j = jq + grp;
-            const bool vj = j < cnt;
-            bool cand = act_i && vj;
-            int code_j = vj ? s_code[warp][j] : 0;
-            const bool real_j = code_j >= 0;
-            const int idx_j = real_j ? code_j : -code_j - 1;
-            if (cand) {
-              if (nonper) {
-                if (self && same) cand = (jb + j) > ii;
-              } else if (self) {
-                if (tri) cand = idx_i < idx_j;
-                else if (same) cand = ((jb + j) > ii) && (real_i || real_j);
-                else cand = real_i || real_j;
-              } else {
-                if (!tri && !same) cand = real_i || real_j;
-                else cand = real_i;
-              }
+          // ---- phase A: 32 FP32 distance tests per lane into a bit mask
+          unsigned mask = 0u;
+          {
+            const float4* pp = &s_pf[warp][grp];
+#pragma unroll
+            for (int b = 0; b < 32; b++) {
+              const float4 p = pp[b * G];
+              const float dx = pi[0] - p.x, dy = pi[1] - p.y, dz = (N == 3) ? pi[2] - p.z : 0.f;
+              const float d2f = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+              mask |= (d2f <= g.thr_hi) ? (1u << b) : 0u;
             }
-            bool hit = false;
-            bool sure = false;
+          }
+          if (!act_i) mask = 0u;
+          // ---- phase B: compact the candidates of all lanes into a queue and process them with every lane
+          // busy; each lane takes a contiguous run of the queue (runs are grouped by particle, so force
+          // sums stay in registers and are flushed to shared memory only when the particle changes)
+          int H;
+          {
+            const int nh = __popc(mask);
+            int incl = nh;
+#pragma unroll
+            for (int o2 = 1; o2 < 32; o2 <<= 1) {
+              int y = __shfl_up_sync(FULL, incl, o2);
+              if (lane >= o2) incl += y;
+            }
+            H = __shfl_sync(FULL, incl, 31);
+            int pos = incl - nh;
+            unsigned m = mask;
+            while (m) {
+              const int b = __ffs(m) - 1;
+              m &= m - 1u;
+              s_q[warp][pos++] = (unsigned short)((il << 8) | (b * G + grp));
+            }
+          }
+          __syncwarp();
+          const int per = (H + 31) >> 5;
+          const int qbeg = lane * per;
+          int cur = -1;
+          FA acc[3] = {0, 0, 0};
+          for (int t = 0; t < per; t++) {
+            const int q = qbeg + t;
+            const bool has = q < H;
+            int j = 0, ie = 0;
+            if (has) {
+              const int ent = s_q[warp][q];
+              ie = ent >> 8;
+              j = ent & 255;
+            }
+            T xi[3] = {s_ix[warp][0][ie], s_ix[warp][1][ie], s_ix[warp][2][ie]};
+            const float pi[3] = {s_ipf[warp][0][ie], s_ipf[warp][1][ie], s_ipf[warp][2][ie]};
+            const int code_i = s_icode[warp][ie];
+            const bool real_i = code_i >= 0;
+            const int idx_i = real_i ? code_i : -code_i - 1;
+            const int ii = ib + ie;
+            bool hit = false, sure = false;
+            bool count_e = true;
+            int idx_j = 0;
             float d2f = 0.f;
             float dvf[3] = {0.f, 0.f, 0.f};
-            if (cand && use_prefilter) {
-              float4 oj = s_off[warp][j];
-              dvf[0] = (oi.x - oj.x) - dcf[0];
-              dvf[1] = (oi.y - oj.y) - dcf[1];
-              dvf[2] = (N == 3) ? ((oi.z - oj.z) - dcf[2]) : 0.f;
-              d2f = fmaf(dvf[2], dvf[2], fmaf(dvf[1], dvf[1], dvf[0] * dvf[0]));
-              if (!(d2f <= g.thr_hi)) cand = false;
-              else if (SPLIT && d2f <= g.thr_lo) {
-                // certainly inside; the projection filter never removes such pairs
-                sure = same || (s_proj[warp][j] == s_proj[warp][j]);
-                if (sure) hit = true;
-                cand = false;
-              }
-            }
             T d2 = 0;
-            if (cand) {
-              // exact re-test with the reference's arithmetic
-              bool pass = true;
-              if (!same) pass = fabs(xsub(s_proj[warp][j], proj_i)) <= g.cutoff;
-              if (pass) {
-                T dx = xsub(xi[0], s_x[warp][0][j]);
-                d2 = xmul(dx, dx);
-#pragma unroll
-                for (int d = 1; d < N; d++) {
-                  T dd = xsub(xi[d], s_x[warp][d][j]);
-                  d2 = xadd(d2, xmul(dd, dd));
+            T xj[3] = {0, 0, 0};
+            if (has) {
+              const float4 p = s_pf[warp][j];
+              const int code_j = __float_as_int(p.w);
+              const bool real_j = code_j >= 0;
+              idx_j = real_j ? code_j : -code_j - 1;
+              const int meta = s_meta[warp][j];
+              const bool same = (meta & F_SAME) != 0;
+              const int slot_j = rb + j;  // position inside the cell when same
+              bool cand = true;
+              bool other_side = false;
+              if (OWNER) {
+                cand = idx_j != idx_i;
+                if (tri) count_e = idx_i < idx_j;
+                else if (same) count_e = nonper ? (slot_j > ii) : (!real_j || slot_j > ii);
+                else if (!(meta & F_BACK)) count_e = true;
+                else {
+                  count_e = !nonper && !real_j && (meta & F_REALCELL);
+                  other_side = count_e;
                 }
-                hit = d2 <= g.cutoff_sqr;
+              } else if (!CROSS) {
+                if (tri) cand = idx_i < idx_j;
+                else if (same) cand = (slot_j > ii) && (nonper || real_i || real_j);
+                else cand = nonper || real_i || real_j;
+              } else {
+                if (!tri && !nonper) cand = same ? real_i : (real_i || real_j);
+              }
+              if (cand) {
+                dvf[0] = pi[0] - p.x;
+                dvf[1] = pi[1] - p.y;
+                dvf[2] = (N == 3) ? pi[2] - p.z : 0.f;
+                d2f = fmaf(dvf[2], dvf[2], fmaf(dvf[1], dvf[1], dvf[0] * dvf[0]));
+                if (ABS_PF) {
+                  xj[0] = (T)p.x;
+                  xj[1] = (T)p.y;
+                  if (N == 3) xj[N - 1] = (T)p.z;
+                } else {
+#pragma unroll
+                  for (int d = 0; d < N; d++) xj[d] = s_x[warp][d][ABS_PF ? 0 : j];
+                }
+                if (!FP64 || SPLIT) {
+                  // FP32 input or split form: well inside the cutoff the FP32 value decides
+                  if (d2f <= g.thr_lo) {
+                    hit = true;
+                    sure = true;
+                  }
+                }
+                if (!sure) {
+                  T dx = xsub(xi[0], xj[0]);
+                  d2 = xmul(dx, dx);
+#pragma unroll
+                  for (int d = 1; d < N; d++) {
+                    T dd = xsub(xi[d], xj[d]);
+                    d2 = xadd(d2, xmul(dd, dd));
+                  }
+                  hit = d2 <= g.cutoff_sqr;
+                  if (hit && d2 > band) {
+                    if (!same) {
+                      int cj[3] = {ci[0] + (meta & 255) - 128, ci[1] + ((meta >> 8) & 255) - 128,
+                                   ci[2] + ((meta >> 16) & 255) - 128};
+                      T ctr_j[3];
+                      cell_center<T, N>(g, cj, ctr_j);
+                      hit = projection_pass<T, N>(g, ctr_i, ctr_j, xi, xj);
+                      if (hit && other_side) count_e = projection_pass<T, N>(g, ctr_j, ctr_i, xj, xi);
+                    }
+                  }
+                }
               }
             }
             // ---------------- operator epilogues
@@ -425,11 +611,24 @@ __global__ void __launch_bounds__(kThreads) k_pairs(const PairArgs<T> A) {
                 if (lane == leader) base = atomicAdd(A.nl_count, (unsigned long long)__popc(bal));
                 base = __shfl_sync(FULL, base, leader);
                 if (hit) {
+                  T dval;
+                  if (sure && ABS_PF) {
+                    T dx = xsub(xi[0], xj[0]);
+                    T e2 = xmul(dx, dx);
+#pragma unroll
+                    for (int d = 1; d < N; d++) {
+                      T dd = xsub(xi[d], xj[d]);
+                      e2 = xadd(e2, xmul(dd, dd));
+                    }
+                    dval = xsqrt(e2);
+                  } else {
+                    dval = sure ? (T)sqrtf(d2f) : xsqrt(d2);
+                  }
                   unsigned long long pos = base + __popc(bal & ((1u << lane) - 1u));
                   if ((long long)pos < A.nl_cap) {
                     A.nl_i[pos] = idx_i;
                     A.nl_j[pos] = idx_j;
-                    A.nl_d[pos] = sure ? (T)sqrtf(d2f) : xsqrt(d2);
+                    A.nl_d[pos] = dval;
                   }
                 }
               }
@@ -440,17 +639,17 @@ __global__ void __launch_bounds__(kThreads) k_pairs(const PairArgs<T> A) {
                 } else if (sure) {
                   float uu, gg;
                   pair_value<float, T>(A, A.op, d2f, idx_i, idx_j, uu, gg);
-                  e_acc.add((FA)uu);
+                  e_part += (FA)uu;
                 } else {
                   V uu, gg;
                   pair_value<V, T>(A, A.op, (V)d2, idx_i, idx_j, uu, gg);
-                  e_acc.add((FA)uu);
+                  e_part += (FA)uu;
                 }
               }
             } else if constexpr (OPK == OPK_FORCES) {
-              FA df[3] = {0, 0, 0};
               if (hit) {
                 FA uu, gg;
+                FA df[3] = {0, 0, 0};
                 if (sure) {
                   float uf, gf;
                   pair_value<float, T>(A, A.op, d2f, idx_i, idx_j, uf, gf);
@@ -464,31 +663,37 @@ __global__ void __launch_bounds__(kThreads) k_pairs(const PairArgs<T> A) {
                   uu = (FA)uv;
                   gg = (FA)gv;
 #pragma unroll
-                  for (int d = 0; d < N; d++) df[d] = gg * (FA)xsub(xi[d], s_x[warp][d][j]);
+                  for (int d = 0; d < N; d++) df[d] = gg * (FA)xsub(xi[d], xj[d]);
                 }
-                e_acc.add(uu);
+                if (ie != cur) {
+                  if (cur >= 0) {
 #pragma unroll
-                for (int d = 0; d < N; d++) fi[d] -= df[d];
-              }
-              unsigned bal = __ballot_sync(FULL, hit) & gmask;
-              if (__ballot_sync(FULL, bal != 0u)) {
-                // reduce df over the lanes of each group (they share the same j)
+                    for (int d = 0; d < N; d++) atomicAdd(&s_if[warp][d][cur], acc[d]);
+                  }
+                  cur = ie;
 #pragma unroll
-                for (int d = 0; d < N; d++) {
-                  FA v = df[d];
-                  for (int s = LP / 2; s > 0; s >>= 1) v += __shfl_xor_sync(FULL, v, s);
-                  df[d] = v;
+                  for (int d = 0; d < N; d++) acc[d] = FA(0);
                 }
-                if (il == 0 && bal != 0u) {
-                  double* F = self ? A.fx : A.fy;
 #pragma unroll
-                  for (int d = 0; d < N; d++) atomicAdd(&F[(int64_t)idx_j * N + d], (double)df[d]);
+                for (int d = 0; d < N; d++) acc[d] -= df[d];
+                if (!OWNER || count_e) e_part += uu;
+                if (CROSS) {
+#pragma unroll
+                  for (int d = 0; d < N; d++) atomicAdd(&A.fy[(int64_t)idx_j * N + d], (double)df[d]);
                 }
               }
             } else if constexpr (OPK == OPK_MIN) {
               if (hit) {
-                T dd2 = d2;
-                if (sure) dd2 = (T)d2f;  // split form: FP32 estimate
+                T dd2 = sure ? (T)d2f : d2;
+                if (sure && ABS_PF) {
+                  T dx = xsub(xi[0], xj[0]);
+                  dd2 = xmul(dx, dx);
+#pragma unroll
+                  for (int d = 1; d < N; d++) {
+                    T dd = xsub(xi[d], xj[d]);
+                    dd2 = xadd(dd2, xmul(dd, dd));
+                  }
+                }
                 if (dd2 < best_d2 || (dd2 == best_d2 && (idx_i < best_i || (idx_i == best_i && idx_j < best_j)))) {
                   best_d2 = dd2;
                   best_i = idx_i;
@@ -497,7 +702,6 @@ __global__ void __launch_bounds__(kThreads) k_pairs(const PairArgs<T> A) {
               }
             } else if constexpr (OPK == OPK_HIST) {
               if (hit) {
-                // searchsortedfirst(bins, r) - 1 with r = sqrt(d2)
                 bool exact_r = !sure;
                 T r = 0;
                 int b = -1;
@@ -510,19 +714,18 @@ __global__ void __launch_bounds__(kThreads) k_pairs(const PairArgs<T> A) {
                     else lo = mid + 1;
                   }
                   b = lo - 1;
-                  // an edge within 2^-12 relative of r: decide with the exact distance
-                  const float tol = rf * 2.44140625e-4f;
+                  const float tol = rf * 2.44140625e-4f;  // an edge within 2^-12: decide exactly
                   if ((lo <= A.nbins && fabsf((float)A.bins[lo] - rf) <= tol) ||
                       (lo >= 1 && fabsf((float)A.bins[lo - 1] - rf) <= tol))
                     exact_r = true;
                   r = (T)rf;
                 }
                 if (exact_r) {
-                  T dx = xsub(xi[0], s_x[warp][0][j]);
+                  T dx = xsub(xi[0], xj[0]);
                   T e2 = xmul(dx, dx);
 #pragma unroll
                   for (int d = 1; d < N; d++) {
-                    T dd = xsub(xi[d], s_x[warp][d][j]);
+                    T dd = xsub(xi[d], xj[d]);
                     e2 = xadd(e2, xmul(dd, dd));
                   }
                   r = xsqrt(e2);
@@ -541,7 +744,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(const PairArgs<T> A) {
                     for (int d = 0; d < N; d++) dv[d] = (FA)dvf[d];
                   } else {
 #pragma unroll
-                    for (int d = 0; d < N; d++) dv[d] = (FA)xsub(xi[d], s_x[warp][d][j]);
+                    for (int d = 0; d < N; d++) dv[d] = (FA)xsub(xi[d], xj[d]);
                   }
                   if (tri) {
                     FA rv[3];
@@ -555,7 +758,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(const PairArgs<T> A) {
 #pragma unroll
                     for (int a = 0; a < N; a++) dv[a] = rv[a];
                   }
-                  const T* vy = self ? A.vx : A.vy;
+                  const T* vy = CROSS ? A.vy : A.vx;
                   FA dot = 0;
 #pragma unroll
                   for (int d = 0; d < N; d++)
@@ -566,28 +769,40 @@ __global__ void __launch_bounds__(kThreads) k_pairs(const PairArgs<T> A) {
               }
             }
           }
+          if constexpr (OPK == OPK_FORCES) {
+            if (cur >= 0) {
+#pragma unroll
+              for (int d = 0; d < N; d++) atomicAdd(&s_if[warp][d][cur], acc[d]);
+            }
+          }
           __syncwarp();
         }
+        __syncwarp();
       }
+      e_tot += (double)e_part;
+      e_part = 0;
       if constexpr (OPK == OPK_FORCES) {
-        // combine the groups' partial forces on i, then one atomic per component
+        __syncwarp();
+        if (grp == 0 && vi) {
+          FA f[3] = {s_if[warp][0][il], s_if[warp][1][il], s_if[warp][2][il]};
+          if (OWNER) {
+            if (act_i) {
 #pragma unroll
-        for (int d = 0; d < N; d++) {
-          FA v = fi[d];
-          for (int s = LP; s < 32; s <<= 1) v += __shfl_xor_sync(FULL, v, s);
-          fi[d] = v;
-        }
-        if (vi && grp == 0 && (fi[0] != FA(0) || fi[1] != FA(0) || fi[2] != FA(0))) {
+              for (int d = 0; d < N; d++) A.fx[(int64_t)idx_i * N + d] = (double)f[d];
+            }
+          } else if (f[0] != FA(0) || f[1] != FA(0) || f[2] != FA(0)) {
 #pragma unroll
-          for (int d = 0; d < N; d++) atomicAdd(&A.fx[(int64_t)idx_i * N + d], (double)fi[d]);
+            for (int d = 0; d < N; d++) atomicAdd(&A.fx[(int64_t)idx_i * N + d], (double)f[d]);
+          }
         }
+        __syncwarp();
       }
     }
   }
 
   // ---------------- block reductions to per-block partials
   if constexpr (OPK == OPK_SCALAR || OPK == OPK_FORCES) {
-    double e = e_acc.value();
+    double e = e_tot;
     unsigned long long c = c_acc;
 #pragma unroll
     for (int s = 16; s > 0; s >>= 1) {
@@ -764,21 +979,48 @@ inline int opkind_of(int op) {
   }
 }
 
-template <class T, int N, bool SPLIT>
-cudaError_t launch_s(int opk, int grid, cudaStream_t st, const PairArgs<T>& A) {
-  switch (opk) {
-    case OPK_NL: k_pairs<T, N, OPK_NL, SPLIT><<<grid, kThreads, 0, st>>>(A); break;
-    case OPK_SCALAR: k_pairs<T, N, OPK_SCALAR, SPLIT><<<grid, kThreads, 0, st>>>(A); break;
-    case OPK_FORCES: k_pairs<T, N, OPK_FORCES, SPLIT><<<grid, kThreads, 0, st>>>(A); break;
-    case OPK_MIN: k_pairs<T, N, OPK_MIN, SPLIT><<<grid, kThreads, 0, st>>>(A); break;
-    case OPK_HIST: k_pairs<T, N, OPK_HIST, SPLIT><<<grid, kThreads, 0, st>>>(A); break;
+// One wave of resident blocks (the warps loop over cells): grid = min(cells/warps, SMs x blocks per SM).
+template <class K> int resident_grid(K kernel, int want) {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
   }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0) != cudaSuccess || per_sm <= 0) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  return std::max(1, std::min(want, per_sm * sms));
+}
+
+template <class T, int N, int OPK, bool SPLIT, bool CROSS>
+cudaError_t launch_k(int& grid, cudaStream_t st, const PairArgs<T>& A) {
+  auto k = k_pairs<T, N, OPK, SPLIT, CROSS>;
+  grid = resident_grid(k, grid);
+  k<<<grid, kThreads, 0, st>>>(A);
   return cudaGetLastError();
 }
 
+template <class T, int N, bool SPLIT, bool CROSS>
+cudaError_t launch_s(int opk, int& grid, cudaStream_t st, const PairArgs<T>& A) {
+  switch (opk) {
+    case OPK_NL: return launch_k<T, N, OPK_NL, SPLIT, CROSS>(grid, st, A);
+    case OPK_SCALAR: return launch_k<T, N, OPK_SCALAR, SPLIT, CROSS>(grid, st, A);
+    case OPK_FORCES: return launch_k<T, N, OPK_FORCES, SPLIT, CROSS>(grid, st, A);
+    case OPK_MIN: return launch_k<T, N, OPK_MIN, SPLIT, CROSS>(grid, st, A);
+    case OPK_HIST: return launch_k<T, N, OPK_HIST, SPLIT, CROSS>(grid, st, A);
+  }
+  return cudaErrorInvalidValue;
+}
+
 template <class T, int N>
-cudaError_t launch(int opk, int grid, cudaStream_t st, const PairArgs<T>& A) {
-  return A.split ? launch_s<T, N, true>(opk, grid, st, A) : launch_s<T, N, false>(opk, grid, st, A);
+cudaError_t launch(int opk, int& grid, cudaStream_t st, const PairArgs<T>& A) {
+  if (A.self)
+    return A.split ? launch_s<T, N, true, false>(opk, grid, st, A) : launch_s<T, N, false, false>(opk, grid, st, A);
+  return A.split ? launch_s<T, N, true, true>(opk, grid, st, A) : launch_s<T, N, false, true>(opk, grid, st, A);
 }
 
 }  // namespace
@@ -809,6 +1051,7 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
   A.X = view_of<T>(X);
   A.Y = view_of<T>(Y);
   A.real_list = X.real_list.as<int>();
+  A.xflags = X.cell_flags.as<int>();
   A.n_real = (int)X.n_real_cells;
   A.self = (h.nsets == 1);
   A.split = (h.precision == 1);
@@ -886,28 +1129,30 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
     CLM_CUDA_TRY(h, cudaStreamSynchronize(h.stream));  // the host vector b goes out of scope
   }
   // grid: static round-robin of real cells over warps (deterministic)
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((A.n_real + kWarps - 1) / kWarps, 152 * 16));
+  const int grid_want = (int)std::max<int64_t>(1, std::min<int64_t>((A.n_real + kWarps - 1) / kWarps, 1 << 16));
+  int grid = grid_want;
   // partials
-  const size_t part_bytes = align(sizeof(double) * grid) + align(sizeof(unsigned long long) * grid) +
-                            align(sizeof(T) * grid) + align(sizeof(int) * 2 * grid) +
-                            (hist ? align(sizeof(unsigned long long) * grid * A.nbins) + align(sizeof(double) * grid * A.nbins) : 0) +
+  const size_t part_bytes = align(sizeof(double) * grid_want) + align(sizeof(unsigned long long) * grid_want) +
+                            align(sizeof(T) * grid_want) + align(sizeof(int) * 2 * grid_want) +
+                            (hist ? align(sizeof(unsigned long long) * grid_want * A.nbins) +
+                                        align(sizeof(double) * grid_want * A.nbins) : 0) +
                             4 * align(sizeof(double) * 512);
   if (!h.partial.reserve(part_bytes)) return ERR_NOMEM;
   char* pb = h.partial.as<char>();
   at = 0;
   A.part_e = (double*)(pb + at);
-  at += align(sizeof(double) * grid);
+  at += align(sizeof(double) * grid_want);
   A.part_c = (unsigned long long*)(pb + at);
-  at += align(sizeof(unsigned long long) * grid);
+  at += align(sizeof(unsigned long long) * grid_want);
   A.part_min_d2 = (T*)(pb + at);
-  at += align(sizeof(T) * grid);
+  at += align(sizeof(T) * grid_want);
   A.part_min_ij = (int*)(pb + at);
-  at += align(sizeof(int) * 2 * grid);
+  at += align(sizeof(int) * 2 * grid_want);
   if (hist) {
     A.part_hc = (unsigned long long*)(pb + at);
-    at += align(sizeof(unsigned long long) * grid * A.nbins);
+    at += align(sizeof(unsigned long long) * grid_want * A.nbins);
     A.part_hs = (double*)(pb + at);
-    at += align(sizeof(double) * grid * A.nbins);
+    at += align(sizeof(double) * grid_want * A.nbins);
   }
   char* res = pb + at;  // final results
   double* r_e = (double*)res;
@@ -944,6 +1189,7 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
       CLM_CUDA_TRY(h, cudaMemsetAsync(A.nl_count, 0, sizeof(unsigned long long), h.stream));
     }
     cudaEventRecord(h.ev[2], h.stream);  // brackets the pair kernel alone
+    grid = grid_want;
     cudaError_t e = (N == 3) ? launch<T, 3>(opk, grid, h.stream, A) : launch<T, 2>(opk, grid, h.stream, A);
     cudaEventRecord(h.ev[3], h.stream);
     if (e != cudaSuccess) {
