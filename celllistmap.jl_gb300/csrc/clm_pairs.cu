@@ -316,8 +316,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
   __shared__ float s_ipf[kWarps][3][32];
   __shared__ int s_icode[kWarps][32];
   __shared__ FA s_if[kWarps][3][(OPK == OPK_FORCES) ? 32 : 1];  // force sums of those particles
-  __shared__ unsigned int s_hc[(OPK == OPK_HIST) ? kWarps : 1][(OPK == OPK_HIST) ? 256 : 1];
-  __shared__ double s_hs[(OPK == OPK_HIST) ? kWarps : 1][(OPK == OPK_HIST) ? 256 : 1];
+  __shared__ unsigned int s_hc[(OPK == OPK_HIST) ? 256 : 1];  // block-wide histogram
+  __shared__ double s_hs[(OPK == OPK_HIST) ? 256 : 1];
   __shared__ double s_red[kWarps];
   __shared__ unsigned long long s_redc[kWarps];
 
@@ -332,11 +332,11 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
   const T band = (T)g.thr_lo;                           // d2 above this: projection filter applies
 
   if constexpr (OPK == OPK_HIST) {
-    for (int b = lane; b < A.nbins; b += 32) {
-      s_hc[warp][b] = 0u;
-      s_hs[warp][b] = 0.0;
+    for (int b = threadIdx.x; b < A.nbins; b += kThreads) {
+      s_hc[b] = 0u;
+      s_hs[b] = 0.0;
     }
-    __syncwarp();
+    __syncthreads();
   }
 
   double e_tot = 0.0;  // per-lane energy (FP64); FP32 partial sums are folded in per particle chunk
@@ -763,8 +763,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
 #pragma unroll
                   for (int d = 0; d < N; d++)
                     dot += ((FA)A.vx[(int64_t)idx_i * N + d] - (FA)vy[(int64_t)idx_j * N + d]) * dv[d];
-                  atomicAdd(&s_hc[warp][b], 1u);
-                  atomicAdd(&s_hs[warp][b], (double)(dot / (FA)r));
+                  atomicAdd(&s_hc[b], 1u);
+                  atomicAdd(&s_hs[b], (double)(dot / (FA)r));
                 }
               }
             }
@@ -861,14 +861,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
   } else if constexpr (OPK == OPK_HIST) {
     __syncthreads();
     for (int b = threadIdx.x; b < A.nbins; b += kThreads) {
-      unsigned long long c = 0;
-      double s = 0;
-      for (int k = 0; k < kWarps; k++) {
-        c += s_hc[k][b];
-        s += s_hs[k][b];
-      }
-      A.part_hc[(int64_t)blockIdx.x * A.nbins + b] = c;
-      A.part_hs[(int64_t)blockIdx.x * A.nbins + b] = s;
+      A.part_hc[(int64_t)blockIdx.x * A.nbins + b] = s_hc[b];
+      A.part_hs[(int64_t)blockIdx.x * A.nbins + b] = s_hs[b];
     }
   }
 }
@@ -1290,6 +1284,8 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
   }
   return OK;
 }
+
+
 
 template int run_pairs<float>(Handle&, const Geometry<float>&, int, const void*, void*);
 template int run_pairs<double>(Handle&, const Geometry<double>&, int, const void*, void*);
