@@ -29,7 +29,7 @@ STATUS = {
 # Every symbol declared in include/celllistmap_gb300.h
 EXPORTS = [
     "clm_create", "clm_destroy", "clm_set_stream", "clm_set_box", "clm_set_positions", "clm_build",
-    "clm_set_precision", "clm_run", "clm_nl_count", "clm_nl_fetch", "clm_get_box", "clm_get_celllist_info",
+    "clm_set_precision", "clm_run", "clm_run_noalloc", "clm_nl_count", "clm_nl_fetch", "clm_get_box", "clm_get_celllist_info",
     "clm_fetch_celllist", "clm_last_timings", "clm_stats", "clm_last_error", "clm_version",
 ]
 
@@ -62,6 +62,7 @@ def _declare(L):
     L.clm_build.argtypes = [vp]
     L.clm_set_precision.argtypes = [vp, i32]
     L.clm_run.argtypes = [vp, i32, C.POINTER(OpParams), C.POINTER(Outputs)]
+    L.clm_run_noalloc.argtypes = [vp, i32, C.POINTER(OpParams), C.POINTER(Outputs)]
     L.clm_nl_count.argtypes = [vp, C.POINTER(i64)]
     L.clm_nl_fetch.argtypes = [vp, vp, vp, vp, i64, i32, i32]
     L.clm_get_box.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp]

@@ -18,7 +18,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libcelllist_cuda.so")
-SOURCES = ["clm_api.cu", "clm_build.cu", "clm_pairs.cu"]
+SOURCES = ["clm_api.cu", "clm_build.cu", "clm_pairs.cu", "clm_noalloc.cu"]
 PEAKS_SRC = "clm_peaks.cu"
 PEAKS_LIB = os.path.join(OUT_DIR, "libclm_peaks.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -117,5 +117,9 @@ template <class T> void fill_devgeom(const Geometry<T>& g, int precision, DevGeo
 // Map (clm_pairs.cu)
 struct OpRequest;
 template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const void* params, void* outputs);
+template <class T>
+int run_pairs_scalar_scratch(Handle& h, const Geometry<T>& g, int op, const void* params, void* outputs, void* scratch,
+                             size_t scratch_bytes);
+int pairs_scalar_blocks_needed(Handle& h, int op);
 
 }  // namespace clm

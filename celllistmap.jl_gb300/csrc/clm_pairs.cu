@@ -1286,6 +1286,135 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
 }
 
 
+// Scalar reductions (COUNT, SUM_D2, SUM_D, SUM_INV_D, SOFT_ENERGY, LJ_ENERGY without type tables) and
+// MINDIST on an already built handle, with the per-block partials and the final result placed in
+// caller-provided device scratch instead of handle buffers.  Allocates nothing; used by clm_run_noalloc.
+template <class T>
+int run_pairs_scalar_scratch(Handle& h, const Geometry<T>& g, int op, const void* vparams, void* vout, void* scratch,
+                             size_t scratch_bytes) {
+  const clm_op_params* P = static_cast<const clm_op_params*>(vparams);
+  clm_outputs* O = static_cast<clm_outputs*>(vout);
+  const int opk = opkind_of(op);
+  if (opk != OPK_SCALAR && opk != OPK_MIN) {
+    h.last_error = "the allocation-free entry point supports COUNT, SUM_D2, SUM_D, SUM_INV_D, SOFT_ENERGY, "
+                   "LJ_ENERGY and MINDIST";
+    return ERR_ARG;
+  }
+  if (P && P->ntypes > 0) {
+    h.last_error = "the allocation-free entry point does not take per-type tables";
+    return ERR_ARG;
+  }
+  const int N = g.dim;
+  SetData& X = h.sets[0];
+  SetData& Y = (h.nsets == 2) ? h.sets[1] : h.sets[0];
+  PairArgs<T> A;
+  std::memset(&A, 0, sizeof(A));
+  fill_devgeom(g, h.precision, A.g);
+  A.X = view_of<T>(X);
+  A.Y = view_of<T>(Y);
+  A.real_list = X.real_list.as<int>();
+  A.xflags = X.cell_flags.as<int>();
+  A.n_real = (int)X.n_real_cells;
+  A.self = (h.nsets == 1);
+  A.split = (h.precision == 1);
+  A.op = op;
+  A.err = h.err.as<int>();
+  for (int k = 0; k < 4; k++) A.p[k] = P ? P->p[k] : 0.0;
+  if (op == 6 && A.p[0] == 0.0) A.p[0] = (double)g.cutoff;
+  // scratch layout: [results, 256 B][partial energy][partial count][partial min d2][partial min ij]
+  const size_t slot = sizeof(double) + sizeof(unsigned long long) + sizeof(T) + 2 * sizeof(int);
+  const size_t cap_blocks = scratch_bytes > 256 ? (scratch_bytes - 256) / slot : 0;
+  const int needed = pairs_scalar_blocks_needed(h, op);
+  if (needed < 0 || (size_t)needed > cap_blocks) {
+    h.last_error = "the pair map needs more per-block partial slots than the allocation-free scratch holds";
+    return ERR_CAPACITY;
+  }
+  int grid = needed;
+  char* base = static_cast<char*>(scratch);
+  const size_t nb = cap_blocks;
+  A.part_e = (double*)(base + 256);
+  A.part_c = (unsigned long long*)(base + 256 + sizeof(double) * nb);
+  A.part_min_d2 = (T*)(base + 256 + (sizeof(double) + sizeof(unsigned long long)) * nb);
+  A.part_min_ij = (int*)(base + 256 + (sizeof(double) + sizeof(unsigned long long) + sizeof(T)) * nb);
+  double* r_e = (double*)base;
+  unsigned long long* r_c = (unsigned long long*)(base + 8);
+  T* r_md = (T*)(base + 16);
+  int* r_mij = (int*)(base + 24);
+  cudaError_t e = (N == 3) ? launch<T, 3>(opk, grid, h.stream, A) : launch<T, 2>(opk, grid, h.stream, A);
+  if (e != cudaSuccess) {
+    h.last_error = std::string("pair kernel launch failed: ") + cudaGetErrorString(e);
+    return ERR_CUDA;
+  }
+  h.launches++;
+  if (opk == OPK_SCALAR) k_reduce_scalar<<<1, 256, 0, h.stream>>>(A.part_e, A.part_c, grid, r_e, r_c);
+  else k_reduce_min<T><<<1, 32, 0, h.stream>>>(A.part_min_d2, A.part_min_ij, grid, r_md, r_mij);
+  CLM_CUDA_TRY(h, cudaGetLastError());
+  h.launches++;
+  // results through the handle's pinned staging area (allocated when the handle was created)
+  CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 8, base, 32, cudaMemcpyDeviceToHost, h.stream));
+  CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 4, h.err.p, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+  CLM_CUDA_TRY(h, cudaStreamSynchronize(h.stream));
+  if (h.pinned[4] & DERR_CELL_RANGE) {
+    h.last_error = "pair map consistency check failed (stencil cell outside the grid)";
+    return ERR_INTERNAL;
+  }
+  const char* hr = reinterpret_cast<const char*>(h.pinned + 8);
+  unsigned long long cnt;
+  std::memcpy(&O->scalar, hr, 8);
+  std::memcpy(&cnt, hr + 8, 8);
+  O->count = (int64_t)cnt;
+  if (op == 2) O->scalar = (double)cnt;
+  if (opk == OPK_MIN) {
+    T md;
+    int mij[2];
+    std::memcpy(&md, hr + 16, sizeof(T));
+    std::memcpy(mij, hr + 24, 8);
+    if (std::isinf((double)md)) {
+      O->min_d = INFINITY;
+      O->min_i = -1;
+      O->min_j = -1;
+    } else {
+      O->min_d = (double)std::sqrt(md);
+      O->min_i = mij[0] + O->index_base;
+      O->min_j = mij[1] + O->index_base;
+    }
+  }
+  return OK;
+}
+
+// Number of per-block partial slots the scalar map needs on this device (one resident wave).
+int pairs_scalar_blocks_needed(Handle& h, int op) {
+  const int opk = opkind_of(op);
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int per_sm = 0;
+  cudaError_t e = cudaErrorInvalidValue;
+  const bool self = (h.nsets == 1), split = (h.precision == 1);
+  auto occ = [&](auto k) { return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, 0); };
+#define CLM_OCC(T, N)                                                                                    \
+  if (opk == OPK_SCALAR)                                                                                 \
+    e = split ? (self ? occ(k_pairs<T, N, OPK_SCALAR, true, false>) : occ(k_pairs<T, N, OPK_SCALAR, true, true>)) \
+              : (self ? occ(k_pairs<T, N, OPK_SCALAR, false, false>) : occ(k_pairs<T, N, OPK_SCALAR, false, true>)); \
+  else                                                                                                   \
+    e = split ? (self ? occ(k_pairs<T, N, OPK_MIN, true, false>) : occ(k_pairs<T, N, OPK_MIN, true, true>))       \
+              : (self ? occ(k_pairs<T, N, OPK_MIN, false, false>) : occ(k_pairs<T, N, OPK_MIN, false, true>));
+  if (h.dtype == 1) {
+    if (h.dim == 3) { CLM_OCC(double, 3) } else { CLM_OCC(double, 2) }
+  } else {
+    if (h.dim == 3) { CLM_OCC(float, 3) } else { CLM_OCC(float, 2) }
+  }
+#undef CLM_OCC
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  const int64_t want = std::max<int64_t>(1, (h.sets[0].n_real_cells + kWarps - 1) / kWarps);
+  return (int)std::min<int64_t>(want, (int64_t)per_sm * sms);
+}
+
+template int run_pairs_scalar_scratch<float>(Handle&, const Geometry<float>&, int, const void*, void*, void*, size_t);
+template int run_pairs_scalar_scratch<double>(Handle&, const Geometry<double>&, int, const void*, void*, void*, size_t);
 
 template int run_pairs<float>(Handle&, const Geometry<float>&, int, const void*, void*);
 template int run_pairs<double>(Handle&, const Geometry<double>&, int, const void*, void*);
