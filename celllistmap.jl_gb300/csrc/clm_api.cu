@@ -70,43 +70,59 @@ template <class T> bool same_geometry(const Geometry<T>& a, const Geometry<T>& b
   return a.cutoff == b.cutoff;
 }
 
-template <class T> int build_all(Handle& h) {
+template <class T> int build_all(Handle& h, bool sync) {
   if (!h.box_set) return fail(&h, ERR_STATE, "clm_set_box must be called before building");
-  cudaEventRecord(h.ev[0], h.stream);
-  bool rebuild_all = false;
-  if (h.kind == CLM_NONPERIODIC) {
-    bool any_dirty = false;
-    for (int s = 0; s < h.nsets; s++) any_dirty = any_dirty || h.sets[s].dirty || !h.sets[s].built;
-    if (any_dirty) {
-      T lo[3], hi[3], M[3][3], origin[3] = {0, 0, 0};
-      int st = set_limits<T>(h, lo, hi);
-      if (st) return st;
-      for (int d = 0; d < h.dim; d++)
-        if (std::isnan((double)lo[d]) || std::isnan((double)hi[d]))
-          return fail(&h, ERR_NAN, "Invalid coordinates found (NaN) in the particle positions.");
-      nonperiodic_cell<T>(h.dim, lo, hi, (T)h.cutoff, M, origin);
-      Geometry<T> g;
-      st = make_geometry<T>(g, h.dim, CLM_NONPERIODIC, M, (T)h.cutoff, h.lcell, origin);
-      if (st == 2) return fail(&h, ERR_CELL_TOO_SMALL, "Unit cell matrix does not satisfy required conditions.");
-      if (st) return fail(&h, st, "invalid non-periodic box");
-      if (!same_geometry(g, geom<T>(h))) rebuild_all = true;
-      geom<T>(h) = g;
+  for (int attempt = 0; attempt < 3; attempt++) {
+    if (attempt > 0) CLM_CUDA_TRY(h, cudaMemsetAsync(h.err.p, 0, 64, h.stream));  // drop the overflow flag
+    cudaEventRecord(h.ev[0], h.stream);
+    bool rebuild_all = false;
+    if (h.kind == CLM_NONPERIODIC) {
+      bool any_dirty = false;
+      for (int s = 0; s < h.nsets; s++) any_dirty = any_dirty || h.sets[s].dirty || !h.sets[s].built;
+      if (any_dirty) {
+        T lo[3], hi[3], M[3][3], origin[3] = {0, 0, 0};
+        int st = set_limits<T>(h, lo, hi);
+        if (st) return st;
+        for (int d = 0; d < h.dim; d++)
+          if (std::isnan((double)lo[d]) || std::isnan((double)hi[d]))
+            return fail(&h, ERR_NAN, "Invalid coordinates found (NaN) in the particle positions.");
+        nonperiodic_cell<T>(h.dim, lo, hi, (T)h.cutoff, M, origin);
+        Geometry<T> g;
+        st = make_geometry<T>(g, h.dim, CLM_NONPERIODIC, M, (T)h.cutoff, h.lcell, origin);
+        if (st == 2) return fail(&h, ERR_CELL_TOO_SMALL, "Unit cell matrix does not satisfy required conditions.");
+        if (st) return fail(&h, st, "invalid non-periodic box");
+        if (!same_geometry(g, geom<T>(h))) rebuild_all = true;
+        geom<T>(h) = g;
+      }
     }
-  }
-  for (int s = 0; s < h.nsets; s++) {
-    SetData& S = h.sets[s];
-    if (S.dirty || !S.built || rebuild_all) {
-      int st = build_set<T>(h, s, geom<T>(h));
-      if (st) return st;
+    for (int s = 0; s < h.nsets; s++) {
+      SetData& S = h.sets[s];
+      if (S.dirty || !S.built || rebuild_all) {
+        int st = build_set<T>(h, s, geom<T>(h));
+        if (st) return st;
+      }
     }
+    cudaEventRecord(h.ev[1], h.stream);
+    if (!sync) {
+      h.build_timing_pending = true;
+      return OK;
+    }
+    int st = enqueue_build_totals(h);
+    if (st) return st;
+    CLM_CUDA_TRY(h, cudaStreamSynchronize(h.stream));
+    cudaEventElapsedTime(&h.build_ms, h.ev[0], h.ev[1]);
+    h.build_timing_pending = false;
+    bool overflow = false;
+    st = check_build_totals(h, &overflow);
+    if (st) return st;
+    if (!overflow) return OK;
   }
-  cudaEventRecord(h.ev[1], h.stream);
-  cudaEventSynchronize(h.ev[1]);
-  cudaEventElapsedTime(&h.build_ms, h.ev[0], h.ev[1]);
-  return OK;
+  return fail(&h, ERR_INTERNAL, "cell-list build did not converge on a copy capacity");
 }
 
-int build_dispatch(Handle& h) { return h.dtype == CLM_F64 ? build_all<double>(h) : build_all<float>(h); }
+int build_dispatch(Handle& h, bool sync = true) {
+  return h.dtype == CLM_F64 ? build_all<double>(h, sync) : build_all<float>(h, sync);
+}
 
 }  // namespace
 
@@ -250,16 +266,21 @@ int32_t clm_build(clm_handle h) {
 int32_t clm_run(clm_handle h, int32_t op_id, const clm_op_params* params, clm_outputs* out) {
   if (!h || !out) return ERR_ARG;
   if (!h->box_set) return fail(h, ERR_STATE, "clm_set_box must be called before clm_run");
-  bool need = false;
-  for (int s = 0; s < h->nsets; s++) need = need || h->sets[s].dirty || !h->sets[s].built;
-  cudaMemsetAsync(h->err.p, 0, 64, h->stream);
-  if (need) {
-    int st = build_dispatch(*h);
-    if (st) return st;
+  for (int attempt = 0; attempt < 3; attempt++) {
+    bool need = false;
+    for (int s = 0; s < h->nsets; s++) need = need || h->sets[s].dirty || !h->sets[s].built;
+    cudaMemsetAsync(h->err.p, 0, 64, h->stream);
+    if (need) {
+      // enqueued without waiting for the device; its totals are checked with the map's results
+      int st = build_dispatch(*h, false);
+      if (st) return st;
+    }
+    h->nl_valid = false;
+    int st = (h->dtype == CLM_F64) ? run_pairs<double>(*h, h->gd, op_id, params, out)
+                                   : run_pairs<float>(*h, h->gf, op_id, params, out);
+    if (st != RERUN_BUILD) return st;
   }
-  h->nl_valid = false;
-  if (h->dtype == CLM_F64) return run_pairs<double>(*h, h->gd, op_id, params, out);
-  return run_pairs<float>(*h, h->gf, op_id, params, out);
+  return fail(h, ERR_INTERNAL, "cell-list build did not converge on a copy capacity");
 }
 
 int32_t clm_nl_count(clm_handle h, int64_t* n) {

@@ -95,9 +95,10 @@ constexpr int RS_IPT = 8;
 constexpr int RS_TILE = kBlock * RS_IPT;  // 2048 keys per tile
 constexpr int RS_WARPS = kBlock / 32;
 
-__global__ void __launch_bounds__(kBlock) k_rs_hist(const uint32_t* __restrict__ keys, int n, int shift,
-                                                    int* __restrict__ hist, int ntiles) {
+__global__ void __launch_bounds__(kBlock) k_rs_hist(const uint32_t* __restrict__ keys, const int* __restrict__ n_dev,
+                                                    int cap, int shift, int* __restrict__ hist, int ntiles) {
   __shared__ int h[256];
+  const int n = min(*n_dev, cap);
   h[threadIdx.x] = 0;
   __syncthreads();
   const int64_t base = (int64_t)blockIdx.x * RS_TILE;
@@ -114,9 +115,11 @@ __global__ void __launch_bounds__(kBlock) k_rs_hist(const uint32_t* __restrict__
 // slot, then lane) with warp-level match_any, then placed at the scanned
 // digit offset of the tile.
 __global__ void __launch_bounds__(kBlock) k_rs_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
-                                                       uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, int n,
-                                                       int shift, const int* __restrict__ offs, int ntiles) {
+                                                       uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                       const int* __restrict__ n_dev, int cap, int shift,
+                                                       const int* __restrict__ offs, int ntiles) {
   __shared__ int wcnt[RS_WARPS][257];
+  const int n = min(*n_dev, cap);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int d = threadIdx.x; d < RS_WARPS * 257; d += kBlock) (&wcnt[0][0])[d] = 0;
   __syncthreads();
@@ -262,15 +265,29 @@ __global__ void __launch_bounds__(kBlock) k_emit(DevGeom<T> g, const T* __restri
 }
 
 // ------------------------------------------------------------------ K4: gather in cell order
+// origin of cell c along one axis as an unevaluated float pair (hi + lo): cbmin + cs*(c-1) with the
+// product and the sum carried exactly (TwoProduct with an FMA, TwoSum)
+__device__ __forceinline__ void origin_ff(float cb_hi, float cb_lo, float cs_hi, float cs_lo, int c1, float& hi,
+                                          float& lo) {
+  const float k = (float)c1;
+  const float p = cs_hi * k;
+  const float pe = fmaf(cs_hi, k, -p) + cs_lo * k;
+  const float s = cb_hi + p;
+  const float bb = s - cb_hi;
+  const float se = (cb_hi - (s - bb)) + (p - bb);
+  hi = s;
+  lo = se + pe + cb_lo;
+}
+
 template <class T, int N>
 __global__ void __launch_bounds__(kBlock) k_gather(DevGeom<T> g, const T* __restrict__ wrapped,
                                                    const uint32_t* __restrict__ skeys,
-                                                   const uint32_t* __restrict__ svals, int ncopies, int n,
-                                                   T* __restrict__ px, T* __restrict__ py, T* __restrict__ pz,
-                                                   float4* __restrict__ off, int* __restrict__ code,
+                                                   const uint32_t* __restrict__ svals, const int* __restrict__ n_dev,
+                                                   int cap, int n, T* __restrict__ px, T* __restrict__ py,
+                                                   T* __restrict__ pz, float4* __restrict__ off, int* __restrict__ code,
                                                    int* __restrict__ err) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ncopies) return;
+  if (t >= min(*n_dev, cap)) return;
   uint32_t v = svals[t];
   int p = (int)(v >> 5);
   int k = (int)(v & 31u);
@@ -291,8 +308,12 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom<T> g, const T* __rest
   float o[3] = {0.f, 0.f, 0.f};
 #pragma unroll
   for (int d = 0; d < N; d++) {
-    double origin = (double)g.cbmin[d] + (double)g.cs[d] * (double)(c[d] - 1);
-    o[d] = (float)((double)q[d] - origin);
+    // FP32 offset of the copy from its cell origin, all in float pairs: (qh + ql) - (oh + ol)
+    float oh, ol;
+    origin_ff(g.cbf_hi[d], g.cbf_lo[d], g.csf[d], g.csf_lo[d], c[d] - 1, oh, ol);
+    const float qh = (float)q[d];
+    const float ql = (float)(q[d] - (T)qh);
+    o[d] = (qh - oh) + (ql - ol);
   }
   px[t] = q[0];
   py[t] = q[1];
@@ -399,6 +420,9 @@ template <class T> void fill_devgeom(const Geometry<T>& g, int precision, DevGeo
     d.cbmax[i] = g.cbmax[i];
     d.cs[i] = g.cs[i];
     d.csf[i] = (float)g.cs[i];
+    d.csf_lo[i] = (float)((double)g.cs[i] - (double)d.csf[i]);
+    d.cbf_hi[i] = (float)g.cbmin[i];
+    d.cbf_lo[i] = (float)((double)g.cbmin[i] - (double)d.cbf_hi[i]);
     for (int j = 0; j < 3; j++) {
       d.Min[i][j] = g.Min[i][j];
       d.R[i][j] = g.R[i][j];
@@ -472,6 +496,21 @@ template <class T> int set_limits(Handle& h, T* lo, T* hi) {
   return OK;
 }
 
+// Capacity for the copies (reals + images) of a set: the largest of the previous build's count and the
+// uniform-density estimate (computing-box volume / unit-cell volume), with a margin.  The build never
+// waits for the device: if the copies exceed the capacity, k_emit flags it, the result is discarded at
+// the next host synchronization and the build is repeated with the exact size.
+template <class T> int64_t copy_capacity(const SetData& S, const Geometry<T>& g) {
+  const int64_t n = S.n;
+  if (g.kind == NONPERIODIC) return n + 64;
+  double vbox = 1.0;
+  for (int i = 0; i < g.dim; i++) vbox *= (double)g.cbmax[i] - (double)g.cbmin[i];
+  const double vcell = std::fabs((double)g.det_in);
+  double est = (vcell > 0) ? (double)n * vbox / vcell : 27.0 * (double)n;
+  est = std::min(est * 1.15 + 4096.0, 27.0 * (double)n + 64.0);
+  return std::max<int64_t>(std::max<int64_t>(S.copy_cap, (int64_t)est), n + 64);
+}
+
 template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
   SetData& S = h.sets[set];
   const int N = g.dim;
@@ -487,20 +526,33 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
   int* err = h.err.as<int>();
   if (!S.cell_count.reserve(sizeof(int) * (ncells + 1)) || !S.cell_start.reserve(sizeof(int) * (ncells + 1)) ||
       !S.cell_flags.reserve(sizeof(int) * (ncells + 1)) || !S.real_scan.reserve(sizeof(int) * (ncells + 1)) ||
-      !S.real_list.reserve(sizeof(int) * (ncells + 1)))
+      !S.real_list.reserve(sizeof(int) * (ncells + 1)) || !S.copy_off.reserve(sizeof(int) * (n + 1)))
     return ERR_NOMEM;
   CLM_CUDA_TRY(h, cudaMemsetAsync(S.cell_count.p, 0, sizeof(int) * (ncells + 1), h.stream));
   CLM_CUDA_TRY(h, cudaMemsetAsync(S.cell_flags.p, 0, sizeof(int) * (ncells + 1), h.stream));
+  S.built = true;
+  S.dirty = false;
+  S.pending = true;
   if (n == 0) {
     CLM_CUDA_TRY(h, cudaMemsetAsync(S.cell_start.p, 0, sizeof(int) * (ncells + 1), h.stream));
-    S.n_copies = 0;
-    S.n_real_cells = 0;
-    S.built = true;
-    S.dirty = false;
+    CLM_CUDA_TRY(h, cudaMemsetAsync(S.real_scan.p, 0, sizeof(int) * (ncells + 1), h.stream));
+    CLM_CUDA_TRY(h, cudaMemsetAsync(S.copy_off.p, 0, sizeof(int), h.stream));
+    S.cap_used = 0;
     return OK;
   }
+  const int64_t cap = copy_capacity(S, g);
+  if (cap > (int64_t)INT32_MAX - 1) {
+    h.last_error = "too many particle copies for one set";
+    return ERR_ARG;
+  }
+  S.cap_used = cap;
+  const int ntiles = (int)((cap + RS_TILE - 1) / RS_TILE);
   if (!S.wrapped.reserve(sizeof(T) * N * n) || !S.mask.reserve(sizeof(uint32_t) * n) ||
-      !S.ncopy.reserve(sizeof(int) * (n + 1)) || !S.copy_off.reserve(sizeof(int) * (n + 1)))
+      !S.ncopy.reserve(sizeof(int) * (n + 1)) || !S.keys[0].reserve(sizeof(uint32_t) * cap) ||
+      !S.keys[1].reserve(sizeof(uint32_t) * cap) || !S.vals[0].reserve(sizeof(uint32_t) * cap) ||
+      !S.vals[1].reserve(sizeof(uint32_t) * cap) || !S.px.reserve(sizeof(T) * cap) || !S.py.reserve(sizeof(T) * cap) ||
+      !S.pz.reserve(sizeof(T) * cap) || !S.off.reserve(sizeof(float4) * cap) || !S.code.reserve(sizeof(int) * cap) ||
+      !S.rs_hist.reserve(sizeof(int) * (256 * (int64_t)ntiles + 1)))
     return ERR_NOMEM;
   const int gn = grid_for(n);
   if (N == 3)
@@ -510,53 +562,37 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
     k_wrap_count<T, 2><<<gn, kBlock, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
                                                    S.ncopy.as<int>(), err);
   CLM_CUDA_TRY(h, cudaGetLastError());
-    h.launches++;
-  int* d_total = S.copy_off.as<int>() + n;
-  int st = scan_exclusive(h, S.ncopy.as<int>(), S.copy_off.as<int>(), n, d_total);
+  h.launches++;
+  int* n_dev = S.copy_off.as<int>() + n;  // total number of copies, on the device
+  int st = scan_exclusive(h, S.ncopy.as<int>(), S.copy_off.as<int>(), n, n_dev);
   if (st) return st;
-  // one host sync: number of copies and the error word
-  CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned, d_total, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
-  CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 1, err, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
-  CLM_CUDA_TRY(h, cudaStreamSynchronize(h.stream));
-  if (h.pinned[1] & DERR_NAN) {
-    h.last_error = "Invalid coordinates found (NaN) in the particle positions.";
-    return ERR_NAN;
-  }
-  const int64_t nc = h.pinned[0];
-  if (nc < n || nc > (int64_t)INT32_MAX - 1) {
-    h.last_error = "copy count out of range";
-    return ERR_INTERNAL;
-  }
-  S.n_copies = nc;
-  for (int b = 0; b < 2; b++)
-    if (!S.keys[b].reserve(sizeof(uint32_t) * nc) || !S.vals[b].reserve(sizeof(uint32_t) * nc)) return ERR_NOMEM;
   if (N == 3)
     k_emit<T, 3><<<gn, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(),
-                                             S.copy_off.as<int>(), (int)n, (int)nc, S.keys[0].as<uint32_t>(),
+                                             S.copy_off.as<int>(), (int)n, (int)cap, S.keys[0].as<uint32_t>(),
                                              S.vals[0].as<uint32_t>(), S.cell_count.as<int>(), S.cell_flags.as<int>(), err);
   else
     k_emit<T, 2><<<gn, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(),
-                                             S.copy_off.as<int>(), (int)n, (int)nc, S.keys[0].as<uint32_t>(),
+                                             S.copy_off.as<int>(), (int)n, (int)cap, S.keys[0].as<uint32_t>(),
                                              S.vals[0].as<uint32_t>(), S.cell_count.as<int>(), S.cell_flags.as<int>(), err);
   CLM_CUDA_TRY(h, cudaGetLastError());
-    h.launches++;
+  h.launches++;
   // stable LSD radix sort by cell
   int bits = 1;
   while (((int64_t)1 << bits) < ncells) bits++;
   const int passes = (bits + 7) / 8;
-  const int ntiles = (int)((nc + RS_TILE - 1) / RS_TILE);
-  if (!S.rs_hist.reserve(sizeof(int) * (256 * (int64_t)ntiles + 1))) return ERR_NOMEM;
   int cur = 0;
   for (int pss = 0; pss < passes; pss++) {
     int shift = 8 * pss;
-    k_rs_hist<<<ntiles, kBlock, 0, h.stream>>>(S.keys[cur].as<uint32_t>(), (int)nc, shift, S.rs_hist.as<int>(), ntiles);
+    k_rs_hist<<<ntiles, kBlock, 0, h.stream>>>(S.keys[cur].as<uint32_t>(), n_dev, (int)cap, shift, S.rs_hist.as<int>(),
+                                               ntiles);
     CLM_CUDA_TRY(h, cudaGetLastError());
     h.launches++;
-    st = scan_exclusive(h, S.rs_hist.as<int>(), S.rs_hist.as<int>(), 256 * (int64_t)ntiles, S.rs_hist.as<int>() + 256 * (int64_t)ntiles);
+    st = scan_exclusive(h, S.rs_hist.as<int>(), S.rs_hist.as<int>(), 256 * (int64_t)ntiles,
+                        S.rs_hist.as<int>() + 256 * (int64_t)ntiles);
     if (st) return st;
     k_rs_scatter<<<ntiles, kBlock, 0, h.stream>>>(S.keys[cur].as<uint32_t>(), S.vals[cur].as<uint32_t>(),
-                                                  S.keys[1 - cur].as<uint32_t>(), S.vals[1 - cur].as<uint32_t>(),
-                                                  (int)nc, shift, S.rs_hist.as<int>(), ntiles);
+                                                  S.keys[1 - cur].as<uint32_t>(), S.vals[1 - cur].as<uint32_t>(), n_dev,
+                                                  (int)cap, shift, S.rs_hist.as<int>(), ntiles);
     CLM_CUDA_TRY(h, cudaGetLastError());
     h.launches++;
     cur = 1 - cur;
@@ -565,38 +601,68 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
   st = scan_exclusive(h, S.cell_count.as<int>(), S.cell_start.as<int>(), ncells, S.cell_start.as<int>() + ncells);
   if (st) return st;
   // gather coordinates in cell order
-  if (!S.px.reserve(sizeof(T) * nc) || !S.py.reserve(sizeof(T) * nc) || !S.pz.reserve(sizeof(T) * nc) ||
-      !S.off.reserve(sizeof(float4) * nc) || !S.code.reserve(sizeof(int) * nc))
-    return ERR_NOMEM;
-  const int gc = grid_for(nc);
+  const int gc = grid_for(cap);
   if (N == 3)
     k_gather<T, 3><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
-                                               S.vals[cur].as<uint32_t>(), (int)nc, (int)n, S.px.as<T>(), S.py.as<T>(),
-                                               S.pz.as<T>(), S.off.as<float4>(), S.code.as<int>(), err);
+                                               S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
+                                               S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.code.as<int>(), err);
   else
     k_gather<T, 2><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
-                                               S.vals[cur].as<uint32_t>(), (int)nc, (int)n, S.px.as<T>(), S.py.as<T>(),
-                                               S.pz.as<T>(), S.off.as<float4>(), S.code.as<int>(), err);
+                                               S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
+                                               S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.code.as<int>(), err);
   CLM_CUDA_TRY(h, cudaGetLastError());
-    h.launches++;
-  // cells with real particles, in linear order
+  h.launches++;
+  // cells with real particles, in linear order; their number stays on the device (real_scan[ncells])
   st = scan_exclusive(h, S.cell_flags.as<int>(), S.real_scan.as<int>(), ncells, S.real_scan.as<int>() + ncells);
   if (st) return st;
   k_compact<<<grid_for(ncells), kBlock, 0, h.stream>>>(S.cell_flags.as<int>(), S.real_scan.as<int>(), (int)ncells,
                                                        S.real_list.as<int>());
   CLM_CUDA_TRY(h, cudaGetLastError());
-    h.launches++;
-  CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 2, S.real_scan.as<int>() + ncells, sizeof(int), cudaMemcpyDeviceToHost,
-                                  h.stream));
-  CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 3, err, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
-  CLM_CUDA_TRY(h, cudaStreamSynchronize(h.stream));
-  if (h.pinned[3] & (DERR_CELL_RANGE | DERR_COPY_OVERFLOW)) {
+  h.launches++;
+  return OK;
+}
+
+// Reads the device totals of the last build of every set (after the caller synchronized the stream
+// through `staged`, which the caller filled with enqueue_build_totals) and checks the error word.
+int enqueue_build_totals(Handle& h) {
+  for (int s = 0; s < h.nsets; s++) {
+    SetData& S = h.sets[s];
+    if (!S.pending) continue;
+    CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 32 + 2 * s, S.copy_off.as<int>() + S.n, sizeof(int),
+                                    cudaMemcpyDeviceToHost, h.stream));
+    CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 33 + 2 * s, S.real_scan.as<int>() + S.ncells, sizeof(int),
+                                    cudaMemcpyDeviceToHost, h.stream));
+  }
+  CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 40, h.err.p, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+  return OK;
+}
+
+int check_build_totals(Handle& h, bool* overflow) {
+  *overflow = false;
+  const int errw = h.pinned[40];
+  if (errw & DERR_NAN) {
+    for (int s = 0; s < h.nsets; s++) h.sets[s].dirty = true;
+    h.last_error = "Invalid coordinates found (NaN) in the particle positions.";
+    return ERR_NAN;
+  }
+  for (int s = 0; s < h.nsets; s++) {
+    SetData& S = h.sets[s];
+    if (!S.pending) continue;
+    S.n_copies = h.pinned[32 + 2 * s];
+    S.n_real_cells = h.pinned[33 + 2 * s];
+    S.pending = false;
+    if (S.n_copies > S.cap_used || (errw & DERR_COPY_OVERFLOW)) {
+      S.copy_cap = S.n_copies + S.n_copies / 8 + 1024;
+      S.dirty = true;
+      *overflow = true;
+    } else if (S.n_copies > S.copy_cap) {
+      S.copy_cap = S.n_copies;
+    }
+  }
+  if (!*overflow && (errw & DERR_CELL_RANGE)) {
     h.last_error = "cell-list build consistency check failed (particle outside the computing box)";
     return ERR_INTERNAL;
   }
-  S.n_real_cells = h.pinned[2];
-  S.built = true;
-  S.dirty = false;
   return OK;
 }
 

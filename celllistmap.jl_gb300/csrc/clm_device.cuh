@@ -38,7 +38,9 @@ template <class T> struct DevGeom {
   T cbmin[3], cbmax[3], cs[3];
   T cutoff, cutoff_sqr;
   double margin_wide;   // projection margin when lcell > 1 (computed in double, as the reference does)
-  float csf[3];         // cell sizes in FP32 for the prefilter
+  float csf[3];         // cell sizes in FP32 for the prefilter (high part)
+  float csf_lo[3];      // cell size - csf (low part of the float pair)
+  float cbf_hi[3], cbf_lo[3];  // computing-box minimum as a float pair
   float thr_hi, thr_lo; // FP32 prefilter bounds on d2 (maybe-inside / surely-inside)
   int zero_code;        // image code of the zero shift (13 in 3D, 4 in 2D)
   int nimg;             // 3^dim

@@ -12,6 +12,7 @@
 namespace clm {
 
 enum Status {
+  RERUN_BUILD = -1,  // internal: the copies overflowed the capacity; rebuild with the exact size and rerun
   OK = 0, ERR_ARG = 1, ERR_CELL_TOO_SMALL = 2, ERR_NAN = 3, ERR_DIM = 4, ERR_CUDA = 5, ERR_CAPACITY = 6,
   ERR_STATE = 7, ERR_TIMEOUT = 8, ERR_NOMEM = 9, ERR_LCELL = 10, ERR_NONPERIODIC_CELL = 11, ERR_INTERNAL = 12
 };
@@ -60,8 +61,11 @@ struct SetData {
   DevBuf code;              // particle index (>= 0 real copy, -(index+1) image)
   DevBuf rs_hist;
   DevBuf minmax;            // non-periodic limits scratch
-  int64_t n_copies = 0;
+  int64_t n_copies = 0;      // valid once the build was synchronized (pending == false)
   int64_t n_real_cells = 0;
+  int64_t copy_cap = 0;      // capacity for copies learned from previous builds
+  int64_t cap_used = 0;      // capacity used by the last build
+  bool pending = false;      // the device totals of the last build were not read back yet
   int64_t n_cells_with_particles = 0;
   int64_t ncells = 0;
 };
@@ -94,6 +98,7 @@ struct Handle {
   int* pinned = nullptr;       // small pinned host staging area (256 bytes)
   cudaEvent_t ev[4] = {};
   float build_ms = 0, map_ms = 0;
+  bool build_timing_pending = false;
   int64_t launches = 0;        // kernels launched by this handle (cumulative)
   std::string last_error;
 };
@@ -111,6 +116,8 @@ struct Handle {
 // Build (clm_build.cu)
 int scan_exclusive(Handle& h, const int* in, int* out, int64_t m, int* total, int depth = 0);
 template <class T> int build_set(Handle& h, int set, const Geometry<T>& g);
+int enqueue_build_totals(Handle& h);
+int check_build_totals(Handle& h, bool* overflow);
 template <class T> int set_limits(Handle& h, T* lo, T* hi);
 template <class T> void fill_devgeom(const Geometry<T>& g, int precision, DevGeom<T>& d);
 

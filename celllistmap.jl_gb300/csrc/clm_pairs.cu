@@ -61,7 +61,7 @@ template <class T> struct PairArgs {
   SetView<T> X, Y;
   const int* real_list;
   const int* xflags;  // per cell of set x: contains real particles
-  int n_real;
+  const int* n_real_dev;  // number of cells with real particles (device)
   int self;
   int split;
   int op;
@@ -347,7 +347,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
 
   const int gw = blockIdx.x * kWarps + warp;
   const int nw = gridDim.x * kWarps;
-  for (int r = gw; r < A.n_real; r += nw) {
+  const int n_real = *A.n_real_dev;
+  for (int r = gw; r < n_real; r += nw) {
     const int li = A.real_list[r];
     int ci[3];
     cart_of(li, g.nc, N, ci);
@@ -1046,7 +1047,7 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
   A.Y = view_of<T>(Y);
   A.real_list = X.real_list.as<int>();
   A.xflags = X.cell_flags.as<int>();
-  A.n_real = (int)X.n_real_cells;
+  A.n_real_dev = X.real_scan.as<int>() + X.ncells;
   A.self = (h.nsets == 1);
   A.split = (h.precision == 1);
   A.op = op;
@@ -1123,7 +1124,8 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
     CLM_CUDA_TRY(h, cudaStreamSynchronize(h.stream));  // the host vector b goes out of scope
   }
   // grid: static round-robin of real cells over warps (deterministic)
-  const int grid_want = (int)std::max<int64_t>(1, std::min<int64_t>((A.n_real + kWarps - 1) / kWarps, 1 << 16));
+  // the number of real cells is only known on the device: size for all cells (one resident wave at most)
+  const int grid_want = (int)std::max<int64_t>(1, std::min<int64_t>((X.ncells + kWarps - 1) / kWarps, 1 << 16));
   int grid = grid_want;
   // partials
   const size_t part_bytes = align(sizeof(double) * grid_want) + align(sizeof(unsigned long long) * grid_want) +
@@ -1239,13 +1241,26 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
         CLM_CUDA_TRY(h, cudaMemcpyAsync(O->forces_y, dst_y, sizeof(T) * ny * N, cudaMemcpyDeviceToHost, h.stream));
     }
   }
-  // scalar results
+  // scalar results (and the totals of a build enqueued without synchronization)
   char hostres[256 + 16 * 256];
   CLM_CUDA_TRY(h, cudaMemcpyAsync(hostres, res, sizeof(hostres), cudaMemcpyDeviceToHost, h.stream));
-  CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 4, h.err.p, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+  {
+    int st = enqueue_build_totals(h);
+    if (st) return st;
+  }
   CLM_CUDA_TRY(h, cudaStreamSynchronize(h.stream));
   cudaEventElapsedTime(&h.map_ms, h.ev[2], h.ev[3]);
-  if (h.pinned[4] & DERR_CELL_RANGE) {
+  if (h.build_timing_pending) {
+    cudaEventElapsedTime(&h.build_ms, h.ev[0], h.ev[1]);
+    h.build_timing_pending = false;
+  }
+  {
+    bool overflow = false;
+    int st = check_build_totals(h, &overflow);
+    if (st) return st;
+    if (overflow) return RERUN_BUILD;
+  }
+  if (h.pinned[40] & DERR_CELL_RANGE) {
     h.last_error = "pair map consistency check failed (stencil cell outside the grid)";
     return ERR_INTERNAL;
   }
@@ -1314,7 +1329,7 @@ int run_pairs_scalar_scratch(Handle& h, const Geometry<T>& g, int op, const void
   A.Y = view_of<T>(Y);
   A.real_list = X.real_list.as<int>();
   A.xflags = X.cell_flags.as<int>();
-  A.n_real = (int)X.n_real_cells;
+  A.n_real_dev = X.real_scan.as<int>() + X.ncells;
   A.self = (h.nsets == 1);
   A.split = (h.precision == 1);
   A.op = op;
@@ -1409,7 +1424,7 @@ int pairs_scalar_blocks_needed(Handle& h, int op) {
     cudaGetLastError();
     return -1;
   }
-  const int64_t want = std::max<int64_t>(1, (h.sets[0].n_real_cells + kWarps - 1) / kWarps);
+  const int64_t want = std::max<int64_t>(1, (h.sets[0].ncells + kWarps - 1) / kWarps);
   return (int)std::min<int64_t>(want, (int64_t)per_sm * sms);
 }
 

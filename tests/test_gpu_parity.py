@@ -301,3 +301,21 @@ def test_determinism(clm):
     e2 = clm.pairwise(clm.SoftEnergy(), s)
     assert e1 == e2  # fixed-order reductions: bitwise reproducible
     s.close()
+
+
+@pytest.mark.parametrize("via_run", [False, True])
+def test_copy_capacity_overflow_rebuilds(clm, orc, via_run):
+    """Particles packed in a corner have 7 images each, far above the uniform-density capacity estimate:
+    the build must detect the overflow on the device and repeat with the exact size."""
+    rng = np.random.default_rng(4)
+    x = 0.05 + 0.04 * rng.random((6000, 3))
+    uc = [10.0, 10.0, 10.0]
+    s = clm.ParticleSystem(xpositions=x[:10], unitcell=uc, cutoff=1.0)
+    s.update(xpositions=x)  # dirty: the next pairwise builds without waiting for the device
+    if not via_run:
+        s.build()
+    got = clm.pairwise(clm.NeighborList(), s)
+    ref = orc.run("nl", x, unitcell=uc, cutoff=1.0)
+    assert_same_pairs(orc, got, ref)
+    assert s.celllist_info()["n_particles"] == 8 * len(x)
+    s.close()
