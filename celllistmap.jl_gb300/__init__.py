@@ -13,6 +13,7 @@ from . import api as _api
 from .api import (ArgumentError, Box, CUDAError, DimensionMismatch, EnergyAndForces, InPlaceNeighborList,
                   ParticleSystem, neighborlist, neighborlist_, pairwise, pairwise_, update, version)
 from . import api as ops  # operator classes live in api; exposed as `ops`
+from . import workloads
 
 Count = _api.Count
 SumD2 = _api.SumD2
@@ -22,6 +23,7 @@ SoftEnergy = _api.SoftEnergy
 SoftForces = _api.SoftForces
 LennardJones = _api.LennardJones
 LennardJonesForces = _api.LennardJonesForces
+LennardJonesAdjoint = _api.LennardJonesAdjoint
 InverseDistanceForces = _api.InverseDistanceForces
 MinimumDistance = _api.MinimumDistance
 RadialHistogram = _api.RadialHistogram
@@ -30,7 +32,7 @@ NeighborList = _api.NeighborList
 __all__ = [
     "ArgumentError", "Box", "CUDAError", "DimensionMismatch", "EnergyAndForces", "InPlaceNeighborList",
     "ParticleSystem", "neighborlist", "neighborlist_", "pairwise", "pairwise_", "update", "version", "ops",
-    "Count", "SumD2", "SumD", "SumInvD", "SoftEnergy", "SoftForces", "LennardJones", "LennardJonesForces",
+    "Count", "SumD2", "SumD", "SumInvD", "SoftEnergy", "SoftForces", "LennardJones", "LennardJonesForces", "LennardJonesAdjoint",
     "InverseDistanceForces", "MinimumDistance", "RadialHistogram", "NeighborList",
 ]
 

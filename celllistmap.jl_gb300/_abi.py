@@ -18,7 +18,7 @@ CLM_ORTHO, CLM_TRICLINIC, CLM_NONPERIODIC = 0, 1, 2
 CLM_PREC_EXACT, CLM_PREC_SPLIT = 0, 1
 OP = {
     "nl": 1, "count": 2, "sum_d2": 3, "sum_d": 4, "sum_inv_d": 5, "soft_energy": 6, "soft_forces": 7,
-    "lj_energy": 8, "lj_forces": 9, "mindist": 10, "rhist": 11, "inv_d_forces": 12,
+    "lj_energy": 8, "lj_forces": 9, "mindist": 10, "rhist": 11, "inv_d_forces": 12, "lj_adjoint": 13,
 }
 STATUS = {
     0: "CLM_OK", 1: "CLM_ERR_ARG", 2: "CLM_ERR_CELL_TOO_SMALL", 3: "CLM_ERR_NAN", 4: "CLM_ERR_DIM",
@@ -45,7 +45,7 @@ class Outputs(C.Structure):
     _fields_ = [("scalar", C.c_double), ("count", C.c_int64), ("min_i", C.c_int64), ("min_j", C.c_int64),
                 ("min_d", C.c_double), ("forces_x", C.c_void_p), ("forces_y", C.c_void_p),
                 ("hist_count", C.c_void_p), ("hist_sum", C.c_void_p), ("out_on_device", C.c_int32),
-                ("index_base", C.c_int32)]
+                ("index_base", C.c_int32), ("adjoint", C.c_void_p)]
 
 
 _lib = None

@@ -172,6 +172,65 @@ class LennardJonesForces(_ForcesOp, LennardJones):
     op = "lj_forces"
 
 
+@dataclass
+class LJAdjoint:
+    """Energy of a Lennard-Jones system and its adjoint (gradients of U)."""
+    energy: float
+    forces: Any              # -dU/dx (n x dim)
+    virial: Any              # W = sum g dx dx^T, g = u'(r)/r (dim x dim)
+    dU_dcell: Any            # dU/dM = W M^-T for the cell matrix M, scaled coordinates fixed (periodic cells)
+    dU_deps: Any             # per type pair (ntypes x ntypes, symmetric) or scalar
+    dU_dsigma: Any
+
+    @property
+    def grad_positions(self):
+        return -np.asarray(self.forces)
+
+    def dU_dL(self, L):
+        """Derivative w.r.t. the side of a cubic box (all sides scaled together)."""
+        return float(np.trace(self.virial)) / float(L)
+
+
+class LennardJonesAdjoint(LennardJones):
+    """Energy, forces and the adjoint of U w.r.t. the cell matrix and the per-type eps/sigma (at most 2
+    types).  No reference counterpart: the reference differentiates closures with ForwardDiff
+    (test/examples/generic_types.jl:10-20,102)."""
+    op = "lj_adjoint"
+
+    def outputs(self, system):
+        o = _abi.Outputs()
+        fx = np.zeros((system.n_x, system.dim), dtype=system.dtype)
+        adj = np.zeros(32, np.float64)
+        o.forces_x = fx.ctypes.data
+        o.adjoint = adj.ctypes.data
+        return o, {"fx": fx, "adj": adj}
+
+    def result(self, system, out, bufs):
+        adj = bufs["adj"]
+        d = system.dim
+        W = adj[:9].reshape(3, 3)[:d, :d].copy()
+        nt = 0 if self.types_x is None else int(np.asarray(self.eps_table).shape[0])
+        ncls = nt * (nt + 1) // 2 if nt else 1
+        de, ds = adj[9:9 + ncls], adj[9 + ncls:9 + 2 * ncls]
+        if nt:
+            tde = np.zeros((nt, nt))
+            tds = np.zeros((nt, nt))
+            k = 0
+            for a in range(nt):
+                for b in range(a, nt):
+                    tde[a, b] = tde[b, a] = de[k]
+                    tds[a, b] = tds[b, a] = ds[k]
+                    k += 1
+            de, ds = tde, tds
+        else:
+            de, ds = float(de[0]), float(ds[0])
+        dcell = None
+        if system.unitcell is not None:
+            _, M = _cell_kind_and_matrix(system.unitcell, d)
+            dcell = W @ np.linalg.inv(M).T
+        return LJAdjoint(out.scalar, bufs["fx"], W, dcell, de, ds)
+
+
 class InverseDistanceForces(_ForcesOp):
     """energy += 1/d, forces[i] += (y - x)/d^3, forces[j] -= (y - x)/d^3 (the gradient convention of
     docs/src/ParticleSystem/single_set_compound.md:79-86).  Returned forces follow that convention."""
@@ -251,7 +310,8 @@ class NeighborList(Operator):
 
 
 OPERATORS = {c.op: c for c in [Count, SumD2, SumD, SumInvD, SoftEnergy, SoftForces, LennardJones, LennardJonesForces,
-                               InverseDistanceForces, MinimumDistance, RadialHistogram, NeighborList]}
+                               LennardJonesAdjoint, InverseDistanceForces, MinimumDistance, RadialHistogram,
+                               NeighborList]}
 
 
 # ---------------------------------------------------------------------------- helpers

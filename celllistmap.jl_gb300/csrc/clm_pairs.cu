@@ -91,6 +91,7 @@ template <class T> struct PairArgs {
   int* part_min_ij;
   unsigned long long* part_hc;  // nbins per block
   double* part_hs;              // nbins per block
+  double* part_v;               // kAdjVals per block (adjoint)
 };
 
 __device__ __forceinline__ void stencil_offset(bool forward, int l, int dim, int k, int* o) {
@@ -154,7 +155,8 @@ template <class A> struct Acc {
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
-enum OpKind { OPK_NL = 0, OPK_SCALAR = 1, OPK_FORCES = 2, OPK_MIN = 3, OPK_HIST = 4 };
+enum OpKind { OPK_NL = 0, OPK_SCALAR = 1, OPK_FORCES = 2, OPK_MIN = 3, OPK_HIST = 4, OPK_ADJ = 5 };
+constexpr int kAdjVals = 13;  // energy, virial (xx yy zz xy xz yz), dU/deps[3], dU/dsigma[3]
 
 // Reciprocal and reciprocal square root for pair VALUES (energies, forces), which are checked against
 // tolerances, never used for pair membership or neighbour-list distances.
@@ -216,7 +218,8 @@ __device__ __forceinline__ void pair_value(const PairArgs<T>& A, int op, V d2, i
       break;
     }
     case 8:
-    case 9: {  // LJ eps*(c12 (s/d)^12 - c6 (s/d)^6)
+    case 9:
+    case 13: {  // LJ eps*(c12 (s/d)^12 - c6 (s/d)^6)
       V eps = (V)A.p[0], sig = (V)A.p[1];
       if (A.ntypes > 0) {
         int ti = A.tx[i];
@@ -296,7 +299,8 @@ template <class T, int N, int OPK, bool SPLIT, bool CROSS>
 __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(const PairArgs<T> A) {
   using V = T;
   using FA = typename std::conditional<std::is_same<T, double>::value && !SPLIT, double, float>::type;
-  constexpr bool OWNER = (OPK == OPK_FORCES) && !CROSS;
+  constexpr bool IS_F = (OPK == OPK_FORCES) || (OPK == OPK_ADJ);
+  constexpr bool OWNER = IS_F && !CROSS;
   constexpr bool FP64 = std::is_same<T, double>::value;
   constexpr bool ABS_PF = !FP64 && !SPLIT;  // FP32 exact form: the prefilter uses the coordinates themselves
   constexpr int JC = 128;                   // staging capacity: 32 candidates per lane group (G <= 4)
@@ -315,7 +319,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
   __shared__ T s_ix[kWarps][3][32];              // particles of the current chunk of the cell
   __shared__ float s_ipf[kWarps][3][32];
   __shared__ int s_icode[kWarps][32];
-  __shared__ FA s_if[kWarps][3][(OPK == OPK_FORCES) ? 32 : 1];  // force sums of those particles
+  __shared__ FA s_if[kWarps][3][IS_F ? 32 : 1];  // force sums of those particles
   __shared__ unsigned int s_hc[(OPK == OPK_HIST) ? 256 : 1];  // block-wide histogram
   __shared__ double s_hs[(OPK == OPK_HIST) ? 256 : 1];
   __shared__ double s_red[kWarps];
@@ -341,6 +345,9 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
 
   double e_tot = 0.0;  // per-lane energy (FP64); FP32 partial sums are folded in per particle chunk
   FA e_part = 0;
+  FA adj[kAdjVals - 1];  // adjoint accumulators: virial (6), dU/deps (3), dU/dsigma (3)
+#pragma unroll
+  for (int k = 0; k < kAdjVals - 1; k++) adj[k] = FA(0);
   unsigned long long c_acc = 0;
   T best_d2 = INFINITY;
   int best_i = 0x7fffffff, best_j = 0x7fffffff;
@@ -390,7 +397,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
         for (int d = 0; d < 3; d++) {
           s_ix[warp][d][il] = xi[d];
           s_ipf[warp][d][il] = pi[d];
-          if constexpr (OPK == OPK_FORCES) s_if[warp][d][il] = FA(0);
+          if constexpr (IS_F) s_if[warp][d][il] = FA(0);
         }
         s_icode[warp][il] = code_i;
       }
@@ -647,24 +654,58 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
                   e_part += (FA)uu;
                 }
               }
-            } else if constexpr (OPK == OPK_FORCES) {
+            } else if constexpr (IS_F) {
               if (hit) {
                 FA uu, gg;
                 FA df[3] = {0, 0, 0};
+                FA dv[3] = {0, 0, 0};
                 if (sure) {
                   float uf, gf;
                   pair_value<float, T>(A, A.op, d2f, idx_i, idx_j, uf, gf);
                   uu = (FA)uf;
                   gg = (FA)gf;
 #pragma unroll
-                  for (int d = 0; d < N; d++) df[d] = gg * (FA)dvf[d];
+                  for (int d = 0; d < N; d++) dv[d] = (FA)dvf[d];
                 } else {
                   V uv, gv;
                   pair_value<V, T>(A, A.op, (V)d2, idx_i, idx_j, uv, gv);
                   uu = (FA)uv;
                   gg = (FA)gv;
 #pragma unroll
-                  for (int d = 0; d < N; d++) df[d] = gg * (FA)xsub(xi[d], xj[d]);
+                  for (int d = 0; d < N; d++) dv[d] = (FA)xsub(xi[d], xj[d]);
+                }
+#pragma unroll
+                for (int d = 0; d < N; d++) df[d] = gg * dv[d];
+                if constexpr (OPK == OPK_ADJ) {
+                  if (count_e) {
+                    // virial W += g dx dx^T (g = u'(r)/r), and the parameter derivatives of the LJ term
+                    adj[0] += gg * dv[0] * dv[0];
+                    adj[1] += gg * dv[1] * dv[1];
+                    adj[2] += gg * dv[2] * dv[2];
+                    adj[3] += gg * dv[0] * dv[1];
+                    adj[4] += gg * dv[0] * dv[2];
+                    adj[5] += gg * dv[1] * dv[2];
+                    FA eps = (FA)A.p[0], sig = (FA)A.p[1];
+                    int cls = 0;
+                    if (A.ntypes > 0) {
+                      const int ti = A.tx[idx_i], tj = A.tx[idx_j];
+                      eps = (FA)A.eps_t[ti * A.ntypes + tj];
+                      sig = (FA)A.sig_t[ti * A.ntypes + tj];
+                      cls = ti + tj;  // 2 types: AA = 0, AB = 1, BB = 2
+                    }
+                    const FA c12 = (FA)A.p[2], c6 = (FA)A.p[3];
+                    const FA dd2 = sure ? (FA)d2f : (FA)d2;
+                    const FA sr2 = sig * sig / dd2;
+                    const FA sr6 = sr2 * sr2 * sr2;
+                    const FA sr12 = sr6 * sr6;
+                    const FA lj = c12 * sr12 - c6 * sr6;
+                    const FA dsg = eps * (FA(12) * c12 * sr12 - FA(6) * c6 * sr6) / sig;
+#pragma unroll
+                    for (int k = 0; k < 3; k++) {
+                      adj[6 + k] += (cls == k) ? lj : FA(0);
+                      adj[9 + k] += (cls == k) ? dsg : FA(0);
+                    }
+                  }
                 }
                 if (ie != cur) {
                   if (cur >= 0) {
@@ -770,7 +811,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
               }
             }
           }
-          if constexpr (OPK == OPK_FORCES) {
+          if constexpr (IS_F) {
             if (cur >= 0) {
 #pragma unroll
               for (int d = 0; d < N; d++) atomicAdd(&s_if[warp][d][cur], acc[d]);
@@ -782,7 +823,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
       }
       e_tot += (double)e_part;
       e_part = 0;
-      if constexpr (OPK == OPK_FORCES) {
+      if constexpr (IS_F) {
         __syncwarp();
         if (grp == 0 && vi) {
           FA f[3] = {s_if[warp][0][il], s_if[warp][1][il], s_if[warp][2][il]};
@@ -824,6 +865,27 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
       }
       A.part_e[blockIdx.x] = es;
       A.part_c[blockIdx.x] = cs;
+    }
+  } else if constexpr (OPK == OPK_ADJ) {
+    __shared__ double s_adj[kWarps][kAdjVals];
+    double v[kAdjVals];
+    v[0] = e_tot;
+#pragma unroll
+    for (int k = 1; k < kAdjVals; k++) v[k] = (double)adj[k - 1];
+#pragma unroll
+    for (int k = 0; k < kAdjVals; k++) {
+#pragma unroll
+      for (int s = 16; s > 0; s >>= 1) v[k] += __shfl_xor_sync(FULL, v[k], s);
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < kAdjVals; k++) s_adj[warp][k] = v[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < kAdjVals) {
+      double acc = 0;
+      for (int w = 0; w < kWarps; w++) acc += s_adj[w][threadIdx.x];
+      A.part_v[(int64_t)blockIdx.x * kAdjVals + threadIdx.x] = acc;
     }
   } else if constexpr (OPK == OPK_MIN) {
 #pragma unroll
@@ -914,6 +976,14 @@ __global__ void k_reduce_min(const T* __restrict__ pd, const int* __restrict__ p
   out_ij[1] = bj;
 }
 
+__global__ void k_reduce_vec(const double* __restrict__ pv, int nb, int k, double* __restrict__ out) {
+  const int c = threadIdx.x;
+  if (c >= k) return;
+  double s = 0;
+  for (int b = 0; b < nb; b++) s += pv[(int64_t)b * k + c];
+  out[c] = s;
+}
+
 __global__ void k_reduce_hist(const unsigned long long* __restrict__ pc, const double* __restrict__ ps, int nb,
                               int nbins, unsigned long long* oc, double* os) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -968,6 +1038,7 @@ inline int opkind_of(int op) {
     case 1: return OPK_NL;
     case 2: case 3: case 4: case 5: case 6: case 8: return OPK_SCALAR;
     case 7: case 9: case 12: return OPK_FORCES;
+    case 13: return OPK_ADJ;
     case 10: return OPK_MIN;
     case 11: return OPK_HIST;
     default: return -1;
@@ -1007,6 +1078,9 @@ cudaError_t launch_s(int opk, int& grid, cudaStream_t st, const PairArgs<T>& A) 
     case OPK_FORCES: return launch_k<T, N, OPK_FORCES, SPLIT, CROSS>(grid, st, A);
     case OPK_MIN: return launch_k<T, N, OPK_MIN, SPLIT, CROSS>(grid, st, A);
     case OPK_HIST: return launch_k<T, N, OPK_HIST, SPLIT, CROSS>(grid, st, A);
+    case OPK_ADJ:
+      if constexpr (!CROSS) return launch_k<T, N, OPK_ADJ, SPLIT, false>(grid, st, A);
+      return cudaErrorInvalidValue;
   }
   return cudaErrorInvalidValue;
 }
@@ -1059,8 +1133,22 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
   size_t need = 0;
   auto align = [](size_t v) { return (v + 255) & ~(size_t)255; };
   const int64_t nx = X.n, ny = (h.nsets == 2) ? Y.n : 0;
-  const bool types = P && (op == 8 || op == 9) && P->ntypes > 0;
+  const bool types = P && (op == 8 || op == 9 || op == 13) && P->ntypes > 0;
   const bool hist = (op == 11);
+  if (opk == OPK_ADJ) {
+    if (h.nsets != 1) {
+      h.last_error = "the LJ adjoint is defined for a single set of particles";
+      return ERR_ARG;
+    }
+    if (P && P->ntypes > 2) {
+      h.last_error = "the LJ adjoint supports at most 2 particle types";
+      return ERR_ARG;
+    }
+    if (!O->adjoint) {
+      h.last_error = "the LJ adjoint needs clm_outputs.adjoint (9 + 2 x type classes doubles)";
+      return ERR_ARG;
+    }
+  }
   if (types) {
     if (!P->types_x || !P->eps_table || !P->sig_table || (h.nsets == 2 && !P->types_y)) {
       h.last_error = "LJ with types needs types_x (types_y), eps_table and sig_table";
@@ -1132,7 +1220,7 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
                             align(sizeof(T) * grid_want) + align(sizeof(int) * 2 * grid_want) +
                             (hist ? align(sizeof(unsigned long long) * grid_want * A.nbins) +
                                         align(sizeof(double) * grid_want * A.nbins) : 0) +
-                            4 * align(sizeof(double) * 512);
+                            align(sizeof(double) * kAdjVals * grid_want) + 4 * align(sizeof(double) * 512);
   if (!h.partial.reserve(part_bytes)) return ERR_NOMEM;
   char* pb = h.partial.as<char>();
   at = 0;
@@ -1150,6 +1238,8 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
     A.part_hs = (double*)(pb + at);
     at += align(sizeof(double) * grid_want * A.nbins);
   }
+  A.part_v = (double*)(pb + at);
+  at += align(sizeof(double) * kAdjVals * grid_want);
   char* res = pb + at;  // final results
   double* r_e = (double*)res;
   unsigned long long* r_c = (unsigned long long*)(res + 8);
@@ -1158,7 +1248,8 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
   unsigned long long* r_hc = (unsigned long long*)(res + 256);
   double* r_hs = (double*)(res + 256 + 8 * 256);
   // outputs
-  const bool forces = (opk == OPK_FORCES);
+  const bool forces = (opk == OPK_FORCES || opk == OPK_ADJ);
+  double* r_v = (double*)(res + 256 + 16 * 256);  // adjoint sums (kAdjVals)
   if (forces) {
     size_t fb = sizeof(double) * (nx + ny) * N;
     if (!h.outbuf.reserve(fb + sizeof(T) * (nx + ny) * N + 256)) return ERR_NOMEM;
@@ -1201,7 +1292,9 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
     if ((int64_t)n_pairs <= h.nl_cap) break;
     h.nl_cap = (int64_t)n_pairs + n_pairs / 16 + 1024;  // retry once with the exact size
   }
-  if (opk == OPK_SCALAR || opk == OPK_FORCES) {
+  if (opk == OPK_ADJ) {
+    k_reduce_vec<<<1, 32, 0, h.stream>>>(A.part_v, grid, kAdjVals, r_v);
+  } else if (opk == OPK_SCALAR || opk == OPK_FORCES) {
     k_reduce_scalar<<<1, 256, 0, h.stream>>>(A.part_e, A.part_c, grid, r_e, r_c);
   } else if (opk == OPK_MIN) {
     k_reduce_min<T><<<1, 32, 0, h.stream>>>(A.part_min_d2, A.part_min_ij, grid, r_md, r_mij);
@@ -1242,7 +1335,7 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
     }
   }
   // scalar results (and the totals of a build enqueued without synchronization)
-  char hostres[256 + 16 * 256];
+  char hostres[256 + 16 * 256 + 128];
   CLM_CUDA_TRY(h, cudaMemcpyAsync(hostres, res, sizeof(hostres), cudaMemcpyDeviceToHost, h.stream));
   {
     int st = enqueue_build_totals(h);
@@ -1286,6 +1379,32 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
       O->min_d = (double)std::sqrt(md);
       O->min_i = mij[0] + O->index_base;
       O->min_j = mij[1] + O->index_base;
+    }
+  }
+  if (opk == OPK_ADJ) {
+    double v[kAdjVals];
+    std::memcpy(v, hostres + 256 + 16 * 256, sizeof(v));
+    O->scalar = v[0];
+    // virial of the rotated frame -> original frame: W = Rinv W' Rinv^T
+    double Wp[3][3] = {{v[1], v[4], v[5]}, {v[4], v[2], v[6]}, {v[5], v[6], v[3]}};
+    double W[3][3];
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++) {
+        double acc = 0;
+        for (int c = 0; c < 3; c++)
+          for (int d = 0; d < 3; d++) {
+            double ra = (a < N && c < N) ? (double)g.Rinv[a][c] : (a == c ? 1.0 : 0.0);
+            double rb = (b < N && d < N) ? (double)g.Rinv[b][d] : (b == d ? 1.0 : 0.0);
+            acc += ra * Wp[c][d] * rb;
+          }
+        W[a][b] = acc;
+      }
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++) O->adjoint[a * 3 + b] = W[a][b];
+    const int ncls = (P && P->ntypes > 0) ? P->ntypes * (P->ntypes + 1) / 2 : 1;
+    for (int k = 0; k < ncls; k++) {
+      O->adjoint[9 + k] = v[7 + k];
+      O->adjoint[9 + ncls + k] = v[10 + k];
     }
   }
   if (opk == OPK_HIST) {

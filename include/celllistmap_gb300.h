@@ -66,7 +66,10 @@ enum clm_op_id {
   CLM_OP_LJ_FORCES = 9,      /* energy and forces of the same, per-type eps/sigma tables optional */
   CLM_OP_MINDIST = 10,       /* argmin d, test/examples/nearest_neighbor.jl:9-16,43 */
   CLM_OP_RHIST = 11,         /* radial histogram with per-bin velocity accumulator, test/examples/pairwise_velocities.jl:17-24 */
-  CLM_OP_INV_D_FORCES = 12   /* energy 1/d with gradient accumulation, docs/src/ParticleSystem/single_set_compound.md:79-86 */
+  CLM_OP_INV_D_FORCES = 12,  /* energy 1/d with gradient accumulation, docs/src/ParticleSystem/single_set_compound.md:79-86 */
+  CLM_OP_LJ_ADJOINT = 13     /* LJ energy, forces and the adjoint of the energy w.r.t. the cell and the per-type
+                                eps/sigma (no reference counterpart: the reference differentiates closures with
+                                ForwardDiff, test/examples/generic_types.jl:10-20,102) */
 };
 
 /* Precision forms of the map (see clm_set_precision). */
@@ -104,6 +107,10 @@ typedef struct {
   double* hist_sum;          /* nbins */
   int32_t out_on_device;
   int32_t index_base;        /* 0 or 1 for MINDIST indices */
+  double* adjoint;           /* LJ_ADJOINT (host): virial W = sum g dx dx^T (3x3 row-major, original frame;
+                                dU/dM = W M^-T for the cell matrix M with scaled coordinates fixed), then
+                                dU/deps and dU/dsigma per type pair (a <= b, row-major upper triangle; one
+                                entry without types).  Length 9 + 2 * ntypes (ntypes + 1) / 2 (or 11). */
 } clm_outputs;
 
 /* Handle lifecycle.  nsets = 1 (self pairs) or 2 (x-y cross pairs).

@@ -101,6 +101,7 @@ typedef struct {
   double min_d;
   int64_t* hist_count;
   double* hist_sum;
+  double adj[32];  // LJ adjoint: virial W (9, row-major), dU/deps (classes), dU/dsigma (classes)
 } orc_result;
 
 }  // extern "C"
@@ -111,7 +112,7 @@ enum { KIND_ORTHO = 0, KIND_TRI = 1, KIND_NONPER = 2 };
 enum {
   OP_NL = 1, OP_COUNT = 2, OP_SUM_D2 = 3, OP_SUM_D = 4, OP_SUM_INV_D = 5,
   OP_SOFT_ENERGY = 6, OP_SOFT_FORCES = 7, OP_LJ_ENERGY = 8, OP_LJ_FORCES = 9,
-  OP_MINDIST = 10, OP_RHIST = 11, OP_INV_D_FORCES = 12
+  OP_MINDIST = 10, OP_RHIST = 11, OP_INV_D_FORCES = 12, OP_LJ_ADJOINT = 13
 };
 enum {
   ERR_OK = 0, ERR_ARG = 1, ERR_CELL_TOO_SMALL = 2, ERR_NAN = 3, ERR_DIM = 4,
@@ -598,6 +599,7 @@ struct Local {
   int64_t min_i = -1, min_j = -1;
   std::vector<int64_t> hc;
   std::vector<Acc> hs;
+  Acc adj[15];
 };
 
 template <class T, int N> struct OpCtx {
@@ -658,7 +660,8 @@ inline void apply_op(const OpCtx<T, N>& ctx, Local& L, int64_t i, int64_t j, con
       break;
     }
     case OP_LJ_ENERGY:
-    case OP_LJ_FORCES: {
+    case OP_LJ_FORCES:
+    case OP_LJ_ADJOINT: {
       double eps = op->p[0], sig = op->p[1];
       if (op->ntypes > 0) {
         int ti = op->types_x[i];
@@ -671,7 +674,22 @@ inline void apply_op(const OpCtx<T, N>& ctx, Local& L, int64_t i, int64_t j, con
       double sr6 = sr2 * sr2 * sr2;
       double sr12 = sr6 * sr6;
       L.energy.add(eps * (c12 * sr12 - c6 * sr6));
-      if (code == OP_LJ_FORCES) {
+      if (code == OP_LJ_ADJOINT) {
+        // adjoint of U: virial W = sum g dx dx^T with g = u'(r)/r; dU/deps and dU/dsigma per type pair
+        double g = eps * (-12.0 * c12 * sr12 + 6.0 * c6 * sr6) / dd2;
+        for (int a = 0; a < N; a++)
+          for (int b = 0; b < N; b++) L.adj[a * 3 + b].add(g * dv[a] * dv[b]);
+        int cls = 0;
+        if (op->ntypes > 0) {
+          int ti = op->types_x[i];
+          int tj = ctx.cross ? op->types_y[j] : op->types_x[j];
+          int a = ti < tj ? ti : tj, b = ti < tj ? tj : ti;
+          cls = a * op->ntypes - a * (a - 1) / 2 + (b - a);  // upper triangle, row-major
+        }
+        L.adj[9 + cls].add(c12 * sr12 - c6 * sr6);
+        L.adj[12 + cls].add(eps * (12.0 * c12 * sr12 - 6.0 * c6 * sr6) / sig);
+      }
+      if (code == OP_LJ_FORCES || code == OP_LJ_ADJOINT) {
         double g = eps * (-12.0 * c12 * sr12 + 6.0 * c6 * sr6) / dd2;  // (du/dr)/r
         for (int k = 0; k < N; k++) {
           double df = g * dv[k];
@@ -852,7 +870,8 @@ template <class T, int N> void stencil(const Box<T, N>& B, bool forward, std::ve
 
 template <class T, int N> void alloc_local(Local& L, const orc_op* op, int64_t nx, int64_t ny, bool cross) {
   L.energy.comp = op->compensated != 0;
-  if (op->op == OP_SOFT_FORCES || op->op == OP_LJ_FORCES || op->op == OP_INV_D_FORCES) {
+  for (auto& a : L.adj) a.comp = op->compensated != 0;
+  if (op->op == OP_SOFT_FORCES || op->op == OP_LJ_FORCES || op->op == OP_INV_D_FORCES || op->op == OP_LJ_ADJOINT) {
     Acc z; z.comp = op->compensated != 0;
     L.fx.assign((size_t)(nx * N), z);
     if (cross) L.fy.assign((size_t)(ny * N), z);
@@ -968,6 +987,11 @@ int run_map(const orc_spec* s, const T* x, int64_t nx, const T* y, int64_t ny, c
   }
   res->scalar = e.value();
   res->count = cnt;
+  for (int k = 0; k < 15; k++) {
+    Acc a; a.comp = op->compensated != 0;
+    for (auto& L : locals) a.add(L.adj[k].value());
+    res->adj[k] = a.value();
+  }
   if (!locals[0].fx.empty()) {
     for (int64_t q = 0; q < nx * N; q++) {
       Acc a; a.comp = op->compensated != 0;
@@ -1054,6 +1078,7 @@ int run_naive(const orc_spec* s, const T* x, int64_t nx, const T* y, int64_t ny,
   }
   res->scalar = L.energy.value();
   res->count = L.count;
+  for (int k = 0; k < 15; k++) res->adj[k] = L.adj[k].value();
   res->nl_n = (int64_t)L.ni.size();
   for (size_t q = 0; q < L.ni.size() && (int64_t)q < res->nl_cap; q++) {
     res->nl_i[q] = L.ni[q]; res->nl_j[q] = L.nj[q]; res->nl_d[q] = L.nd[q];

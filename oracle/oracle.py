@@ -25,7 +25,7 @@ KIND = {"ortho": 0, "orthorhombic": 0, "tri": 1, "triclinic": 1, "nonperiodic": 
 OPS = {
     "nl": 1, "count": 2, "sum_d2": 3, "sum_d": 4, "sum_inv_d": 5,
     "soft_energy": 6, "soft_forces": 7, "lj_energy": 8, "lj_forces": 9,
-    "mindist": 10, "rhist": 11, "inv_d_forces": 12,
+    "mindist": 10, "rhist": 11, "inv_d_forces": 12, "lj_adjoint": 13,
 }
 ERRORS = {1: "invalid argument", 2: "unit cell too small for cutoff", 3: "invalid (NaN) coordinates",
           4: "dimension mismatch", 6: "capacity", 10: "lcell must be >= 1"}
@@ -60,7 +60,7 @@ class _Result(C.Structure):
     _fields_ = [("nl_cap", C.c_int64), ("nl_n", C.c_int64), ("nl_i", C.c_void_p), ("nl_j", C.c_void_p),
                 ("nl_d", C.c_void_p), ("scalar", C.c_double), ("count", C.c_int64), ("forces_x", C.c_void_p),
                 ("forces_y", C.c_void_p), ("min_i", C.c_int64), ("min_j", C.c_int64), ("min_d", C.c_double),
-                ("hist_count", C.c_void_p), ("hist_sum", C.c_void_p)]
+                ("hist_count", C.c_void_p), ("hist_sum", C.c_void_p), ("adj", C.c_double * 32)]
 
 
 _lib = None
@@ -231,7 +231,7 @@ def run(op, x, y=None, *, dim=3, kind="ortho", unitcell=None, cutoff, lcell=1, d
             n = r.nl_n
             return {"i": ni[:n].copy(), "j": nj[:n].copy(), "d": nd[:n].copy()}
     fx = fy = hc = hs = None
-    if o.op in (OPS["soft_forces"], OPS["lj_forces"], OPS["inv_d_forces"]):
+    if o.op in (OPS["soft_forces"], OPS["lj_forces"], OPS["inv_d_forces"], OPS["lj_adjoint"]):
         fx = np.zeros((nx, dim), np.float64)
         r.forces_x = fx.ctypes.data
         if ya is not None:
@@ -253,6 +253,12 @@ def run(op, x, y=None, *, dim=3, kind="ortho", unitcell=None, cutoff, lcell=1, d
             out["forces_y"] = fy
     if o.op == OPS["mindist"]:
         out["min"] = (r.min_i, r.min_j, r.min_d)
+    if o.op == OPS["lj_adjoint"]:
+        nt = o.ntypes
+        ncls = nt * (nt + 1) // 2 if nt > 0 else 1
+        out["virial"] = np.array(r.adj[:9]).reshape(3, 3)[:dim, :dim].copy()
+        out["deps"] = np.array(r.adj[9:9 + ncls])
+        out["dsig"] = np.array(r.adj[12:12 + ncls])
     if hc is not None:
         out["hist_count"], out["hist_sum"] = hc, hs
     return out
