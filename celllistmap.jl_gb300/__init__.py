@@ -10,7 +10,7 @@ importlib (see ``tests/conftest.py``).
 """
 from . import _abi
 from . import api as _api
-from .api import (ArgumentError, Box, CUDAError, DimensionMismatch, EnergyAndForces, InPlaceNeighborList,
+from .api import (ArgumentError, BatchedSystems, Box, CUDAError, DimensionMismatch, EnergyAndForces, InPlaceNeighborList,
                   ParticleSystem, neighborlist, neighborlist_, pairwise, pairwise_, update, version)
 from . import api as ops  # operator classes live in api; exposed as `ops`
 from . import workloads
@@ -30,7 +30,7 @@ RadialHistogram = _api.RadialHistogram
 NeighborList = _api.NeighborList
 
 __all__ = [
-    "ArgumentError", "Box", "CUDAError", "DimensionMismatch", "EnergyAndForces", "InPlaceNeighborList",
+    "ArgumentError", "BatchedSystems", "Box", "CUDAError", "DimensionMismatch", "EnergyAndForces", "InPlaceNeighborList",
     "ParticleSystem", "neighborlist", "neighborlist_", "pairwise", "pairwise_", "update", "version", "ops",
     "Count", "SumD2", "SumD", "SumInvD", "SoftEnergy", "SoftForces", "LennardJones", "LennardJonesForces", "LennardJonesAdjoint",
     "InverseDistanceForces", "MinimumDistance", "RadialHistogram", "NeighborList",

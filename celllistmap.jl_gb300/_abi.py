@@ -30,7 +30,9 @@ STATUS = {
 EXPORTS = [
     "clm_create", "clm_destroy", "clm_set_stream", "clm_set_box", "clm_set_positions", "clm_build",
     "clm_set_precision", "clm_run", "clm_run_noalloc", "clm_nl_count", "clm_nl_fetch", "clm_get_box", "clm_get_celllist_info",
-    "clm_fetch_celllist", "clm_last_timings", "clm_stats", "clm_last_error", "clm_version",
+    "clm_fetch_celllist", "clm_last_timings", "clm_lj_adjoint", "clm_batched_create", "clm_batched_set_systems",
+    "clm_batched_run", "clm_batched_status", "clm_batched_set_graph", "clm_batched_set_config",
+    "clm_batched_autotune", "clm_batched_last_step", "clm_stats", "clm_last_error", "clm_version",
 ]
 
 
@@ -46,6 +48,11 @@ class Outputs(C.Structure):
                 ("min_d", C.c_double), ("forces_x", C.c_void_p), ("forces_y", C.c_void_p),
                 ("hist_count", C.c_void_p), ("hist_sum", C.c_void_p), ("out_on_device", C.c_int32),
                 ("index_base", C.c_int32), ("adjoint", C.c_void_p)]
+
+
+class BatchOutputs(C.Structure):
+    _fields_ = [("scalar", C.c_void_p), ("count", C.c_void_p), ("forces", C.c_void_p), ("out_on_device", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 _lib = None
@@ -69,6 +76,15 @@ def _declare(L):
     L.clm_get_celllist_info.argtypes = [vp, i32, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)]
     L.clm_fetch_celllist.argtypes = [vp, i32, i64, vp, vp, vp, vp, i32]
     L.clm_last_timings.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    L.clm_lj_adjoint.argtypes = [vp, C.POINTER(OpParams), C.POINTER(Outputs)]
+    L.clm_batched_create.argtypes = [i32, i32, C.POINTER(vp)]
+    L.clm_batched_set_systems.argtypes = [vp, i64, vp, vp, i32, C.c_double, i32]
+    L.clm_batched_run.argtypes = [vp, i32, vp, vp, vp]
+    L.clm_batched_status.argtypes = [vp, vp, i64]
+    L.clm_batched_set_graph.argtypes = [vp, i32]
+    L.clm_batched_set_config.argtypes = [vp, i32, i32, i32]
+    L.clm_batched_autotune.argtypes = [vp, i32, vp, vp, i32, vp, C.POINTER(C.c_float)]
+    L.clm_batched_last_step.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(i64)]
     L.clm_stats.argtypes = [vp, C.POINTER(i64)]
     L.clm_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
     for name in EXPORTS:

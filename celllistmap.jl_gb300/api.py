@@ -656,6 +656,170 @@ def neighborlist(*, xpositions=None, positions=None, ypositions=None, cutoff, un
 
 
 # ---------------------------------------------------------------------------- Box / CellList
+class BatchedSystems:
+    """Many independent periodic systems evaluated together: the loop
+    ``for sys in systems: pairwise!(f, sys)`` of the reference (src/API/pairwise.jl:48-63) as one build and one
+    launch per kernel for all systems, optionally replayed as a CUDA graph.
+
+    positions: a list of (n_s, dim) arrays, or one (n_total, dim) array (numpy or a torch CUDA tensor) with
+    ``offsets`` (n_sys + 1).  unitcells: (n_sys, dim) sides (orthorhombic) or (n_sys, dim, dim) matrices
+    (triclinic, columns are the cell vectors).  A system whose cell fails the reference's check
+    (Box.jl:243) gets status CLM_ERR_CELL_TOO_SMALL and NaN sums; the others are unaffected.
+    """
+
+    def __init__(self, *, positions, unitcells, cutoff, offsets=None, lcell: int = 1, dtype=None,
+                 precision: str = "exact", graph: bool = False):
+        uc = np.asarray(unitcells, dtype=np.float64)
+        if uc.ndim not in (2, 3):
+            raise ArgumentError("unitcells must be (nsys, dim) sides or (nsys, dim, dim) matrices")
+        self.dim = uc.shape[1]
+        if self.dim not in (2, 3) or (uc.ndim == 3 and uc.shape[2] != self.dim):
+            raise ArgumentError("unit cells must be 2x2 or 3x3 (or 2 / 3 sides)")
+        self.kind = _abi.CLM_ORTHO if uc.ndim == 2 else _abi.CLM_TRICLINIC
+        self.dtype = _promote_dtype(uc, cutoff, dtype)
+        if isinstance(positions, (list, tuple)):
+            arrs = [np.asarray(a, dtype=self.dtype).reshape(-1, self.dim) for a in positions]
+            sizes = [a.shape[0] for a in arrs]
+            offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+            positions = np.concatenate(arrs) if arrs else np.zeros((0, self.dim), self.dtype)
+        if offsets is None:
+            raise ArgumentError("offsets are required with concatenated positions")
+        self.offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        self.nsys = len(self.offsets) - 1
+        if uc.shape[0] != self.nsys:
+            raise DimensionMismatch("one unit cell per system is required")
+        self.cutoff = float(cutoff)
+        L = _abi.load()
+        h = C.c_void_p()
+        st = L.clm_batched_create(_abi.CLM_F64 if self.dtype == np.float64 else _abi.CLM_F32, self.dim, C.byref(h))
+        if st:
+            _raise(None, st)
+        self._handle = _Handle.__new__(_Handle)
+        self._handle.h, self._handle.L = h, L
+        # column-major cells per system (the ABI's layout)
+        self._cells = np.ascontiguousarray(uc if uc.ndim == 2 else np.transpose(uc, (0, 2, 1)))
+        self._handle.check(L.clm_batched_set_systems(h, self.nsys, self.offsets.ctypes.data, self._cells.ctypes.data,
+                                                     self.kind, self.cutoff, int(lcell)))
+        if precision != "exact":
+            self.set_precision(precision)
+        self.graph = graph
+        self.update(positions=positions)
+
+    @property
+    def graph(self) -> bool:
+        return self._graph
+
+    @graph.setter
+    def graph(self, on: bool):
+        self._handle.check(self._handle.L.clm_batched_set_graph(self._handle.h, 1 if on else 0))
+        self._graph = bool(on)
+
+    def set_precision(self, precision: str):
+        p = {"exact": _abi.CLM_PREC_EXACT, "split": _abi.CLM_PREC_SPLIT}[precision]
+        self._handle.check(self._handle.L.clm_set_precision(self._handle.h, p))
+
+    def set_config(self, lcell: int = 0, cell_split: int = 0, grid_div: int = 0):
+        self._handle.check(self._handle.L.clm_batched_set_config(self._handle.h, lcell, cell_split, grid_div))
+
+    def update(self, *, positions):
+        arr, n, dev, keep = _as_positions(positions, self.dim, self.dtype)
+        if n != int(self.offsets[-1]):
+            raise DimensionMismatch("positions do not match the systems' offsets")
+        ptr = arr.data_ptr() if hasattr(arr, "data_ptr") else arr.ctypes.data
+        self._handle.check(self._handle.L.clm_set_positions(self._handle.h, 0, ptr if n else None, n, 1 if dev else 0))
+        self._x, self.n = keep, n
+
+    @staticmethod
+    def _params(ops):
+        arr = (_abi.OpParams * len(ops))()
+        for k, op in enumerate(ops):
+            p, _ = op.params(None) if not isinstance(op, (LennardJones,)) else (None, None)
+            if isinstance(op, LennardJones):
+                if op.types_x is not None:
+                    raise ArgumentError("batches take no per-type tables")
+                arr[k].p[0], arr[k].p[1], arr[k].p[2], arr[k].p[3] = float(op.eps), float(op.sigma), float(op.c12), \
+                    float(op.c6)
+            elif p is not None:
+                arr[k] = p
+        return arr
+
+    def run(self, *ops):
+        """One step with the given operators; returns one result per operator: per-system sums (numpy,
+        NaN for a failed system), per-system counts for Count and NeighborList, and forces for the force
+        operators (as EnergyAndForces with per-system energies)."""
+        if not ops:
+            raise ArgumentError("at least one operator")
+        ids = np.array([_abi.OP[o.op] for o in ops], np.int32)
+        params = self._params(ops)
+        outs = (_abi.BatchOutputs * len(ops))()
+        keep = []
+        for k, op in enumerate(ops):
+            sc = np.zeros(self.nsys, np.float64)
+            ct = np.zeros(self.nsys, np.int64)
+            outs[k].scalar, outs[k].count = sc.ctypes.data, ct.ctypes.data
+            f = None
+            if isinstance(op, _ForcesOp):
+                f = np.zeros((self.n, self.dim), self.dtype)
+                outs[k].forces = f.ctypes.data
+            keep.append((sc, ct, f))
+        self._handle.check(self._handle.L.clm_batched_run(self._handle.h, len(ops), ids.ctypes.data,
+                                                          C.cast(params, C.c_void_p), C.cast(outs, C.c_void_p)))
+        res = []
+        for op, (sc, ct, f) in zip(ops, keep):
+            if isinstance(op, NeighborList):
+                res.append(self._neighbor_lists(ct, op.index_base))
+            elif isinstance(op, Count):
+                res.append(ct)
+            elif f is not None:
+                res.append(EnergyAndForces(sc, f))
+            else:
+                res.append(sc)
+        return res
+
+    def _neighbor_lists(self, counts, base=0):
+        """Per-system neighbour lists with indices local to each system."""
+        L, h = self._handle.L, self._handle.h
+        n = C.c_int64()
+        self._handle.check(L.clm_nl_count(h, C.byref(n)))
+        i = np.empty(n.value, np.int64)
+        j = np.empty(n.value, np.int64)
+        d = np.empty(n.value, self.dtype)
+        self._handle.check(L.clm_nl_fetch(h, i.ctypes.data, j.ctypes.data, d.ctypes.data, n.value, 0, 0))
+        sysid = np.searchsorted(self.offsets, i, side="right") - 1
+        order = np.argsort(sysid, kind="stable")
+        i, j, d, sysid = i[order], j[order], d[order], sysid[order]
+        bounds = np.concatenate([[0], np.cumsum(np.bincount(sysid, minlength=self.nsys))])
+        out = []
+        for s in range(self.nsys):
+            a, b = bounds[s], bounds[s + 1]
+            o = self.offsets[s]
+            out.append((i[a:b] - o + base, j[a:b] - o + base, d[a:b]))
+        return out
+
+    def status(self):
+        st = np.zeros(self.nsys, np.int32)
+        self._handle.check(self._handle.L.clm_batched_status(self._handle.h, st.ctypes.data, self.nsys))
+        return st
+
+    def autotune(self, *ops, reps: int = 3):
+        ids = np.array([_abi.OP[o.op] for o in ops], np.int32)
+        params = self._params(ops)
+        cfg = np.zeros(3, np.int32)
+        best = C.c_float()
+        self._handle.check(self._handle.L.clm_batched_autotune(self._handle.h, len(ops), ids.ctypes.data,
+                                                               C.cast(params, C.c_void_p), reps, cfg.ctypes.data,
+                                                               C.byref(best)))
+        return {"lcell": int(cfg[0]), "cell_split": int(cfg[1]), "grid_div": int(cfg[2]), "step_ms": best.value}
+
+    def last_step(self):
+        ms, nl = C.c_float(), C.c_int64()
+        self._handle.check(self._handle.L.clm_batched_last_step(self._handle.h, C.byref(ms), C.byref(nl)))
+        return {"step_ms": ms.value, "launches": nl.value}
+
+    def close(self):
+        self._handle.close()
+
+
 class Box:
     """Mirror of `Box(unitcell, cutoff; lcell)` (src/internals/Box.jl:191-203, 330-335): the geometry as
     computed by the library (nc, cell_size, computing_box, aligned unit cell, rotation)."""

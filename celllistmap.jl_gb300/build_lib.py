@@ -18,7 +18,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libcelllist_cuda.so")
-SOURCES = ["clm_api.cu", "clm_build.cu", "clm_pairs.cu", "clm_noalloc.cu"]
+SOURCES = ["clm_api.cu", "clm_build.cu", "clm_pairs.cu", "clm_pairs_f32.cu", "clm_pairs_f64.cu", "clm_pairs_batch.cu",
+           "clm_batched.cu", "clm_noalloc.cu"]
 PEAKS_SRC = "clm_peaks.cu"
 PEAKS_LIB = os.path.join(OUT_DIR, "libclm_peaks.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

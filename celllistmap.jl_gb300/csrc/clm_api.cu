@@ -187,6 +187,7 @@ int32_t clm_set_stream(clm_handle h, void* stream) {
 
 int32_t clm_set_box(clm_handle h, const double* M, int32_t kind, double cutoff, int32_t lcell) {
   if (!h) return ERR_ARG;
+  if (h->batch.on) return fail(h, ERR_STATE, "a batch handle takes clm_batched_set_systems / clm_batched_run");
   if (lcell < 1) return fail(h, ERR_LCELL, "lcell must be greater or equal to 1");
   if (!(cutoff > 0) || !std::isfinite(cutoff)) return fail(h, ERR_ARG, "cutoff must be a positive finite number");
   if (kind != CLM_ORTHO && kind != CLM_TRICLINIC && kind != CLM_NONPERIODIC) return fail(h, ERR_ARG, "unknown cell kind");
@@ -259,12 +260,14 @@ int32_t clm_set_precision(clm_handle h, int32_t precision) {
 
 int32_t clm_build(clm_handle h) {
   if (!h) return ERR_ARG;
+  if (h->batch.on) return fail(h, ERR_STATE, "a batch handle takes clm_batched_set_systems / clm_batched_run");
   cudaMemsetAsync(h->err.p, 0, 64, h->stream);
   return build_dispatch(*h);
 }
 
 int32_t clm_run(clm_handle h, int32_t op_id, const clm_op_params* params, clm_outputs* out) {
   if (!h || !out) return ERR_ARG;
+  if (h->batch.on) return fail(h, ERR_STATE, "a batch handle takes clm_batched_set_systems / clm_batched_run");
   if (!h->box_set) return fail(h, ERR_STATE, "clm_set_box must be called before clm_run");
   for (int attempt = 0; attempt < 3; attempt++) {
     bool need = false;
@@ -321,6 +324,7 @@ int32_t clm_nl_fetch(clm_handle h, int64_t* i, int64_t* j, void* d, int64_t cap,
 int32_t clm_get_box(clm_handle h, int64_t* nc, double* cell_size, double* cbmin, double* cbmax, double* aligned,
                     double* rotation, double* inv_rotation, double* cutoff) {
   if (!h) return ERR_ARG;
+  if (h->batch.on) return fail(h, ERR_STATE, "a batch handle takes clm_batched_set_systems / clm_batched_run");
   if (!h->box_set) return fail(h, ERR_STATE, "box not set");
   if (h->kind == CLM_NONPERIODIC) {
     bool built = true;
@@ -353,6 +357,7 @@ int32_t clm_get_box(clm_handle h, int64_t* nc, double* cell_size, double* cbmin,
 int32_t clm_get_celllist_info(clm_handle h, int32_t set, int64_t* n_real, int64_t* n_particles,
                               int64_t* n_cells_with_particles, int64_t* n_cells_with_real) {
   if (!h || set < 0 || set >= h->nsets) return ERR_ARG;
+  if (h->batch.on) return fail(h, ERR_STATE, "a batch handle takes clm_batched_set_systems / clm_batched_run");
   SetData& S = h->sets[set];
   if (!S.built || S.dirty) {
     int st = clm_build(h);
@@ -375,6 +380,7 @@ int32_t clm_get_celllist_info(clm_handle h, int32_t set, int64_t* n_real, int64_
 int32_t clm_fetch_celllist(clm_handle h, int32_t set, int64_t cap, int64_t* cell, int64_t* index, int8_t* real,
                            void* coords, int32_t index_base) {
   if (!h || set < 0 || set >= h->nsets) return ERR_ARG;
+  if (h->batch.on) return fail(h, ERR_STATE, "a batch handle takes clm_batched_set_systems / clm_batched_run");
   SetData& S = h->sets[set];
   if (!S.built || S.dirty) {
     int st = clm_build(h);

@@ -168,12 +168,11 @@ __global__ void __launch_bounds__(kBlock) k_rs_scatter(const uint32_t* __restric
 }
 
 // ------------------------------------------------------------------ K1: wrap, images, copy count
+// Returns false if the particle has a NaN coordinate (it then gets no copy).
 template <class T, int N>
-__global__ void __launch_bounds__(kBlock) k_wrap_count(DevGeom<T> g, const T* __restrict__ x, int n,
-                                                       T* __restrict__ wrapped, uint32_t* __restrict__ mask,
-                                                       int* __restrict__ ncopy, int* __restrict__ err) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+__device__ __forceinline__ bool wrap_count_at(const DevGeom<T>& g, const T* __restrict__ x, int i,
+                                              T* __restrict__ wrapped, uint32_t* __restrict__ mask,
+                                              int* __restrict__ ncopy) {
   T xi[N];
   bool bad = false;
 #pragma unroll
@@ -182,12 +181,11 @@ __global__ void __launch_bounds__(kBlock) k_wrap_count(DevGeom<T> g, const T* __
     bad = bad || isnan(xi[k]);
   }
   if (bad) {
-    atomicOr(err, DERR_NAN);
 #pragma unroll
     for (int k = 0; k < N; k++) wrapped[(int64_t)i * N + k] = T(0);
     mask[i] = 0;
     ncopy[i] = 0;
-    return;
+    return false;
   }
   T p[N];
   if (g.kind == NONPERIODIC) {
@@ -214,18 +212,47 @@ __global__ void __launch_bounds__(kBlock) k_wrap_count(DevGeom<T> g, const T* __
   }
   mask[i] = m;
   ncopy[i] = cnt;
+  return true;
+}
+
+template <class T, int N>
+__global__ void __launch_bounds__(kBlock) k_wrap_count(DevGeom<T> g, const T* __restrict__ x, int n,
+                                                       T* __restrict__ wrapped, uint32_t* __restrict__ mask,
+                                                       int* __restrict__ ncopy, int* __restrict__ err) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (!wrap_count_at<T, N>(g, x, i, wrapped, mask, ncopy)) atomicOr(err, DERR_NAN);
+}
+
+// Batches: each particle uses its system's geometry; a NaN marks only its system; particles of systems
+// that failed the unit-cell check get no copies.
+template <class T, int N>
+__global__ void __launch_bounds__(kBlock) k_wrap_count_b(const DevGeom<T>* __restrict__ gtab,
+                                                         const int* __restrict__ psys, const T* __restrict__ x, int n,
+                                                         T* __restrict__ wrapped, uint32_t* __restrict__ mask,
+                                                         int* __restrict__ ncopy, int* __restrict__ sys_err) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int s = psys[i];
+  const DevGeom<T>& g = gtab[s];
+  if (g.ncells == 0) {
+#pragma unroll
+    for (int k = 0; k < N; k++) wrapped[(int64_t)i * N + k] = T(0);
+    mask[i] = 0;
+    ncopy[i] = 0;
+    return;
+  }
+  if (!wrap_count_at<T, N>(g, x, i, wrapped, mask, ncopy)) atomicOr(&sys_err[s], DERR_NAN);
 }
 
 // ------------------------------------------------------------------ K2: keys, histogram, real flags
+// `cb` is the first global cell of the particle's system (0 for one system).
 template <class T, int N>
-__global__ void __launch_bounds__(kBlock) k_emit(DevGeom<T> g, const T* __restrict__ wrapped,
-                                                 const uint32_t* __restrict__ mask, const int* __restrict__ ncopy,
-                                                 const int* __restrict__ copy_off, int n, int cap,
-                                                 uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
-                                                 int* __restrict__ cell_count, int* __restrict__ cell_flags,
-                                                 int* __restrict__ err) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+__device__ __forceinline__ void emit_at(const DevGeom<T>& g, int cb, const T* __restrict__ wrapped,
+                                        const uint32_t* __restrict__ mask, const int* __restrict__ ncopy,
+                                        const int* __restrict__ copy_off, int i, int cap, uint32_t* __restrict__ keys,
+                                        uint32_t* __restrict__ vals, int* __restrict__ cell_count,
+                                        int* __restrict__ cell_flags, int* __restrict__ err) {
   if (ncopy[i] == 0) return;
   int base = copy_off[i];
   if (base < 0 || base + ncopy[i] > cap) {
@@ -240,6 +267,7 @@ __global__ void __launch_bounds__(kBlock) k_emit(DevGeom<T> g, const T* __restri
     atomicOr(err, DERR_CELL_RANGE);
     li = 0;
   }
+  li += cb;
   keys[base] = (uint32_t)li;
   vals[base] = ((uint32_t)i << 5) | (uint32_t)g.zero_code;
   atomicAdd(&cell_count[li], 1);
@@ -257,11 +285,38 @@ __global__ void __launch_bounds__(kBlock) k_emit(DevGeom<T> g, const T* __restri
       atomicOr(err, DERR_CELL_RANGE);
       lk = 0;
     }
+    lk += cb;
     keys[base + t] = (uint32_t)lk;
     vals[base + t] = ((uint32_t)i << 5) | (uint32_t)k;
     atomicAdd(&cell_count[lk], 1);
     t++;
   }
+}
+
+template <class T, int N>
+__global__ void __launch_bounds__(kBlock) k_emit(DevGeom<T> g, const T* __restrict__ wrapped,
+                                                 const uint32_t* __restrict__ mask, const int* __restrict__ ncopy,
+                                                 const int* __restrict__ copy_off, int n, int cap,
+                                                 uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                                 int* __restrict__ cell_count, int* __restrict__ cell_flags,
+                                                 int* __restrict__ err) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  emit_at<T, N>(g, 0, wrapped, mask, ncopy, copy_off, i, cap, keys, vals, cell_count, cell_flags, err);
+}
+
+template <class T, int N>
+__global__ void __launch_bounds__(kBlock) k_emit_b(const DevGeom<T>* __restrict__ gtab, const int* __restrict__ psys,
+                                                   const int* __restrict__ cbase, const T* __restrict__ wrapped,
+                                                   const uint32_t* __restrict__ mask, const int* __restrict__ ncopy,
+                                                   const int* __restrict__ copy_off, int n, int cap,
+                                                   uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                                   int* __restrict__ cell_count, int* __restrict__ cell_flags,
+                                                   int* __restrict__ err) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int s = psys[i];
+  emit_at<T, N>(gtab[s], cbase[s], wrapped, mask, ncopy, copy_off, i, cap, keys, vals, cell_count, cell_flags, err);
 }
 
 // ------------------------------------------------------------------ K4: gather in cell order
@@ -279,30 +334,17 @@ __device__ __forceinline__ void origin_ff(float cb_hi, float cb_lo, float cs_hi,
   lo = se + pe + cb_lo;
 }
 
+// Copy t of the sorted list: particle p, image k, in the cell `li` (local index of its system).
 template <class T, int N>
-__global__ void __launch_bounds__(kBlock) k_gather(DevGeom<T> g, const T* __restrict__ wrapped,
-                                                   const uint32_t* __restrict__ skeys,
-                                                   const uint32_t* __restrict__ svals, const int* __restrict__ n_dev,
-                                                   int cap, int n, T* __restrict__ px, T* __restrict__ py,
-                                                   T* __restrict__ pz, float4* __restrict__ off, int* __restrict__ code,
-                                                   int* __restrict__ err) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= min(*n_dev, cap)) return;
-  uint32_t v = svals[t];
-  int p = (int)(v >> 5);
-  int k = (int)(v & 31u);
-  if (p >= n || k >= g.nimg) {
-    atomicOr(err, DERR_CELL_RANGE);
-    p = 0;
-    k = g.zero_code;
-  }
+__device__ __forceinline__ void gather_at(const DevGeom<T>& g, const T* __restrict__ wrapped, int t, int p, int k,
+                                          int li, T* __restrict__ px, T* __restrict__ py, T* __restrict__ pz,
+                                          float4* __restrict__ off, int* __restrict__ code) {
   T q[N];
 #pragma unroll
   for (int d = 0; d < N; d++) {
     T w = wrapped[(int64_t)p * N + d];
     q[d] = (k == g.zero_code) ? w : xadd(w, g.shift[k][d]);
   }
-  int li = (int)skeys[t];
   int c[3];
   cart_of(li, g.nc, N, c);
   float o[3] = {0.f, 0.f, 0.f};
@@ -320,6 +362,56 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom<T> g, const T* __rest
   if (N == 3) pz[t] = q[N - 1];
   off[t] = make_float4(o[0], o[1], o[2], 0.f);
   code[t] = (k == g.zero_code) ? p : -(p + 1);
+}
+
+template <class T, int N>
+__global__ void __launch_bounds__(kBlock) k_gather(DevGeom<T> g, const T* __restrict__ wrapped,
+                                                   const uint32_t* __restrict__ skeys,
+                                                   const uint32_t* __restrict__ svals, const int* __restrict__ n_dev,
+                                                   int cap, int n, T* __restrict__ px, T* __restrict__ py,
+                                                   T* __restrict__ pz, float4* __restrict__ off, int* __restrict__ code,
+                                                   int* __restrict__ err) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= min(*n_dev, cap)) return;
+  uint32_t v = svals[t];
+  int p = (int)(v >> 5);
+  int k = (int)(v & 31u);
+  int li = (int)skeys[t];
+  if (p >= n || k >= g.nimg || li < 0 || li >= g.ncells) {
+    atomicOr(err, DERR_CELL_RANGE);
+    p = 0;
+    k = g.zero_code;
+    li = 0;
+  }
+  gather_at<T, N>(g, wrapped, t, p, k, li, px, py, pz, off, code);
+}
+
+template <class T, int N>
+__global__ void __launch_bounds__(kBlock) k_gather_b(const DevGeom<T>* __restrict__ gtab, const int* __restrict__ psys,
+                                                     const int* __restrict__ cbase, const T* __restrict__ wrapped,
+                                                     const uint32_t* __restrict__ skeys,
+                                                     const uint32_t* __restrict__ svals, const int* __restrict__ n_dev,
+                                                     int cap, int n, T* __restrict__ px, T* __restrict__ py,
+                                                     T* __restrict__ pz, float4* __restrict__ off,
+                                                     int* __restrict__ code, int* __restrict__ err) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= min(*n_dev, cap)) return;
+  uint32_t v = svals[t];
+  int p = (int)(v >> 5);
+  int k = (int)(v & 31u);
+  if (p >= n) {
+    atomicOr(err, DERR_CELL_RANGE);
+    p = 0;
+  }
+  const int s = psys[p];
+  const DevGeom<T>& g = gtab[s];
+  int li = (int)skeys[t] - cbase[s];
+  if (k >= g.nimg || li < 0 || li >= g.ncells) {
+    atomicOr(err, DERR_CELL_RANGE);
+    k = g.zero_code;
+    li = 0;
+  }
+  gather_at<T, N>(g, wrapped, t, p, k, li, px, py, pz, off, code);
 }
 
 __global__ void k_compact(const int* __restrict__ flags, const int* __restrict__ scanned, int ncells,
@@ -515,7 +607,12 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
   SetData& S = h.sets[set];
   const int N = g.dim;
   const int64_t n = S.n;
-  const int64_t ncells = g.ncells();
+  const bool batch = h.batch.on;
+  const int64_t ncells = batch ? h.batch.ncells : g.ncells();
+  if (batch && (!h.batch.tables_ready || set != 0)) {
+    h.last_error = "batch tables are not ready";
+    return ERR_STATE;
+  }
   if (ncells > (int64_t)1 << 30) {
     h.last_error = "too many cells for the cell grid (reduce lcell or enlarge cutoff)";
     return ERR_ARG;
@@ -540,9 +637,20 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
     S.cap_used = 0;
     return OK;
   }
-  const int64_t cap = copy_capacity(S, g);
+  int64_t cap = 0;
+  if (batch) {
+    const double est = std::min(h.batch.copies_est * 1.15 + 4096.0, 27.0 * (double)n + 64.0);
+    cap = std::max<int64_t>(std::max<int64_t>(S.copy_cap, (int64_t)est), n + 64);
+    CLM_CUDA_TRY(h, cudaMemsetAsync(h.batch.sys_err.p, 0, sizeof(int) * (h.batch.nsys + 1), h.stream));
+  } else {
+    cap = copy_capacity(S, g);
+  }
   if (cap > (int64_t)INT32_MAX - 1) {
     h.last_error = "too many particle copies for one set";
+    return ERR_ARG;
+  }
+  if (n >= ((int64_t)1 << 27)) {
+    h.last_error = "at most 2^27 - 1 particles per set";
     return ERR_ARG;
   }
   S.cap_used = cap;
@@ -555,7 +663,17 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
       !S.rs_hist.reserve(sizeof(int) * (256 * (int64_t)ntiles + 1)))
     return ERR_NOMEM;
   const int gn = grid_for(n);
-  if (N == 3)
+  const DevGeom<T>* gtab = h.batch.gtab.as<DevGeom<T>>();
+  const int* psys = h.batch.psys.as<int>();
+  const int* cbase = h.batch.cbase_d.as<int>();
+  if (batch) {
+    if (N == 3)
+      k_wrap_count_b<T, 3><<<gn, kBlock, 0, h.stream>>>(gtab, psys, S.x.as<T>(), (int)n, S.wrapped.as<T>(),
+                                                       S.mask.as<uint32_t>(), S.ncopy.as<int>(), h.batch.sys_err.as<int>());
+    else
+      k_wrap_count_b<T, 2><<<gn, kBlock, 0, h.stream>>>(gtab, psys, S.x.as<T>(), (int)n, S.wrapped.as<T>(),
+                                                       S.mask.as<uint32_t>(), S.ncopy.as<int>(), h.batch.sys_err.as<int>());
+  } else if (N == 3)
     k_wrap_count<T, 3><<<gn, kBlock, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
                                                    S.ncopy.as<int>(), err);
   else
@@ -566,7 +684,18 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
   int* n_dev = S.copy_off.as<int>() + n;  // total number of copies, on the device
   int st = scan_exclusive(h, S.ncopy.as<int>(), S.copy_off.as<int>(), n, n_dev);
   if (st) return st;
-  if (N == 3)
+  if (batch) {
+    if (N == 3)
+      k_emit_b<T, 3><<<gn, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
+                                                 S.ncopy.as<int>(), S.copy_off.as<int>(), (int)n, (int)cap,
+                                                 S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
+                                                 S.cell_count.as<int>(), S.cell_flags.as<int>(), err);
+    else
+      k_emit_b<T, 2><<<gn, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
+                                                 S.ncopy.as<int>(), S.copy_off.as<int>(), (int)n, (int)cap,
+                                                 S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
+                                                 S.cell_count.as<int>(), S.cell_flags.as<int>(), err);
+  } else if (N == 3)
     k_emit<T, 3><<<gn, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(),
                                              S.copy_off.as<int>(), (int)n, (int)cap, S.keys[0].as<uint32_t>(),
                                              S.vals[0].as<uint32_t>(), S.cell_count.as<int>(), S.cell_flags.as<int>(), err);
@@ -602,7 +731,16 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
   if (st) return st;
   // gather coordinates in cell order
   const int gc = grid_for(cap);
-  if (N == 3)
+  if (batch) {
+    if (N == 3)
+      k_gather_b<T, 3><<<gc, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
+                                                   S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
+                                                   S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.code.as<int>(), err);
+    else
+      k_gather_b<T, 2><<<gc, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
+                                                   S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
+                                                   S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.code.as<int>(), err);
+  } else if (N == 3)
     k_gather<T, 3><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
                                                S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
                                                S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.code.as<int>(), err);

@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <vector>
 
 #include "clm_device.cuh"
 #include "clm_geometry.hpp"
@@ -74,6 +75,52 @@ struct ScanTemp {
   DevBuf level[4];
 };
 
+// Many independent periodic systems in one handle (one cell list over a global cell index; every
+// system keeps its own box, cells and images).  Set 0 of the handle holds the concatenated positions.
+struct BatchState {
+  bool on = false;
+  int64_t nsys = 0;
+  int kind = 0;                  // ORTHO or TRICLINIC (all systems)
+  int lcell = 1;
+  double cutoff = 0;
+  std::vector<int64_t> offsets;  // nsys + 1: particles of system s are offsets[s] .. offsets[s+1]-1
+  std::vector<double> cells;     // nsys x dim x dim, column-major per system
+  std::vector<int> status;       // per system: OK, ERR_CELL_TOO_SMALL, ERR_NAN
+  std::vector<int> cbase;        // nsys + 1: first global cell of each system
+  int64_t ncells = 0;            // total cells
+  double real_cells = 0;         // cells with real particles (geometric estimate)
+  double copies_est = 0;         // reals + images (uniform-density estimate)
+  double pairs_est = 0;          // pairs within the cutoff (uniform-density estimate)
+  bool tables_ready = false;     // device tables match (systems, lcell, precision)
+  int tables_dtype = -1;
+  DevBuf gtab;                   // DevGeom<T> per system
+  DevBuf psys;                   // system of each particle
+  DevBuf cbase_d;                // cbase on the device
+  DevBuf cell_sys;               // system of each global cell
+  DevBuf sys_err;                // per-system device error bits
+  DevBuf part;                   // per work item partial sums and counts
+  DevBuf sys_out;                // per op: per-system sums and counts
+  DevBuf forces;                 // forces in the handle dtype (n x dim)
+  int cell_split = 1;            // parts per cell (autotuned)
+  int grid_div = 1;              // resident blocks per SM divided by this (autotuned)
+  // one step (build + operators) captured as a CUDA graph
+  bool use_graph = false;
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<int> graph_ops;
+  std::vector<double> graph_params;
+  int64_t graph_n = -1;
+  float step_ms = 0;
+  int64_t step_launches = 0;
+  int64_t graph_launches = 0;     // kernels in the recorded step
+  unsigned char* hres = nullptr;  // pinned host results of one step
+  size_t hres_bytes = 0;
+  int nl_slot = -1;               // which op of the step produced the neighbour list
+  ~BatchState() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (hres) cudaFreeHost(hres);
+  }
+};
+
 struct Handle {
   int dtype = 1, dim = 3, nsets = 1;
   cudaStream_t stream = nullptr;
@@ -101,6 +148,8 @@ struct Handle {
   bool build_timing_pending = false;
   int64_t launches = 0;        // kernels launched by this handle (cumulative)
   std::string last_error;
+  BatchState batch;
+  bool capturing = false;      // a stream capture is open: no synchronization, no timing events
 };
 
 // Status helpers
@@ -128,5 +177,6 @@ template <class T>
 int run_pairs_scalar_scratch(Handle& h, const Geometry<T>& g, int op, const void* params, void* outputs, void* scratch,
                              size_t scratch_bytes);
 int pairs_scalar_blocks_needed(Handle& h, int op);
+template <class T> int cell_split_for(const Handle& h, const Geometry<T>& g, int opk);
 
 }  // namespace clm

@@ -65,6 +65,10 @@ int scratch_address(clm::Handle& h, void** out) {
 
 extern "C" int32_t clm_run_noalloc(clm_handle h, int32_t op_id, const clm_op_params* params, clm_outputs* out) {
   if (!h || !out) return clm::ERR_ARG;
+  if (h->batch.on) {
+    h->last_error = "a batch handle takes clm_batched_run";
+    return clm::ERR_STATE;
+  }
   if (!h->box_set) {
     h->last_error = "clm_set_box and clm_build must be called before clm_run_noalloc";
     return clm::ERR_STATE;

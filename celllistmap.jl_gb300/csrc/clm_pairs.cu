@@ -1,4 +1,4 @@
-// Cell-pair map on the GPU (K5 self, K6 cross, K7 operator epilogues).
+// Cell-pair map on the GPU, host side: operator staging, launches, reductions and results.
 //
 // Replaces _pairwise! and its inner loops:
 //   self  src/internals/self.jl:106-184      cross src/internals/cross.jl:265-313
@@ -7,8 +7,8 @@
 //   non-periodic inner loops                 src/internals/NonPeriodicCells.jl:281-352
 // and the per-batch output copies + reduce_output! with on-chip reductions.
 //
-// Work decomposition: one warp per cell that contains real particles (the
-// reference's batches of `cell_indices_real`).  The warp's lanes hold the
+// Work decomposition: one warp per cell (or part of a cell) that contains real
+// particles (the reference's batches of `cell_indices_real`).  The warp's lanes hold the
 // particles of that cell (split into 1, 2 or 4 lane groups for small cells so
 // that each group takes every G-th neighbour); the particles of each cell of
 // the stencil are staged 32 at a time in shared memory and broadcast.
@@ -28,6 +28,10 @@
 // Split form (CLM_PREC_SPLIT): pairs certainly inside are accepted from the
 // FP32 test and evaluated in FP32; only the band is re-tested in the input
 // dtype.  Sums are accumulated in FP64 (Kahan-compensated FP32 per lane).
+//
+// Cells holding many particles are split into parts (interleaved chunks of 32
+// particles) so that every resident warp has work; batches of independent
+// systems share one launch, each cell reading its system's geometry.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -37,898 +41,14 @@
 #include <vector>
 
 #include "clm_internal.hpp"
+#include "clm_pairs_args.hpp"
 #include "celllistmap_gb300.h"
 
 namespace clm {
 
+using namespace pk;
+
 namespace {
-
-constexpr int kWarps = 4;
-constexpr int kThreads = kWarps * 32;
-
-
-template <class T> struct SetView {
-  const T* px;
-  const T* py;
-  const T* pz;
-  const float4* off;
-  const int* code;
-  const int* cell_start;
-};
-
-template <class T> struct PairArgs {
-  DevGeom<T> g;
-  SetView<T> X, Y;
-  const int* real_list;
-  const int* xflags;  // per cell of set x: contains real particles
-  const int* n_real_dev;  // number of cells with real particles (device)
-  int self;
-  int split;
-  int op;
-  int* err;
-  // operator parameters
-  double p[4];
-  int ntypes;
-  const int* tx;
-  const int* ty;
-  const double* eps_t;
-  const double* sig_t;
-  const T* vx;
-  const T* vy;
-  const T* bins;
-  int nbins;
-  // outputs
-  int* nl_i;
-  int* nl_j;
-  T* nl_d;
-  unsigned long long* nl_count;
-  long long nl_cap;
-  double* fx;       // forces accumulators (double), n_x * dim
-  double* fy;       // n_y * dim (cross)
-  double* part_e;   // per-block energy
-  unsigned long long* part_c;  // per-block count
-  T* part_min_d2;
-  int* part_min_ij;
-  unsigned long long* part_hc;  // nbins per block
-  double* part_hs;              // nbins per block
-  double* part_v;               // kAdjVals per block (adjoint)
-};
-
-__device__ __forceinline__ void stencil_offset(bool forward, int l, int dim, int k, int* o) {
-  const int w = 2 * l + 1;
-  o[2] = 0;
-  if (forward) {
-    if (dim == 3) {
-      const int nA = l * w * w, nB = l * w;
-      if (k < nA) {
-        o[0] = 1 + k % l;
-        int r = k / l;
-        o[1] = r % w - l;
-        o[2] = r / w - l;
-      } else if (k < nA + nB) {
-        int k2 = k - nA;
-        o[0] = 0;
-        o[1] = 1 + k2 % l;
-        o[2] = k2 / l - l;
-      } else {
-        o[0] = 0;
-        o[1] = 0;
-        o[2] = 1 + (k - nA - nB);
-      }
-    } else {
-      const int nA = l * w;
-      if (k < nA) {
-        o[0] = 1 + k % l;
-        o[1] = k / l - l;
-      } else {
-        o[0] = 0;
-        o[1] = 1 + (k - nA);
-      }
-    }
-  } else {
-    int total = (dim == 3) ? w * w * w : w * w;
-    int center = (total - 1) / 2;
-    int kk = (k < center) ? k : k + 1;
-    o[0] = kk % w - l;
-    o[1] = (kk / w) % w - l;
-    if (dim == 3) o[2] = kk / (w * w) - l;
-  }
-}
-
-template <class T> __device__ __forceinline__ T pos_of(const SetView<T>& S, int d, int t) {
-  return d == 0 ? S.px[t] : (d == 1 ? S.py[t] : S.pz[t]);
-}
-
-// Kahan-compensated accumulator (FP32) or plain FP64
-template <class A> struct Acc {
-  A s = 0, c = 0;
-  __device__ __forceinline__ void add(A v) {
-    if (std::is_same<A, float>::value) {
-      A y = v - c;
-      A t = s + y;
-      c = (t - s) - y;
-      s = t;
-    } else {
-      s += v;
-    }
-  }
-  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
-};
-
-enum OpKind { OPK_NL = 0, OPK_SCALAR = 1, OPK_FORCES = 2, OPK_MIN = 3, OPK_HIST = 4, OPK_ADJ = 5 };
-constexpr int kAdjVals = 13;  // energy, virial (xx yy zz xy xz yz), dU/deps[3], dU/dsigma[3]
-
-// Reciprocal and reciprocal square root for pair VALUES (energies, forces), which are checked against
-// tolerances, never used for pair membership or neighbour-list distances.
-//  FP32: hardware approximations (rcp.approx / rsqrt.approx, a couple of ulp).
-//  FP64: the hardware FP64 estimate refined by two Newton-Raphson steps, each of which squares the
-//        relative error (y <- y + y(1 - x y) for 1/x; y <- y + y/2 (1 - x y^2) for 1/sqrt(x)).
-__device__ __forceinline__ float vrcp(float x) {
-  float y;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ float vrsqrt(float x) { return rsqrtf(x); }
-__device__ __forceinline__ double vrcp(double x) {
-  double y;
-  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-  double e = fma(-x, y, 1.0);
-  y = fma(y, e, y);
-  e = fma(-x, y, 1.0);
-  return fma(y, e, y);
-}
-__device__ __forceinline__ double vrsqrt(double x) {
-  double y;
-  asm("rsqrt.approx.f64 %0, %1;" : "=d"(y) : "d"(x));
-#pragma unroll
-  for (int k = 0; k < 2; k++) {
-    double e = fma(-x, y * y, 1.0);
-    y = fma(0.5 * y, e, y);
-  }
-  return y;
-}
-
-// Per-pair energy u and g = (du/dr)/r (force contribution df = g*(x_i - x_j)).
-template <class V, class T>
-__device__ __forceinline__ void pair_value(const PairArgs<T>& A, int op, V d2, int i, int j, V& u, V& g) {
-  switch (op) {
-    case 2:  // COUNT
-      u = V(1);
-      g = V(0);
-      break;
-    case 3:  // SUM_D2
-      u = d2;
-      g = V(0);
-      break;
-    case 4:  // SUM_D
-      u = d2 * vrsqrt(d2);
-      g = V(0);
-      break;
-    case 5:  // SUM_INV_D
-      u = vrsqrt(d2);
-      g = V(0);
-      break;
-    case 6:
-    case 7: {  // SOFT (c - d)^2
-      V ri = vrsqrt(d2);
-      V d = d2 * ri;
-      V c = (V)A.p[0];
-      u = (c - d) * (c - d);
-      g = V(-2) * (c - d) * ri;
-      break;
-    }
-    case 8:
-    case 9:
-    case 13: {  // LJ eps*(c12 (s/d)^12 - c6 (s/d)^6)
-      V eps = (V)A.p[0], sig = (V)A.p[1];
-      if (A.ntypes > 0) {
-        int ti = A.tx[i];
-        int tj = A.self ? A.tx[j] : A.ty[j];
-        eps = (V)A.eps_t[ti * A.ntypes + tj];
-        sig = (V)A.sig_t[ti * A.ntypes + tj];
-      }
-      V c12 = (V)A.p[2], c6 = (V)A.p[3];
-      V r2i = vrcp(d2);
-      V sr2 = (sig * sig) * r2i;
-      V sr6 = sr2 * sr2 * sr2;
-      V sr12 = sr6 * sr6;
-      u = eps * (c12 * sr12 - c6 * sr6);
-      g = eps * (V(-12) * c12 * sr12 + V(6) * c6 * sr6) * r2i;
-      break;
-    }
-    case 12: {  // 1/d with gradient accumulation
-      V ri = vrsqrt(d2);
-      u = ri;
-      g = ri * ri * ri;
-      break;
-    }
-    default:
-      u = V(0);
-      g = V(0);
-  }
-}
-
-__device__ __forceinline__ bool is_forward(const int* o) {
-  // neighbor_cells_forward (src/internals/Box.jl:436-457): lexicographically positive in (x, y, z)
-  return o[0] > 0 || (o[0] == 0 && (o[1] > 0 || (o[1] == 0 && o[2] > 0)));
-}
-
-template <class T, int N>
-__device__ __forceinline__ T exact_dot_rel(const T* x, const T* c, const T* u) {
-  T s = xmul(xsub(x[0], c[0]), u[0]);
-#pragma unroll
-  for (int d = 1; d < N; d++) s = xadd(s, xmul(xsub(x[d], c[d]), u[d]));
-  return s;
-}
-
-// The reference's projection filter for a pair seen from cell `from` (center cf) towards cell `to`
-// (center ct): the particle of `to` must satisfy |proj| <= margin and |proj_to - proj_from| <= cutoff
-// (src/internals/vicinal_cells.jl:4-75, auxiliary_functions.jl:166-186).
-template <class T, int N>
-__device__ bool projection_pass(const DevGeom<T>& g, const T* cf, const T* ct, const T* x_from, const T* x_to) {
-  T dc[3] = {0, 0, 0};
-#pragma unroll
-  for (int d = 0; d < N; d++) dc[d] = xsub(ct[d], cf[d]);
-  T s2 = xmul(dc[0], dc[0]);
-#pragma unroll
-  for (int d = 1; d < N; d++) s2 = xadd(s2, xmul(dc[d], dc[d]));
-  T dcn = xsqrt(s2);
-  T u[3] = {0, 0, 0};
-#pragma unroll
-  for (int d = 0; d < N; d++) u[d] = xdiv(dc[d], dcn);
-  T pt = exact_dot_rel<T, N>(x_to, cf, u);
-  bool keep = (g.lcell == 1) ? (fabs(pt) <= xadd(g.cutoff, xdiv(dcn, T(2)))) : ((double)fabs(pt) <= g.margin_wide);
-  if (!keep) return false;
-  T pf = exact_dot_rel<T, N>(x_from, cf, u);
-  return fabs(xsub(pt, pf)) <= g.cutoff;
-}
-
-// Pair map kernel.  CROSS: x-y pairs; otherwise self pairs.  For OPK_FORCES on a single set each real
-// particle owns its force ("owner computes": full stencil, no atomics on the partner) and the energy is
-// counted only on the side from which the reference visits the pair.
-//
-// Each warp takes one cell; the cells of its stencil are concatenated into one candidate stream,
-// staged 64 at a time.  Phase A: every lane tests its particle against its share of the staged
-// candidates with an FP32 distance (FMA) and records the candidates inside cutoff^2 (1 + 2^-13) in a
-// bit mask.  Phase B: the lanes walk their masks, apply the reference's pair rules, re-test in the input
-// dtype where needed, and run the operator epilogue.  The projection filter of the reference is
-// evaluated only for pairs with d2 > cutoff^2 (1 - 2^-13): any pair further inside passes it (the
-// projection of the separation on a unit vector cannot exceed the separation, and the margin covers the
-// half cell), so skipping it elsewhere leaves the pair set unchanged.
-template <class T, int N, int OPK, bool SPLIT, bool CROSS>
-__global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(const PairArgs<T> A) {
-  using V = T;
-  using FA = typename std::conditional<std::is_same<T, double>::value && !SPLIT, double, float>::type;
-  constexpr bool IS_F = (OPK == OPK_FORCES) || (OPK == OPK_ADJ);
-  constexpr bool OWNER = IS_F && !CROSS;
-  constexpr bool FP64 = std::is_same<T, double>::value;
-  constexpr bool ABS_PF = !FP64 && !SPLIT;  // FP32 exact form: the prefilter uses the coordinates themselves
-  constexpr int JC = 128;                   // staging capacity: 32 candidates per lane group (G <= 4)
-  const DevGeom<T>& g = A.g;
-  const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
-  const unsigned FULL = 0xffffffffu;
-
-  __shared__ int s_st_start[kWarps][32];
-  __shared__ int s_st_pref[kWarps][33];
-  __shared__ int s_st_meta[kWarps][32];
-  __shared__ float4 s_pf[kWarps][JC];       // prefilter coordinates; .w carries the particle code
-  __shared__ int s_meta[kWarps][JC];        // stencil offset and flags of the candidate's cell
-  __shared__ T s_x[kWarps][3][ABS_PF ? 1 : JC];
-  __shared__ unsigned short s_q[kWarps][1024];  // compacted candidates: (particle slot << 8) | staged index
-  __shared__ T s_ix[kWarps][3][32];              // particles of the current chunk of the cell
-  __shared__ float s_ipf[kWarps][3][32];
-  __shared__ int s_icode[kWarps][32];
-  __shared__ FA s_if[kWarps][3][IS_F ? 32 : 1];  // force sums of those particles
-  __shared__ unsigned int s_hc[(OPK == OPK_HIST) ? 256 : 1];  // block-wide histogram
-  __shared__ double s_hs[(OPK == OPK_HIST) ? 256 : 1];
-  __shared__ double s_red[kWarps];
-  __shared__ unsigned long long s_redc[kWarps];
-
-  constexpr int F_SAME = 1 << 24, F_BACK = 1 << 25, F_REALCELL = 1 << 26;
-  const bool tri = (g.kind == TRICLINIC);
-  const bool nonper = (g.kind == NONPERIODIC);
-  const bool full = tri || CROSS || OWNER;
-  const int l = g.lcell;
-  const int w = 2 * l + 1;
-  const int wN = (N == 3) ? w * w * w : w * w;
-  const int nent = (full ? wN - 1 : (wN - 1) / 2) + 1;  // entry 0 is the cell itself
-  const T band = (T)g.thr_lo;                           // d2 above this: projection filter applies
-
-  if constexpr (OPK == OPK_HIST) {
-    for (int b = threadIdx.x; b < A.nbins; b += kThreads) {
-      s_hc[b] = 0u;
-      s_hs[b] = 0.0;
-    }
-    __syncthreads();
-  }
-
-  double e_tot = 0.0;  // per-lane energy (FP64); FP32 partial sums are folded in per particle chunk
-  FA e_part = 0;
-  FA adj[kAdjVals - 1];  // adjoint accumulators: virial (6), dU/deps (3), dU/dsigma (3)
-#pragma unroll
-  for (int k = 0; k < kAdjVals - 1; k++) adj[k] = FA(0);
-  unsigned long long c_acc = 0;
-  T best_d2 = INFINITY;
-  int best_i = 0x7fffffff, best_j = 0x7fffffff;
-
-  const int gw = blockIdx.x * kWarps + warp;
-  const int nw = gridDim.x * kWarps;
-  const int n_real = *A.n_real_dev;
-  for (int r = gw; r < n_real; r += nw) {
-    const int li = A.real_list[r];
-    int ci[3];
-    cart_of(li, g.nc, N, ci);
-    T ctr_i[3] = {0, 0, 0};
-    cell_center<T, N>(g, ci, ctr_i);
-    const int si = A.X.cell_start[li];
-    const int ni = A.X.cell_start[li + 1] - si;
-    const int G = (ni <= 8) ? 4 : ((ni <= 16) ? 2 : 1);
-    const int LP = 32 / G;
-    const int grp = lane / LP;
-    const int il = lane % LP;
-
-    for (int ib = 0; ib < ni; ib += LP) {
-      const int ii = ib + il;
-      const bool vi = ii < ni;
-      const int ti = si + (vi ? ii : 0);
-      T xi[3] = {0, 0, 0};
-      float pi[3] = {0.f, 0.f, 0.f};
-      int code_i = 0;
-      if (vi) {
-#pragma unroll
-        for (int d = 0; d < N; d++) xi[d] = pos_of(A.X, d, ti);
-        code_i = A.X.code[ti];
-        if (ABS_PF) {
-#pragma unroll
-          for (int d = 0; d < N; d++) pi[d] = (float)xi[d];
-        } else {
-          float4 oi = A.X.off[ti];
-          pi[0] = oi.x;
-          pi[1] = oi.y;
-          pi[2] = oi.z;
-        }
-      }
-      const bool real_i = code_i >= 0;
-      const int idx_i = real_i ? code_i : -code_i - 1;
-      const bool act_i = (OWNER || tri) ? (vi && real_i) : vi;
-      if (grp == 0) {
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-          s_ix[warp][d][il] = xi[d];
-          s_ipf[warp][d][il] = pi[d];
-          if constexpr (IS_F) s_if[warp][d][il] = FA(0);
-        }
-        s_icode[warp][il] = code_i;
-      }
-      __syncwarp();
-
-      for (int k0 = 0; k0 < nent; k0 += 32) {
-        // ---- stencil table for entries k0 .. k0+31
-        {
-          const int kk = k0 + lane;
-          int cnt = 0, start = 0, meta = 0;
-          if (kk < nent) {
-            int o[3] = {0, 0, 0};
-            if (kk > 0) stencil_offset(!full, l, N, kk - 1, o);
-            int cj[3] = {1, 1, 1};
-            bool inr = true;
-#pragma unroll
-            for (int d = 0; d < N; d++) {
-              cj[d] = ci[d] + o[d];
-              inr = inr && cj[d] >= 1 && cj[d] <= g.nc[d];
-            }
-            if (!inr) {
-              atomicOr(A.err, DERR_CELL_RANGE);
-            } else {
-              int lj = cj[0] - 1;
-              if (N == 3) lj += g.nc[0] * ((cj[1] - 1) + g.nc[1] * (cj[2] - 1));
-              else lj += g.nc[0] * (cj[1] - 1);
-              start = A.Y.cell_start[lj];
-              cnt = A.Y.cell_start[lj + 1] - start;
-              meta = (o[0] + 128) | ((o[1] + 128) << 8) | ((o[2] + 128) << 16);
-              if (kk == 0) meta |= F_SAME;
-              if (kk > 0 && full && !is_forward(o)) meta |= F_BACK;
-              if (OWNER && A.xflags[lj]) meta |= F_REALCELL;
-            }
-          }
-          int incl = cnt;
-#pragma unroll
-          for (int o2 = 1; o2 < 32; o2 <<= 1) {
-            int y = __shfl_up_sync(FULL, incl, o2);
-            if (lane >= o2) incl += y;
-          }
-          s_st_pref[warp][lane + 1] = incl;
-          if (lane == 0) s_st_pref[warp][0] = 0;
-          s_st_start[warp][lane] = start;
-          s_st_meta[warp][lane] = meta;
-        }
-        __syncwarp();
-        const int total = s_st_pref[warp][32];
-
-        const int JR = 32 * G;  // candidates per round: each lane tests exactly 32
-        for (int rb = 0; rb < total; rb += JR) {
-          const int cntr = min(JR, total - rb);
-          // ---- stage candidates rb .. rb+JR-1 (positions past the stream are padded with NaN)
-          for (int q = lane; q < JR; q += 32) {
-            if (q < cntr) {
-              const int e = rb + q;
-              int lo = 0, hi = 31;
-              while (lo < hi) {
-                int mid = (lo + hi + 1) >> 1;
-                if (s_st_pref[warp][mid] <= e) lo = mid;
-                else hi = mid - 1;
-              }
-              const int tj = s_st_start[warp][lo] + (e - s_st_pref[warp][lo]);
-              const int meta = s_st_meta[warp][lo];
-              const int code = A.Y.code[tj];
-              s_meta[warp][q] = meta;
-              if (ABS_PF) {
-                s_pf[warp][q] = make_float4((float)pos_of(A.Y, 0, tj), (float)pos_of(A.Y, 1, tj),
-                                            N == 3 ? (float)pos_of(A.Y, N - 1, tj) : 0.f, __int_as_float(code));
-              } else {
-                const float4 oj = A.Y.off[tj];
-                // shift the offset by the cell displacement so that x_i - x_j ~ off_i - pf
-                s_pf[warp][q] = make_float4(oj.x + g.csf[0] * (float)((meta & 255) - 128),
-                                            oj.y + g.csf[1] * (float)(((meta >> 8) & 255) - 128),
-                                            oj.z + g.csf[2] * (float)(((meta >> 16) & 255) - 128),
-                                            __int_as_float(code));
-#pragma unroll
-                for (int d = 0; d < N; d++) s_x[warp][d][ABS_PF ? 0 : q] = pos_of(A.Y, d, tj);
-              }
-            } else {
-              s_pf[warp][q] = make_float4(NAN, NAN, NAN, 0.f);
-            }
-          }
-          __syncwarp();
-          // ---- phase A: 32 FP32 distance tests per lane into a bit mask
-          unsigned mask = 0u;
-          {
-            const float4* pp = &s_pf[warp][grp];
-#pragma unroll
-            for (int b = 0; b < 32; b++) {
-              const float4 p = pp[b * G];
-              const float dx = pi[0] - p.x, dy = pi[1] - p.y, dz = (N == 3) ? pi[2] - p.z : 0.f;
-              const float d2f = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-              mask |= (d2f <= g.thr_hi) ? (1u << b) : 0u;
-            }
-          }
-          if (!act_i) mask = 0u;
-          // ---- phase B: compact the candidates of all lanes into a queue and process them with every lane
-          // busy; each lane takes a contiguous run of the queue (runs are grouped by particle, so force
-          // sums stay in registers and are flushed to shared memory only when the particle changes)
-          int H;
-          {
-            const int nh = __popc(mask);
-            int incl = nh;
-#pragma unroll
-            for (int o2 = 1; o2 < 32; o2 <<= 1) {
-              int y = __shfl_up_sync(FULL, incl, o2);
-              if (lane >= o2) incl += y;
-            }
-            H = __shfl_sync(FULL, incl, 31);
-            int pos = incl - nh;
-            unsigned m = mask;
-            while (m) {
-              const int b = __ffs(m) - 1;
-              m &= m - 1u;
-              s_q[warp][pos++] = (unsigned short)((il << 8) | (b * G + grp));
-            }
-          }
-          __syncwarp();
-          const int per = (H + 31) >> 5;
-          const int qbeg = lane * per;
-          int cur = -1;
-          FA acc[3] = {0, 0, 0};
-          for (int t = 0; t < per; t++) {
-            const int q = qbeg + t;
-            const bool has = q < H;
-            int j = 0, ie = 0;
-            if (has) {
-              const int ent = s_q[warp][q];
-              ie = ent >> 8;
-              j = ent & 255;
-            }
-            T xi[3] = {s_ix[warp][0][ie], s_ix[warp][1][ie], s_ix[warp][2][ie]};
-            const float pi[3] = {s_ipf[warp][0][ie], s_ipf[warp][1][ie], s_ipf[warp][2][ie]};
-            const int code_i = s_icode[warp][ie];
-            const bool real_i = code_i >= 0;
-            const int idx_i = real_i ? code_i : -code_i - 1;
-            const int ii = ib + ie;
-            bool hit = false, sure = false;
-            bool count_e = true;
-            int idx_j = 0;
-            float d2f = 0.f;
-            float dvf[3] = {0.f, 0.f, 0.f};
-            T d2 = 0;
-            T xj[3] = {0, 0, 0};
-            if (has) {
-              const float4 p = s_pf[warp][j];
-              const int code_j = __float_as_int(p.w);
-              const bool real_j = code_j >= 0;
-              idx_j = real_j ? code_j : -code_j - 1;
-              const int meta = s_meta[warp][j];
-              const bool same = (meta & F_SAME) != 0;
-              const int slot_j = rb + j;  // position inside the cell when same
-              bool cand = true;
-              bool other_side = false;
-              if (OWNER) {
-                cand = idx_j != idx_i;
-                if (tri) count_e = idx_i < idx_j;
-                else if (same) count_e = nonper ? (slot_j > ii) : (!real_j || slot_j > ii);
-                else if (!(meta & F_BACK)) count_e = true;
-                else {
-                  count_e = !nonper && !real_j && (meta & F_REALCELL);
-                  other_side = count_e;
-                }
-              } else if (!CROSS) {
-                if (tri) cand = idx_i < idx_j;
-                else if (same) cand = (slot_j > ii) && (nonper || real_i || real_j);
-                else cand = nonper || real_i || real_j;
-              } else {
-                if (!tri && !nonper) cand = same ? real_i : (real_i || real_j);
-              }
-              if (cand) {
-                dvf[0] = pi[0] - p.x;
-                dvf[1] = pi[1] - p.y;
-                dvf[2] = (N == 3) ? pi[2] - p.z : 0.f;
-                d2f = fmaf(dvf[2], dvf[2], fmaf(dvf[1], dvf[1], dvf[0] * dvf[0]));
-                if (ABS_PF) {
-                  xj[0] = (T)p.x;
-                  xj[1] = (T)p.y;
-                  if (N == 3) xj[N - 1] = (T)p.z;
-                } else {
-#pragma unroll
-                  for (int d = 0; d < N; d++) xj[d] = s_x[warp][d][ABS_PF ? 0 : j];
-                }
-                if (!FP64 || SPLIT) {
-                  // FP32 input or split form: well inside the cutoff the FP32 value decides
-                  if (d2f <= g.thr_lo) {
-                    hit = true;
-                    sure = true;
-                  }
-                }
-                if (!sure) {
-                  T dx = xsub(xi[0], xj[0]);
-                  d2 = xmul(dx, dx);
-#pragma unroll
-                  for (int d = 1; d < N; d++) {
-                    T dd = xsub(xi[d], xj[d]);
-                    d2 = xadd(d2, xmul(dd, dd));
-                  }
-                  hit = d2 <= g.cutoff_sqr;
-                  if (hit && d2 > band) {
-                    if (!same) {
-                      int cj[3] = {ci[0] + (meta & 255) - 128, ci[1] + ((meta >> 8) & 255) - 128,
-                                   ci[2] + ((meta >> 16) & 255) - 128};
-                      T ctr_j[3];
-                      cell_center<T, N>(g, cj, ctr_j);
-                      hit = projection_pass<T, N>(g, ctr_i, ctr_j, xi, xj);
-                      if (hit && other_side) count_e = projection_pass<T, N>(g, ctr_j, ctr_i, xj, xi);
-                    }
-                  }
-                }
-              }
-            }
-            // ---------------- operator epilogues
-            if constexpr (OPK == OPK_NL) {
-              unsigned bal = __ballot_sync(FULL, hit);
-              if (bal) {
-                unsigned long long base = 0;
-                int leader = __ffs(bal) - 1;
-                if (lane == leader) base = atomicAdd(A.nl_count, (unsigned long long)__popc(bal));
-                base = __shfl_sync(FULL, base, leader);
-                if (hit) {
-                  T dval;
-                  if (sure && ABS_PF) {
-                    T dx = xsub(xi[0], xj[0]);
-                    T e2 = xmul(dx, dx);
-#pragma unroll
-                    for (int d = 1; d < N; d++) {
-                      T dd = xsub(xi[d], xj[d]);
-                      e2 = xadd(e2, xmul(dd, dd));
-                    }
-                    dval = xsqrt(e2);
-                  } else {
-                    dval = sure ? (T)sqrtf(d2f) : xsqrt(d2);
-                  }
-                  unsigned long long pos = base + __popc(bal & ((1u << lane) - 1u));
-                  if ((long long)pos < A.nl_cap) {
-                    A.nl_i[pos] = idx_i;
-                    A.nl_j[pos] = idx_j;
-                    A.nl_d[pos] = dval;
-                  }
-                }
-              }
-            } else if constexpr (OPK == OPK_SCALAR) {
-              if (hit) {
-                if (A.op == 2) {
-                  c_acc++;
-                } else if (sure) {
-                  float uu, gg;
-                  pair_value<float, T>(A, A.op, d2f, idx_i, idx_j, uu, gg);
-                  e_part += (FA)uu;
-                } else {
-                  V uu, gg;
-                  pair_value<V, T>(A, A.op, (V)d2, idx_i, idx_j, uu, gg);
-                  e_part += (FA)uu;
-                }
-              }
-            } else if constexpr (IS_F) {
-              if (hit) {
-                FA uu, gg;
-                FA df[3] = {0, 0, 0};
-                FA dv[3] = {0, 0, 0};
-                if (sure) {
-                  float uf, gf;
-                  pair_value<float, T>(A, A.op, d2f, idx_i, idx_j, uf, gf);
-                  uu = (FA)uf;
-                  gg = (FA)gf;
-#pragma unroll
-                  for (int d = 0; d < N; d++) dv[d] = (FA)dvf[d];
-                } else {
-                  V uv, gv;
-                  pair_value<V, T>(A, A.op, (V)d2, idx_i, idx_j, uv, gv);
-                  uu = (FA)uv;
-                  gg = (FA)gv;
-#pragma unroll
-                  for (int d = 0; d < N; d++) dv[d] = (FA)xsub(xi[d], xj[d]);
-                }
-#pragma unroll
-                for (int d = 0; d < N; d++) df[d] = gg * dv[d];
-                if constexpr (OPK == OPK_ADJ) {
-                  if (count_e) {
-                    // virial W += g dx dx^T (g = u'(r)/r), and the parameter derivatives of the LJ term
-                    adj[0] += gg * dv[0] * dv[0];
-                    adj[1] += gg * dv[1] * dv[1];
-                    adj[2] += gg * dv[2] * dv[2];
-                    adj[3] += gg * dv[0] * dv[1];
-                    adj[4] += gg * dv[0] * dv[2];
-                    adj[5] += gg * dv[1] * dv[2];
-                    FA eps = (FA)A.p[0], sig = (FA)A.p[1];
-                    int cls = 0;
-                    if (A.ntypes > 0) {
-                      const int ti = A.tx[idx_i], tj = A.tx[idx_j];
-                      eps = (FA)A.eps_t[ti * A.ntypes + tj];
-                      sig = (FA)A.sig_t[ti * A.ntypes + tj];
-                      cls = ti + tj;  // 2 types: AA = 0, AB = 1, BB = 2
-                    }
-                    const FA c12 = (FA)A.p[2], c6 = (FA)A.p[3];
-                    const FA dd2 = sure ? (FA)d2f : (FA)d2;
-                    const FA sr2 = sig * sig / dd2;
-                    const FA sr6 = sr2 * sr2 * sr2;
-                    const FA sr12 = sr6 * sr6;
-                    const FA lj = c12 * sr12 - c6 * sr6;
-                    const FA dsg = eps * (FA(12) * c12 * sr12 - FA(6) * c6 * sr6) / sig;
-#pragma unroll
-                    for (int k = 0; k < 3; k++) {
-                      adj[6 + k] += (cls == k) ? lj : FA(0);
-                      adj[9 + k] += (cls == k) ? dsg : FA(0);
-                    }
-                  }
-                }
-                if (ie != cur) {
-                  if (cur >= 0) {
-#pragma unroll
-                    for (int d = 0; d < N; d++) atomicAdd(&s_if[warp][d][cur], acc[d]);
-                  }
-                  cur = ie;
-#pragma unroll
-                  for (int d = 0; d < N; d++) acc[d] = FA(0);
-                }
-#pragma unroll
-                for (int d = 0; d < N; d++) acc[d] -= df[d];
-                if (!OWNER || count_e) e_part += uu;
-                if (CROSS) {
-#pragma unroll
-                  for (int d = 0; d < N; d++) atomicAdd(&A.fy[(int64_t)idx_j * N + d], (double)df[d]);
-                }
-              }
-            } else if constexpr (OPK == OPK_MIN) {
-              if (hit) {
-                T dd2 = sure ? (T)d2f : d2;
-                if (sure && ABS_PF) {
-                  T dx = xsub(xi[0], xj[0]);
-                  dd2 = xmul(dx, dx);
-#pragma unroll
-                  for (int d = 1; d < N; d++) {
-                    T dd = xsub(xi[d], xj[d]);
-                    dd2 = xadd(dd2, xmul(dd, dd));
-                  }
-                }
-                if (dd2 < best_d2 || (dd2 == best_d2 && (idx_i < best_i || (idx_i == best_i && idx_j < best_j)))) {
-                  best_d2 = dd2;
-                  best_i = idx_i;
-                  best_j = idx_j;
-                }
-              }
-            } else if constexpr (OPK == OPK_HIST) {
-              if (hit) {
-                bool exact_r = !sure;
-                T r = 0;
-                int b = -1;
-                if (sure) {
-                  float rf = sqrtf(d2f);
-                  int lo = 0, hi = A.nbins + 1;
-                  while (lo < hi) {
-                    int mid = (lo + hi) >> 1;
-                    if ((float)A.bins[mid] >= rf) hi = mid;
-                    else lo = mid + 1;
-                  }
-                  b = lo - 1;
-                  const float tol = rf * 2.44140625e-4f;  // an edge within 2^-12: decide exactly
-                  if ((lo <= A.nbins && fabsf((float)A.bins[lo] - rf) <= tol) ||
-                      (lo >= 1 && fabsf((float)A.bins[lo - 1] - rf) <= tol))
-                    exact_r = true;
-                  r = (T)rf;
-                }
-                if (exact_r) {
-                  T dx = xsub(xi[0], xj[0]);
-                  T e2 = xmul(dx, dx);
-#pragma unroll
-                  for (int d = 1; d < N; d++) {
-                    T dd = xsub(xi[d], xj[d]);
-                    e2 = xadd(e2, xmul(dd, dd));
-                  }
-                  r = xsqrt(e2);
-                  int lo = 0, hi = A.nbins + 1;
-                  while (lo < hi) {
-                    int mid = (lo + hi) >> 1;
-                    if (A.bins[mid] >= r) hi = mid;
-                    else lo = mid + 1;
-                  }
-                  b = lo - 1;
-                }
-                if (b >= 0 && b < A.nbins) {
-                  FA dv[3] = {0, 0, 0};
-                  if (sure) {
-#pragma unroll
-                    for (int d = 0; d < N; d++) dv[d] = (FA)dvf[d];
-                  } else {
-#pragma unroll
-                    for (int d = 0; d < N; d++) dv[d] = (FA)xsub(xi[d], xj[d]);
-                  }
-                  if (tri) {
-                    FA rv[3];
-#pragma unroll
-                    for (int a = 0; a < N; a++) {
-                      FA s = 0;
-#pragma unroll
-                      for (int k = 0; k < N; k++) s += (FA)g.Rinv[a][k] * dv[k];
-                      rv[a] = s;
-                    }
-#pragma unroll
-                    for (int a = 0; a < N; a++) dv[a] = rv[a];
-                  }
-                  const T* vy = CROSS ? A.vy : A.vx;
-                  FA dot = 0;
-#pragma unroll
-                  for (int d = 0; d < N; d++)
-                    dot += ((FA)A.vx[(int64_t)idx_i * N + d] - (FA)vy[(int64_t)idx_j * N + d]) * dv[d];
-                  atomicAdd(&s_hc[b], 1u);
-                  atomicAdd(&s_hs[b], (double)(dot / (FA)r));
-                }
-              }
-            }
-          }
-          if constexpr (IS_F) {
-            if (cur >= 0) {
-#pragma unroll
-              for (int d = 0; d < N; d++) atomicAdd(&s_if[warp][d][cur], acc[d]);
-            }
-          }
-          __syncwarp();
-        }
-        __syncwarp();
-      }
-      e_tot += (double)e_part;
-      e_part = 0;
-      if constexpr (IS_F) {
-        __syncwarp();
-        if (grp == 0 && vi) {
-          FA f[3] = {s_if[warp][0][il], s_if[warp][1][il], s_if[warp][2][il]};
-          if (OWNER) {
-            if (act_i) {
-#pragma unroll
-              for (int d = 0; d < N; d++) A.fx[(int64_t)idx_i * N + d] = (double)f[d];
-            }
-          } else if (f[0] != FA(0) || f[1] != FA(0) || f[2] != FA(0)) {
-#pragma unroll
-            for (int d = 0; d < N; d++) atomicAdd(&A.fx[(int64_t)idx_i * N + d], (double)f[d]);
-          }
-        }
-        __syncwarp();
-      }
-    }
-  }
-
-  // ---------------- block reductions to per-block partials
-  if constexpr (OPK == OPK_SCALAR || OPK == OPK_FORCES) {
-    double e = e_tot;
-    unsigned long long c = c_acc;
-#pragma unroll
-    for (int s = 16; s > 0; s >>= 1) {
-      e += __shfl_xor_sync(FULL, e, s);
-      c += __shfl_xor_sync(FULL, c, s);
-    }
-    if (lane == 0) {
-      s_red[warp] = e;
-      s_redc[warp] = c;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double es = 0;
-      unsigned long long cs = 0;
-      for (int k = 0; k < kWarps; k++) {
-        es += s_red[k];
-        cs += s_redc[k];
-      }
-      A.part_e[blockIdx.x] = es;
-      A.part_c[blockIdx.x] = cs;
-    }
-  } else if constexpr (OPK == OPK_ADJ) {
-    __shared__ double s_adj[kWarps][kAdjVals];
-    double v[kAdjVals];
-    v[0] = e_tot;
-#pragma unroll
-    for (int k = 1; k < kAdjVals; k++) v[k] = (double)adj[k - 1];
-#pragma unroll
-    for (int k = 0; k < kAdjVals; k++) {
-#pragma unroll
-      for (int s = 16; s > 0; s >>= 1) v[k] += __shfl_xor_sync(FULL, v[k], s);
-    }
-    if (lane == 0) {
-#pragma unroll
-      for (int k = 0; k < kAdjVals; k++) s_adj[warp][k] = v[k];
-    }
-    __syncthreads();
-    if (threadIdx.x < kAdjVals) {
-      double acc = 0;
-      for (int w = 0; w < kWarps; w++) acc += s_adj[w][threadIdx.x];
-      A.part_v[(int64_t)blockIdx.x * kAdjVals + threadIdx.x] = acc;
-    }
-  } else if constexpr (OPK == OPK_MIN) {
-#pragma unroll
-    for (int s = 16; s > 0; s >>= 1) {
-      T od = __shfl_xor_sync(FULL, best_d2, s);
-      int oi_ = __shfl_xor_sync(FULL, best_i, s);
-      int oj_ = __shfl_xor_sync(FULL, best_j, s);
-      if (od < best_d2 || (od == best_d2 && (oi_ < best_i || (oi_ == best_i && oj_ < best_j)))) {
-        best_d2 = od;
-        best_i = oi_;
-        best_j = oj_;
-      }
-    }
-    __shared__ T s_md[kWarps];
-    __shared__ int s_mi[kWarps], s_mj[kWarps];
-    if (lane == 0) {
-      s_md[warp] = best_d2;
-      s_mi[warp] = best_i;
-      s_mj[warp] = best_j;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      T bd = s_md[0];
-      int bi = s_mi[0], bj = s_mj[0];
-      for (int k = 1; k < kWarps; k++) {
-        if (s_md[k] < bd || (s_md[k] == bd && (s_mi[k] < bi || (s_mi[k] == bi && s_mj[k] < bj)))) {
-          bd = s_md[k];
-          bi = s_mi[k];
-          bj = s_mj[k];
-        }
-      }
-      A.part_min_d2[blockIdx.x] = bd;
-      A.part_min_ij[2 * blockIdx.x] = bi;
-      A.part_min_ij[2 * blockIdx.x + 1] = bj;
-    }
-  } else if constexpr (OPK == OPK_HIST) {
-    __syncthreads();
-    for (int b = threadIdx.x; b < A.nbins; b += kThreads) {
-      A.part_hc[(int64_t)blockIdx.x * A.nbins + b] = s_hc[b];
-      A.part_hs[(int64_t)blockIdx.x * A.nbins + b] = s_hs[b];
-    }
-  }
-}
 
 // Fixed-order reductions of the per-block partials (deterministic results).
 __global__ void k_reduce_scalar(const double* __restrict__ pe, const unsigned long long* __restrict__ pc, int nb,
@@ -1022,75 +142,6 @@ __global__ void k_forces_out(const double* __restrict__ facc, int64_t n, DevGeom
   for (int d = 0; d < N; d++) out[i * N + d] = (T)f[d];
 }
 
-template <class T> SetView<T> view_of(const SetData& S) {
-  SetView<T> v;
-  v.px = S.px.as<T>();
-  v.py = S.py.as<T>();
-  v.pz = S.pz.as<T>();
-  v.off = S.off.as<float4>();
-  v.code = S.code.as<int>();
-  v.cell_start = S.cell_start.as<int>();
-  return v;
-}
-
-inline int opkind_of(int op) {
-  switch (op) {
-    case 1: return OPK_NL;
-    case 2: case 3: case 4: case 5: case 6: case 8: return OPK_SCALAR;
-    case 7: case 9: case 12: return OPK_FORCES;
-    case 13: return OPK_ADJ;
-    case 10: return OPK_MIN;
-    case 11: return OPK_HIST;
-    default: return -1;
-  }
-}
-
-// One wave of resident blocks (the warps loop over cells): grid = min(cells/warps, SMs x blocks per SM).
-template <class K> int resident_grid(K kernel, int want) {
-  static int sms = 0;
-  if (sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  }
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0) != cudaSuccess || per_sm <= 0) {
-    cudaGetLastError();
-    per_sm = 1;
-  }
-  return std::max(1, std::min(want, per_sm * sms));
-}
-
-template <class T, int N, int OPK, bool SPLIT, bool CROSS>
-cudaError_t launch_k(int& grid, cudaStream_t st, const PairArgs<T>& A) {
-  auto k = k_pairs<T, N, OPK, SPLIT, CROSS>;
-  grid = resident_grid(k, grid);
-  k<<<grid, kThreads, 0, st>>>(A);
-  return cudaGetLastError();
-}
-
-template <class T, int N, bool SPLIT, bool CROSS>
-cudaError_t launch_s(int opk, int& grid, cudaStream_t st, const PairArgs<T>& A) {
-  switch (opk) {
-    case OPK_NL: return launch_k<T, N, OPK_NL, SPLIT, CROSS>(grid, st, A);
-    case OPK_SCALAR: return launch_k<T, N, OPK_SCALAR, SPLIT, CROSS>(grid, st, A);
-    case OPK_FORCES: return launch_k<T, N, OPK_FORCES, SPLIT, CROSS>(grid, st, A);
-    case OPK_MIN: return launch_k<T, N, OPK_MIN, SPLIT, CROSS>(grid, st, A);
-    case OPK_HIST: return launch_k<T, N, OPK_HIST, SPLIT, CROSS>(grid, st, A);
-    case OPK_ADJ:
-      if constexpr (!CROSS) return launch_k<T, N, OPK_ADJ, SPLIT, false>(grid, st, A);
-      return cudaErrorInvalidValue;
-  }
-  return cudaErrorInvalidValue;
-}
-
-template <class T, int N>
-cudaError_t launch(int opk, int& grid, cudaStream_t st, const PairArgs<T>& A) {
-  if (A.self)
-    return A.split ? launch_s<T, N, true, false>(opk, grid, st, A) : launch_s<T, N, false, false>(opk, grid, st, A);
-  return A.split ? launch_s<T, N, true, true>(opk, grid, st, A) : launch_s<T, N, false, true>(opk, grid, st, A);
-}
 
 }  // namespace
 
@@ -1101,6 +152,24 @@ static double estimated_pairs(const Handle& h, double vol) {
   double nx = (double)h.sets[0].n;
   if (h.nsets == 1) return std::max(0.0, nx * (nx - 1) / 2 * sph / vol);
   return std::max(0.0, nx * (double)h.sets[1].n * sph / vol);
+}
+
+// Parts per cell: cells holding many particles (large cutoff at high density) are split into parts
+// that take interleaved particle chunks, so that there are enough work items for every resident warp.
+// Each part keeps at least two chunks of 32 particles.
+template <class T> int cell_split_for(const Handle& h, const Geometry<T>& g, int opk) {
+  (void)opk;
+  const double nx = (double)h.sets[0].n;
+  double real_cells = 1.0;
+  for (int i = 0; i < g.dim; i++) {
+    const double inner = (g.kind == NONPERIODIC) ? (double)g.nc[i] : (double)(g.nc[i] - 2 * g.lcell - 1);
+    real_cells *= std::max(1.0, inner);
+  }
+  const double per_cell = nx / real_cells;
+  const double warps = 152.0 * 16.0 * 2.0;  // two items per resident warp slot
+  int s = (int)std::ceil(warps / real_cells);
+  s = std::min(s, (int)(per_cell / 64.0));
+  return std::max(1, std::min(s, 64));
 }
 
 template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const void* vparams, void* vout) {
@@ -1126,6 +195,8 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
   A.split = (h.precision == 1);
   A.op = op;
   A.err = h.err.as<int>();
+  A.cell_split = cell_split_for(h, g, opk);
+  const LaunchSel sel{N, opk, A.self != 0, A.split != 0, false};
   const double c_default = (double)g.cutoff;
   for (int k = 0; k < 4; k++) A.p[k] = P ? P->p[k] : 0.0;
   if ((op == 6 || op == 7) && A.p[0] == 0.0) A.p[0] = c_default;
@@ -1277,7 +348,7 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
     }
     cudaEventRecord(h.ev[2], h.stream);  // brackets the pair kernel alone
     grid = grid_want;
-    cudaError_t e = (N == 3) ? launch<T, 3>(opk, grid, h.stream, A) : launch<T, 2>(opk, grid, h.stream, A);
+    cudaError_t e = launch_pairs(sel, grid, h.stream, A);
     cudaEventRecord(h.ev[3], h.stream);
     if (e != cudaSuccess) {
       h.last_error = std::string("pair kernel launch failed: ") + cudaGetErrorString(e);
@@ -1453,6 +524,8 @@ int run_pairs_scalar_scratch(Handle& h, const Geometry<T>& g, int op, const void
   A.split = (h.precision == 1);
   A.op = op;
   A.err = h.err.as<int>();
+  A.cell_split = 1;
+  const LaunchSel sel{N, opk, A.self != 0, A.split != 0, false};
   for (int k = 0; k < 4; k++) A.p[k] = P ? P->p[k] : 0.0;
   if (op == 6 && A.p[0] == 0.0) A.p[0] = (double)g.cutoff;
   // scratch layout: [results, 256 B][partial energy][partial count][partial min d2][partial min ij]
@@ -1474,7 +547,7 @@ int run_pairs_scalar_scratch(Handle& h, const Geometry<T>& g, int op, const void
   unsigned long long* r_c = (unsigned long long*)(base + 8);
   T* r_md = (T*)(base + 16);
   int* r_mij = (int*)(base + 24);
-  cudaError_t e = (N == 3) ? launch<T, 3>(opk, grid, h.stream, A) : launch<T, 2>(opk, grid, h.stream, A);
+  cudaError_t e = launch_pairs(sel, grid, h.stream, A);
   if (e != cudaSuccess) {
     h.last_error = std::string("pair kernel launch failed: ") + cudaGetErrorString(e);
     return ERR_CUDA;
@@ -1519,30 +592,14 @@ int run_pairs_scalar_scratch(Handle& h, const Geometry<T>& g, int op, const void
 // Number of per-block partial slots the scalar map needs on this device (one resident wave).
 int pairs_scalar_blocks_needed(Handle& h, int op) {
   const int opk = opkind_of(op);
+  if (opk != OPK_SCALAR && opk != OPK_MIN) return -1;
   int sms = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  int per_sm = 0;
-  cudaError_t e = cudaErrorInvalidValue;
-  const bool self = (h.nsets == 1), split = (h.precision == 1);
-  auto occ = [&](auto k) { return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, 0); };
-#define CLM_OCC(T, N)                                                                                    \
-  if (opk == OPK_SCALAR)                                                                                 \
-    e = split ? (self ? occ(k_pairs<T, N, OPK_SCALAR, true, false>) : occ(k_pairs<T, N, OPK_SCALAR, true, true>)) \
-              : (self ? occ(k_pairs<T, N, OPK_SCALAR, false, false>) : occ(k_pairs<T, N, OPK_SCALAR, false, true>)); \
-  else                                                                                                   \
-    e = split ? (self ? occ(k_pairs<T, N, OPK_MIN, true, false>) : occ(k_pairs<T, N, OPK_MIN, true, true>))       \
-              : (self ? occ(k_pairs<T, N, OPK_MIN, false, false>) : occ(k_pairs<T, N, OPK_MIN, false, true>));
-  if (h.dtype == 1) {
-    if (h.dim == 3) { CLM_OCC(double, 3) } else { CLM_OCC(double, 2) }
-  } else {
-    if (h.dim == 3) { CLM_OCC(float, 3) } else { CLM_OCC(float, 2) }
-  }
-#undef CLM_OCC
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    return -1;
-  }
+  const LaunchSel sel{h.dim, opk, h.nsets == 1, h.precision == 1, false};
+  const int per_sm = (h.dtype == 1) ? pairs_blocks_per_sm(sel, (const PairArgs<double>*)nullptr)
+                                    : pairs_blocks_per_sm(sel, (const PairArgs<float>*)nullptr);
+  if (per_sm <= 0 || sms <= 0) return -1;
   const int64_t want = std::max<int64_t>(1, (h.sets[0].ncells + kWarps - 1) / kWarps);
   return (int)std::min<int64_t>(want, (int64_t)per_sm * sms);
 }

@@ -186,6 +186,62 @@ int32_t clm_last_timings(clm_handle h, float* build_ms, float* map_ms);
  * the handle's device current. */
 int32_t clm_run_noalloc(clm_handle h, int32_t op_id, const clm_op_params* params, clm_outputs* out);
 
+/* LJ energy, forces and adjoint in one call: clm_run(h, CLM_OP_LJ_ADJOINT, params, out).  The
+ * reference has no such entry point (it differentiates its map with ForwardDiff dual numbers,
+ * test/examples/generic_types.jl:10-20,102); out->forces_x and out->adjoint are required. */
+int32_t clm_lj_adjoint(clm_handle h, const clm_op_params* params, clm_outputs* out);
+
+/* ---------------------------------------------------------------- batches of independent systems
+ * Many periodic systems of uneven size in one handle: one cell list over a global cell index, one
+ * launch per kernel for all systems, and optionally the whole step (build + operators) replayed
+ * as a CUDA graph.  The reference handles one system per ParticleSystem (src/API/ParticleSystem.jl:
+ * 142-202); a batch is the loop `for sys in systems; pairwise!(f, sys); end` in one call.
+ * Positions: clm_set_positions(h, 0, xyz, n_total, is_device) with the systems concatenated. */
+typedef struct {
+  double* scalar;         /* nsys: the operator's sum per system (COUNT: the count); NaN for a failed system */
+  int64_t* count;         /* nsys: pairs per system (COUNT, NL) */
+  void* forces;           /* n_total x dim, handle dtype (force operators) */
+  int32_t out_on_device;  /* 1 if scalar/count/forces are device pointers */
+  int32_t reserved;
+} clm_batch_outputs;
+
+/* A handle for batches (set 0 only).  clm_set_box/clm_build/clm_run refuse it (CLM_ERR_STATE). */
+int32_t clm_batched_create(int32_t dtype, int32_t dim, clm_handle* h);
+
+/* nsys systems; offsets[nsys+1] delimit each system's particles in the concatenated positions;
+ * cells: nsys unit cells, dim x dim column-major each (CLM_TRICLINIC), or dim sides each
+ * (CLM_ORTHO); one cutoff and lcell for all.  A system whose cell fails the reference's check
+ * (Box.jl:243, plane distance > 2 cutoff) gets status CLM_ERR_CELL_TOO_SMALL and is skipped. */
+int32_t clm_batched_set_systems(clm_handle h, int64_t nsys, const int64_t* offsets, const double* cells,
+                                int32_t cell_kind, double cutoff, int32_t lcell);
+
+/* One step: build the cell lists of all systems, then run `nops` operators (NL, COUNT, SUM_*,
+ * SOFT_ENERGY, LJ_ENERGY, SOFT_FORCES, LJ_FORCES, INV_D_FORCES; no type tables), outs[k] receiving
+ * the results of ops[k].  The neighbour list (at most one NL op per step) is read with clm_nl_count /
+ * clm_nl_fetch (global particle indices).  With the graph on, the first call runs the step directly
+ * and records it; later calls with the same operators, parameters and sizes replay the recording. */
+int32_t clm_batched_run(clm_handle h, int32_t nops, const int32_t* ops, const clm_op_params* params,
+                        clm_batch_outputs* outs);
+
+/* Per-system status of the last step (CLM_OK, CLM_ERR_CELL_TOO_SMALL, CLM_ERR_NAN). */
+int32_t clm_batched_status(clm_handle h, int32_t* status, int64_t nsys);
+
+/* Replay steps as a CUDA graph (1) or launch them one by one (0, the default). */
+int32_t clm_batched_set_graph(clm_handle h, int32_t enable);
+
+/* Cell-tile and block shape: lcell (cells per cutoff), parts per cell, resident blocks per SM
+ * divided by grid_div.  Any value <= 0 keeps the current one. */
+int32_t clm_batched_set_config(clm_handle h, int32_t lcell, int32_t cell_split, int32_t grid_div);
+
+/* Autotuner: times every candidate (lcell 1..3, parts per cell 1..2, grid_div 1..2) on `reps`
+ * steps of the given operators with the current positions, keeps the fastest, and returns it in
+ * config[3] (lcell, cell_split, grid_div) with its median step time in best_ms. */
+int32_t clm_batched_autotune(clm_handle h, int32_t nops, const int32_t* ops, const clm_op_params* params,
+                             int32_t reps, int32_t* config, float* best_ms);
+
+/* Device time of the last step (build + operators, CUDA events) and kernels it launched. */
+int32_t clm_batched_last_step(clm_handle h, float* step_ms, int64_t* launches);
+
 /* Number of CUDA kernels this handle has launched so far (cumulative). */
 int32_t clm_stats(clm_handle h, int64_t* kernel_launches);
 
