@@ -120,6 +120,261 @@ def cpu_reference(x, M, steps, warmup, threads):
     return pairs, dt
 
 
+# ---------------------------------------------------------------------------------------------- other forms
+# Algorithmic flops per within-cutoff pair of each operator epilogue (sqrt/div = 1, FMA = 2).
+F_OP = {"nl": 1.0, "soft_energy": 4.0, "soft_forces": 15.0, "lj_forces": 20.0, "lj_forces_types": 22.0,
+        "lj_adjoint_types": 42.0, "rhist": 11.0}
+
+
+def candidates_per_hit(h, cutoff, dim=3):
+    """R = 27 h^3 / ((4/3) pi rc^3) in 3D, 9 h^2 / (pi rc^2) in 2D, for cell sides h."""
+    h = np.asarray(h, np.float64)
+    if dim == 3:
+        return 27.0 * float(np.prod(h)) / (4.0 / 3.0 * math.pi * cutoff ** 3)
+    return 9.0 * float(np.prod(h)) / (math.pi * cutoff ** 2)
+
+
+def roofline_pairs(F, peak_tflops, bytes_per_pair=0.0, hbm_gbs=None):
+    """min(peak_pipe / F, peak_HBM / bytes per pair) in pairs/s."""
+    r = peak_tflops * 1e12 / F
+    if bytes_per_pair and hbm_gbs:
+        r = min(r, hbm_gbs * 1e9 / bytes_per_pair)
+    return r
+
+
+class Plain:
+    """One library handle driven through the C ABI with device-resident inputs, on a torch stream."""
+
+    def __init__(self, L, A, dtype, dim, nsets, stream):
+        self.L, self.A = L, A
+        self.h = C.c_void_p()
+        assert L.clm_create(A.CLM_F64 if dtype == np.float64 else A.CLM_F32, dim, nsets, C.byref(self.h)) == 0
+        assert L.clm_set_stream(self.h, C.c_void_p(stream.cuda_stream)) == 0
+        self.stream = stream
+
+    def box(self, M, kind, cutoff, lcell=1):
+        Mf = np.ascontiguousarray(np.asarray(M, np.float64).flatten(order="F"))
+        assert self.L.clm_set_box(self.h, Mf.ctypes.data_as(C.POINTER(C.c_double)), kind, cutoff, lcell) == 0
+
+    def step(self, sets, op, p, o):
+        L = self.L
+        st = 0
+        for k, t in enumerate(sets):
+            st = st or L.clm_set_positions(self.h, k, C.c_void_p(t.data_ptr()), t.shape[0], 1)
+        st = st or L.clm_run(self.h, op, C.byref(p), C.byref(o))
+        if st:
+            buf = C.create_string_buffer(512)
+            L.clm_last_error(self.h, buf, 512)
+            raise RuntimeError(f"clm status {st}: {buf.value.decode()}")
+
+    def timed(self, sets, op, p, o, steps, warmup, flush):
+        import torch
+        for _ in range(warmup):
+            self.step(sets, op, p, o)
+        torch.cuda.synchronize()
+        tot, kern, build = 0.0, [], []
+        for _ in range(steps):
+            with torch.cuda.stream(self.stream):
+                flush.add_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(self.stream)
+            self.step(sets, op, p, o)
+            e1.record(self.stream)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+            bm, mm = C.c_float(), C.c_float()
+            self.L.clm_last_timings(self.h, C.byref(bm), C.byref(mm))
+            kern.append(mm.value)
+            build.append(bm.value)
+        return tot / steps, statistics.median(kern), statistics.median(build)
+
+    def count(self, sets):
+        o = self.A.Outputs()
+        self.step(sets, self.A.OP["count"], self.A.OpParams(), o)
+        return int(o.count)
+
+    def cell_size(self):
+        cs = np.zeros(3)
+        self.L.clm_get_box(self.h, None, cs.ctypes.data, None, None, None, None, None, None)
+        return cs
+
+    def close(self):
+        self.L.clm_destroy(self.h)
+
+
+def log(msg):
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
+def measure_forms(pkg, L, A, dev, stream, flush, peaks, which, steps, warmup):
+    """The other configurations of the metric: plain FP64 box (neighbour list, soft energy, forces), the
+    batched form, the adjoint form and the two-set radial histogram, each exact and FP32-split."""
+    import torch
+    W = pkg.workloads
+    out = {}
+    p32, p64, hbm = peaks["fp32_tflops"], peaks["fp64_tflops"], peaks["hbm_gbs"]
+
+    def frac_entry(pairs, ms, F, peak, bpp=0.0):
+        v = pairs / (ms * 1e-3)
+        roof = roofline_pairs(F, peak, bpp, hbm)
+        return {"pairs_per_s": v, "kernel_ms": ms, "roofline_pairs_per_s": roof, "frac": v / roof}
+
+    if "cfg1" in which:
+        log("cfg1")
+        x, side = W.cfg1()
+        xd = torch.from_numpy(x).to(dev)
+        f = torch.zeros_like(xd)
+        P = Plain(L, A, np.float64, 3, 1, stream)
+        P.box(np.diag(side), A.CLM_ORTHO, 8.0)
+        pairs = P.count([xd])
+        R = candidates_per_hit(P.cell_size(), 8.0)
+        res = {"workload": "uniform 100k f64 orthorhombic [0,100)^3 rc 8", "pairs": pairs, "candidates_per_hit": R}
+        for opname in ("nl", "soft_energy", "soft_forces"):
+            o = A.Outputs()
+            o.forces_x = f.data_ptr()
+            o.out_on_device = 1
+            p = A.OpParams()
+            for prec, tag in ((A.CLM_PREC_EXACT, "exact"), (A.CLM_PREC_SPLIT, "split")):
+                L.clm_set_precision(P.h, prec)
+                st_ms, k_ms, b_ms = P.timed([xd], A.OP[opname], p, o, steps, warmup, flush)
+                F = 8 * R + F_OP[opname]
+                e = frac_entry(pairs, k_ms, F, p64, 16.0 if opname == "nl" else 0.0)
+                e.update({"step_ms": st_ms, "build_ms": b_ms, "step_pairs_per_s": pairs / (st_ms * 1e-3),
+                          "frac_of_fp32_roofline": e["pairs_per_s"] / roofline_pairs(F, p32)})
+                res[f"{opname}/{tag}"] = e
+        P.close()
+        out["cfg1"] = res
+
+    if "cfg3" in which:
+        log("cfg3")
+        x, off, sides = W.cfg3()
+        n = x.shape[0]
+        xd = torch.from_numpy(x).to(dev)
+        cells = np.repeat(sides[:, None], 3, axis=1)
+        bs = pkg.BatchedSystems(positions=xd, offsets=off, unitcells=cells, cutoff=6.0)
+        cnt = bs.run(pkg.Count())[0]
+        pairs = int(cnt.sum())
+        valid = bs.status() == 0
+        h = sides / np.floor(sides / 6.0)
+        Rs = np.array([candidates_per_hit([hh] * 3, 6.0) for hh in h])
+        R = float(np.sum(Rs[valid] * cnt[valid]) / max(1, pairs))
+        F = (8 * R + F_OP["nl"]) + (8 * R + F_OP["soft_energy"])  # one step: neighbour list + soft energy
+        res = {"workload": "4096 uniform f64 systems, n log-uniform 64-20000, rho 0.1, rc 6 (NL + soft energy)",
+               "n_particles": n, "pairs": pairs, "invalid_systems": int((~valid).sum()), "candidates_per_hit": R}
+        tune = bs.autotune(pkg.NeighborList(), pkg.SoftEnergy(), reps=2)
+        res["autotuned"] = tune
+        for tag in ("exact", "split"):
+            bs.set_precision(tag)
+            bs.graph = True
+            ts = []
+            for k in range(warmup + steps):
+                with torch.cuda.stream(stream):
+                    flush.add_(1.0)
+                torch.cuda.synchronize()
+                bs.run(pkg.NeighborList(), pkg.SoftEnergy())
+                if k >= warmup:
+                    ts.append(bs.last_step()["step_ms"])
+            ms = statistics.median(ts)
+            e = frac_entry(pairs, ms, F, p64, 16.0)
+            e.update({"graph_launches": bs.last_step()["launches"], "step_ms": ms})
+            res[tag] = e
+            bs.graph = False
+        # the plain path on the same systems: one handle, one system at a time (host loop)
+        P = Plain(L, A, np.float64, 3, 1, stream)
+        o = A.Outputs()
+        p = A.OpParams()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for s in range(len(sides)):
+            if not valid[s]:
+                continue
+            P.box(np.diag([sides[s]] * 3), A.CLM_ORTHO, 6.0)
+            xs = xd[off[s]:off[s + 1]]
+            P.step([xs], A.OP["nl"], p, o)
+            P.step([xs], A.OP["soft_energy"], p, o)
+        torch.cuda.synchronize()
+        plain_ms = (time.perf_counter() - t0) * 1e3
+        P.close()
+        res["plain_loop"] = {"step_ms": plain_ms, "pairs_per_s": pairs / (plain_ms * 1e-3)}
+        res["batched_over_plain"] = {t: plain_ms / res[t]["step_ms"] for t in ("exact", "split")}
+        bs.close()
+        del xd
+        out["cfg3"] = res
+
+    if "cfg4" in which:
+        log("cfg4")
+        x, Lb, t, eps, sig = W.cfg4()
+        n = x.shape[0]
+        xd = torch.from_numpy(x).to(dev)
+        f = torch.zeros_like(xd)
+        P = Plain(L, A, np.float32, 3, 1, stream)
+        P.box(np.diag([Lb] * 3), A.CLM_ORTHO, 2.5)
+        pairs = P.count([xd])
+        R = candidates_per_hit(P.cell_size(), 2.5)
+        ti = np.ascontiguousarray(t, np.int32)
+        et, stb = np.ascontiguousarray(eps), np.ascontiguousarray(sig)
+        p = A.OpParams()
+        p.p[0], p.p[1], p.p[2], p.p[3] = 1.0, 1.0, 4.0, 4.0
+        p.ntypes, p.types_x, p.eps_table, p.sig_table = 2, ti.ctypes.data, et.ctypes.data, stb.ctypes.data
+        adj = np.zeros(32)
+        o = A.Outputs()
+        o.forces_x = f.data_ptr()
+        o.out_on_device = 1
+        o.adjoint = adj.ctypes.data
+        res = {"workload": "200k f32 80:20 LJ mixture, jittered fcc rho 1.2, cubic, rc 2.5", "pairs": pairs,
+               "candidates_per_hit": R}
+        st_ms, k_ms, b_ms = P.timed([xd], A.OP["lj_adjoint"], p, o, steps, warmup, flush)
+        e = frac_entry(pairs, k_ms, 8 * R + F_OP["lj_adjoint_types"], p32)
+        e.update({"step_ms": st_ms, "build_ms": b_ms})
+        res["adjoint"] = e
+        st_ms, k_ms, b_ms = P.timed([xd], A.OP["lj_forces"], p, o, steps, warmup, flush)
+        e = frac_entry(pairs, k_ms, 8 * R + F_OP["lj_forces_types"], p32)
+        e.update({"step_ms": st_ms, "build_ms": b_ms})
+        res["forces_only"] = e
+        P.close()
+        out["cfg4"] = res
+
+    for dim in (3, 2):
+        key = "cfg5" if dim == 3 else "cfg5_2d"
+        if key not in which:
+            continue
+        log(key)
+        x, y, vx, vy, side = W.cfg5(dim=dim)
+        bins = np.ascontiguousarray(W.cfg5_bins())
+        xd, yd = torch.from_numpy(x).to(dev), torch.from_numpy(y).to(dev)
+        vxa, vya = np.ascontiguousarray(vx), np.ascontiguousarray(vy)
+        P = Plain(L, A, np.float64, dim, 2, stream)
+        P.box(np.diag(side), A.CLM_ORTHO, 25.0)
+        p = A.OpParams()
+        p.nbins, p.vel_x, p.vel_y, p.bins = 50, vxa.ctypes.data, vya.ctypes.data, bins.ctypes.data
+        hc = np.zeros(50, np.int64)
+        hs = np.zeros(50)
+        o = A.Outputs()
+        o.hist_count, o.hist_sum = hc.ctypes.data, hs.ctypes.data
+        R = candidates_per_hit(P.cell_size()[:dim], 25.0, dim)
+        res = {"workload": f"2 x 2M f64 {dim}D uniform, side 250, rc 25, 50 log bins 0.1-25, v ~ N(0, 300^2)",
+               "candidates_per_hit": R}
+        pairs = None
+        for prec, tag in ((A.CLM_PREC_SPLIT, "split"), (A.CLM_PREC_EXACT, "exact")):
+            L.clm_set_precision(P.h, prec)
+            st_ms, k_ms, b_ms = P.timed([xd, yd], A.OP["rhist"], p, o, 1 if dim == 2 else max(1, steps // 5),
+                                        1, flush)
+            log(f"{key} {tag}: {k_ms:.1f} ms per map")
+            if pairs is None:
+                pairs = int(hc.sum())  # pairs with r >= 0.1 that fall in a bin
+                res["pairs_in_bins"] = pairs
+            e = frac_entry(pairs, k_ms, 8 * R + F_OP["rhist"], p64)
+            e.update({"step_ms": st_ms, "build_ms": b_ms, "frac_of_fp32_roofline":
+                      e["pairs_per_s"] / roofline_pairs(8 * R + F_OP["rhist"], p32)})
+            res[tag] = e
+            if dim == 2:
+                break  # the exact FP64 form of the 2D case is left to the test-suite (minutes per step)
+        P.close()
+        out[key] = res
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -128,6 +383,8 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--ncell", type=int, default=64, help="fcc cells per side (64 -> 1,048,576 particles)")
     ap.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU baseline sample")
+    ap.add_argument("--forms", default="cfg1,cfg3,cfg4,cfg5,cfg5_2d",
+                    help="other configurations measured beside the headline (comma list, '' for none)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -276,6 +533,20 @@ def main():
     if os.path.exists(tj):
         traffic = json.load(open(tj)).get("k_pairs_lj_forces_f32_per_launch_bytes")
 
+    peaks.clm_peak_fp64_gflops.restype = C.c_double
+    peaks.clm_peak_fp64_gflops.argtypes = [C.c_int]
+    fp64_peak = peaks.clm_peak_fp64_gflops(1 << 12) / 1e3
+    hbm = None
+    mp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(mp):
+        hbm = json.load(open(mp)).get("hbm_gbs")
+    forms_other = {}
+    which = [w for w in args.forms.split(",") if w]
+    if which:
+        forms_other = measure_forms(pkg, L, A, dev, stream, flush,
+                                    {"fp32_tflops": fp32_peak, "fp64_tflops": fp64_peak, "hbm_gbs": hbm or 6795.1},
+                                    which, max(3, min(args.steps, 10)), 3)
+
     cpu = None
     if rank == 0:
         try:
@@ -293,7 +564,10 @@ def main():
                    "cell": "triclinic", "op": "lj_energy_forces", "l2": "flushed between steps (256 MiB write)",
                    "parallelism": f"replicas x{world}", "energy": energy},
         "forms": {"exact": {"value": value, "kernel_ms": k_exact},
-                  "split": {"value": split_value, "kernel_ms": k_split, "ms_per_step": t_split / args.steps}},
+                  "split": {"value": split_value, "kernel_ms": k_split, "ms_per_step": t_split / args.steps},
+                  **forms_other},
+        "peaks": {"fp32_tflops": fp32_peak, "fp64_tflops": fp64_peak, "hbm_gbs": hbm,
+                  "source": "FMA-loop probes (libclm_peaks.so) in this run; HBM from MEASURED_PEAKS.json"},
         "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": int(x_pin.numel() * 4),
                 "d2h_bytes_per_step": int(f_pin.numel() * 4 + 8)},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",

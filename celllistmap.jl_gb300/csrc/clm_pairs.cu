@@ -50,6 +50,11 @@ using namespace pk;
 
 namespace {
 
+template <class T> __global__ void k_to_f32(const T* __restrict__ in, int64_t n, float* __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)in[i];
+}
+
 // Fixed-order reductions of the per-block partials (deterministic results).
 __global__ void k_reduce_scalar(const double* __restrict__ pe, const unsigned long long* __restrict__ pc, int nb,
                                 double* __restrict__ out_e, unsigned long long* __restrict__ out_c) {
@@ -169,7 +174,9 @@ template <class T> int cell_split_for(const Handle& h, const Geometry<T>& g, int
   const double warps = 152.0 * 16.0 * 2.0;  // two items per resident warp slot
   int s = (int)std::ceil(warps / real_cells);
   s = std::min(s, (int)(per_cell / 64.0));
-  return std::max(1, std::min(s, 64));
+  s = std::max(1, std::min(s, 64));
+  while (s > 1 && (double)g.ncells() * s >= 2147483647.0) s--;
+  return s;
 }
 
 template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const void* vparams, void* vout) {
@@ -233,6 +240,7 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
       return ERR_ARG;
     }
     need += align(sizeof(T) * (P->nbins + 1)) + align(sizeof(T) * nx * N) + align(sizeof(T) * ny * N);
+    need += align(sizeof(float) * nx * N) + align(sizeof(float) * ny * N);  // FP32 copies (split form)
   }
   if (need && !h.opbuf.reserve(need)) return ERR_NOMEM;
   char* ob = h.opbuf.as<char>();
@@ -280,11 +288,27 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
     A.bins = bins;
     A.vx = vx;
     A.vy = vy;
+    if (std::is_same<T, float>::value) {
+      A.vxf = reinterpret_cast<const float*>(vx);
+      A.vyf = reinterpret_cast<const float*>(vy);
+    } else if (A.split) {
+      float* fx = (float*)(ob + at);
+      at += align(sizeof(float) * nx * N);
+      float* fy = (float*)(ob + at);
+      at += align(sizeof(float) * ny * N);
+      if (nx) k_to_f32<T><<<(unsigned)((nx * N + 255) / 256), 256, 0, h.stream>>>(vx, nx * N, fx);
+      if (ny) k_to_f32<T><<<(unsigned)((ny * N + 255) / 256), 256, 0, h.stream>>>(vy, ny * N, fy);
+      CLM_CUDA_TRY(h, cudaGetLastError());
+      h.launches += (nx > 0) + (ny > 0);
+      A.vxf = fx;
+      A.vyf = fy;
+    }
     CLM_CUDA_TRY(h, cudaStreamSynchronize(h.stream));  // the host vector b goes out of scope
   }
   // grid: static round-robin of real cells over warps (deterministic)
   // the number of real cells is only known on the device: size for all cells (one resident wave at most)
-  const int grid_want = (int)std::max<int64_t>(1, std::min<int64_t>((X.ncells + kWarps - 1) / kWarps, 1 << 16));
+  const int grid_want =
+      (int)std::max<int64_t>(1, std::min<int64_t>((X.ncells * A.cell_split + kWarps - 1) / kWarps, 1 << 16));
   int grid = grid_want;
   // partials
   const size_t part_bytes = align(sizeof(double) * grid_want) + align(sizeof(unsigned long long) * grid_want) +

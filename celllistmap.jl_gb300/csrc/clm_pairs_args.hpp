@@ -44,6 +44,8 @@ template <class T> struct PairArgs {
   const T* vy;
   const T* bins;
   int nbins;
+  const float* vxf;  // velocities in FP32 (pair values of the FP32 forms)
+  const float* vyf;
   // outputs
   int* nl_i;
   int* nl_j;
@@ -68,6 +70,24 @@ template <class T> struct PairArgs {
 
 enum OpKind { OPK_NL = 0, OPK_SCALAR = 1, OPK_FORCES = 2, OPK_MIN = 3, OPK_HIST = 4, OPK_ADJ = 5 };
 constexpr int kAdjVals = 13;  // energy, virial (xx yy zz xy xz yz), dU/deps[3], dU/dsigma[3]
+
+// Dynamic shared memory of the radial-histogram kernel: block bins (FP64 sums, 64-bit counts), the bin
+// edges in the handle dtype and in FP32, and per-warp bins (sums in the accumulation type, counts).
+struct HistSmem {
+  size_t hs, hc, bins, binf, ws, wc, total;
+};
+__host__ __device__ inline HistSmem hist_smem(int nb, int tsize, int fsize) {
+  auto up = [](size_t v) { return (v + 15) / 16 * 16; };
+  HistSmem m;
+  m.hs = 0;
+  m.hc = up(m.hs + 8 * (size_t)nb);
+  m.bins = up(m.hc + 8 * (size_t)nb);
+  m.binf = up(m.bins + (size_t)tsize * (nb + 1));
+  m.ws = up(m.binf + 4 * (size_t)(nb + 1));
+  m.wc = up(m.ws + (size_t)fsize * kWarps * nb);
+  m.total = up(m.wc + 4 * (size_t)kWarps * nb);
+  return m;
+}
 
 // Which instantiation of the kernel a launch needs.
 struct LaunchSel {

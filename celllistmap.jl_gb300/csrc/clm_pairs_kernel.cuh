@@ -206,6 +206,26 @@ __device__ bool projection_pass(const DevGeom<T>& g, const T* cf, const T* ct, c
   return fabs(xsub(pt, pf)) <= g.cutoff;
 }
 
+// Sum of `v` over the lanes of a match group (`peers`: the lanes sharing this lane's key), returned in
+// the group's lowest lane.  Pairwise tree: at each step every lane at an even position of its group adds
+// the value of the next remaining peer, and the lanes at odd positions drop out, so a group of g lanes
+// needs ceil(log2 g) steps and the whole warp at most 5, however many groups there are.  All lanes of
+// the warp call it.
+template <class V> __device__ __forceinline__ V group_sum(unsigned peers, V v, int lane) {
+  unsigned pos = __popc(peers & ((1u << lane) - 1u));  // position of this lane in its group
+  unsigned rest = peers & ~((2u << lane) - 1u);         // peers above this lane (lane 31: none)
+  if (lane == 31) rest = 0u;
+  while (__any_sync(0xffffffffu, rest != 0u)) {
+    const int nxt = __ffs(rest);                          // 1 + lane of the next remaining peer, 0 if none
+    const V t = __shfl_sync(0xffffffffu, v, nxt > 0 ? nxt - 1 : lane);
+    if (nxt > 0) v += t;
+    const unsigned gone = __ballot_sync(0xffffffffu, (pos & 1u) != 0u);  // consumed by their left neighbour
+    rest &= ~gone;
+    pos >>= 1;
+  }
+  return v;
+}
+
 // Geometry of the cell being processed: the launch's own (one system) or that of the cell's system
 // (batches); `cb` returns the first global cell of that system.
 template <bool B, class T>
@@ -257,8 +277,16 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
   __shared__ float s_ipf[kWarps][3][32];
   __shared__ int s_icode[kWarps][32];
   __shared__ FA s_if[kWarps][3][IS_F ? 32 : 1];  // force sums of those particles
-  __shared__ unsigned int s_hc[(OPK == OPK_HIST) ? 256 : 1];  // block-wide histogram
-  __shared__ double s_hs[(OPK == OPK_HIST) ? 256 : 1];
+  // radial histogram (dynamic shared memory, layout in hist_smem): block bins in FP64, bin edges, and
+  // per-warp bins that the warp updates without atomics
+  extern __shared__ __align__(16) unsigned char s_dyn[];
+  const HistSmem hl = hist_smem((OPK == OPK_HIST) ? A.nbins : 0, (int)sizeof(T), (int)sizeof(FA));
+  double* s_hs = reinterpret_cast<double*>(s_dyn + hl.hs);
+  unsigned long long* s_hc = reinterpret_cast<unsigned long long*>(s_dyn + hl.hc);
+  T* s_bins = reinterpret_cast<T*>(s_dyn + hl.bins);
+  float* s_binf = reinterpret_cast<float*>(s_dyn + hl.binf);
+  FA* s_ws = reinterpret_cast<FA*>(s_dyn + hl.ws) + warp * A.nbins;
+  unsigned* s_wc = reinterpret_cast<unsigned*>(s_dyn + hl.wc) + warp * A.nbins;
   __shared__ double s_red[kWarps];
   __shared__ unsigned long long s_redc[kWarps];
 
@@ -274,8 +302,16 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
 
   if constexpr (OPK == OPK_HIST) {
     for (int b = threadIdx.x; b < A.nbins; b += kThreads) {
-      s_hc[b] = 0u;
+      s_hc[b] = 0ull;
       s_hs[b] = 0.0;
+    }
+    for (int b = lane; b < A.nbins; b += 32) {
+      s_ws[b] = FA(0);
+      s_wc[b] = 0u;
+    }
+    for (int b = threadIdx.x; b <= A.nbins; b += kThreads) {
+      s_bins[b] = A.bins[b];
+      s_binf[b] = (float)A.bins[b];
     }
     __syncthreads();
   }
@@ -687,6 +723,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
                 }
               }
             } else if constexpr (OPK == OPK_HIST) {
+              int hb = -1;   // bin of this lane's pair (-1: none)
+              FA hv = 0;     // its accumulator term
               if (hit) {
                 bool exact_r = !sure;
                 T r = 0;
@@ -696,13 +734,12 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
                   int lo = 0, hi = A.nbins + 1;
                   while (lo < hi) {
                     int mid = (lo + hi) >> 1;
-                    if ((float)A.bins[mid] >= rf) hi = mid;
+                    if (s_binf[mid] >= rf) hi = mid;
                     else lo = mid + 1;
                   }
                   b = lo - 1;
                   const float tol = rf * 2.44140625e-4f;  // an edge within 2^-12: decide exactly
-                  if ((lo <= A.nbins && fabsf((float)A.bins[lo] - rf) <= tol) ||
-                      (lo >= 1 && fabsf((float)A.bins[lo - 1] - rf) <= tol))
+                  if ((lo <= A.nbins && fabsf(s_binf[lo] - rf) <= tol) || (lo >= 1 && fabsf(s_binf[lo - 1] - rf) <= tol))
                     exact_r = true;
                   r = (T)rf;
                 }
@@ -718,7 +755,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
                   int lo = 0, hi = A.nbins + 1;
                   while (lo < hi) {
                     int mid = (lo + hi) >> 1;
-                    if (A.bins[mid] >= r) hi = mid;
+                    if (s_bins[mid] >= r) hi = mid;
                     else lo = mid + 1;
                   }
                   b = lo - 1;
@@ -744,13 +781,32 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
 #pragma unroll
                     for (int a = 0; a < N; a++) dv[a] = rv[a];
                   }
-                  const T* vy = CROSS ? A.vy : A.vx;
                   FA dot = 0;
+                  if constexpr (std::is_same<FA, float>::value) {
+                    // FP32 pair values: velocities converted once by the host code
+                    const float* vy = CROSS ? A.vyf : A.vxf;
 #pragma unroll
-                  for (int d = 0; d < N; d++)
-                    dot += ((FA)A.vx[(int64_t)idx_i * N + d] - (FA)vy[(int64_t)idx_j * N + d]) * dv[d];
-                  atomicAdd(&s_hc[b], 1u);
-                  atomicAdd(&s_hs[b], (double)(dot / (FA)r));
+                    for (int d = 0; d < N; d++)
+                      dot += (A.vxf[(int64_t)idx_i * N + d] - vy[(int64_t)idx_j * N + d]) * dv[d];
+                    hv = dot * vrcp((float)r);
+                  } else {
+                    const T* vy = CROSS ? A.vy : A.vx;
+#pragma unroll
+                    for (int d = 0; d < N; d++)
+                      dot += ((FA)A.vx[(int64_t)idx_i * N + d] - (FA)vy[(int64_t)idx_j * N + d]) * dv[d];
+                    hv = dot / (FA)r;
+                  }
+                  hb = b;
+                }
+              }
+              // lanes holding the same bin are summed by a tree over their group; the group's first lane
+              // then updates the warp's own bin (groups have distinct bins: no atomics)
+              if (__any_sync(FULL, hb >= 0)) {
+                const unsigned peers = __match_any_sync(FULL, hb);
+                const FA v = group_sum(peers, hv, lane);
+                if (hb >= 0 && lane == __ffs(peers) - 1) {
+                  s_ws[hb] += v;
+                  s_wc[hb] += (unsigned)__popc(peers);
                 }
               }
             }
@@ -759,6 +815,19 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
             if (cur >= 0) {
 #pragma unroll
               for (int d = 0; d < N; d++) atomicAdd(&s_if[warp][d][cur], acc[d]);
+            }
+          }
+          if constexpr (OPK == OPK_HIST) {
+            // move the warp's bins (at most 1024 pairs of this round) into the block's FP64 bins
+            __syncwarp();
+            for (int b = lane; b < A.nbins; b += 32) {
+              const unsigned c = s_wc[b];
+              if (c) {
+                atomicAdd(&s_hc[b], (unsigned long long)c);
+                atomicAdd(&s_hs[b], (double)s_ws[b]);
+                s_wc[b] = 0u;
+                s_ws[b] = FA(0);
+              }
             }
           }
           __syncwarp();
@@ -892,7 +961,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
 }
 
 // One wave of resident blocks (the warps loop over cells): grid = min(cells/warps, SMs x blocks per SM).
-template <class K> int resident_grid(K kernel, int want) {
+template <class K> int resident_grid(K kernel, int want, size_t dyn = 0) {
   static int sms = 0;
   if (sms == 0) {
     int dev = 0;
@@ -901,7 +970,7 @@ template <class K> int resident_grid(K kernel, int want) {
     if (sms <= 0) sms = 1;
   }
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0) != cudaSuccess || per_sm <= 0) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, dyn) != cudaSuccess || per_sm <= 0) {
     cudaGetLastError();
     per_sm = 1;
   }
@@ -911,8 +980,15 @@ template <class K> int resident_grid(K kernel, int want) {
 template <class T, int N, int OPK, bool SPLIT, bool CROSS, bool BATCH = false>
 cudaError_t launch_k(int& grid, cudaStream_t st, const PairArgs<T>& A) {
   auto k = k_pairs<T, N, OPK, SPLIT, CROSS, BATCH>;
-  grid = resident_grid(k, grid);
-  k<<<grid, kThreads, 0, st>>>(A);
+  using FA = typename std::conditional<std::is_same<T, double>::value && !SPLIT, double, float>::type;
+  size_t dyn = 0;
+  if (OPK == OPK_HIST) {
+    dyn = hist_smem(A.nbins, (int)sizeof(T), (int)sizeof(FA)).total;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return e;
+  }
+  grid = resident_grid(k, grid, dyn);
+  k<<<grid, kThreads, dyn, st>>>(A);
   return cudaGetLastError();
 }
 

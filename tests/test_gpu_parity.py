@@ -188,6 +188,32 @@ def test_min_distance_and_histogram(clm, orc, cross):
     s.close()
 
 
+@pytest.mark.parametrize("dim", [3, 2])
+@pytest.mark.parametrize("cross", [False, True])
+def test_histogram_split_form(clm, orc, cross, dim):
+    """FP32-split histogram: counts exact; per-bin sums within 1e-5 of the bin's sum of |v_i - v_j|
+    (a bound on the sum of |terms|), the FP32 pair arithmetic being accumulated in FP64."""
+    x = gen(3000, dim, 20.0, 87)
+    y = gen(2500, dim, 20.0, 88) if cross else None
+    uc = [20.0] * dim
+    rng = np.random.default_rng(3)
+    vx = rng.normal(0, 300.0, x.shape)
+    vy = rng.normal(0, 300.0, y.shape) if cross else None
+    bins = 10 ** np.linspace(np.log10(0.1), np.log10(2.0), 21)
+    s = clm.ParticleSystem(xpositions=x, ypositions=y, unitcell=uc, cutoff=2.0, precision="split")
+    hc, hs = clm.pairwise(clm.RadialHistogram(bins, vx, vy), s)
+    rr = orc.run("rhist", x, y, dim=dim, unitcell=uc, cutoff=2.0, bins=bins, vel_x=vx, vel_y=vy)
+    np.testing.assert_array_equal(hc, rr["hist_count"])
+    nl = orc.run("nl", x, y, dim=dim, unitcell=uc, cutoff=2.0)
+    vyy = vy if cross else vx
+    dv = np.linalg.norm(vx[nl["i"]] - vyy[nl["j"]], axis=1)
+    b = np.searchsorted(bins, nl["d"], side="left") - 1
+    ok = (b >= 0) & (b < len(bins) - 1)
+    scale = np.bincount(b[ok], weights=dv[ok], minlength=len(bins) - 1)
+    assert np.all(np.abs(hs - rr["hist_sum"]) <= 1e-5 * scale + 1e-9)
+    s.close()
+
+
 @pytest.mark.parametrize("case", [CASES[0], CASES[2], CASES[4]], ids=ids)
 def test_split_form_keeps_sets_exact(clm, orc, case):
     dim, uc, cut, lcell, n, span = case
