@@ -767,7 +767,7 @@ class BatchedSystems:
         res = []
         for op, (sc, ct, f) in zip(ops, keep):
             if isinstance(op, NeighborList):
-                res.append(self._neighbor_lists(ct, op.index_base))
+                res.append(BatchNeighborLists(self, ct, op.index_base))
             elif isinstance(op, Count):
                 res.append(ct)
             elif f is not None:
@@ -776,8 +776,8 @@ class BatchedSystems:
                 res.append(sc)
         return res
 
-    def _neighbor_lists(self, counts, base=0):
-        """Per-system neighbour lists with indices local to each system."""
+    def _neighbor_lists(self, base=0):
+        """Per-system neighbour lists with indices local to each system (copied to the host)."""
         L, h = self._handle.L, self._handle.h
         n = C.c_int64()
         self._handle.check(L.clm_nl_count(h, C.byref(n)))
@@ -818,6 +818,26 @@ class BatchedSystems:
 
     def close(self):
         self._handle.close()
+
+
+class BatchNeighborLists:
+    """Neighbour lists of one batched step.  They stay on the device until a system's list is asked for
+    (indexing copies all lists to the host once and splits them by system)."""
+
+    def __init__(self, batch, counts, base):
+        self._batch, self.counts, self._base, self._lists = batch, counts, base, None
+
+    def __len__(self):
+        return len(self.counts)
+
+    def __getitem__(self, s):
+        if self._lists is None:
+            self._lists = self._batch._neighbor_lists(self._base)
+        return self._lists[s]
+
+    @property
+    def total(self) -> int:
+        return int(np.sum(self.counts))
 
 
 class Box:
