@@ -14,6 +14,7 @@ from .api import (ArgumentError, BatchedSystems, Box, CUDAError, DimensionMismat
                   ParticleSystem, neighborlist, neighborlist_, pairwise, pairwise_, update, version)
 from . import api as ops  # operator classes live in api; exposed as `ops`
 from . import workloads
+from . import trajectory
 
 Count = _api.Count
 SumD2 = _api.SumD2

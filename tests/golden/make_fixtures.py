@@ -18,7 +18,6 @@ Only coordinates are extracted.  The expected values these fixtures are checked
 against are quoted, with their source lines, in tests/test_oracle_kat.py.
 """
 import os
-import struct
 import sys
 
 import numpy as np
@@ -26,39 +25,18 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
+def _trajectory():
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    import __graft_entry__ as ge
+    return ge.load_package().trajectory
+
+
 def read_pdb_coords(path):
-    xyz = []
-    with open(path) as f:
-        for line in f:
-            if line.startswith("ATOM") or line.startswith("HETATM"):
-                xyz.append([float(line[30:38]), float(line[38:46]), float(line[46:54])])
-    return np.array(xyz, dtype=np.float64)
+    return _trajectory().read_pdb(path)[0]
 
 
 def read_dcd_first_frame(path):
-    """Minimal CHARMM/NAMD DCD reader (Fortran unformatted records, little endian)."""
-    data = open(path, "rb").read()
-    pos = 0
-    recs = []
-    while pos < len(data):
-        (n,) = struct.unpack_from("<i", data, pos)
-        recs.append(data[pos + 4:pos + 4 + n])
-        (n2,) = struct.unpack_from("<i", data, pos + 4 + n)
-        assert n == n2, "corrupt DCD record"
-        pos += 8 + n
-    hdr = recs[0]
-    assert hdr[:4] == b"CORD"
-    icntrl = struct.unpack_from("<20i", hdr, 4)
-    has_cell = icntrl[10] != 0
-    natoms = struct.unpack_from("<i", recs[2])[0]
-    k = 3
-    if has_cell:
-        k += 1  # unit-cell record (6 doubles) precedes the coordinates
-    x = np.frombuffer(recs[k], dtype="<f4")
-    y = np.frombuffer(recs[k + 1], dtype="<f4")
-    z = np.frombuffer(recs[k + 2], dtype="<f4")
-    assert x.size == natoms == y.size == z.size
-    return np.stack([x, y, z], axis=1).astype(np.float32)
+    return _trajectory().read_dcd(path).frames[0]
 
 
 def main(ref_root):
