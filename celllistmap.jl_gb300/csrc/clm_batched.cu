@@ -66,32 +66,6 @@ __global__ void k_seg_reduce(const double* __restrict__ pe, const unsigned long 
   }
 }
 
-// Forces of every particle in the handle dtype, rotated back to each system's original frame.
-template <class T, int N>
-__global__ void k_forces_out_b(const double* __restrict__ facc, int64_t n, const DevGeom<T>* __restrict__ gtab,
-                               const int* __restrict__ psys, T* __restrict__ out) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const DevGeom<T>& g = gtab[psys[i]];
-  double f[N];
-#pragma unroll
-  for (int d = 0; d < N; d++) f[d] = facc[i * N + d];
-  if (g.kind == TRICLINIC) {
-    double r[N];
-#pragma unroll
-    for (int a = 0; a < N; a++) {
-      double s = 0;
-#pragma unroll
-      for (int k = 0; k < N; k++) s += (double)g.Rinv[a][k] * f[k];
-      r[a] = s;
-    }
-#pragma unroll
-    for (int d = 0; d < N; d++) f[d] = r[d];
-  }
-#pragma unroll
-  for (int d = 0; d < N; d++) out[i * N + d] = (T)f[d];
-}
-
 template <class T> Geometry<T>& tmpl_geom(Handle& h);
 template <> Geometry<double>& tmpl_geom<double>(Handle& h) { return h.gd; }
 template <> Geometry<float>& tmpl_geom<float>(Handle& h) { return h.gf; }
@@ -252,7 +226,10 @@ template <class T> int enqueue_op(Handle& h, int slot, int op, const clm_op_para
     if (!h.outbuf.reserve(sizeof(double) * n * N + 256) || !B.forces.reserve(sizeof(T) * n * N + 256))
       return fail(&h, ERR_NOMEM, "device allocation failed (forces)");
     A.fx = h.outbuf.as<double>();
-    CLM_CUDA_TRY(h, cudaMemsetAsync(A.fx, 0, sizeof(double) * n * N, h.stream));
+    A.fout = B.forces.as<T>();  // owner warps write the force of every particle of a valid system
+    bool failed = false;
+    for (int st : B.status) failed = failed || st == ERR_CELL_TOO_SMALL;
+    if (failed) CLM_CUDA_TRY(h, cudaMemsetAsync(A.fout, 0, sizeof(T) * n * N, h.stream));
   }
   if (opk == OPK_NL) {
     const int64_t est = (int64_t)(B.pairs_est * 1.15) + 4096;
@@ -296,16 +273,6 @@ template <class T> int enqueue_op(Handle& h, int slot, int op, const clm_op_para
       CLM_CUDA_TRY(h, cudaGetLastError());
       h.launches++;
     }
-  }
-  if (forces && n > 0) {
-    if (N == 3)
-      k_forces_out_b<T, 3><<<(unsigned)((n + 255) / 256), 256, 0, h.stream>>>(A.fx, n, A.gtab, B.psys.as<int>(),
-                                                                               B.forces.as<T>());
-    else
-      k_forces_out_b<T, 2><<<(unsigned)((n + 255) / 256), 256, 0, h.stream>>>(A.fx, n, A.gtab, B.psys.as<int>(),
-                                                                               B.forces.as<T>());
-    CLM_CUDA_TRY(h, cudaGetLastError());
-    h.launches++;
   }
   if (nsys > 0)
     CLM_CUDA_TRY(h, cudaMemcpyAsync(B.hres + (size_t)slot * nsys * 16, o_e, (size_t)nsys * 16, cudaMemcpyDeviceToHost,

@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "clm_internal.hpp"
@@ -338,7 +339,8 @@ __device__ __forceinline__ void origin_ff(float cb_hi, float cb_lo, float cs_hi,
 template <class T, int N>
 __device__ __forceinline__ void gather_at(const DevGeom<T>& g, const T* __restrict__ wrapped, int t, int p, int k,
                                           int li, T* __restrict__ px, T* __restrict__ py, T* __restrict__ pz,
-                                          float4* __restrict__ off, int* __restrict__ code) {
+                                          float4* __restrict__ off, float4* __restrict__ xq,
+                                          int* __restrict__ code) {
   T q[N];
 #pragma unroll
   for (int d = 0; d < N; d++) {
@@ -357,11 +359,14 @@ __device__ __forceinline__ void gather_at(const DevGeom<T>& g, const T* __restri
     const float ql = (float)(q[d] - (T)qh);
     o[d] = (qh - oh) + (ql - ol);
   }
+  const int pc = (k == g.zero_code) ? p : -(p + 1);
   px[t] = q[0];
   py[t] = q[1];
   if (N == 3) pz[t] = q[N - 1];
-  off[t] = make_float4(o[0], o[1], o[2], 0.f);
-  code[t] = (k == g.zero_code) ? p : -(p + 1);
+  off[t] = make_float4(o[0], o[1], o[2], __int_as_float(pc));
+  if constexpr (std::is_same<T, float>::value)
+    xq[t] = make_float4((float)q[0], (float)q[1], N == 3 ? (float)q[N - 1] : 0.f, __int_as_float(pc));
+  code[t] = pc;
 }
 
 template <class T, int N>
@@ -369,8 +374,8 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom<T> g, const T* __rest
                                                    const uint32_t* __restrict__ skeys,
                                                    const uint32_t* __restrict__ svals, const int* __restrict__ n_dev,
                                                    int cap, int n, T* __restrict__ px, T* __restrict__ py,
-                                                   T* __restrict__ pz, float4* __restrict__ off, int* __restrict__ code,
-                                                   int* __restrict__ err) {
+                                                   T* __restrict__ pz, float4* __restrict__ off, float4* __restrict__ xq,
+                                                   int* __restrict__ code, int* __restrict__ err) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= min(*n_dev, cap)) return;
   uint32_t v = svals[t];
@@ -383,7 +388,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom<T> g, const T* __rest
     k = g.zero_code;
     li = 0;
   }
-  gather_at<T, N>(g, wrapped, t, p, k, li, px, py, pz, off, code);
+  gather_at<T, N>(g, wrapped, t, p, k, li, px, py, pz, off, xq, code);
 }
 
 template <class T, int N>
@@ -393,7 +398,8 @@ __global__ void __launch_bounds__(kBlock) k_gather_b(const DevGeom<T>* __restric
                                                      const uint32_t* __restrict__ svals, const int* __restrict__ n_dev,
                                                      int cap, int n, T* __restrict__ px, T* __restrict__ py,
                                                      T* __restrict__ pz, float4* __restrict__ off,
-                                                     int* __restrict__ code, int* __restrict__ err) {
+                                                     float4* __restrict__ xq, int* __restrict__ code,
+                                                     int* __restrict__ err) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= min(*n_dev, cap)) return;
   uint32_t v = svals[t];
@@ -411,7 +417,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_b(const DevGeom<T>* __restric
     k = g.zero_code;
     li = 0;
   }
-  gather_at<T, N>(g, wrapped, t, p, k, li, px, py, pz, off, code);
+  gather_at<T, N>(g, wrapped, t, p, k, li, px, py, pz, off, xq, code);
 }
 
 __global__ void k_compact(const int* __restrict__ flags, const int* __restrict__ scanned, int ncells,
@@ -660,6 +666,7 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
       !S.keys[1].reserve(sizeof(uint32_t) * cap) || !S.vals[0].reserve(sizeof(uint32_t) * cap) ||
       !S.vals[1].reserve(sizeof(uint32_t) * cap) || !S.px.reserve(sizeof(T) * cap) || !S.py.reserve(sizeof(T) * cap) ||
       !S.pz.reserve(sizeof(T) * cap) || !S.off.reserve(sizeof(float4) * cap) || !S.code.reserve(sizeof(int) * cap) ||
+      !S.xq.reserve(std::is_same<T, float>::value ? sizeof(float4) * cap : 16) ||
       !S.rs_hist.reserve(sizeof(int) * (256 * (int64_t)ntiles + 1)))
     return ERR_NOMEM;
   const int gn = grid_for(n);
@@ -735,19 +742,19 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
     if (N == 3)
       k_gather_b<T, 3><<<gc, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
                                                    S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
-                                                   S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.code.as<int>(), err);
+                                                   S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), err);
     else
       k_gather_b<T, 2><<<gc, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
                                                    S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
-                                                   S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.code.as<int>(), err);
+                                                   S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), err);
   } else if (N == 3)
     k_gather<T, 3><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
                                                S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
-                                               S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.code.as<int>(), err);
+                                               S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), err);
   else
     k_gather<T, 2><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
                                                S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
-                                               S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.code.as<int>(), err);
+                                               S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), err);
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
   // cells with real particles, in linear order; their number stays on the device (real_scan[ncells])

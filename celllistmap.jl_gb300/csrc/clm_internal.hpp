@@ -58,7 +58,8 @@ struct SetData {
   DevBuf cell_count, cell_start, cell_flags;
   DevBuf real_list, real_scan;
   DevBuf px, py, pz;        // copies in cell order (SoA), handle dtype
-  DevBuf off;               // FP32 cell-relative offsets (float4) for the prefilter
+  DevBuf off;               // FP32 cell-relative offsets (float4, .w = code) for the prefilter
+  DevBuf xq;                // Float32 handles: coordinates (float4, .w = code)
   DevBuf code;              // particle index (>= 0 real copy, -(index+1) image)
   DevBuf rs_hist;
   DevBuf minmax;            // non-periodic limits scratch

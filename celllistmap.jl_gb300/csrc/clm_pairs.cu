@@ -171,7 +171,7 @@ template <class T> int cell_split_for(const Handle& h, const Geometry<T>& g, int
     real_cells *= std::max(1.0, inner);
   }
   const double per_cell = nx / real_cells;
-  const double warps = 152.0 * 16.0 * 2.0;  // two items per resident warp slot
+  const double warps = 152.0 * 24.0 * 2.0;  // two items per resident warp slot (24 warps per SM)
   int s = (int)std::ceil(warps / real_cells);
   s = std::min(s, (int)(per_cell / 64.0));
   s = std::max(1, std::min(s, 64));
@@ -345,12 +345,29 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
   // outputs
   const bool forces = (opk == OPK_FORCES || opk == OPK_ADJ);
   double* r_v = (double*)(res + 256 + 16 * 256);  // adjoint sums (kAdjVals)
+  // self forces are complete when the owner warp finishes a particle: it writes them (rotated back, in
+  // the handle dtype) straight to the output; cross forces are accumulated in FP64 and converted after
+  const bool owner = forces && h.nsets == 1;
+  T* dst_x = nullptr;
+  T* dst_y = nullptr;
+  const size_t acc_bytes = sizeof(double) * (nx + ny) * N;
   if (forces) {
-    size_t fb = sizeof(double) * (nx + ny) * N;
-    if (!h.outbuf.reserve(fb + sizeof(T) * (nx + ny) * N + 256)) return ERR_NOMEM;
+    if (!h.outbuf.reserve(acc_bytes + sizeof(T) * (nx + ny) * N + 256)) return ERR_NOMEM;
     A.fx = h.outbuf.as<double>();
     A.fy = A.fx + nx * N;
-    CLM_CUDA_TRY(h, cudaMemsetAsync(A.fx, 0, fb, h.stream));
+    if (!O->out_on_device) {
+      // staged after the accumulators when the caller gave host pointers
+      dst_x = (T*)(h.outbuf.as<char>() + acc_bytes);
+      dst_y = dst_x + nx * N;
+    } else {
+      dst_x = (T*)O->forces_x;
+      dst_y = (T*)O->forces_y;
+    }
+    if (owner) {
+      A.fout = dst_x;
+    } else {
+      CLM_CUDA_TRY(h, cudaMemsetAsync(A.fx, 0, acc_bytes, h.stream));
+    }
   }
   if (opk == OPK_NL) {
     double vol = std::fabs((double)g.det_in);
@@ -401,19 +418,8 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
   if (forces) {
     const int rot = (g.kind == TRICLINIC) ? 1 : 0;
     DevGeom<T>& dg = A.g;
-    T* dst_x = nullptr;
-    T* dst_y = nullptr;
-    // stage into outbuf after the accumulators when the caller gave host pointers
-    size_t acc_bytes = sizeof(double) * (nx + ny) * N;
-    if (!O->out_on_device) {
-      dst_x = (T*)(h.outbuf.as<char>() + acc_bytes);
-      dst_y = dst_x + nx * N;
-    } else {
-      dst_x = (T*)O->forces_x;
-      dst_y = (T*)O->forces_y;
-    }
-    h.launches += (nx && dst_x) + (ny && dst_y);
-    if (nx && dst_x) {
+    h.launches += (nx && dst_x && !owner) + (ny && dst_y);
+    if (nx && dst_x && !owner) {
       if (N == 3) k_forces_out<T, 3><<<(unsigned)((nx + 255) / 256), 256, 0, h.stream>>>(A.fx, nx, dg, rot, dst_x);
       else k_forces_out<T, 2><<<(unsigned)((nx + 255) / 256), 256, 0, h.stream>>>(A.fx, nx, dg, rot, dst_x);
     }

@@ -18,7 +18,8 @@ template <class T> struct SetView {
   const T* px;
   const T* py;
   const T* pz;
-  const float4* off;
+  const float4* off;  // FP32 offsets from the cell origin; .w = particle code
+  const float4* xq;   // Float32 handles: coordinates; .w = particle code
   const int* code;
   const int* cell_start;
 };
@@ -52,6 +53,7 @@ template <class T> struct PairArgs {
   T* nl_d;
   unsigned long long* nl_count;
   long long nl_cap;
+  T* fout;          // self forces: final output (handle dtype, original frame), or null
   double* fx;       // forces accumulators (double), n_x * dim
   double* fy;       // n_y * dim (cross)
   double* part_e;   // per-block energy
@@ -113,6 +115,7 @@ template <class T> inline SetView<T> view_of(const SetData& S) {
   v.py = S.py.as<T>();
   v.pz = S.pz.as<T>();
   v.off = S.off.as<float4>();
+  v.xq = S.xq.as<float4>();
   v.code = S.code.as<int>();
   v.cell_start = S.cell_start.as<int>();
   return v;

@@ -226,6 +226,14 @@ template <class V> __device__ __forceinline__ V group_sum(unsigned peers, V v, i
   return v;
 }
 
+// Asynchronous global -> shared copies (cp.async, sm_80+): 16 bytes, cached in L1.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // Geometry of the cell being processed: the launch's own (one system) or that of the cell's system
 // (batches); `cb` returns the first global cell of that system.
 template <bool B, class T>
@@ -252,8 +260,10 @@ __device__ __forceinline__ const DevGeom<T>& geo_of(const PairArgs<T>& A, int li
 // evaluated only for pairs with d2 > cutoff^2 (1 - 2^-13): any pair further inside passes it (the
 // projection of the separation on a unit vector cannot exceed the separation, and the margin covers the
 // half cell), so skipping it elsewhere leaves the pair set unchanged.
+// Resident blocks per SM (6 for Float32, 3 for Float64: 85 / 170 registers per thread) were picked by
+// timing 4..8 and 3..4 on GB300; fewer registers spill in the pair epilogues.
 template <class T, int N, int OPK, bool SPLIT, bool CROSS, bool BATCH>
-__global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(const PairArgs<T> A) {
+__global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(const PairArgs<T> A) {
   using V = T;
   using FA = typename std::conditional<std::is_same<T, double>::value && !SPLIT, double, float>::type;
   constexpr bool IS_F = (OPK == OPK_FORCES) || (OPK == OPK_ADJ);
@@ -269,9 +279,10 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
   __shared__ int s_st_start[kWarps][32];
   __shared__ int s_st_pref[kWarps][33];
   __shared__ int s_st_meta[kWarps][32];
-  __shared__ float4 s_pf[kWarps][JC];       // prefilter coordinates; .w carries the particle code
-  __shared__ int s_meta[kWarps][JC];        // stencil offset and flags of the candidate's cell
-  __shared__ T s_x[kWarps][3][ABS_PF ? 1 : JC];
+  // staged candidates, two rounds (the next one is copied while the current one is tested)
+  __shared__ __align__(16) float4 s_pf[2][kWarps][JC];  // prefilter coordinates; .w carries the particle code
+  __shared__ int s_meta[2][kWarps][JC];                 // stencil offset and flags of the candidate's cell
+  __shared__ int s_tj[2][kWarps][ABS_PF ? 1 : JC];       // position of the candidate in the cell list
   __shared__ unsigned short s_q[kWarps][1024];  // compacted candidates: (particle slot << 8) | staged index
   __shared__ T s_ix[kWarps][3][32];              // particles of the current chunk of the cell
   __shared__ float s_ipf[kWarps][3][32];
@@ -426,44 +437,56 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
         const int total = s_st_pref[warp][32];
 
         const int JR = 32 * G;  // candidates per round: each lane tests exactly 32
-        for (int rb = 0; rb < total; rb += JR) {
-          const int cntr = min(JR, total - rb);
-          // ---- stage candidates rb .. rb+JR-1 (positions past the stream are padded with NaN)
+        // ---- stage candidates rbx .. rbx+JR-1 of the stream into buffer bsel with asynchronous copies
+        // (cp.async, 16 B per candidate: coordinates or cell offsets with the particle code in .w);
+        // positions past the stream are padded with NaN
+        auto stage = [&](int rbx, int bsel) {
+          const int cnt = min(JR, total - rbx);
           for (int q = lane; q < JR; q += 32) {
-            if (q < cntr) {
-              const int e = rb + q;
-              int lo = 0, hi = 31;
-              while (lo < hi) {
-                int mid = (lo + hi + 1) >> 1;
-                if (s_st_pref[warp][mid] <= e) lo = mid;
-                else hi = mid - 1;
-              }
-              const int tj = s_st_start[warp][lo] + (e - s_st_pref[warp][lo]);
-              const int meta = s_st_meta[warp][lo];
-              const int code = A.Y.code[tj];
-              s_meta[warp][q] = meta;
-              if (ABS_PF) {
-                s_pf[warp][q] = make_float4((float)pos_of(A.Y, 0, tj), (float)pos_of(A.Y, 1, tj),
-                                            N == 3 ? (float)pos_of(A.Y, N - 1, tj) : 0.f, __int_as_float(code));
-              } else {
-                const float4 oj = A.Y.off[tj];
-                // shift the offset by the cell displacement so that x_i - x_j ~ off_i - pf
-                s_pf[warp][q] = make_float4(oj.x + gc.csf[0] * (float)((meta & 255) - 128),
-                                            oj.y + gc.csf[1] * (float)(((meta >> 8) & 255) - 128),
-                                            oj.z + gc.csf[2] * (float)(((meta >> 16) & 255) - 128),
-                                            __int_as_float(code));
+            if (q < cnt) {
+              const int e = rbx + q;
+              int lo = 0;  // last stencil entry whose prefix is <= e (that entry is not empty)
 #pragma unroll
-                for (int d = 0; d < N; d++) s_x[warp][d][ABS_PF ? 0 : q] = pos_of(A.Y, d, tj);
+              for (int st = 16; st > 0; st >>= 1)
+                if (s_st_pref[warp][lo + st] <= e) lo += st;
+              const int tj = s_st_start[warp][lo] + (e - s_st_pref[warp][lo]);
+              s_meta[bsel][warp][q] = s_st_meta[warp][lo];
+              if constexpr (ABS_PF) {
+                cp_async16(&s_pf[bsel][warp][q], &A.Y.xq[tj]);
+              } else {
+                cp_async16(&s_pf[bsel][warp][q], &A.Y.off[tj]);
+                s_tj[bsel][warp][q] = tj;
               }
             } else {
-              s_pf[warp][q] = make_float4(NAN, NAN, NAN, 0.f);
+              s_pf[bsel][warp][q] = make_float4(NAN, NAN, NAN, 0.f);
             }
           }
+          cp_async_commit();
+        };
+        if (total > 0) stage(0, 0);
+        int buf = 0;
+        for (int rb = 0; rb < total; rb += JR, buf ^= 1) {
+          const int cntr = min(JR, total - rb);
+          cp_async_wait_all();
           __syncwarp();
+          if constexpr (!ABS_PF) {
+            // shift the offsets by the cell displacement so that x_i - x_j ~ off_i - pf (own slots only:
+            // a lane sees its own asynchronous copies after the wait)
+            for (int q = lane; q < cntr; q += 32) {
+              const int meta = s_meta[buf][warp][q];
+              float4 v = s_pf[buf][warp][q];
+              v.x += gc.csf[0] * (float)((meta & 255) - 128);
+              v.y += gc.csf[1] * (float)(((meta >> 8) & 255) - 128);
+              v.z += gc.csf[2] * (float)(((meta >> 16) & 255) - 128);
+              s_pf[buf][warp][q] = v;
+            }
+            __syncwarp();
+          }
+          if (rb + JR < total) stage(rb + JR, buf ^ 1);  // the next round's copies overlap this round
           // ---- phase A: 32 FP32 distance tests per lane into a bit mask
           unsigned mask = 0u;
           {
-            const float4* pp = &s_pf[warp][grp];
+            const float4* pp = &s_pf[buf][warp][grp];
 #pragma unroll
             for (int b = 0; b < 32; b++) {
               const float4 p = pp[b * G];
@@ -508,8 +531,13 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
               ie = ent >> 8;
               j = ent & 255;
             }
-            T xi[3] = {s_ix[warp][0][ie], s_ix[warp][1][ie], s_ix[warp][2][ie]};
-            const float pi[3] = {s_ipf[warp][0][ie], s_ipf[warp][1][ie], s_ipf[warp][2][ie]};
+            T xi[3];
+            float pi[3];
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+              xi[d] = s_ix[warp][d][ie];
+              pi[d] = ABS_PF ? (float)xi[d] : s_ipf[warp][d][ie];
+            }
             const int code_i = s_icode[warp][ie];
             const bool real_i = code_i >= 0;
             const int idx_i = real_i ? code_i : -code_i - 1;
@@ -521,12 +549,20 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
             float dvf[3] = {0.f, 0.f, 0.f};
             T d2 = 0;
             T xj[3] = {0, 0, 0};
+            int tjj = 0;  // the candidate's position in the cell list (coordinates read only when needed)
+            auto load_xj = [&]() {
+              if constexpr (!ABS_PF) {
+#pragma unroll
+                for (int d = 0; d < N; d++) xj[d] = pos_of(A.Y, d, tjj);
+              }
+            };
             if (has) {
-              const float4 p = s_pf[warp][j];
+              const float4 p = s_pf[buf][warp][j];
               const int code_j = __float_as_int(p.w);
               const bool real_j = code_j >= 0;
               idx_j = real_j ? code_j : -code_j - 1;
-              const int meta = s_meta[warp][j];
+              const int meta = s_meta[buf][warp][j];
+              if constexpr (!ABS_PF) tjj = s_tj[buf][warp][j];
               const bool same = (meta & F_SAME) != 0;
               const int slot_j = rb + j;  // position inside the cell when same
               bool cand = true;
@@ -556,9 +592,6 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
                   xj[0] = (T)p.x;
                   xj[1] = (T)p.y;
                   if (N == 3) xj[N - 1] = (T)p.z;
-                } else {
-#pragma unroll
-                  for (int d = 0; d < N; d++) xj[d] = s_x[warp][d][ABS_PF ? 0 : j];
                 }
                 if (!FP64 || SPLIT) {
                   // FP32 input or split form: well inside the cutoff the FP32 value decides
@@ -568,6 +601,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
                   }
                 }
                 if (!sure) {
+                  load_xj();
                   T dx = xsub(xi[0], xj[0]);
                   d2 = xmul(dx, dx);
 #pragma unroll
@@ -744,6 +778,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
                   r = (T)rf;
                 }
                 if (exact_r) {
+                  if (sure) load_xj();  // near a bin edge: the exact distance decides
                   T dx = xsub(xi[0], xj[0]);
                   T e2 = xmul(dx, dx);
 #pragma unroll
@@ -838,12 +873,25 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 8 : 4) k_pairs(co
       e_part = 0;
       if constexpr (IS_F) {
         __syncwarp();
-        if (grp == 0 && vi) {
-          FA f[3] = {s_if[warp][0][il], s_if[warp][1][il], s_if[warp][2][il]};
-          if (OWNER) {
-            if (act_i) {
+        FA f[3];
 #pragma unroll
-              for (int d = 0; d < N; d++) A.fx[(int64_t)idx_i * N + d] = (double)f[d];
+        for (int d = 0; d < 3; d++) f[d] = s_if[warp][d][il];
+        if (grp == 0 && vi) {
+          if (OWNER) {
+            if (act_i && A.fout) {
+              // the particle's force is complete: back to the original frame, in the handle dtype
+              FA o[3] = {f[0], f[1], f[2]};
+              if (tri) {
+#pragma unroll
+                for (int a = 0; a < N; a++) {
+                  FA sacc = 0;
+#pragma unroll
+                  for (int k = 0; k < N; k++) sacc += (FA)gc.Rinv[a][k] * f[k];
+                  o[a] = sacc;
+                }
+              }
+#pragma unroll
+              for (int d = 0; d < N; d++) A.fout[(int64_t)idx_i * N + d] = (T)o[d];
             }
           } else if (f[0] != FA(0) || f[1] != FA(0) || f[2] != FA(0)) {
 #pragma unroll
