@@ -408,7 +408,7 @@ def main():
                 "config": {"workload": WORKLOAD, "n_particles": n, "pairs_per_step": int(pairs), "cutoff": CUTOFF,
                            "cell": "triclinic", "op": "lj_energy_forces"},
                 "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": threads, "kind": "port",
-                                 "sample": f"full workload, {args.steps} steps (serial build + OpenMP map)"},
+                                 "sample": f"full workload, {args.steps} steps (OpenMP build and map on {threads} threads)"},
                 "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return 0
@@ -553,7 +553,7 @@ def main():
         try:
             cpairs, cdt = cpu_reference(x_host, M, args.cpu_steps, 0, threads)
             cpu = {"value": cpairs * args.cpu_steps / cdt, "unit": "pairs/s", "cores": threads, "kind": "port",
-                   "sample": f"full workload, {args.cpu_steps} step(s), serial build + OpenMP map on {threads} threads"}
+                   "sample": f"full workload, {args.cpu_steps} step(s), OpenMP build and map on {threads} threads"}
         except Exception as ex:  # pragma: no cover
             cpu = {"value": None, "unit": "pairs/s", "cores": threads, "kind": "port", "sample": f"failed: {ex}"}
 

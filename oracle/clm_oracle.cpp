@@ -120,6 +120,14 @@ enum {
 };
 
 // Julia's min/max on floats prefer -0.0 / +0.0 respectively (no NaNs here).
+inline int orc_max_threads_impl() {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
 template <class T> inline T jmin(T a, T b) {
   if (a < b) return a;
   if (b < a) return b;
@@ -463,14 +471,32 @@ template <class T, int N> struct Particle {
   T x[N];
 };
 
+// Read-only view of the particles of one cell.
+template <class P> struct Span {
+  const P* b = nullptr;
+  int64_t n = 0;
+  const P* begin() const { return b; }
+  const P* end() const { return b + n; }
+  size_t size() const { return (size_t)n; }
+  bool empty() const { return n == 0; }
+  const P& operator[](int64_t i) const { return b[i]; }
+};
+
+// The cell list in one flat array: the copies of cell c (linear index, x fastest) are
+// parts[start[c] .. start[c+1]), in the order the reference's serial build appends them
+// (particle index order; a particle's real copy, then its images in image order).
 template <class T, int N> struct CellList {
   const Box<T, N>* box;
   int64_t n_real = 0, n_particles = 0;
-  std::vector<int64_t> cell_of;              // linear -> position in `cells` (-1 if empty)
-  std::vector<std::vector<Particle<T, N>>> cells;
-  std::vector<int64_t> cell_lin;             // per used cell: linear index
-  std::vector<char> contains_real;
-  std::vector<int64_t> real_cells;           // positions in `cells`, first-touch order
+  std::vector<Particle<T, N>> parts;
+  std::vector<int64_t> start;                // ncells + 1
+  std::vector<int64_t> real_cells;           // linear indices of the cells holding real particles, ascending
+  Span<Particle<T, N>> cell(int64_t li) const {
+    Span<Particle<T, N>> sp;
+    sp.b = parts.data() + start[(size_t)li];
+    sp.n = start[(size_t)li + 1] - start[(size_t)li];
+    return sp;
+  }
 };
 
 template <class T, int N> inline void wrap_to_first(const Box<T, N>& B, const T* x, T* out) {
@@ -503,9 +529,9 @@ template <class T, int N> void cart_from_linear(const Box<T, N>& B, int64_t li, 
   for (int i = 0; i < N; i++) { c[i] = li % B.nc[i] + 1; li /= B.nc[i]; }
 }
 
-template <class T, int N> void add_particle(CellList<T, N>& cl, int64_t ip, const T* x, bool real) {
-  const Box<T, N>& B = *cl.box;
-  cl.n_particles++;
+// Cell of a copy: particle_cell (Box.jl:499-508) with real_particle_border_case (CellLists.jl:956-967)
+// for real copies.
+template <class T, int N> inline int64_t copy_cell(const Box<T, N>& B, const T* x, bool real) {
   int64_t c[N];
   particle_cell(B, x, c);
   if (real) {
@@ -514,24 +540,7 @@ template <class T, int N> void add_particle(CellList<T, N>& cl, int64_t ip, cons
       if (c[i] == B.nc[i] - B.lcell + 1) c[i] -= 1;
     }
   }
-  int64_t li = linear_index(B, c);
-  int64_t pos = cl.cell_of[li];
-  if (pos < 0) {
-    pos = (int64_t)cl.cells.size();
-    cl.cell_of[li] = pos;
-    cl.cells.emplace_back();
-    cl.cell_lin.push_back(li);
-    cl.contains_real.push_back(0);
-  }
-  if (real && !cl.contains_real[pos]) {
-    cl.contains_real[pos] = 1;
-    cl.real_cells.push_back(pos);
-  }
-  Particle<T, N> p;
-  p.index = ip;
-  p.real = real;
-  for (int i = 0; i < N; i++) p.x[i] = x[i];
-  cl.cells[pos].push_back(p);
+  return linear_index(B, c);
 }
 
 template <class T, int N> inline bool in_computing_box(const Box<T, N>& B, const T* x) {
@@ -540,37 +549,102 @@ template <class T, int N> inline bool in_computing_box(const Box<T, N>& B, const
   return true;
 }
 
-template <class T, int N> void build(CellList<T, N>& cl, const Box<T, N>& B, const T* x, int64_t n) {
+// UpdateCellList! (CellLists.jl:727-927, 940-1057): the copies of every particle (wrap_to_first, then
+// replicate_particle! over Iterators.product(-1:1, ...) with the first index fastest) are generated in
+// parallel into particle order, then placed by a stable counting sort on the cell, which reproduces the
+// serial append order of the reference inside every cell.
+template <class T, int N>
+void build(CellList<T, N>& cl, const Box<T, N>& B, const T* x, int64_t n, int nthreads = 1) {
   cl.box = &B;
   cl.n_real = n;
-  cl.cell_of.assign((size_t)B.ncells(), -1);
+  const int64_t ncells = B.ncells();
+  int nimg = 1;
+  for (int i = 0; i < N; i++) nimg *= 3;
+  const int zero = (nimg - 1) / 2;
+  T shift[27][N];
+  for (int k = 0; k < nimg; k++) {
+    int sv[N];
+    int kk = k;
+    for (int i = 0; i < N; i++) { sv[i] = kk % 3 - 1; kk /= 3; }
+    for (int i = 0; i < N; i++) {
+      T acc = B.Mal.a[i][0] * T(sv[0]);
+      for (int j = 1; j < N; j++) acc = acc + B.Mal.a[i][j] * T(sv[j]);
+      shift[k][i] = acc;
+    }
+  }
+  const bool nonper = (B.kind == KIND_NONPER);
+  std::vector<T> w((size_t)(n * N));
+  std::vector<uint32_t> mask((size_t)n);
+  std::vector<int64_t> off((size_t)n + 1, 0);
+  int nth = nthreads > 0 ? nthreads : 1;
+#ifndef _OPENMP
+  nth = 1;
+#endif
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nth) schedule(static)
+#endif
   for (int64_t ip = 0; ip < n; ip++) {
-    T p[N];
-    if (B.kind == KIND_NONPER) {
+    T* p = w.data() + ip * N;
+    if (nonper) {
       for (int i = 0; i < N; i++) p[i] = x[ip * N + i];
-      add_particle(cl, ip, p, true);
+      mask[(size_t)ip] = 0;
+      off[(size_t)ip + 1] = 1;
       continue;
     }
     wrap_to_first(B, x + ip * N, p);
-    add_particle(cl, ip, p, true);
-    // replicate_particle!: Iterators.product(-1:1, ...) with the first index fastest
-    int nimg = 1;
-    for (int i = 0; i < N; i++) nimg *= 3;
+    uint32_t m = 0;
+    int cnt = 1;
     for (int k = 0; k < nimg; k++) {
-      int s[N];
-      int kk = k, nz = 0;
-      for (int i = 0; i < N; i++) { s[i] = kk % 3 - 1; kk /= 3; nz += (s[i] == 0); }
-      if (nz == N) continue;
-      T sh[N], g[N];
-      for (int i = 0; i < N; i++) {
-        T acc = B.Mal.a[i][0] * T(s[0]);
-        for (int j = 1; j < N; j++) acc = acc + B.Mal.a[i][j] * T(s[j]);
-        sh[i] = acc;
-      }
-      for (int i = 0; i < N; i++) g[i] = p[i] + sh[i];
-      if (in_computing_box(B, g)) add_particle(cl, ip, g, false);
+      if (k == zero) continue;
+      T g[N];
+      for (int i = 0; i < N; i++) g[i] = p[i] + shift[k][i];
+      if (in_computing_box(B, g)) { m |= 1u << k; cnt++; }
+    }
+    mask[(size_t)ip] = m;
+    off[(size_t)ip + 1] = cnt;
+  }
+  for (int64_t ip = 0; ip < n; ip++) off[(size_t)ip + 1] += off[(size_t)ip];
+  const int64_t nc = off[(size_t)n];
+  std::vector<Particle<T, N>> tmp((size_t)nc);
+  std::vector<int64_t> cellof((size_t)nc);
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nth) schedule(static)
+#endif
+  for (int64_t ip = 0; ip < n; ip++) {
+    const T* p = w.data() + ip * N;
+    int64_t at = off[(size_t)ip];
+    Particle<T, N>& r = tmp[(size_t)at];
+    r.index = ip;
+    r.real = true;
+    for (int i = 0; i < N; i++) r.x[i] = p[i];
+    cellof[(size_t)at] = copy_cell(B, p, true);
+    at++;
+    uint32_t m = mask[(size_t)ip];
+    for (int k = 0; k < nimg; k++) {
+      if (!(m & (1u << k))) continue;
+      Particle<T, N>& q = tmp[(size_t)at];
+      q.index = ip;
+      q.real = false;
+      for (int i = 0; i < N; i++) q.x[i] = p[i] + shift[k][i];
+      cellof[(size_t)at] = copy_cell(B, q.x, false);
+      at++;
     }
   }
+  // stable counting sort by cell
+  cl.start.assign((size_t)ncells + 1, 0);
+  std::vector<char> has_real((size_t)ncells, 0);
+  for (int64_t t = 0; t < nc; t++) {
+    cl.start[(size_t)cellof[(size_t)t] + 1]++;
+    if (tmp[(size_t)t].real) has_real[(size_t)cellof[(size_t)t]] = 1;
+  }
+  for (int64_t c = 0; c < ncells; c++) cl.start[(size_t)c + 1] += cl.start[(size_t)c];
+  std::vector<int64_t> fill(cl.start.begin(), cl.start.end() - 1);
+  cl.parts.resize((size_t)nc);
+  for (int64_t t = 0; t < nc; t++) cl.parts[(size_t)fill[(size_t)cellof[(size_t)t]]++] = tmp[(size_t)t];
+  cl.n_particles = nc;
+  cl.real_cells.clear();
+  for (int64_t c = 0; c < ncells; c++)
+    if (has_real[(size_t)c]) cl.real_cells.push_back(c);
 }
 
 // ----------------------------------------------------------------------------
@@ -759,7 +833,7 @@ template <class T, int N> struct Mapper {
   }
 
   // same-cell, self
-  void current_self(Local& L, const std::vector<Particle<T, N>>& cell) const {
+  void current_self(Local& L, const Span<Particle<T, N>>& cell) const {
     const int64_t n = (int64_t)cell.size();
     if (!tri) {
       for (int64_t a = 0; a + 1 < n; a++) {
@@ -786,7 +860,7 @@ template <class T, int N> struct Mapper {
   }
 
   // same-cell, cross
-  void current_cross(Local& L, const std::vector<Particle<T, N>>& ci, const std::vector<Particle<T, N>>& cj) const {
+  void current_cross(Local& L, const Span<Particle<T, N>>& ci, const Span<Particle<T, N>>& cj) const {
     for (const auto& pi : ci) {
       if (!nonper && !pi.real) continue;
       for (const auto& pj : cj) {
@@ -797,7 +871,7 @@ template <class T, int N> struct Mapper {
   }
 
   // vicinal cells with projection culling; skip = index rule for triclinic self
-  void vicinal(Local& L, const std::vector<Particle<T, N>>& ci, const int64_t* cci, const std::vector<Particle<T, N>>& cj,
+  void vicinal(Local& L, const Span<Particle<T, N>>& ci, const int64_t* cci, const Span<Particle<T, N>>& cj,
                const int64_t* ccj, bool skip, std::vector<Particle<T, N>>& pp, std::vector<T>& ppx) const {
     T ctr_i[N], ctr_j[N], dc[N];
     cell_center(B, cci, ctr_i);
@@ -892,8 +966,8 @@ int run_map(const orc_spec* s, const T* x, int64_t nx, const T* y, int64_t ny, c
   if (st) return st;
   const bool cross = (y != nullptr);
   CellList<T, N> clx, cly;
-  build(clx, B, x, nx);
-  if (cross) build(cly, B, y, ny);
+  build(clx, B, x, nx, op->nthreads);
+  if (cross) build(cly, B, y, ny, op->nthreads);
   OpCtx<T, N> ctx;
   ctx.op = op;
   ctx.cross = cross;
@@ -931,32 +1005,29 @@ int run_map(const orc_spec* s, const T* x, int64_t nx, const T* y, int64_t ny, c
 #pragma omp for schedule(dynamic, 8)
 #endif
     for (int64_t r = 0; r < nreal; r++) {
-      int64_t pos = clx.real_cells[(size_t)r];
-      const auto& cell = clx.cells[(size_t)pos];
+      const int64_t li = clx.real_cells[(size_t)r];
+      const auto cell = clx.cell(li);
       int64_t cc[N];
-      cart_from_linear(B, clx.cell_lin[(size_t)pos], cc);
+      cart_from_linear(B, li, cc);
       if (!cross) {
         mp.current_self(L, cell);
         const auto& sten = (tri ? st_all : st_fw);
         for (const auto& o : sten) {
           int64_t cj[N];
           for (int k = 0; k < N; k++) cj[k] = cc[k] + o[k];
-          int64_t lj = linear_index(B, cj);
-          int64_t pj = clx.cell_of[lj];
-          if (pj < 0) continue;
-          mp.vicinal(L, cell, cc, clx.cells[(size_t)pj], cj, true, pp, ppx);
+          const auto other = clx.cell(linear_index(B, cj));
+          if (other.empty()) continue;
+          mp.vicinal(L, cell, cc, other, cj, true, pp, ppx);
         }
       } else {
-        int64_t lj0 = clx.cell_lin[(size_t)pos];
-        int64_t pj0 = cly.cell_of[lj0];
-        if (pj0 >= 0) mp.current_cross(L, cell, cly.cells[(size_t)pj0]);
+        const auto same = cly.cell(li);
+        if (!same.empty()) mp.current_cross(L, cell, same);
         for (const auto& o : st_all) {
           int64_t cj[N];
           for (int k = 0; k < N; k++) cj[k] = cc[k] + o[k];
-          int64_t lj = linear_index(B, cj);
-          int64_t pj = cly.cell_of[lj];
-          if (pj < 0) continue;
-          mp.vicinal(L, cell, cc, cly.cells[(size_t)pj], cj, false, pp, ppx);
+          const auto other = cly.cell(linear_index(B, cj));
+          if (other.empty()) continue;
+          mp.vicinal(L, cell, cc, other, cj, false, pp, ppx);
         }
       }
     }
@@ -1126,23 +1197,20 @@ int run_celllist(const orc_spec* s, const T* x, int64_t n, int64_t* n_copies, in
   int st = make_box<T, N>(s, x, n, nullptr, 0, B);
   if (st) return st;
   CellList<T, N> cl;
-  build(cl, B, x, n);
+  build(cl, B, x, n, orc_max_threads_impl());
   *n_copies = cl.n_particles;
   *n_cells_real = (int64_t)cl.real_cells.size();
   if (!cell) return ERR_OK;
   if (cap < cl.n_particles) return ERR_CAPACITY;
-  // emit in cell linear-index order, particles in the reference's in-cell order
-  std::vector<int64_t> order(cl.cells.size());
-  for (size_t q = 0; q < order.size(); q++) order[q] = (int64_t)q;
-  std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return cl.cell_lin[(size_t)a] < cl.cell_lin[(size_t)b]; });
-  int64_t k = 0;
-  for (int64_t pos : order) {
-    for (const auto& p : cl.cells[(size_t)pos]) {
-      cell[k] = cl.cell_lin[(size_t)pos];
+  // cell linear-index order, particles in the reference's in-cell order
+  const int64_t ncells = B.ncells();
+  for (int64_t c = 0; c < ncells; c++) {
+    for (int64_t k = cl.start[(size_t)c]; k < cl.start[(size_t)c + 1]; k++) {
+      const auto& p = cl.parts[(size_t)k];
+      cell[k] = c;
       idx[k] = p.index;
       real[k] = p.real ? 1 : 0;
       for (int d = 0; d < N; d++) coords[k * N + d] = (double)p.x[d];
-      k++;
     }
   }
   return ERR_OK;
