@@ -6,7 +6,8 @@ Workload (one "step" = cell-list build + pair map over the whole system):
   cell a=(L,0,0), b=(0.2L,L,0), c=(0.1L,0.15L,L), Gaussian jitter sigma=0.05, Lennard-Jones
   (sigma=1, eps=1) energy + forces with cutoff 2.5.  Seeded synthetic data (seed 2).
 Forms: exact (input-dtype arithmetic, bit-exact pair set) is `value`; the FP32-split form is reported
-beside it.  `e2e` goes through the C ABI with host buffers (H2D of positions and D2H of energy+forces
+beside it (for Float32 inputs it is the exact form; `forms.cfg2_f64` runs the same workload with Float64
+positions, where the split form does its distance work in FP32).  `e2e` goes through the C ABI with host buffers (H2D of positions and D2H of energy+forces
 inside the timed region).  `--impl reference` times the CPU restatement of the reference algorithm
 (OpenMP over all host cores) on the same workload.
 
@@ -118,6 +119,17 @@ def cpu_reference(x, M, steps, warmup, threads):
         orc.run("lj_forces", x, **kw)
     dt = time.perf_counter() - t0
     return pairs, dt
+
+
+def max_over_ranks(value, world, device=None):
+    """Replicas: the job's time is the slowest rank's (all_reduce MAX over the process group)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 # ---------------------------------------------------------------------------------------------- other forms
@@ -245,6 +257,34 @@ def measure_forms(pkg, L, A, dev, stream, flush, peaks, which, steps, warmup):
                 res[f"{opname}/{tag}"] = e
         P.close()
         out["cfg1"] = res
+
+    if "cfg2_f64" in which:
+        log("cfg2_f64")
+        # the headline geometry with Float64 positions: the FP32-split form against the exact FP64 form
+        x2, M2 = make_workload(64)
+        xd = torch.from_numpy(x2.astype(np.float64)).to(dev)
+        f = torch.zeros_like(xd)
+        P = Plain(L, A, np.float64, 3, 1, stream)
+        P.box(M2, A.CLM_TRICLINIC, CUTOFF)
+        pairs = P.count([xd])
+        R = candidates_per_hit(P.cell_size(), CUTOFF)
+        p = A.OpParams()
+        p.p[0], p.p[1], p.p[2], p.p[3] = 1.0, 1.0, 4.0, 4.0
+        o = A.Outputs()
+        o.forces_x = f.data_ptr()
+        o.out_on_device = 1
+        res = {"workload": "the headline fcc triclinic LJ workload with Float64 positions", "pairs": pairs,
+               "candidates_per_hit": R}
+        for prec, tag in ((A.CLM_PREC_EXACT, "exact"), (A.CLM_PREC_SPLIT, "split")):
+            L.clm_set_precision(P.h, prec)
+            st_ms, k_ms, b_ms = P.timed([xd], A.OP["lj_forces"], p, o, steps, warmup, flush)
+            F = 8 * R + F_OP["lj_forces"]
+            e = frac_entry(pairs, k_ms, F, p64)
+            e.update({"step_ms": st_ms, "build_ms": b_ms, "frac_of_fp32_roofline": e["pairs_per_s"] / roofline_pairs(F, p32)})
+            res[tag] = e
+        res["split_over_exact"] = res["exact"]["kernel_ms"] / res["split"]["kernel_ms"]
+        P.close()
+        out["cfg2_f64"] = res
 
     if "cfg3" in which:
         log("cfg3")
@@ -383,7 +423,7 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--ncell", type=int, default=64, help="fcc cells per side (64 -> 1,048,576 particles)")
     ap.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU baseline sample")
-    ap.add_argument("--forms", default="cfg1,cfg3,cfg4,cfg5,cfg5_2d",
+    ap.add_argument("--forms", default="cfg1,cfg2_f64,cfg3,cfg4,cfg5,cfg5_2d",
                     help="other configurations measured beside the headline (comma list, '' for none; "
                          "cfg5_small and cfg5_2d_small are 2 x 200k-point versions of the two-set histogram)")
     args = ap.parse_args()
@@ -484,10 +524,7 @@ def main():
         torch.cuda.synchronize()
         l1 = C.c_int64()
         L.clm_stats(h, C.byref(l1))
-        if world > 1:
-            t = torch.tensor([tot_ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            tot_ms = float(t.item())
+        tot_ms = max_over_ranks(tot_ms, world, dev)
         return tot_ms, statistics.mean(kern_ms), (l1.value - l0.value)
 
     clocks = ClockSampler(local)

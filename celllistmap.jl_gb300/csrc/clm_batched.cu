@@ -200,7 +200,7 @@ template <class T> int enqueue_op(Handle& h, int slot, int op, const clm_op_para
   A.xflags = X.cell_flags.as<int>();
   A.n_real_dev = X.real_scan.as<int>() + X.ncells;
   A.self = 1;
-  A.split = (h.precision == CLM_PREC_SPLIT);
+  A.split = (h.precision == CLM_PREC_SPLIT) && sizeof(T) == 8;  // Float32: the split form is the exact form
   A.op = op;
   A.err = h.err.as<int>();
   A.cell_split = B.cell_split;

@@ -199,7 +199,7 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
   A.xflags = X.cell_flags.as<int>();
   A.n_real_dev = X.real_scan.as<int>() + X.ncells;
   A.self = (h.nsets == 1);
-  A.split = (h.precision == 1);
+  A.split = (h.precision == 1) && sizeof(T) == 8;  // Float32 inputs: the split form is the exact form
   A.op = op;
   A.err = h.err.as<int>();
   A.cell_split = cell_split_for(h, g, opk);
@@ -551,7 +551,7 @@ int run_pairs_scalar_scratch(Handle& h, const Geometry<T>& g, int op, const void
   A.xflags = X.cell_flags.as<int>();
   A.n_real_dev = X.real_scan.as<int>() + X.ncells;
   A.self = (h.nsets == 1);
-  A.split = (h.precision == 1);
+  A.split = (h.precision == 1) && sizeof(T) == 8;  // Float32 inputs: the split form is the exact form
   A.op = op;
   A.err = h.err.as<int>();
   A.cell_split = 1;
@@ -626,7 +626,7 @@ int pairs_scalar_blocks_needed(Handle& h, int op) {
   int sms = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const LaunchSel sel{h.dim, opk, h.nsets == 1, h.precision == 1, false};
+  const LaunchSel sel{h.dim, opk, h.nsets == 1, h.precision == 1 && h.dtype == 1, false};
   const int per_sm = (h.dtype == 1) ? pairs_blocks_per_sm(sel, (const PairArgs<double>*)nullptr)
                                     : pairs_blocks_per_sm(sel, (const PairArgs<float>*)nullptr);
   if (per_sm <= 0 || sms <= 0) return -1;

@@ -1058,12 +1058,18 @@ cudaError_t launch_s(int opk, int& grid, cudaStream_t st, const PairArgs<T>& A) 
 // Plain launches of one dtype: every operator kind, self and cross pairs, exact and split forms.
 template <class T>
 cudaError_t launch_plain_t(const LaunchSel& s, int& grid, cudaStream_t st, const PairArgs<T>& A) {
-  if (s.dim == 3) {
-    if (s.self) return s.split ? launch_s<T, 3, true, false>(s.opk, grid, st, A) : launch_s<T, 3, false, false>(s.opk, grid, st, A);
-    return s.split ? launch_s<T, 3, true, true>(s.opk, grid, st, A) : launch_s<T, 3, false, true>(s.opk, grid, st, A);
+  if constexpr (std::is_same<T, float>::value) {
+    // Float32 inputs: the split form is the exact form (the input arithmetic is FP32 already)
+    if (s.dim == 3) return s.self ? launch_s<T, 3, false, false>(s.opk, grid, st, A) : launch_s<T, 3, false, true>(s.opk, grid, st, A);
+    return s.self ? launch_s<T, 2, false, false>(s.opk, grid, st, A) : launch_s<T, 2, false, true>(s.opk, grid, st, A);
+  } else {
+    if (s.dim == 3) {
+      if (s.self) return s.split ? launch_s<T, 3, true, false>(s.opk, grid, st, A) : launch_s<T, 3, false, false>(s.opk, grid, st, A);
+      return s.split ? launch_s<T, 3, true, true>(s.opk, grid, st, A) : launch_s<T, 3, false, true>(s.opk, grid, st, A);
+    }
+    if (s.self) return s.split ? launch_s<T, 2, true, false>(s.opk, grid, st, A) : launch_s<T, 2, false, false>(s.opk, grid, st, A);
+    return s.split ? launch_s<T, 2, true, true>(s.opk, grid, st, A) : launch_s<T, 2, false, true>(s.opk, grid, st, A);
   }
-  if (s.self) return s.split ? launch_s<T, 2, true, false>(s.opk, grid, st, A) : launch_s<T, 2, false, false>(s.opk, grid, st, A);
-  return s.split ? launch_s<T, 2, true, true>(s.opk, grid, st, A) : launch_s<T, 2, false, true>(s.opk, grid, st, A);
 }
 
 // Batched launches: self pairs of many systems; neighbour lists, scalar reductions and forces.
@@ -1080,8 +1086,12 @@ cudaError_t launch_b(int opk, int& grid, cudaStream_t st, const PairArgs<T>& A) 
 template <class T>
 cudaError_t launch_batch_t(const LaunchSel& s, int& grid, cudaStream_t st, const PairArgs<T>& A) {
   if (!s.self) return cudaErrorInvalidValue;
-  if (s.dim == 3) return s.split ? launch_b<T, 3, true>(s.opk, grid, st, A) : launch_b<T, 3, false>(s.opk, grid, st, A);
-  return s.split ? launch_b<T, 2, true>(s.opk, grid, st, A) : launch_b<T, 2, false>(s.opk, grid, st, A);
+  if constexpr (std::is_same<T, float>::value) {
+    return s.dim == 3 ? launch_b<T, 3, false>(s.opk, grid, st, A) : launch_b<T, 2, false>(s.opk, grid, st, A);
+  } else {
+    if (s.dim == 3) return s.split ? launch_b<T, 3, true>(s.opk, grid, st, A) : launch_b<T, 3, false>(s.opk, grid, st, A);
+    return s.split ? launch_b<T, 2, true>(s.opk, grid, st, A) : launch_b<T, 2, false>(s.opk, grid, st, A);
+  }
 }
 
 template <class K> int occupancy_of(K kernel) {
@@ -1094,24 +1104,24 @@ template <class K> int occupancy_of(K kernel) {
 }
 
 // Occupancy of the scalar and min-distance instantiations (the allocation-free entry point sizes its
-// partials with it).
+// partials with it).  Float32 handles have no split instantiation (their split form is the exact one).
+template <class T, int N, int OPK> int occupancy_pick(bool split, bool self) {
+  if constexpr (std::is_same<T, float>::value) {
+    (void)split;
+    return self ? occupancy_of(k_pairs<T, N, OPK, false, false, false>) : occupancy_of(k_pairs<T, N, OPK, false, true, false>);
+  } else {
+    if (split)
+      return self ? occupancy_of(k_pairs<T, N, OPK, true, false, false>) : occupancy_of(k_pairs<T, N, OPK, true, true, false>);
+    return self ? occupancy_of(k_pairs<T, N, OPK, false, false, false>) : occupancy_of(k_pairs<T, N, OPK, false, true, false>);
+  }
+}
+
 template <class T>
 int occupancy_t(const LaunchSel& s) {
-  if (s.dim == 3) {
-    if (s.opk == OPK_SCALAR)
-      return s.split ? (s.self ? occupancy_of(k_pairs<T, 3, OPK_SCALAR, true, false, false>) : occupancy_of(k_pairs<T, 3, OPK_SCALAR, true, true, false>))
-                     : (s.self ? occupancy_of(k_pairs<T, 3, OPK_SCALAR, false, false, false>) : occupancy_of(k_pairs<T, 3, OPK_SCALAR, false, true, false>));
-    if (s.opk == OPK_MIN)
-      return s.split ? (s.self ? occupancy_of(k_pairs<T, 3, OPK_MIN, true, false, false>) : occupancy_of(k_pairs<T, 3, OPK_MIN, true, true, false>))
-                     : (s.self ? occupancy_of(k_pairs<T, 3, OPK_MIN, false, false, false>) : occupancy_of(k_pairs<T, 3, OPK_MIN, false, true, false>));
-  } else {
-    if (s.opk == OPK_SCALAR)
-      return s.split ? (s.self ? occupancy_of(k_pairs<T, 2, OPK_SCALAR, true, false, false>) : occupancy_of(k_pairs<T, 2, OPK_SCALAR, true, true, false>))
-                     : (s.self ? occupancy_of(k_pairs<T, 2, OPK_SCALAR, false, false, false>) : occupancy_of(k_pairs<T, 2, OPK_SCALAR, false, true, false>));
-    if (s.opk == OPK_MIN)
-      return s.split ? (s.self ? occupancy_of(k_pairs<T, 2, OPK_MIN, true, false, false>) : occupancy_of(k_pairs<T, 2, OPK_MIN, true, true, false>))
-                     : (s.self ? occupancy_of(k_pairs<T, 2, OPK_MIN, false, false, false>) : occupancy_of(k_pairs<T, 2, OPK_MIN, false, true, false>));
-  }
+  if (s.opk == OPK_SCALAR)
+    return s.dim == 3 ? occupancy_pick<T, 3, OPK_SCALAR>(s.split, s.self) : occupancy_pick<T, 2, OPK_SCALAR>(s.split, s.self);
+  if (s.opk == OPK_MIN)
+    return s.dim == 3 ? occupancy_pick<T, 3, OPK_MIN>(s.split, s.self) : occupancy_pick<T, 2, OPK_MIN>(s.split, s.self);
   return 0;
 }
 
