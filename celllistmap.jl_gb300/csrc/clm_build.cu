@@ -252,8 +252,7 @@ template <class T, int N>
 __device__ __forceinline__ void emit_at(const DevGeom<T>& g, int cb, const T* __restrict__ wrapped,
                                         const uint32_t* __restrict__ mask, const int* __restrict__ ncopy,
                                         const int* __restrict__ copy_off, int i, int cap, uint32_t* __restrict__ keys,
-                                        uint32_t* __restrict__ vals, int* __restrict__ cell_count,
-                                        int* __restrict__ cell_flags, int* __restrict__ err) {
+                                        uint32_t* __restrict__ vals, int* __restrict__ err) {
   if (ncopy[i] == 0) return;
   int base = copy_off[i];
   if (base < 0 || base + ncopy[i] > cap) {
@@ -271,8 +270,6 @@ __device__ __forceinline__ void emit_at(const DevGeom<T>& g, int cb, const T* __
   li += cb;
   keys[base] = (uint32_t)li;
   vals[base] = ((uint32_t)i << 5) | (uint32_t)g.zero_code;
-  atomicAdd(&cell_count[li], 1);
-  cell_flags[li] = 1;
   int t = 1;
   uint32_t m = mask[i];
   while (m) {
@@ -289,7 +286,6 @@ __device__ __forceinline__ void emit_at(const DevGeom<T>& g, int cb, const T* __
     lk += cb;
     keys[base + t] = (uint32_t)lk;
     vals[base + t] = ((uint32_t)i << 5) | (uint32_t)k;
-    atomicAdd(&cell_count[lk], 1);
     t++;
   }
 }
@@ -299,11 +295,10 @@ __global__ void __launch_bounds__(kBlock) k_emit(DevGeom<T> g, const T* __restri
                                                  const uint32_t* __restrict__ mask, const int* __restrict__ ncopy,
                                                  const int* __restrict__ copy_off, int n, int cap,
                                                  uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
-                                                 int* __restrict__ cell_count, int* __restrict__ cell_flags,
                                                  int* __restrict__ err) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  emit_at<T, N>(g, 0, wrapped, mask, ncopy, copy_off, i, cap, keys, vals, cell_count, cell_flags, err);
+  emit_at<T, N>(g, 0, wrapped, mask, ncopy, copy_off, i, cap, keys, vals, err);
 }
 
 template <class T, int N>
@@ -312,12 +307,11 @@ __global__ void __launch_bounds__(kBlock) k_emit_b(const DevGeom<T>* __restrict_
                                                    const uint32_t* __restrict__ mask, const int* __restrict__ ncopy,
                                                    const int* __restrict__ copy_off, int n, int cap,
                                                    uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
-                                                   int* __restrict__ cell_count, int* __restrict__ cell_flags,
                                                    int* __restrict__ err) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int s = psys[i];
-  emit_at<T, N>(gtab[s], cbase[s], wrapped, mask, ncopy, copy_off, i, cap, keys, vals, cell_count, cell_flags, err);
+  emit_at<T, N>(gtab[s], cbase[s], wrapped, mask, ncopy, copy_off, i, cap, keys, vals, err);
 }
 
 // ------------------------------------------------------------------ K4: gather in cell order
@@ -340,7 +334,7 @@ template <class T, int N>
 __device__ __forceinline__ void gather_at(const DevGeom<T>& g, const T* __restrict__ wrapped, int t, int p, int k,
                                           int li, T* __restrict__ px, T* __restrict__ py, T* __restrict__ pz,
                                           float4* __restrict__ off, float4* __restrict__ xq,
-                                          int* __restrict__ code) {
+                                          int* __restrict__ code, int* __restrict__ cell_flags, int cb) {
   T q[N];
 #pragma unroll
   for (int d = 0; d < N; d++) {
@@ -367,6 +361,7 @@ __device__ __forceinline__ void gather_at(const DevGeom<T>& g, const T* __restri
   if constexpr (std::is_same<T, float>::value)
     xq[t] = make_float4((float)q[0], (float)q[1], N == 3 ? (float)q[N - 1] : 0.f, __int_as_float(pc));
   code[t] = pc;
+  if (k == g.zero_code) cell_flags[cb + li] = 1;  // the cell holds a real particle
 }
 
 template <class T, int N>
@@ -375,7 +370,8 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom<T> g, const T* __rest
                                                    const uint32_t* __restrict__ svals, const int* __restrict__ n_dev,
                                                    int cap, int n, T* __restrict__ px, T* __restrict__ py,
                                                    T* __restrict__ pz, float4* __restrict__ off, float4* __restrict__ xq,
-                                                   int* __restrict__ code, int* __restrict__ err) {
+                                                   int* __restrict__ code, int* __restrict__ cell_flags,
+                                                   int* __restrict__ err) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= min(*n_dev, cap)) return;
   uint32_t v = svals[t];
@@ -388,7 +384,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom<T> g, const T* __rest
     k = g.zero_code;
     li = 0;
   }
-  gather_at<T, N>(g, wrapped, t, p, k, li, px, py, pz, off, xq, code);
+  gather_at<T, N>(g, wrapped, t, p, k, li, px, py, pz, off, xq, code, cell_flags, 0);
 }
 
 template <class T, int N>
@@ -399,7 +395,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_b(const DevGeom<T>* __restric
                                                      int cap, int n, T* __restrict__ px, T* __restrict__ py,
                                                      T* __restrict__ pz, float4* __restrict__ off,
                                                      float4* __restrict__ xq, int* __restrict__ code,
-                                                     int* __restrict__ err) {
+                                                     int* __restrict__ cell_flags, int* __restrict__ err) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= min(*n_dev, cap)) return;
   uint32_t v = svals[t];
@@ -417,7 +413,19 @@ __global__ void __launch_bounds__(kBlock) k_gather_b(const DevGeom<T>* __restric
     k = g.zero_code;
     li = 0;
   }
-  gather_at<T, N>(g, wrapped, t, p, k, li, px, py, pz, off, xq, code);
+  gather_at<T, N>(g, wrapped, t, p, k, li, px, py, pz, off, xq, code, cell_flags, cbase[s]);
+}
+
+// cell_start from the keys sorted by cell: the thread of copy t writes the starts of the cells between
+// the previous copy's cell (exclusive) and its own (inclusive); the thread t = n closes the list.
+__global__ void __launch_bounds__(kBlock) k_cell_start(const uint32_t* __restrict__ skeys, const int* __restrict__ n_dev,
+                                                       int cap, int ncells, int* __restrict__ cell_start) {
+  const int n = min(*n_dev, cap);
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t > n) return;
+  const int lo = (t == 0) ? 0 : (int)skeys[t - 1] + 1;
+  const int hi = (t == n) ? ncells : (int)skeys[t];
+  for (int c = lo; c <= hi && c <= ncells; c++) cell_start[c] = t;
 }
 
 __global__ void k_compact(const int* __restrict__ flags, const int* __restrict__ scanned, int ncells,
@@ -631,7 +639,6 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
       !S.cell_flags.reserve(sizeof(int) * (ncells + 1)) || !S.real_scan.reserve(sizeof(int) * (ncells + 1)) ||
       !S.real_list.reserve(sizeof(int) * (ncells + 1)) || !S.copy_off.reserve(sizeof(int) * (n + 1)))
     return ERR_NOMEM;
-  CLM_CUDA_TRY(h, cudaMemsetAsync(S.cell_count.p, 0, sizeof(int) * (ncells + 1), h.stream));
   CLM_CUDA_TRY(h, cudaMemsetAsync(S.cell_flags.p, 0, sizeof(int) * (ncells + 1), h.stream));
   S.built = true;
   S.dirty = false;
@@ -696,20 +703,20 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
       k_emit_b<T, 3><<<gn, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
                                                  S.ncopy.as<int>(), S.copy_off.as<int>(), (int)n, (int)cap,
                                                  S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
-                                                 S.cell_count.as<int>(), S.cell_flags.as<int>(), err);
+                                                 err);
     else
       k_emit_b<T, 2><<<gn, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
                                                  S.ncopy.as<int>(), S.copy_off.as<int>(), (int)n, (int)cap,
                                                  S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
-                                                 S.cell_count.as<int>(), S.cell_flags.as<int>(), err);
+                                                 err);
   } else if (N == 3)
     k_emit<T, 3><<<gn, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(),
                                              S.copy_off.as<int>(), (int)n, (int)cap, S.keys[0].as<uint32_t>(),
-                                             S.vals[0].as<uint32_t>(), S.cell_count.as<int>(), S.cell_flags.as<int>(), err);
+                                             S.vals[0].as<uint32_t>(), err);
   else
     k_emit<T, 2><<<gn, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(),
                                              S.copy_off.as<int>(), (int)n, (int)cap, S.keys[0].as<uint32_t>(),
-                                             S.vals[0].as<uint32_t>(), S.cell_count.as<int>(), S.cell_flags.as<int>(), err);
+                                             S.vals[0].as<uint32_t>(), err);
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
   // stable LSD radix sort by cell
@@ -734,27 +741,29 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
     cur = 1 - cur;
   }
   // cell offsets
-  st = scan_exclusive(h, S.cell_count.as<int>(), S.cell_start.as<int>(), ncells, S.cell_start.as<int>() + ncells);
-  if (st) return st;
+  k_cell_start<<<grid_for(cap + 1), kBlock, 0, h.stream>>>(S.keys[cur].as<uint32_t>(), n_dev, (int)cap, (int)ncells,
+                                                          S.cell_start.as<int>());
+  CLM_CUDA_TRY(h, cudaGetLastError());
+  h.launches++;
   // gather coordinates in cell order
   const int gc = grid_for(cap);
   if (batch) {
     if (N == 3)
       k_gather_b<T, 3><<<gc, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
                                                    S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
-                                                   S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), err);
+                                                   S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), S.cell_flags.as<int>(), err);
     else
       k_gather_b<T, 2><<<gc, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
                                                    S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
-                                                   S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), err);
+                                                   S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), S.cell_flags.as<int>(), err);
   } else if (N == 3)
     k_gather<T, 3><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
                                                S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
-                                               S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), err);
+                                               S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), S.cell_flags.as<int>(), err);
   else
     k_gather<T, 2><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
                                                S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
-                                               S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), err);
+                                               S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), S.cell_flags.as<int>(), err);
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
   // cells with real particles, in linear order; their number stays on the device (real_scan[ncells])
