@@ -709,11 +709,11 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                     }
                     const FA c12 = (FA)A.p[2], c6 = (FA)A.p[3];
                     const FA dd2 = sure ? (FA)d2f : (FA)d2;
-                    const FA sr2 = sig * sig / dd2;
+                    const FA sr2 = sig * sig * vrcp(dd2);
                     const FA sr6 = sr2 * sr2 * sr2;
                     const FA sr12 = sr6 * sr6;
                     const FA lj = c12 * sr12 - c6 * sr6;
-                    const FA dsg = eps * (FA(12) * c12 * sr12 - FA(6) * c6 * sr6) / sig;
+                    const FA dsg = eps * (FA(12) * c12 * sr12 - FA(6) * c6 * sr6) * vrcp(sig);
 #pragma unroll
                     for (int k = 0; k < 3; k++) {
                       adj[6 + k] += (cls == k) ? lj : FA(0);
