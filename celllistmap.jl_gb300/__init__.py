@@ -11,7 +11,8 @@ importlib (see ``tests/conftest.py``).
 from . import _abi
 from . import api as _api
 from .api import (ArgumentError, BatchedSystems, Box, CUDAError, DimensionMismatch, EnergyAndForces, InPlaceNeighborList,
-                  ParticleSystem, neighborlist, neighborlist_, pairwise, pairwise_, update, version)
+                  ParticleSystem, device_allocations, neighborlist, neighborlist_, pairwise, pairwise_, update,
+                  version)
 from . import api as ops  # operator classes live in api; exposed as `ops`
 from . import workloads
 from . import trajectory
@@ -32,7 +33,7 @@ NeighborList = _api.NeighborList
 
 __all__ = [
     "ArgumentError", "BatchedSystems", "Box", "CUDAError", "DimensionMismatch", "EnergyAndForces", "InPlaceNeighborList",
-    "ParticleSystem", "neighborlist", "neighborlist_", "pairwise", "pairwise_", "update", "version", "ops",
+    "ParticleSystem", "device_allocations", "neighborlist", "neighborlist_", "pairwise", "pairwise_", "update", "version", "ops",
     "Count", "SumD2", "SumD", "SumInvD", "SoftEnergy", "SoftForces", "LennardJones", "LennardJonesForces", "LennardJonesAdjoint",
     "InverseDistanceForces", "MinimumDistance", "RadialHistogram", "NeighborList",
 ]

@@ -32,7 +32,8 @@ EXPORTS = [
     "clm_set_precision", "clm_run", "clm_run_noalloc", "clm_nl_count", "clm_nl_fetch", "clm_get_box", "clm_get_celllist_info",
     "clm_fetch_celllist", "clm_last_timings", "clm_lj_adjoint", "clm_batched_create", "clm_batched_set_systems",
     "clm_batched_run", "clm_batched_status", "clm_batched_set_graph", "clm_batched_set_config",
-    "clm_batched_autotune", "clm_batched_last_step", "clm_stats", "clm_last_error", "clm_version",
+    "clm_batched_autotune", "clm_batched_last_step", "clm_stats", "clm_device_allocations", "clm_last_error",
+    "clm_version",
 ]
 
 
@@ -86,6 +87,7 @@ def _declare(L):
     L.clm_batched_autotune.argtypes = [vp, i32, vp, vp, i32, vp, C.POINTER(C.c_float)]
     L.clm_batched_last_step.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(i64)]
     L.clm_stats.argtypes = [vp, C.POINTER(i64)]
+    L.clm_device_allocations.argtypes = [C.POINTER(i64), C.POINTER(i64)]
     L.clm_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
     for name in EXPORTS:
         if name != "clm_version":

@@ -880,5 +880,12 @@ class Box:
         self.cutoff_sqr = cut.value * cut.value
 
 
+def device_allocations():
+    """(count, bytes) of the device and pinned allocations the library made in this process so far."""
+    c, b = C.c_int64(), C.c_int64()
+    _abi.load().clm_device_allocations(C.byref(c), C.byref(b))
+    return c.value, b.value
+
+
 def version() -> str:
     return _abi.load().clm_version().decode()

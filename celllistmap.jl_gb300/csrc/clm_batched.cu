@@ -159,6 +159,8 @@ template <class T> int batch_tables(Handle& h) {
     B.hres_bytes = 0;
     if (cudaMallocHost((void**)&B.hres, hres) != cudaSuccess) return fail(&h, ERR_NOMEM, "pinned allocation failed");
     B.hres_bytes = hres;
+    alloc_count()++;
+    alloc_bytes() += (long long)hres;
   }
   B.tables_ready = true;
   B.tables_dtype = h.dtype;
@@ -602,6 +604,12 @@ int32_t clm_batched_autotune(clm_handle h, int32_t nops, const int32_t* ops, con
     config[2] = bg;
   }
   if (best_ms) *best_ms = best;
+  return OK;
+}
+
+int32_t clm_device_allocations(int64_t* count, int64_t* bytes) {
+  if (count) *count = (int64_t)alloc_count().load();
+  if (bytes) *bytes = (int64_t)alloc_bytes().load();
   return OK;
 }
 

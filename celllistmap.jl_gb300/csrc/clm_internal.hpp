@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -17,6 +18,17 @@ enum Status {
   OK = 0, ERR_ARG = 1, ERR_CELL_TOO_SMALL = 2, ERR_NAN = 3, ERR_DIM = 4, ERR_CUDA = 5, ERR_CAPACITY = 6,
   ERR_STATE = 7, ERR_TIMEOUT = 8, ERR_NOMEM = 9, ERR_LCELL = 10, ERR_NONPERIODIC_CELL = 11, ERR_INTERNAL = 12
 };
+
+// Process-wide count and size of the device (and pinned host) allocations the library made; steady-state
+// steps with unchanged sizes make none (reported by clm_device_allocations).
+inline std::atomic<long long>& alloc_count() {
+  static std::atomic<long long> c{0};
+  return c;
+}
+inline std::atomic<long long>& alloc_bytes() {
+  static std::atomic<long long> b{0};
+  return b;
+}
 
 // Grow-only device buffer.
 struct DevBuf {
@@ -37,6 +49,8 @@ struct DevBuf {
       cudaGetLastError();
       return false;
     }
+    alloc_count()++;
+    alloc_bytes() += (long long)want;
     if (p) cudaFree(p);
     p = q;
     bytes = want;

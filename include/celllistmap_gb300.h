@@ -245,6 +245,11 @@ int32_t clm_batched_last_step(clm_handle h, float* step_ms, int64_t* launches);
 /* Number of CUDA kernels this handle has launched so far (cumulative). */
 int32_t clm_stats(clm_handle h, int64_t* kernel_launches);
 
+/* Device (and pinned host) allocations made by the library in this process so far: count and bytes.
+ * Buffers grow only, so repeated steps with unchanged sizes allocate nothing — the GPU counterpart of
+ * the reference's allocation tests for update!/neighborlist! (test/API/neighborlists.jl:114-177). */
+int32_t clm_device_allocations(int64_t* count, int64_t* bytes);
+
 /* Human-readable description of the last error on this handle. */
 int32_t clm_last_error(clm_handle h, char* buf, size_t n);
 
