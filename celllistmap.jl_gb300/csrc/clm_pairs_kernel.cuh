@@ -762,6 +762,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
               if (hit) {
                 bool exact_r = !sure;
                 T r = 0;
+                float rfl = 0.f;  // the distance in FP32 for the FP32 pair value (no FP64 conversions)
                 int b = -1;
                 if (sure) {
                   float rf = sqrtf(d2f);
@@ -775,7 +776,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                   const float tol = rf * 2.44140625e-4f;  // an edge within 2^-12: decide exactly
                   if ((lo <= A.nbins && fabsf(s_binf[lo] - rf) <= tol) || (lo >= 1 && fabsf(s_binf[lo - 1] - rf) <= tol))
                     exact_r = true;
-                  r = (T)rf;
+                  rfl = rf;
+                  if constexpr (!std::is_same<FA, float>::value) r = (T)rf;
                 }
                 if (exact_r) {
                   if (sure) load_xj();  // near a bin edge: the exact distance decides
@@ -787,6 +789,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                     e2 = xadd(e2, xmul(dd, dd));
                   }
                   r = xsqrt(e2);
+                  rfl = (float)r;
                   int lo = 0, hi = A.nbins + 1;
                   while (lo < hi) {
                     int mid = (lo + hi) >> 1;
@@ -823,7 +826,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
 #pragma unroll
                     for (int d = 0; d < N; d++)
                       dot += (A.vxf[(int64_t)idx_i * N + d] - vy[(int64_t)idx_j * N + d]) * dv[d];
-                    hv = dot * vrcp((float)r);
+                    hv = dot * vrcp(rfl);
                   } else {
                     const T* vy = CROSS ? A.vy : A.vx;
 #pragma unroll

@@ -132,8 +132,8 @@ def test_oracle_adjoint_vs_numpy(orc, clm, kind):
 @pytest.mark.parametrize("typed", [True, False])
 @pytest.mark.parametrize("precision", ["exact", "split"])
 def test_gpu_adjoint_vs_oracle(orc, clm, dtype, kind, typed, precision):
-    if precision == "split" and dtype == np.float64:
-        pytest.skip("the split form computes in Float32 pairs")
+    if precision == "split" and dtype == np.float32:
+        pytest.skip("for Float32 inputs the split form is the exact form")
     x, L, t, eps, sig = mixture(clm, n=20000)
     M = np.diag([L] * 3) if kind == "ortho" else tri_cell(L)
     if kind == "tri":
@@ -153,7 +153,7 @@ def test_gpu_adjoint_vs_oracle(orc, clm, dtype, kind, typed, precision):
     ref = orc.run("lj_adjoint", x, dim=3, kind=kind, unitcell=uc, cutoff=CUT, lcell=1, dtype=dtype,
                   params=[1.0, 1.0, C12, C6], types_x=tt, eps_table=teps, sig_table=tsig)
     p = pair_terms(orc, x, M, tt, teps, tsig, kind, dtype=dtype)
-    tol = 1e-12 if dtype == np.float64 else 1e-5
+    tol = 1e-12 if (dtype == np.float64 and precision == "exact") else 1e-5
     assert abs(got.energy - ref["scalar"]) <= tol * np.abs(p["u"]).sum()
     fscale = np.abs(ref["forces_x"]).max()
     assert np.abs(np.asarray(got.forces, np.float64) - ref["forces_x"]).max() <= tol * fscale
@@ -172,3 +172,34 @@ def test_gpu_adjoint_vs_oracle(orc, clm, dtype, kind, typed, precision):
         assert abs(got.dU_deps - ref["deps"][0]) <= tol * np.abs(p["u_over_eps"]).sum()
         assert abs(got.dU_dsigma - ref["dsig"][0]) <= tol * np.abs(p["du_dsig"]).sum()
     np.testing.assert_allclose(got.grad_positions, -np.asarray(got.forces))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_gpu_adjoint_2d(orc, clm, dtype):
+    """2D: a jittered square lattice with two types in a periodic square; same bars as in 3D."""
+    rng = np.random.default_rng(9)
+    m = 60
+    g = np.stack(np.meshgrid(np.arange(m), np.arange(m), indexing="ij"), -1).reshape(-1, 2) * 1.1
+    x = (g + rng.normal(0, 0.05, g.shape)).astype(dtype)
+    L = m * 1.1
+    t = (rng.random(len(x)) < 0.3).astype(np.int32)
+    eps = np.array([[1.0, 1.5], [1.5, 0.5]])
+    sig = np.array([[1.0, 0.8], [0.8, 0.88]])
+    op = clm.LennardJonesAdjoint(c12=C12, c6=C6, types_x=t, eps_table=eps, sig_table=sig)
+    sysm = clm.ParticleSystem(positions=x, unitcell=[L, L], cutoff=CUT, dtype=dtype)
+    got = clm.pairwise(op, sysm)
+    ref = orc.run("lj_adjoint", x, dim=2, kind="ortho", unitcell=[L, L], cutoff=CUT, dtype=dtype,
+                  params=[1.0, 1.0, C12, C6], types_x=t, eps_table=eps, sig_table=sig)
+    nl = orc.run("nl", x, dim=2, kind="ortho", unitcell=[L, L], cutoff=CUT, dtype=dtype)
+    i, j = nl["i"], nl["j"]
+    d2 = np.asarray(nl["d"], np.float64) ** 2
+    e, sg = eps[t[i], t[j]], sig[t[i], t[j]]
+    sr6 = (sg * sg / d2) ** 3
+    u = e * (C12 * sr6 * sr6 - C6 * sr6)
+    gw = np.abs(e * (-12 * C12 * sr6 * sr6 + 6 * C6 * sr6))  # |g| d^2, bounds each virial contribution
+    tol = 1e-12 if dtype == np.float64 else 1e-5
+    assert got.virial.shape == (2, 2)
+    assert abs(got.energy - ref["scalar"]) <= tol * np.abs(u).sum()
+    assert np.abs(got.virial - ref["virial"]).max() <= tol * gw.sum()
+    assert np.abs(np.asarray(got.forces, np.float64) - ref["forces_x"]).max() <= tol * np.abs(ref["forces_x"]).max()

@@ -187,3 +187,27 @@ def test_batch_errors(clm):
         bs.run(clm.MinimumDistance())
     with pytest.raises(clm.DimensionMismatch):
         bs.update(positions=np.concatenate(pos)[:-1])
+
+
+def test_batch_2d(orc, clm):
+    rng = np.random.default_rng(21)
+    pos, cells = [], []
+    for n in (50, 300, 900, 2000):
+        L = (n / 0.3) ** 0.5
+        pos.append(rng.random((n, 2)) * L)
+        cells.append([L, L])
+    bs = clm.BatchedSystems(positions=pos, unitcells=cells, cutoff=RC)
+    nls, e = bs.run(clm.NeighborList(), clm.SoftEnergy())
+    st = bs.status()
+    for s, (x, L) in enumerate(zip(pos, cells)):
+        if min(L) <= 2 * RC:
+            assert st[s] == 2
+            continue
+        ref = orc.run("nl", x, dim=2, kind="ortho", unitcell=L, cutoff=RC)
+        A = orc.canonical_pairs(*nls[s])
+        B = orc.canonical_pairs(ref["i"], ref["j"], ref["d"])
+        np.testing.assert_array_equal(A[0], B[0])
+        np.testing.assert_array_equal(A[1], B[1])
+        np.testing.assert_array_equal(A[2], B[2])
+        er = orc.run("soft_energy", x, dim=2, kind="ortho", unitcell=L, cutoff=RC, params=[RC])["scalar"]
+        assert abs(e[s] - er) <= 1e-12 * max(1.0, abs(er)) * 10
