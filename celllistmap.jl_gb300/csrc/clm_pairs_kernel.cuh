@@ -262,7 +262,8 @@ __device__ __forceinline__ const DevGeom<T>& geo_of(const PairArgs<T>& A, int li
 // half cell), so skipping it elsewhere leaves the pair set unchanged.
 // Resident blocks per SM (6 for Float32, 3 for Float64: 85 / 170 registers per thread) were picked by
 // timing 4..8 and 3..4 on GB300; fewer registers spill in the pair epilogues.
-template <class T, int N, int OPK, bool SPLIT, bool CROSS, bool BATCH>
+// OPC: the operator id when fixed at compile time (the LJ force loop), 0 = read from the arguments.
+template <class T, int N, int OPK, bool SPLIT, bool CROSS, bool BATCH, int OPC = 0>
 __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(const PairArgs<T> A) {
   using V = T;
   using FA = typename std::conditional<std::is_same<T, double>::value && !SPLIT, double, float>::type;
@@ -272,6 +273,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
   constexpr bool ABS_PF = !FP64 && !SPLIT;  // FP32 exact form: the prefilter uses the coordinates themselves
   constexpr int JC = 128;                   // staging capacity: 32 candidates per lane group (G <= 4)
   const DevGeom<T>& g = A.g;
+  const int op = OPC ? OPC : A.op;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const unsigned FULL = 0xffffffffu;
@@ -656,15 +658,15 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
               }
             } else if constexpr (OPK == OPK_SCALAR) {
               if (hit) {
-                if (A.op == 2) {
+                if (op == 2) {
                   c_acc++;
                 } else if (sure) {
                   float uu, gg;
-                  pair_value<float, T>(A, A.op, d2f, idx_i, idx_j, uu, gg);
+                  pair_value<float, T>(A, op, d2f, idx_i, idx_j, uu, gg);
                   e_part += (FA)uu;
                 } else {
                   V uu, gg;
-                  pair_value<V, T>(A, A.op, (V)d2, idx_i, idx_j, uu, gg);
+                  pair_value<V, T>(A, op, (V)d2, idx_i, idx_j, uu, gg);
                   e_part += (FA)uu;
                 }
               }
@@ -675,14 +677,14 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                 FA dv[3] = {0, 0, 0};
                 if (sure) {
                   float uf, gf;
-                  pair_value<float, T>(A, A.op, d2f, idx_i, idx_j, uf, gf);
+                  pair_value<float, T>(A, op, d2f, idx_i, idx_j, uf, gf);
                   uu = (FA)uf;
                   gg = (FA)gf;
 #pragma unroll
                   for (int d = 0; d < N; d++) dv[d] = (FA)dvf[d];
                 } else {
                   V uv, gv;
-                  pair_value<V, T>(A, A.op, (V)d2, idx_i, idx_j, uv, gv);
+                  pair_value<V, T>(A, op, (V)d2, idx_i, idx_j, uv, gv);
                   uu = (FA)uv;
                   gg = (FA)gv;
 #pragma unroll
@@ -1028,9 +1030,9 @@ template <class K> int resident_grid(K kernel, int want, size_t dyn = 0) {
   return std::max(1, std::min(want, per_sm * sms));
 }
 
-template <class T, int N, int OPK, bool SPLIT, bool CROSS, bool BATCH = false>
+template <class T, int N, int OPK, bool SPLIT, bool CROSS, bool BATCH = false, int OPC = 0>
 cudaError_t launch_k(int& grid, cudaStream_t st, const PairArgs<T>& A) {
-  auto k = k_pairs<T, N, OPK, SPLIT, CROSS, BATCH>;
+  auto k = k_pairs<T, N, OPK, SPLIT, CROSS, BATCH, OPC>;
   using FA = typename std::conditional<std::is_same<T, double>::value && !SPLIT, double, float>::type;
   size_t dyn = 0;
   if (OPK == OPK_HIST) {
@@ -1048,11 +1050,13 @@ cudaError_t launch_s(int opk, int& grid, cudaStream_t st, const PairArgs<T>& A) 
   switch (opk) {
     case OPK_NL: return launch_k<T, N, OPK_NL, SPLIT, CROSS>(grid, st, A);
     case OPK_SCALAR: return launch_k<T, N, OPK_SCALAR, SPLIT, CROSS>(grid, st, A);
-    case OPK_FORCES: return launch_k<T, N, OPK_FORCES, SPLIT, CROSS>(grid, st, A);
+    case OPK_FORCES:
+      if (A.op == 9) return launch_k<T, N, OPK_FORCES, SPLIT, CROSS, false, 9>(grid, st, A);  // LJ forces
+      return launch_k<T, N, OPK_FORCES, SPLIT, CROSS>(grid, st, A);
     case OPK_MIN: return launch_k<T, N, OPK_MIN, SPLIT, CROSS>(grid, st, A);
     case OPK_HIST: return launch_k<T, N, OPK_HIST, SPLIT, CROSS>(grid, st, A);
     case OPK_ADJ:
-      if constexpr (!CROSS) return launch_k<T, N, OPK_ADJ, SPLIT, false>(grid, st, A);
+      if constexpr (!CROSS) return launch_k<T, N, OPK_ADJ, SPLIT, false, false, 13>(grid, st, A);
       return cudaErrorInvalidValue;
   }
   return cudaErrorInvalidValue;
