@@ -507,7 +507,7 @@ def main():
         torch.cuda.synchronize()
         l0 = C.c_int64()
         L.clm_stats(h, C.byref(l0))
-        tot_ms, kern_ms = 0.0, []
+        tot_ms, kern_ms, bld_ms = 0.0, [], []
         for _ in range(args.steps):
             with torch.cuda.stream(stream):
                 flush.add_(1.0)  # evict L2 between timed steps (outside the events)
@@ -521,7 +521,9 @@ def main():
             bm, mm = C.c_float(), C.c_float()
             L.clm_last_timings(h, C.byref(bm), C.byref(mm))
             kern_ms.append(mm.value)
+            bld_ms.append(bm.value)
         torch.cuda.synchronize()
+        timed.build_ms = statistics.median(bld_ms)
         l1 = C.c_int64()
         L.clm_stats(h, C.byref(l1))
         tot_ms = max_over_ranks(tot_ms, world, dev)
@@ -530,6 +532,7 @@ def main():
     clocks = ClockSampler(local)
     clocks.start()
     t_exact, k_exact, launches = timed(A.CLM_PREC_EXACT)
+    build_ms = timed.build_ms
     clk = clocks.stop()
     t_split, k_split, _ = timed(A.CLM_PREC_SPLIT)
     value = pairs * args.steps * world / (t_exact * 1e-3)
@@ -566,6 +569,22 @@ def main():
     peaks.clm_peak_fp32_gflops.argtypes = [C.c_int]
     fp32_peak = peaks.clm_peak_fp32_gflops(1 << 16) / 1e3  # TFLOP/s
     achieved = pairs * fpp / (k_exact * 1e-3) / 1e12
+    # binning roofline (HBM): algorithmic bytes = 3s read + g (3s + 4) written per particle + ~12 B per cell
+    info = [C.c_int64() for _ in range(4)]
+    L.clm_get_celllist_info(h, 0, *[C.byref(v) for v in info])
+    ncs = np.zeros(3, np.int64)
+    L.clm_get_box(h, ncs.ctypes.data, None, None, None, None, None, None, None)
+    copies, ncells = info[1].value, int(np.prod(ncs))
+    build_bytes = n * 3 * 4 + copies * (3 * 4 + 4) + 12 * ncells
+    hbm_peak = None
+    mpj = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(mpj):
+        hbm_peak = json.load(open(mpj)).get("hbm_gbs")
+    build_gbs = build_bytes / (build_ms * 1e-3) / 1e9 if build_ms > 0 else None
+    build_roof = {"bound": "hbm", "achieved": build_gbs, "peak": hbm_peak, "unit": "GB/s",
+                  "frac": (build_gbs / hbm_peak) if (build_gbs and hbm_peak) else None,
+                  "bytes_per_build": build_bytes, "copies": copies, "cells": ncells, "build_ms": build_ms,
+                  "note": "cell-list build (K1-K4, sort, scans) as a whole; launch- and latency-bound at this size"}
     traffic = None
     tj = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tj):
@@ -612,6 +631,7 @@ def main():
                      "frac": achieved / fp32_peak if fp32_peak > 0 else None, "traffic": traffic,
                      "kernel": "k_pairs<float,3,FORCES,exact>", "flops_per_pair": fpp, "candidates_per_hit": R,
                      "peak_source": "measured FP32 FMA throughput (libclm_peaks.so, same run)"},
+        "build_roofline": build_roof,
         "cpu_baseline": cpu,
         "clocks": clk,
         "gpu_launches": launches,

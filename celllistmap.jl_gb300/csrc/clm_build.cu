@@ -329,6 +329,15 @@ __device__ __forceinline__ void origin_ff(float cb_hi, float cb_lo, float cs_hi,
   lo = se + pe + cb_lo;
 }
 
+// cell_start from the keys sorted by cell: copy t writes the starts of the cells between the previous
+// copy's cell (exclusive) and its own (inclusive); t = n closes the list up to ncells.
+__device__ __forceinline__ void cell_starts_at(const uint32_t* __restrict__ skeys, int t, int n, int ncells,
+                                               int* __restrict__ cell_start) {
+  const int lo = (t == 0) ? 0 : (int)skeys[t - 1] + 1;
+  const int hi = (t == n) ? ncells : (int)skeys[t];
+  for (int c = lo; c <= hi && c <= ncells; c++) cell_start[c] = t;
+}
+
 // Copy t of the sorted list: particle p, image k, in the cell `li` (local index of its system).
 template <class T, int N>
 __device__ __forceinline__ void gather_at(const DevGeom<T>& g, const T* __restrict__ wrapped, int t, int p, int k,
@@ -371,9 +380,12 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom<T> g, const T* __rest
                                                    int cap, int n, T* __restrict__ px, T* __restrict__ py,
                                                    T* __restrict__ pz, float4* __restrict__ off, float4* __restrict__ xq,
                                                    int* __restrict__ code, int* __restrict__ cell_flags,
-                                                   int* __restrict__ err) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= min(*n_dev, cap)) return;
+                                                   int ncells, int* __restrict__ cell_start, int* __restrict__ err) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nc = min(*n_dev, cap);
+  if (t > nc) return;
+  cell_starts_at(skeys, t, nc, ncells, cell_start);
+  if (t == nc) return;
   uint32_t v = svals[t];
   int p = (int)(v >> 5);
   int k = (int)(v & 31u);
@@ -395,9 +407,13 @@ __global__ void __launch_bounds__(kBlock) k_gather_b(const DevGeom<T>* __restric
                                                      int cap, int n, T* __restrict__ px, T* __restrict__ py,
                                                      T* __restrict__ pz, float4* __restrict__ off,
                                                      float4* __restrict__ xq, int* __restrict__ code,
-                                                     int* __restrict__ cell_flags, int* __restrict__ err) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= min(*n_dev, cap)) return;
+                                                     int* __restrict__ cell_flags, int ncells,
+                                                     int* __restrict__ cell_start, int* __restrict__ err) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nc = min(*n_dev, cap);
+  if (t > nc) return;
+  cell_starts_at(skeys, t, nc, ncells, cell_start);
+  if (t == nc) return;
   uint32_t v = svals[t];
   int p = (int)(v >> 5);
   int k = (int)(v & 31u);
@@ -414,18 +430,6 @@ __global__ void __launch_bounds__(kBlock) k_gather_b(const DevGeom<T>* __restric
     li = 0;
   }
   gather_at<T, N>(g, wrapped, t, p, k, li, px, py, pz, off, xq, code, cell_flags, cbase[s]);
-}
-
-// cell_start from the keys sorted by cell: the thread of copy t writes the starts of the cells between
-// the previous copy's cell (exclusive) and its own (inclusive); the thread t = n closes the list.
-__global__ void __launch_bounds__(kBlock) k_cell_start(const uint32_t* __restrict__ skeys, const int* __restrict__ n_dev,
-                                                       int cap, int ncells, int* __restrict__ cell_start) {
-  const int n = min(*n_dev, cap);
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t > n) return;
-  const int lo = (t == 0) ? 0 : (int)skeys[t - 1] + 1;
-  const int hi = (t == n) ? ncells : (int)skeys[t];
-  for (int c = lo; c <= hi && c <= ncells; c++) cell_start[c] = t;
 }
 
 __global__ void k_compact(const int* __restrict__ flags, const int* __restrict__ scanned, int ncells,
@@ -740,30 +744,29 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
     h.launches++;
     cur = 1 - cur;
   }
-  // cell offsets
-  k_cell_start<<<grid_for(cap + 1), kBlock, 0, h.stream>>>(S.keys[cur].as<uint32_t>(), n_dev, (int)cap, (int)ncells,
-                                                          S.cell_start.as<int>());
-  CLM_CUDA_TRY(h, cudaGetLastError());
-  h.launches++;
-  // gather coordinates in cell order
-  const int gc = grid_for(cap);
+  // gather coordinates in cell order; cell offsets from the sorted keys
+  const int gc = grid_for(cap + 1);  // copies, plus one thread that closes cell_start
   if (batch) {
     if (N == 3)
       k_gather_b<T, 3><<<gc, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
                                                    S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
-                                                   S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), S.cell_flags.as<int>(), err);
+                                                   S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), S.cell_flags.as<int>(), (int)ncells,
+                                                   S.cell_start.as<int>(), err);
     else
       k_gather_b<T, 2><<<gc, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
                                                    S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
-                                                   S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), S.cell_flags.as<int>(), err);
+                                                   S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), S.cell_flags.as<int>(), (int)ncells,
+                                                   S.cell_start.as<int>(), err);
   } else if (N == 3)
     k_gather<T, 3><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
                                                S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
-                                               S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), S.cell_flags.as<int>(), err);
+                                               S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), S.cell_flags.as<int>(), (int)ncells,
+                                                   S.cell_start.as<int>(), err);
   else
     k_gather<T, 2><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
                                                S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
-                                               S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), S.cell_flags.as<int>(), err);
+                                               S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), S.cell_flags.as<int>(), (int)ncells,
+                                                   S.cell_start.as<int>(), err);
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
   // cells with real particles, in linear order; their number stays on the device (real_scan[ncells])

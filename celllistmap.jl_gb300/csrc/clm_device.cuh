@@ -107,8 +107,10 @@ __device__ __forceinline__ int cell_of(const DevGeom<T>& g, const T* x, bool rea
 #pragma unroll
   for (int i = N - 1; i >= 0; i--) {
     T q = xdiv(xsub(x[i], g.cbmin[i]), g.cs[i]);
-    double fq = floor((double)q);
-    if (!(fq >= -1.0 && fq < (double)g.nc[i])) return -1;
+    // floor in the handle dtype (exact; cell indices are far below 2^24), which keeps Float32 builds off
+    // GB300's slow FP64 pipe
+    const T fq = floor(q);
+    if (!(fq >= T(-1) && fq < (T)g.nc[i])) return -1;
     int c = (int)fq + 1;
     if (real) {
       if (c == g.lcell) c += 1;
