@@ -96,33 +96,39 @@ constexpr int RS_IPT = 8;
 constexpr int RS_TILE = kBlock * RS_IPT;  // 2048 keys per tile
 constexpr int RS_WARPS = kBlock / 32;
 
+// B-bit digits (8..10): the host picks the fewest passes that cover the cell index and the smallest
+// digit that does it.
+template <int B>
 __global__ void __launch_bounds__(kBlock) k_rs_hist(const uint32_t* __restrict__ keys, const int* __restrict__ n_dev,
                                                     int cap, int shift, int* __restrict__ hist, int ntiles) {
-  __shared__ int h[256];
+  constexpr int D = 1 << B;
+  __shared__ int h[D];
   const int n = min(*n_dev, cap);
-  h[threadIdx.x] = 0;
+  for (int d = threadIdx.x; d < D; d += kBlock) h[d] = 0;
   __syncthreads();
   const int64_t base = (int64_t)blockIdx.x * RS_TILE;
 #pragma unroll
   for (int k = 0; k < RS_IPT; k++) {
     int64_t idx = base + (int64_t)k * kBlock + threadIdx.x;
-    if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1);
+    if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & (uint32_t)(D - 1)], 1);
   }
   __syncthreads();
-  hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+  for (int d = threadIdx.x; d < D; d += kBlock) hist[(int64_t)d * ntiles + blockIdx.x] = h[d];
 }
 
 // Stable scatter: items of a tile are ranked in tile order (warp, then item
 // slot, then lane) with warp-level match_any, then placed at the scanned
 // digit offset of the tile.
+template <int B>
 __global__ void __launch_bounds__(kBlock) k_rs_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                        uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                                        const int* __restrict__ n_dev, int cap, int shift,
                                                        const int* __restrict__ offs, int ntiles) {
-  __shared__ int wcnt[RS_WARPS][257];
+  constexpr int D = 1 << B;
+  __shared__ int wcnt[RS_WARPS][D + 1];
   const int n = min(*n_dev, cap);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int d = threadIdx.x; d < RS_WARPS * 257; d += kBlock) (&wcnt[0][0])[d] = 0;
+  for (int d = threadIdx.x; d < RS_WARPS * (D + 1); d += kBlock) (&wcnt[0][0])[d] = 0;
   __syncthreads();
   const int64_t wbase = (int64_t)blockIdx.x * RS_TILE + (int64_t)warp * (32 * RS_IPT);
   uint32_t kk[RS_IPT], vv[RS_IPT];
@@ -134,7 +140,7 @@ __global__ void __launch_bounds__(kBlock) k_rs_scatter(const uint32_t* __restric
     bool valid = idx < n;
     kk[k] = valid ? kin[idx] : 0u;
     vv[k] = valid ? vin[idx] : 0u;
-    int d = valid ? (int)((kk[k] >> shift) & 255u) : 256;
+    int d = valid ? (int)((kk[k] >> shift) & (uint32_t)(D - 1)) : D;
     dig[k] = d;
     unsigned peers = __match_any_sync(0xffffffffu, d);
     int leader = __ffs(peers) - 1;
@@ -145,8 +151,7 @@ __global__ void __launch_bounds__(kBlock) k_rs_scatter(const uint32_t* __restric
     rank[k] = cur + __popc(peers & lt);
   }
   __syncthreads();
-  {
-    int d = threadIdx.x;  // one digit per thread (kBlock == 256)
+  for (int d = threadIdx.x; d < D; d += kBlock) {
     int run = offs[(int64_t)d * ntiles + blockIdx.x];
 #pragma unroll
     for (int w = 0; w < RS_WARPS; w++) {
@@ -158,7 +163,7 @@ __global__ void __launch_bounds__(kBlock) k_rs_scatter(const uint32_t* __restric
   __syncthreads();
 #pragma unroll
   for (int k = 0; k < RS_IPT; k++) {
-    if (dig[k] < 256) {
+    if (dig[k] < D) {
       int pos = wcnt[warp][dig[k]] + rank[k];
       if (pos >= 0 && pos < n) {
         kout[pos] = kk[k];
@@ -678,7 +683,7 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
       !S.vals[1].reserve(sizeof(uint32_t) * cap) || !S.px.reserve(sizeof(T) * cap) || !S.py.reserve(sizeof(T) * cap) ||
       !S.pz.reserve(sizeof(T) * cap) || !S.off.reserve(sizeof(float4) * cap) || !S.code.reserve(sizeof(int) * cap) ||
       !S.xq.reserve(std::is_same<T, float>::value ? sizeof(float4) * cap : 16) ||
-      !S.rs_hist.reserve(sizeof(int) * (256 * (int64_t)ntiles + 1)))
+      !S.rs_hist.reserve(sizeof(int) * (1024 * (int64_t)ntiles + 1)))
     return ERR_NOMEM;
   const int gn = grid_for(n);
   const DevGeom<T>* gtab = h.batch.gtab.as<DevGeom<T>>();
@@ -723,23 +728,25 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
                                              S.vals[0].as<uint32_t>(), err);
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
-  // stable LSD radix sort by cell
+  // stable LSD radix sort by cell: the fewest passes of at most 10-bit digits, digits as small as that allows
   int bits = 1;
   while (((int64_t)1 << bits) < ncells) bits++;
-  const int passes = (bits + 7) / 8;
+  const int passes = (bits + 9) / 10;
+  const int dbits = std::max(8, (bits + passes - 1) / passes);
   int cur = 0;
   for (int pss = 0; pss < passes; pss++) {
-    int shift = 8 * pss;
-    k_rs_hist<<<ntiles, kBlock, 0, h.stream>>>(S.keys[cur].as<uint32_t>(), n_dev, (int)cap, shift, S.rs_hist.as<int>(),
-                                               ntiles);
+    const int shift = dbits * pss;
+    const int64_t hn = ((int64_t)1 << dbits) * ntiles;
+    auto hist = (dbits == 8) ? k_rs_hist<8> : (dbits == 9) ? k_rs_hist<9> : k_rs_hist<10>;
+    hist<<<ntiles, kBlock, 0, h.stream>>>(S.keys[cur].as<uint32_t>(), n_dev, (int)cap, shift, S.rs_hist.as<int>(), ntiles);
     CLM_CUDA_TRY(h, cudaGetLastError());
     h.launches++;
-    st = scan_exclusive(h, S.rs_hist.as<int>(), S.rs_hist.as<int>(), 256 * (int64_t)ntiles,
-                        S.rs_hist.as<int>() + 256 * (int64_t)ntiles);
+    st = scan_exclusive(h, S.rs_hist.as<int>(), S.rs_hist.as<int>(), hn, S.rs_hist.as<int>() + hn);
     if (st) return st;
-    k_rs_scatter<<<ntiles, kBlock, 0, h.stream>>>(S.keys[cur].as<uint32_t>(), S.vals[cur].as<uint32_t>(),
-                                                  S.keys[1 - cur].as<uint32_t>(), S.vals[1 - cur].as<uint32_t>(), n_dev,
-                                                  (int)cap, shift, S.rs_hist.as<int>(), ntiles);
+    auto scat = (dbits == 8) ? k_rs_scatter<8> : (dbits == 9) ? k_rs_scatter<9> : k_rs_scatter<10>;
+    scat<<<ntiles, kBlock, 0, h.stream>>>(S.keys[cur].as<uint32_t>(), S.vals[cur].as<uint32_t>(),
+                                          S.keys[1 - cur].as<uint32_t>(), S.vals[1 - cur].as<uint32_t>(), n_dev, (int)cap,
+                                          shift, S.rs_hist.as<int>(), ntiles);
     CLM_CUDA_TRY(h, cudaGetLastError());
     h.launches++;
     cur = 1 - cur;
