@@ -379,6 +379,7 @@ template <class T> int batch_run(Handle& h, int nops, const int* ops, const clm_
   const int64_t l0 = h.launches;
   // key of a recorded step: operators, parameters, sizes
   std::vector<double> key;
+  key.push_back((double)h.precision);  // a recording is only valid for the precision form it ran with
   for (int k = 0; k < nops; k++)
     for (int q = 0; q < 4; q++) key.push_back(P ? P[k].p[q] : 0.0);
   const bool same_ops = B.gexec && B.graph_ops == std::vector<int>(ops, ops + nops) && B.graph_params == key &&

@@ -551,6 +551,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
             float dvf[3] = {0.f, 0.f, 0.f};
             T d2 = 0;
             T xj[3] = {0, 0, 0};
+            T dxs[3] = {0, 0, 0};  // x_i - x_j of the exact re-test, reused by the force epilogues
             int tjj = 0;  // the candidate's position in the cell list (coordinates read only when needed)
             auto load_xj = [&]() {
               if constexpr (!ABS_PF) {
@@ -604,13 +605,11 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                 }
                 if (!sure) {
                   load_xj();
-                  T dx = xsub(xi[0], xj[0]);
-                  d2 = xmul(dx, dx);
 #pragma unroll
-                  for (int d = 1; d < N; d++) {
-                    T dd = xsub(xi[d], xj[d]);
-                    d2 = xadd(d2, xmul(dd, dd));
-                  }
+                  for (int d = 0; d < N; d++) dxs[d] = xsub(xi[d], xj[d]);
+                  d2 = xmul(dxs[0], dxs[0]);
+#pragma unroll
+                  for (int d = 1; d < N; d++) d2 = xadd(d2, xmul(dxs[d], dxs[d]));
                   hit = d2 <= g.cutoff_sqr;
                   if (hit && d2 > band) {
                     if (!same) {
@@ -688,7 +687,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                   uu = (FA)uv;
                   gg = (FA)gv;
 #pragma unroll
-                  for (int d = 0; d < N; d++) dv[d] = (FA)xsub(xi[d], xj[d]);
+                  for (int d = 0; d < N; d++) dv[d] = (FA)dxs[d];
                 }
 #pragma unroll
                 for (int d = 0; d < N; d++) df[d] = gg * dv[d];
@@ -782,13 +781,16 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                   if constexpr (!std::is_same<FA, float>::value) r = (T)rf;
                 }
                 if (exact_r) {
-                  if (sure) load_xj();  // near a bin edge: the exact distance decides
-                  T dx = xsub(xi[0], xj[0]);
-                  T e2 = xmul(dx, dx);
+                  T e2 = d2;  // the exact re-test's d2 (not sure), or recomputed near a bin edge
+                  if (sure) {
+                    load_xj();
+                    T dx = xsub(xi[0], xj[0]);
+                    e2 = xmul(dx, dx);
 #pragma unroll
-                  for (int d = 1; d < N; d++) {
-                    T dd = xsub(xi[d], xj[d]);
-                    e2 = xadd(e2, xmul(dd, dd));
+                    for (int d = 1; d < N; d++) {
+                      T dd = xsub(xi[d], xj[d]);
+                      e2 = xadd(e2, xmul(dd, dd));
+                    }
                   }
                   r = xsqrt(e2);
                   rfl = (float)r;
@@ -807,7 +809,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                     for (int d = 0; d < N; d++) dv[d] = (FA)dvf[d];
                   } else {
 #pragma unroll
-                    for (int d = 0; d < N; d++) dv[d] = (FA)xsub(xi[d], xj[d]);
+                    for (int d = 0; d < N; d++) dv[d] = (FA)dxs[d];
                   }
                   if (tri) {
                     FA rv[3];

@@ -211,3 +211,17 @@ def test_batch_2d(orc, clm):
         np.testing.assert_array_equal(A[2], B[2])
         er = orc.run("soft_energy", x, dim=2, kind="ortho", unitcell=L, cutoff=RC, params=[RC])["scalar"]
         assert abs(e[s] - er) <= 1e-12 * max(1.0, abs(er)) * 10
+
+
+def test_batch_graph_follows_precision(orc, clm):
+    pos, cells = make_batch(nsys=8, seed=14)
+    bs = clm.BatchedSystems(positions=pos, unitcells=cells, cutoff=RC, graph=True)
+    exact = [bs.run(clm.SoftEnergy())[0] for _ in range(2)][-1]  # recorded and replayed
+    bs.set_precision("split")
+    split = bs.run(clm.SoftEnergy())[0]
+    bs.set_precision("exact")
+    again = bs.run(clm.SoftEnergy())[0]
+    np.testing.assert_array_equal(exact, again)
+    ok = ~np.isnan(exact)
+    assert np.any(split[ok] != exact[ok])  # the split form ran (FP32 pair values differ in the last bits)
+    np.testing.assert_allclose(split[ok], exact[ok], rtol=1e-5)
