@@ -252,11 +252,13 @@ __device__ __forceinline__ const DevGeom<T>& geo_of(const PairArgs<T>& A, int li
 // particle owns its force ("owner computes": full stencil, no atomics on the partner) and the energy is
 // counted only on the side from which the reference visits the pair.
 //
-// Each warp takes one cell; the cells of its stencil are concatenated into one candidate stream,
-// staged 64 at a time.  Phase A: every lane tests its particle against its share of the staged
-// candidates with an FP32 distance (FMA) and records the candidates inside cutoff^2 (1 + 2^-13) in a
-// bit mask.  Phase B: the lanes walk their masks, apply the reference's pair rules, re-test in the input
-// dtype where needed, and run the operator epilogue.  The projection filter of the reference is
+// Each warp takes one cell (or one part of a crowded cell); the cells of its stencil are concatenated
+// into one candidate stream, staged 32*G candidates per round into shared memory with asynchronous
+// 16-byte copies (the next round is copied while the current one is tested).  Phase A: every lane tests
+// its particle against 32 staged candidates with an FP32 distance (FMA) and records the candidates inside
+// cutoff^2 (1 + 2^-13) in a bit mask.  Phase B: the set bits of all lanes are compacted into a queue that
+// all lanes work through: the reference's pair rules, the re-test in the input dtype where needed, and
+// the operator epilogue.  The projection filter of the reference is
 // evaluated only for pairs with d2 > cutoff^2 (1 - 2^-13): any pair further inside passes it (the
 // projection of the separation on a unit vector cannot exceed the separation, and the margin covers the
 // half cell), so skipping it elsewhere leaves the pair set unchanged.
