@@ -16,6 +16,7 @@ from .api import (ArgumentError, BatchedSystems, Box, CUDAError, DimensionMismat
 from . import api as ops  # operator classes live in api; exposed as `ops`
 from . import workloads
 from . import trajectory
+from . import autograd
 
 Count = _api.Count
 SumD2 = _api.SumD2

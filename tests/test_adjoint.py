@@ -203,3 +203,40 @@ def test_gpu_adjoint_2d(orc, clm, dtype):
     assert abs(got.energy - ref["scalar"]) <= tol * np.abs(u).sum()
     assert np.abs(got.virial - ref["virial"]).max() <= tol * gw.sum()
     assert np.abs(np.asarray(got.forces, np.float64) - ref["forces_x"]).max() <= tol * np.abs(ref["forces_x"]).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["ortho", "tri"])
+def test_autograd_lj_energy(orc, clm, kind):
+    """torch autograd through the adjoint: gradients equal the oracle's adjoint (the counterpart of the
+    ChainRulesCore rrule written out for the Julia extension)."""
+    torch = pytest.importorskip("torch")
+    import importlib
+    ag = importlib.import_module(clm.__name__ + ".autograd")
+    x, L, t, eps, sig = mixture(clm, n=4000)
+    M = np.diag([L] * 3) if kind == "ortho" else tri_cell(L)
+    if kind == "tri":
+        x = x / L @ M.T
+    xt = torch.tensor(x, requires_grad=True)
+    cell = torch.tensor(np.diag(M) if kind == "ortho" else M, requires_grad=True)
+    et = torch.tensor(eps, requires_grad=True)
+    st = torch.tensor(sig, requires_grad=True)
+    U = ag.lj_energy(xt, cell, et, st, torch.tensor(t), CUT, C12, C6)
+    U.backward()
+    ref = orc_adj(orc, x, M, t, eps, sig, kind=kind)
+    p = pair_terms(orc, x, M, t, eps, sig, kind)
+    tol = 1e-12
+    assert abs(U.item() - ref["scalar"]) <= tol * np.abs(p["u"]).sum()
+    assert np.abs(xt.grad.numpy() + ref["forces_x"]).max() <= tol * np.abs(ref["forces_x"]).max()
+    dM = ref["virial"] @ np.linalg.inv(M).T
+    gcell = cell.grad.numpy()
+    want = np.diag(dM) if kind == "ortho" else dM
+    wscale = np.abs(p["g"] * (p["dx"] ** 2).sum(1)).sum() * np.abs(np.linalg.inv(M)).sum()
+    assert np.abs(gcell - want).max() <= tol * wscale
+    for a in range(2):
+        for b in range(2):
+            k = cls_index(a, b)
+            f = 1.0 if a == b else 0.5
+            m = p["cls"] == k
+            assert abs(et.grad[a, b].item() - f * ref["deps"][k]) <= tol * np.abs(p["u_over_eps"][m]).sum()
+            assert abs(st.grad[a, b].item() - f * ref["dsig"][k]) <= tol * np.abs(p["du_dsig"][m]).sum()
