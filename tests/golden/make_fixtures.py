@@ -11,9 +11,14 @@ It reads
   * test/applications/namd/{o1..o6,t1,t2}.dcd: one frame each of a Neon system,
     CHARMM DCD with float32 coordinates (read by Chemfiles in
     test/applications/namd/ParticleSystem_vs_NAMD.jl:21-26);
+  * test/applications/gromacs/argon/{minimal,cubic,dodecahedron,octahedron}.xtc: the first
+    frame of each GROMACS run (read by Chemfiles in
+    test/applications/gromacs/compare_with_gromacs.jl:15-24), positions and box in Angstrom;
 and writes
   * tests/golden/argon_cubic.npy   (100 x 3 float64)
   * tests/golden/namd_frames.npz   (one (n, 3) float32 array per frame)
+  * tests/golden/gromacs_argon.npz (``<name>_x``: (n, 3) float64, ``<name>_cell``: 3 x 3 float64 with
+    the cell vectors as columns, per run)
 Only coordinates are extracted.  The expected values these fixtures are checked
 against are quoted, with their source lines, in tests/test_oracle_kat.py.
 """
@@ -46,6 +51,13 @@ def main(ref_root):
     for name in ["o1", "o2", "o3", "o4", "o5", "o6", "t1", "t2"]:
         frames[name] = read_dcd_first_frame(os.path.join(ref_root, "test", "applications", "namd", name + ".dcd"))
     np.savez_compressed(os.path.join(HERE, "namd_frames.npz"), **frames)
+    trj = _trajectory()
+    gromacs = {}
+    for name in ["minimal", "cubic", "dodecahedron", "octahedron"]:
+        frame = trj.read_xtc(os.path.join(ref_root, "test", "applications", "gromacs", "argon", name + ".xtc"))[0]
+        gromacs[name + "_x"] = frame.positions
+        gromacs[name + "_cell"] = frame.unitcell
+    np.savez_compressed(os.path.join(HERE, "gromacs_argon.npz"), **gromacs)
     print("wrote fixtures:", sorted(frames), "argon", read_pdb_coords(pdb).shape)
 
 

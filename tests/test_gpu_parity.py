@@ -168,6 +168,21 @@ def test_namd_lj_on_gpu(clm, golden_dir, name, lcell):
     s.close()
 
 
+@pytest.mark.parametrize("lcell", [1, 2, 3])
+@pytest.mark.parametrize("name", ["minimal", "cubic", "dodecahedron", "octahedron"])
+def test_gromacs_lj_on_gpu(clm, orc, golden_dir, name, lcell):
+    from tests.test_oracle_kat import GROMACS_C12, GROMACS_C6, GROMACS_CASES, gromacs_frame
+    x, kind, uc = gromacs_frame(golden_dir, name)
+    expected = dict(GROMACS_CASES)[name]
+    s = clm.ParticleSystem(xpositions=x, unitcell=uc, cutoff=8.0, lcell=lcell)
+    u = clm.pairwise(clm.LennardJones(1.0, 1.0, GROMACS_C12, GROMACS_C6), s)
+    s.close()
+    r = orc.run("lj_energy", x, kind=kind, unitcell=uc, cutoff=8.0, lcell=lcell,
+                params=[1.0, 1.0, GROMACS_C12, GROMACS_C6])
+    assert u == pytest.approx(r["scalar"], rel=1e-12)
+    assert u == pytest.approx(expected, rel=1e-5)
+
+
 @pytest.mark.parametrize("cross", [False, True])
 def test_min_distance_and_histogram(clm, orc, cross):
     x = gen(3000, 3, 20.0, 77)

@@ -103,6 +103,32 @@ def test_namd_lj_energies(orc, namd, name, uc, expected, lcell):
     assert r["scalar"] == pytest.approx(expected, rel=1e-12)
 
 
+# test/applications/gromacs/compare_with_gromacs.jl:7-11,47-60: plain cut-off LJ c12/d^12 - c6/d^6 (kJ/mol,
+# Angstrom) at rc 8 against the "LJ (SR)" energies GROMACS printed (test/applications/gromacs/argon/*.log),
+# which carry 6 significant digits; the reference's own tolerance is rtol 1e-5 for lcell 1, 2 and 3.
+GROMACS_CASES = [("minimal", -3.58447e-01), ("cubic", 1.01353e+04), ("dodecahedron", 4.62904e+05),
+                 ("octahedron", 1.82849e+04)]
+GROMACS_C12, GROMACS_C6 = 9.69576e6, 0.00622127e6
+
+
+def gromacs_frame(golden_dir, name):
+    """Positions and cell of a GROMACS argon frame; (kind, unitcell) as the pair engine takes them."""
+    f = np.load(os.path.join(golden_dir, "gromacs_argon.npz"))
+    x, cell = f[name + "_x"], f[name + "_cell"]
+    if np.count_nonzero(cell - np.diag(np.diag(cell))):
+        return x, "tri", cell
+    return x, "ortho", np.diag(cell).copy()
+
+
+@pytest.mark.parametrize("lcell", [1, 2, 3])
+@pytest.mark.parametrize("name,expected", GROMACS_CASES)
+def test_gromacs_lj_energies(orc, golden_dir, name, expected, lcell):
+    x, kind, uc = gromacs_frame(golden_dir, name)
+    r = orc.run("lj_energy", x, kind=kind, unitcell=uc, cutoff=8.0, lcell=lcell,
+                params=[1.0, 1.0, GROMACS_C12, GROMACS_C6])
+    assert r["scalar"] == pytest.approx(expected, rel=1e-5)
+
+
 def test_small_exact_cases(orc):
     # test/API/neighborlists.jl:183-193
     def nl(x, **kw):
