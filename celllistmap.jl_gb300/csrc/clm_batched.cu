@@ -20,6 +20,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "celllistmap_gb300.h"
@@ -184,6 +185,39 @@ inline unsigned long long* hres_cnt(BatchState& B, int slot) {
 inline unsigned long long* hres_nl(BatchState& B) { return (unsigned long long*)(B.hres + (size_t)kMaxOps * B.nsys * 16); }
 inline int* hres_err(BatchState& B) { return (int*)(B.hres + (size_t)kMaxOps * B.nsys * 16 + 64); }
 
+// Batch forces: sums (rotated frame of each particle's system) -> output dtype in the original frames.
+template <class T, int N, class FA>
+__global__ void k_forces_out_b(const FA* __restrict__ facc, int64_t n, const DevGeom<T>* __restrict__ gtab,
+                               const int* __restrict__ psys, T* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double f[N];
+  if constexpr (std::is_same<FA, float4>::value) {
+    const float4 v = facc[i];
+    f[0] = v.x;
+    f[1] = v.y;
+    if (N == 3) f[N - 1] = v.z;
+  } else {
+#pragma unroll
+    for (int d = 0; d < N; d++) f[d] = facc[i * N + d];
+  }
+  const DevGeom<T>& g = gtab[psys[i]];
+  if (g.kind == TRICLINIC) {
+    double r[N];
+#pragma unroll
+    for (int a = 0; a < N; a++) {
+      double s = 0;
+#pragma unroll
+      for (int k = 0; k < N; k++) s += (double)g.Rinv[a][k] * f[k];
+      r[a] = s;
+    }
+#pragma unroll
+    for (int d = 0; d < N; d++) f[d] = r[d];
+  }
+#pragma unroll
+  for (int d = 0; d < N; d++) out[i * N + d] = (T)f[d];
+}
+
 // One operator of the step, enqueued without synchronization.
 template <class T> int enqueue_op(Handle& h, int slot, int op, const clm_op_params* P) {
   BatchState& B = h.batch;
@@ -224,14 +258,16 @@ template <class T> int enqueue_op(Handle& h, int slot, int op, const clm_op_para
   double* o_e = (double*)(B.sys_out.as<char>() + (size_t)slot * nsys * 16);
   unsigned long long* o_c = (unsigned long long*)(B.sys_out.as<char>() + (size_t)slot * nsys * 16 + (size_t)nsys * 8);
   const bool forces = (opk == OPK_FORCES);
+  // force sums (rotated frames): 16-byte FP32 records, or dim doubles per particle for FP64 pair values;
+  // the systems that failed the cell check keep zero sums
+  const bool f4 = !(std::is_same<T, double>::value && !A.split);
+  const size_t acc_bytes = align((f4 ? sizeof(float4) : sizeof(double) * N) * (size_t)std::max<int64_t>(n, 1));
   if (forces) {
-    if (!h.outbuf.reserve(sizeof(double) * n * N + 256) || !B.forces.reserve(sizeof(T) * n * N + 256))
+    if (!h.outbuf.reserve(acc_bytes) || !B.forces.reserve(sizeof(T) * n * N + 256))
       return fail(&h, ERR_NOMEM, "device allocation failed (forces)");
     A.fx = h.outbuf.as<double>();
-    A.fout = B.forces.as<T>();  // owner warps write the force of every particle of a valid system
-    bool failed = false;
-    for (int st : B.status) failed = failed || st == ERR_CELL_TOO_SMALL;
-    if (failed) CLM_CUDA_TRY(h, cudaMemsetAsync(A.fout, 0, sizeof(T) * n * N, h.stream));
+    A.f4x = h.outbuf.as<float4>();
+    CLM_CUDA_TRY(h, cudaMemsetAsync(h.outbuf.p, 0, acc_bytes, h.stream));
   }
   if (opk == OPK_NL) {
     const int64_t est = (int64_t)(B.pairs_est * 1.15) + 4096;
@@ -267,6 +303,20 @@ template <class T> int enqueue_op(Handle& h, int slot, int op, const clm_op_para
     return ERR_CUDA;
   }
   h.launches++;
+  if (forces && n > 0) {
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    const DevGeom<T>* gt = B.gtab.as<DevGeom<T>>();
+    const int* ps = B.psys.as<int>();
+    if (f4) {
+      if (N == 3) k_forces_out_b<T, 3, float4><<<blocks, 256, 0, h.stream>>>(A.f4x, n, gt, ps, B.forces.as<T>());
+      else k_forces_out_b<T, 2, float4><<<blocks, 256, 0, h.stream>>>(A.f4x, n, gt, ps, B.forces.as<T>());
+    } else {
+      if (N == 3) k_forces_out_b<T, 3, double><<<blocks, 256, 0, h.stream>>>(A.fx, n, gt, ps, B.forces.as<T>());
+      else k_forces_out_b<T, 2, double><<<blocks, 256, 0, h.stream>>>(A.fx, n, gt, ps, B.forces.as<T>());
+    }
+    CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+  }
   if (opk == OPK_SCALAR || opk == OPK_FORCES || opk == OPK_NL) {
     if (nsys > 0) {
       k_seg_reduce<<<(unsigned)((nsys + 3) / 4), 128, 0, h.stream>>>(A.part_e, A.part_c, B.cell_split,

@@ -123,14 +123,22 @@ __global__ void k_reduce_hist(const unsigned long long* __restrict__ pc, const d
   os[b] = s;
 }
 
-// forces: accumulators (rotated frame, double) -> output dtype in the original frame
-template <class T, int N>
-__global__ void k_forces_out(const double* __restrict__ facc, int64_t n, DevGeom<T> g, int rotate, T* __restrict__ out) {
+// forces: sums (rotated frame; 16-byte FP32 records or FP64 components) -> output dtype in the original
+// frame
+template <class T, int N, class FA>
+__global__ void k_forces_out(const FA* __restrict__ facc, int64_t n, DevGeom<T> g, int rotate, T* __restrict__ out) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double f[N];
+  if constexpr (std::is_same<FA, float4>::value) {
+    const float4 v = facc[i];
+    f[0] = v.x;
+    f[1] = v.y;
+    if (N == 3) f[N - 1] = v.z;
+  } else {
 #pragma unroll
-  for (int d = 0; d < N; d++) f[d] = facc[i * N + d];
+    for (int d = 0; d < N; d++) f[d] = facc[i * N + d];
+  }
   if (rotate) {
     double r[N];
 #pragma unroll
@@ -345,16 +353,18 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
   // outputs
   const bool forces = (opk == OPK_FORCES || opk == OPK_ADJ);
   double* r_v = (double*)(res + 256 + 16 * 256);  // adjoint sums (kAdjVals)
-  // self forces are complete when the owner warp finishes a particle: it writes them (rotated back, in
-  // the handle dtype) straight to the output; cross forces are accumulated in FP64 and converted after
-  const bool owner = forces && h.nsets == 1;
+  // forces are summed with atomics (FP32 pair values: 16-byte records; FP64: dim doubles per particle) in
+  // the rotated frame and converted to the output after the map
+  const bool f4 = !(std::is_same<T, double>::value && !A.split);
   T* dst_x = nullptr;
   T* dst_y = nullptr;
-  const size_t acc_bytes = sizeof(double) * (nx + ny) * N;
+  const size_t acc_bytes = align((f4 ? sizeof(float4) : sizeof(double) * N) * (nx + ny));
   if (forces) {
     if (!h.outbuf.reserve(acc_bytes + sizeof(T) * (nx + ny) * N + 256)) return ERR_NOMEM;
     A.fx = h.outbuf.as<double>();
     A.fy = A.fx + nx * N;
+    A.f4x = h.outbuf.as<float4>();
+    A.f4y = A.f4x + nx;
     if (!O->out_on_device) {
       // staged after the accumulators when the caller gave host pointers
       dst_x = (T*)(h.outbuf.as<char>() + acc_bytes);
@@ -363,11 +373,7 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
       dst_x = (T*)O->forces_x;
       dst_y = (T*)O->forces_y;
     }
-    if (owner) {
-      A.fout = dst_x;
-    } else {
-      CLM_CUDA_TRY(h, cudaMemsetAsync(A.fx, 0, acc_bytes, h.stream));
-    }
+    CLM_CUDA_TRY(h, cudaMemsetAsync(h.outbuf.p, 0, acc_bytes, h.stream));
   }
   if (opk == OPK_NL) {
     double vol = std::fabs((double)g.det_in);
@@ -418,15 +424,19 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
   if (forces) {
     const int rot = (g.kind == TRICLINIC) ? 1 : 0;
     DevGeom<T>& dg = A.g;
-    h.launches += (nx && dst_x && !owner) + (ny && dst_y);
-    if (nx && dst_x && !owner) {
-      if (N == 3) k_forces_out<T, 3><<<(unsigned)((nx + 255) / 256), 256, 0, h.stream>>>(A.fx, nx, dg, rot, dst_x);
-      else k_forces_out<T, 2><<<(unsigned)((nx + 255) / 256), 256, 0, h.stream>>>(A.fx, nx, dg, rot, dst_x);
-    }
-    if (ny && dst_y) {
-      if (N == 3) k_forces_out<T, 3><<<(unsigned)((ny + 255) / 256), 256, 0, h.stream>>>(A.fx + nx * N, ny, dg, rot, dst_y);
-      else k_forces_out<T, 2><<<(unsigned)((ny + 255) / 256), 256, 0, h.stream>>>(A.fx + nx * N, ny, dg, rot, dst_y);
-    }
+    h.launches += (nx && dst_x) + (ny && dst_y);
+    auto out = [&](int64_t cnt, int64_t first, T* dst) {
+      const unsigned blocks = (unsigned)((cnt + 255) / 256);
+      if (f4) {
+        if (N == 3) k_forces_out<T, 3, float4><<<blocks, 256, 0, h.stream>>>(A.f4x + first, cnt, dg, rot, dst);
+        else k_forces_out<T, 2, float4><<<blocks, 256, 0, h.stream>>>(A.f4x + first, cnt, dg, rot, dst);
+      } else {
+        if (N == 3) k_forces_out<T, 3, double><<<blocks, 256, 0, h.stream>>>(A.fx + first * N, cnt, dg, rot, dst);
+        else k_forces_out<T, 2, double><<<blocks, 256, 0, h.stream>>>(A.fx + first * N, cnt, dg, rot, dst);
+      }
+    };
+    if (nx && dst_x) out(nx, 0, dst_x);
+    if (ny && dst_y) out(ny, nx, dst_y);
     CLM_CUDA_TRY(h, cudaGetLastError());
     if (!O->out_on_device) {
       if (O->forces_x && nx)

@@ -53,9 +53,12 @@ template <class T> struct PairArgs {
   T* nl_d;
   unsigned long long* nl_count;
   long long nl_cap;
-  T* fout;          // self forces: final output (handle dtype, original frame), or null
-  double* fx;       // forces accumulators (double), n_x * dim
-  double* fy;       // n_y * dim (cross)
+  // force sums in the rotated frame, added with atomics (f[i] -= df, f[j] += df for each visited pair):
+  // FP32 pair values into one 16-byte record per particle, FP64 pair values into n * dim doubles
+  float4* f4x;
+  float4* f4y;      // cross: set y
+  double* fx;
+  double* fy;       // cross: set y
   double* part_e;   // per-block energy
   unsigned long long* part_c;  // per-block count
   T* part_min_d2;

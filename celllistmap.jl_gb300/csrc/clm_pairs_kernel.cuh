@@ -171,11 +171,6 @@ __device__ __forceinline__ void pair_value(const PairArgs<T>& A, int op, V d2, i
   }
 }
 
-__device__ __forceinline__ bool is_forward(const int* o) {
-  // neighbor_cells_forward (src/internals/Box.jl:436-457): lexicographically positive in (x, y, z)
-  return o[0] > 0 || (o[0] == 0 && (o[1] > 0 || (o[1] == 0 && o[2] > 0)));
-}
-
 template <class T, int N>
 __device__ __forceinline__ T exact_dot_rel(const T* x, const T* c, const T* u) {
   T s = xmul(xsub(x[0], c[0]), u[0]);
@@ -248,9 +243,22 @@ __device__ __forceinline__ const DevGeom<T>& geo_of(const PairArgs<T>& A, int li
   }
 }
 
-// Pair map kernel.  CROSS: x-y pairs; otherwise self pairs.  For OPK_FORCES on a single set each real
-// particle owns its force ("owner computes": full stencil, no atomics on the partner) and the energy is
-// counted only on the side from which the reference visits the pair.
+// Adds a force term to the sums of particle `idx` (set y when `ys`): one 16-byte vector atomic for FP32
+// pair values, one FP64 atomic per component otherwise.
+template <class T, int N, class FA>
+__device__ __forceinline__ void force_add(const PairArgs<T>& A, bool ys, int idx, const FA* v) {
+  if constexpr (std::is_same<FA, float>::value) {
+    atomicAdd((ys ? A.f4y : A.f4x) + idx, make_float4(v[0], v[1], (N == 3) ? v[2] : 0.f, 0.f));
+  } else {
+    double* f = (ys ? A.fy : A.fx) + (int64_t)idx * N;
+#pragma unroll
+    for (int d = 0; d < N; d++) atomicAdd(f + d, (double)v[d]);
+  }
+}
+
+// Pair map kernel.  CROSS: x-y pairs; otherwise self pairs.  Every pair is visited once, from the side
+// the reference visits it (forward half stencil, or the full stencil with index_i < index_j for
+// triclinic cells); forces add -df to the particle's sums and +df to the partner's.
 //
 // Each warp takes one cell (or one part of a crowded cell); the cells of its stencil are concatenated
 // into one candidate stream, staged 32*G candidates per round into shared memory with asynchronous
@@ -270,7 +278,6 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
   using V = T;
   using FA = typename std::conditional<std::is_same<T, double>::value && !SPLIT, double, float>::type;
   constexpr bool IS_F = (OPK == OPK_FORCES) || (OPK == OPK_ADJ);
-  constexpr bool OWNER = IS_F && !CROSS;
   constexpr bool FP64 = std::is_same<T, double>::value;
   constexpr bool ABS_PF = !FP64 && !SPLIT;  // FP32 exact form: the prefilter uses the coordinates themselves
   constexpr int JC = 128;                   // staging capacity: 32 candidates per lane group (G <= 4)
@@ -305,10 +312,11 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
   __shared__ double s_red[kWarps];
   __shared__ unsigned long long s_redc[kWarps];
 
-  constexpr int F_SAME = 1 << 24, F_BACK = 1 << 25, F_REALCELL = 1 << 26;
+  constexpr int F_SAME = 1 << 24;
   const bool tri = (g.kind == TRICLINIC);
   const bool nonper = (g.kind == NONPERIODIC);
-  const bool full = tri || CROSS || OWNER;
+  const bool full = tri || CROSS;
+  const bool idx_rule = tri && !CROSS;  // triclinic self pairs: index_i < index_j, applied in phase A
   const int l = g.lcell;
   const int w = 2 * l + 1;
   const int wN = (N == 3) ? w * w * w : w * w;
@@ -385,7 +393,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
       }
       const bool real_i = code_i >= 0;
       const int idx_i = real_i ? code_i : -code_i - 1;
-      const bool act_i = (OWNER || tri) ? (vi && real_i) : vi;
+      const bool act_i = tri ? (vi && real_i) : vi;
       if (grp == 0) {
 #pragma unroll
         for (int d = 0; d < 3; d++) {
@@ -422,8 +430,6 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
               cnt = A.Y.cell_start[lj + 1] - start;
               meta = (o[0] + 128) | ((o[1] + 128) << 8) | ((o[2] + 128) << 16);
               if (kk == 0) meta |= F_SAME;
-              if (kk > 0 && full && !is_forward(o)) meta |= F_BACK;
-              if (OWNER && A.xflags[lj]) meta |= F_REALCELL;
             }
           }
           int incl = cnt;
@@ -487,16 +493,28 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
             __syncwarp();
           }
           if (rb + JR < total) stage(rb + JR, buf ^ 1);  // the next round's copies overlap this round
-          // ---- phase A: 32 FP32 distance tests per lane into a bit mask
+          // ---- phase A: 32 FP32 distance tests per lane into a bit mask (with the index rule of
+          // triclinic self pairs, so that the mirrored visit of a pair never enters the queue)
           unsigned mask = 0u;
           {
             const float4* pp = &s_pf[buf][warp][grp];
+            if (idx_rule) {
 #pragma unroll
-            for (int b = 0; b < 32; b++) {
-              const float4 p = pp[b * G];
-              const float dx = pi[0] - p.x, dy = pi[1] - p.y, dz = (N == 3) ? pi[2] - p.z : 0.f;
-              const float d2f = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-              mask |= (d2f <= g.thr_hi) ? (1u << b) : 0u;
+              for (int b = 0; b < 32; b++) {
+                const float4 p = pp[b * G];
+                const float dx = pi[0] - p.x, dy = pi[1] - p.y, dz = (N == 3) ? pi[2] - p.z : 0.f;
+                const float d2f = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                const int cj = __float_as_int(p.w);  // particle code: index, or -index-1 for a ghost
+                mask |= (d2f <= g.thr_hi && idx_i < (cj ^ (cj >> 31))) ? (1u << b) : 0u;
+              }
+            } else {
+#pragma unroll
+              for (int b = 0; b < 32; b++) {
+                const float4 p = pp[b * G];
+                const float dx = pi[0] - p.x, dy = pi[1] - p.y, dz = (N == 3) ? pi[2] - p.z : 0.f;
+                const float d2f = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                mask |= (d2f <= g.thr_hi) ? (1u << b) : 0u;
+              }
             }
           }
           if (!act_i) mask = 0u;
@@ -547,7 +565,6 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
             const int idx_i = real_i ? code_i : -code_i - 1;
             const int ii = ib + ie;
             bool hit = false, sure = false;
-            bool count_e = true;
             int idx_j = 0;
             float d2f = 0.f;
             float dvf[3] = {0.f, 0.f, 0.f};
@@ -571,17 +588,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
               const bool same = (meta & F_SAME) != 0;
               const int slot_j = rb + j;  // position inside the cell when same
               bool cand = true;
-              bool other_side = false;
-              if (OWNER) {
-                cand = idx_j != idx_i;
-                if (tri) count_e = idx_i < idx_j;
-                else if (same) count_e = nonper ? (slot_j > ii) : (!real_j || slot_j > ii);
-                else if (!(meta & F_BACK)) count_e = true;
-                else {
-                  count_e = !nonper && !real_j && (meta & F_REALCELL);
-                  other_side = count_e;
-                }
-              } else if (!CROSS) {
+              if (!CROSS) {
                 if (tri) cand = idx_i < idx_j;
                 else if (same) cand = (slot_j > ii) && (nonper || real_i || real_j);
                 else cand = nonper || real_i || real_j;
@@ -620,7 +627,6 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                       T ctr_j[3];
                       cell_center<T, N>(gc, cj, ctr_j);
                       hit = projection_pass<T, N>(gc, ctr_i, ctr_j, xi, xj);
-                      if (hit && other_side) count_e = projection_pass<T, N>(gc, ctr_j, ctr_i, xj, xi);
                     }
                   }
                 }
@@ -694,7 +700,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
 #pragma unroll
                 for (int d = 0; d < N; d++) df[d] = gg * dv[d];
                 if constexpr (OPK == OPK_ADJ) {
-                  if (count_e) {
+                  {
                     // virial W += g dx dx^T (g = u'(r)/r), and the parameter derivatives of the LJ term
                     adj[0] += gg * dv[0] * dv[0];
                     adj[1] += gg * dv[1] * dv[1];
@@ -735,11 +741,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                 }
 #pragma unroll
                 for (int d = 0; d < N; d++) acc[d] -= df[d];
-                if (!OWNER || count_e) e_part += uu;
-                if (CROSS) {
-#pragma unroll
-                  for (int d = 0; d < N; d++) atomicAdd(&A.fy[(int64_t)idx_j * N + d], (double)df[d]);
-                }
+                e_part += uu;
+                force_add<T, N, FA>(A, CROSS, idx_j, df);  // the partner's share
               }
             } else if constexpr (OPK == OPK_MIN) {
               if (hit) {
@@ -885,28 +888,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
         FA f[3];
 #pragma unroll
         for (int d = 0; d < 3; d++) f[d] = s_if[warp][d][il];
-        if (grp == 0 && vi) {
-          if (OWNER) {
-            if (act_i && A.fout) {
-              // the particle's force is complete: back to the original frame, in the handle dtype
-              FA o[3] = {f[0], f[1], f[2]};
-              if (tri) {
-#pragma unroll
-                for (int a = 0; a < N; a++) {
-                  FA sacc = 0;
-#pragma unroll
-                  for (int k = 0; k < N; k++) sacc += (FA)gc.Rinv[a][k] * f[k];
-                  o[a] = sacc;
-                }
-              }
-#pragma unroll
-              for (int d = 0; d < N; d++) A.fout[(int64_t)idx_i * N + d] = (T)o[d];
-            }
-          } else if (f[0] != FA(0) || f[1] != FA(0) || f[2] != FA(0)) {
-#pragma unroll
-            for (int d = 0; d < N; d++) atomicAdd(&A.fx[(int64_t)idx_i * N + d], (double)f[d]);
-          }
-        }
+        if (grp == 0 && vi && (f[0] != FA(0) || f[1] != FA(0) || f[2] != FA(0)))
+          force_add<T, N, FA>(A, false, idx_i, f);
         __syncwarp();
       }
     }
