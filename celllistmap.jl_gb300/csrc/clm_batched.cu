@@ -191,7 +191,9 @@ __global__ void k_forces_out_b(const FA* __restrict__ facc, int64_t n, const Dev
                                const int* __restrict__ psys, T* __restrict__ out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double f[N];
+  // FP32 sums are rotated in FP32 (the FP64 pipe is slow on this part); FP64 sums in FP64
+  using R = typename std::conditional<std::is_same<FA, float4>::value, float, double>::type;
+  R f[N];
   if constexpr (std::is_same<FA, float4>::value) {
     const float4 v = facc[i];
     f[0] = v.x;
@@ -203,12 +205,12 @@ __global__ void k_forces_out_b(const FA* __restrict__ facc, int64_t n, const Dev
   }
   const DevGeom<T>& g = gtab[psys[i]];
   if (g.kind == TRICLINIC) {
-    double r[N];
+    R r[N];
 #pragma unroll
     for (int a = 0; a < N; a++) {
-      double s = 0;
+      R s = 0;
 #pragma unroll
-      for (int k = 0; k < N; k++) s += (double)g.Rinv[a][k] * f[k];
+      for (int k = 0; k < N; k++) s += (R)g.Rinv[a][k] * f[k];
       r[a] = s;
     }
 #pragma unroll
@@ -243,8 +245,12 @@ template <class T> int enqueue_op(Handle& h, int slot, int op, const clm_op_para
   A.gtab = B.gtab.as<DevGeom<T>>();
   A.cell_sys = B.cell_sys.as<int>();
   A.cbase = B.cbase_d.as<int>();
-  for (int k = 0; k < 4; k++) A.p[k] = P ? P->p[k] : 0.0;
-  if ((op == CLM_OP_SOFT_ENERGY || op == CLM_OP_SOFT_FORCES) && A.p[0] == 0.0) A.p[0] = B.cutoff;
+  {
+    double pp[4] = {0, 0, 0, 0};
+    for (int k = 0; k < 4; k++) pp[k] = P ? P->p[k] : 0.0;
+    if ((op == CLM_OP_SOFT_ENERGY || op == CLM_OP_SOFT_FORCES) && pp[0] == 0.0) pp[0] = B.cutoff;
+    set_params(A, pp);
+  }
   // partials: one per work item (cells with real particles x parts; sized for all cells)
   const int64_t items = std::max<int64_t>(1, B.ncells) * B.cell_split;
   const size_t al = 256;

@@ -129,7 +129,9 @@ template <class T, int N, class FA>
 __global__ void k_forces_out(const FA* __restrict__ facc, int64_t n, DevGeom<T> g, int rotate, T* __restrict__ out) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double f[N];
+  // FP32 sums are rotated in FP32 (the FP64 pipe is slow on this part); FP64 sums in FP64
+  using R = typename std::conditional<std::is_same<FA, float4>::value, float, double>::type;
+  R f[N];
   if constexpr (std::is_same<FA, float4>::value) {
     const float4 v = facc[i];
     f[0] = v.x;
@@ -140,12 +142,12 @@ __global__ void k_forces_out(const FA* __restrict__ facc, int64_t n, DevGeom<T> 
     for (int d = 0; d < N; d++) f[d] = facc[i * N + d];
   }
   if (rotate) {
-    double r[N];
+    R r[N];
 #pragma unroll
     for (int a = 0; a < N; a++) {
-      double s = 0;
+      R s = 0;
 #pragma unroll
-      for (int k = 0; k < N; k++) s += (double)g.Rinv[a][k] * f[k];
+      for (int k = 0; k < N; k++) s += (R)g.Rinv[a][k] * f[k];
       r[a] = s;
     }
 #pragma unroll
@@ -213,8 +215,12 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
   A.cell_split = cell_split_for(h, g, opk);
   const LaunchSel sel{N, opk, A.self != 0, A.split != 0, false};
   const double c_default = (double)g.cutoff;
-  for (int k = 0; k < 4; k++) A.p[k] = P ? P->p[k] : 0.0;
-  if ((op == 6 || op == 7) && A.p[0] == 0.0) A.p[0] = c_default;
+  {
+    double pp[4] = {0, 0, 0, 0};
+    for (int k = 0; k < 4; k++) pp[k] = P ? P->p[k] : 0.0;
+    if ((op == 6 || op == 7) && pp[0] == 0.0) pp[0] = c_default;
+    set_params(A, pp);
+  }
   // operator tables staged on the device
   size_t need = 0;
   auto align = [](size_t v) { return (v + 255) & ~(size_t)255; };
@@ -240,7 +246,8 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
       h.last_error = "LJ with types needs types_x (types_y), eps_table and sig_table";
       return ERR_ARG;
     }
-    need += align(sizeof(int) * nx) + align(sizeof(int) * ny) + 2 * align(sizeof(double) * P->ntypes * P->ntypes);
+    need += align(sizeof(int) * nx) + align(sizeof(int) * ny) + 2 * align(sizeof(double) * P->ntypes * P->ntypes) +
+            2 * align(sizeof(float) * P->ntypes * P->ntypes);
   }
   if (hist) {
     if (!P || P->nbins < 1 || P->nbins > 256 || !P->bins || !P->vel_x || (h.nsets == 2 && !P->vel_y)) {
@@ -268,10 +275,21 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
     if (ny) CLM_CUDA_TRY(h, cudaMemcpyAsync(ty, P->types_y, sizeof(int) * ny, k_in, h.stream));
     CLM_CUDA_TRY(h, cudaMemcpyAsync(et, P->eps_table, sizeof(double) * P->ntypes * P->ntypes, k_in, h.stream));
     CLM_CUDA_TRY(h, cudaMemcpyAsync(stb, P->sig_table, sizeof(double) * P->ntypes * P->ntypes, k_in, h.stream));
+    const int64_t nt2 = (int64_t)P->ntypes * P->ntypes;
+    float* etf = (float*)(ob + at);
+    at += align(sizeof(float) * nt2);
+    float* stf = (float*)(ob + at);
+    at += align(sizeof(float) * nt2);
+    k_to_f32<double><<<(unsigned)((nt2 + 255) / 256), 256, 0, h.stream>>>(et, nt2, etf);
+    k_to_f32<double><<<(unsigned)((nt2 + 255) / 256), 256, 0, h.stream>>>(stb, nt2, stf);
+    CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches += 2;
     A.tx = tx;
     A.ty = ty;
     A.eps_t = et;
     A.sig_t = stb;
+    A.eps_tf = etf;
+    A.sig_tf = stf;
   }
   if (hist) {
     A.nbins = P->nbins;
@@ -566,8 +584,12 @@ int run_pairs_scalar_scratch(Handle& h, const Geometry<T>& g, int op, const void
   A.err = h.err.as<int>();
   A.cell_split = 1;
   const LaunchSel sel{N, opk, A.self != 0, A.split != 0, false};
-  for (int k = 0; k < 4; k++) A.p[k] = P ? P->p[k] : 0.0;
-  if (op == 6 && A.p[0] == 0.0) A.p[0] = (double)g.cutoff;
+  {
+    double pp[4] = {0, 0, 0, 0};
+    for (int k = 0; k < 4; k++) pp[k] = P ? P->p[k] : 0.0;
+    if (op == 6 && pp[0] == 0.0) pp[0] = (double)g.cutoff;
+    set_params(A, pp);
+  }
   // scratch layout: [results, 256 B][partial energy][partial count][partial min d2][partial min ij]
   const size_t slot = sizeof(double) + sizeof(unsigned long long) + sizeof(T) + 2 * sizeof(int);
   const size_t cap_blocks = scratch_bytes > 256 ? (scratch_bytes - 256) / slot : 0;

@@ -36,11 +36,14 @@ template <class T> struct PairArgs {
   int* err;
   // operator parameters
   double p[4];
+  float pf[4];  // the same in FP32 (set by set_params)
   int ntypes;
   const int* tx;
   const int* ty;
   const double* eps_t;
   const double* sig_t;
+  const float* eps_tf;  // the same tables in FP32 (pair values of the FP32 forms)
+  const float* sig_tf;
   const T* vx;
   const T* vy;
   const T* bins;
@@ -72,6 +75,14 @@ template <class T> struct PairArgs {
   const int* cell_sys;          // batch: system of each global cell
   const int* cbase;             // batch: first global cell of each system
 };
+
+// Operator parameters in both precisions.
+template <class T> inline void set_params(PairArgs<T>& A, const double* p) {
+  for (int k = 0; k < 4; k++) {
+    A.p[k] = p[k];
+    A.pf[k] = (float)p[k];
+  }
+}
 
 enum OpKind { OPK_NL = 0, OPK_SCALAR = 1, OPK_FORCES = 2, OPK_MIN = 3, OPK_HIST = 4, OPK_ADJ = 5 };
 constexpr int kAdjVals = 13;  // energy, virial (xx yy zz xy xz yz), dU/deps[3], dU/dsigma[3]

@@ -111,6 +111,20 @@ __device__ __forceinline__ double vrsqrt(double x) {
   return y;
 }
 
+// Operator parameter k and the LJ type tables in the precision of the pair value (no conversions per pair).
+template <class V, class T> __device__ __forceinline__ V par(const PairArgs<T>& A, int k) {
+  if constexpr (std::is_same<V, float>::value) return A.pf[k];
+  else return (V)A.p[k];
+}
+template <class V, class T> __device__ __forceinline__ V eps_tab(const PairArgs<T>& A, int k) {
+  if constexpr (std::is_same<V, float>::value) return A.eps_tf[k];
+  else return (V)A.eps_t[k];
+}
+template <class V, class T> __device__ __forceinline__ V sig_tab(const PairArgs<T>& A, int k) {
+  if constexpr (std::is_same<V, float>::value) return A.sig_tf[k];
+  else return (V)A.sig_t[k];
+}
+
 // Per-pair energy u and g = (du/dr)/r (force contribution df = g*(x_i - x_j)).
 template <class V, class T>
 __device__ __forceinline__ void pair_value(const PairArgs<T>& A, int op, V d2, int i, int j, V& u, V& g) {
@@ -135,7 +149,7 @@ __device__ __forceinline__ void pair_value(const PairArgs<T>& A, int op, V d2, i
     case 7: {  // SOFT (c - d)^2
       V ri = vrsqrt(d2);
       V d = d2 * ri;
-      V c = (V)A.p[0];
+      V c = par<V>(A, 0);
       u = (c - d) * (c - d);
       g = V(-2) * (c - d) * ri;
       break;
@@ -143,14 +157,14 @@ __device__ __forceinline__ void pair_value(const PairArgs<T>& A, int op, V d2, i
     case 8:
     case 9:
     case 13: {  // LJ eps*(c12 (s/d)^12 - c6 (s/d)^6)
-      V eps = (V)A.p[0], sig = (V)A.p[1];
+      V eps = par<V>(A, 0), sig = par<V>(A, 1);
       if (A.ntypes > 0) {
         int ti = A.tx[i];
         int tj = A.self ? A.tx[j] : A.ty[j];
-        eps = (V)A.eps_t[ti * A.ntypes + tj];
-        sig = (V)A.sig_t[ti * A.ntypes + tj];
+        eps = eps_tab<V>(A, ti * A.ntypes + tj);
+        sig = sig_tab<V>(A, ti * A.ntypes + tj);
       }
-      V c12 = (V)A.p[2], c6 = (V)A.p[3];
+      V c12 = par<V>(A, 2), c6 = par<V>(A, 3);
       V r2i = vrcp(d2);
       V sr2 = (sig * sig) * r2i;
       V sr6 = sr2 * sr2 * sr2;
@@ -367,8 +381,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
     const int ni = A.X.cell_start[li + 1] - si;
     const int G = (ni <= 8) ? 4 : ((ni <= 16) ? 2 : 1);
     const int LP = 32 / G;
-    const int grp = lane / LP;
-    const int il = lane % LP;
+    const int grp = lane % G;  // the G lanes of one particle are adjacent: the hit queue is ordered by particle
+    const int il = lane / G;
 
     for (int ib = part * LP; ib < ni; ib += LP * S) {
       const int ii = ib + il;
@@ -449,7 +463,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
         const int JR = 32 * G;  // candidates per round: each lane tests exactly 32
         // ---- stage candidates rbx .. rbx+JR-1 of the stream into buffer bsel with asynchronous copies
         // (cp.async, 16 B per candidate: coordinates or cell offsets with the particle code in .w);
-        // positions past the stream are padded with NaN
+        // positions past the stream are padded with a far point (its FP32 d2 is finite and above every
+        // threshold)
         auto stage = [&](int rbx, int bsel) {
           const int cnt = min(JR, total - rbx);
           for (int q = lane; q < JR; q += 32) {
@@ -468,7 +483,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                 s_tj[bsel][warp][q] = tj;
               }
             } else {
-              s_pf[bsel][warp][q] = make_float4(NAN, NAN, NAN, 0.f);
+              s_pf[bsel][warp][q] = make_float4(3e18f, 3e18f, 3e18f, 0.f);
             }
           }
           cp_async_commit();
@@ -479,43 +494,63 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
           const int cntr = min(JR, total - rb);
           cp_async_wait_all();
           __syncwarp();
-          if constexpr (!ABS_PF) {
-            // shift the offsets by the cell displacement so that x_i - x_j ~ off_i - pf (own slots only:
-            // a lane sees its own asynchronous copies after the wait)
+          if (!ABS_PF || idx_rule) {
+            // own slots only (a lane sees its own asynchronous copies after the wait): shift the offsets by
+            // the cell displacement so that x_i - x_j ~ off_i - pf, and for triclinic self pairs replace
+            // the particle code by the particle index (the pair rules there need no realness)
             for (int q = lane; q < cntr; q += 32) {
-              const int meta = s_meta[buf][warp][q];
               float4 v = s_pf[buf][warp][q];
-              v.x += gc.csf[0] * (float)((meta & 255) - 128);
-              v.y += gc.csf[1] * (float)(((meta >> 8) & 255) - 128);
-              v.z += gc.csf[2] * (float)(((meta >> 16) & 255) - 128);
+              if constexpr (!ABS_PF) {
+                const int meta = s_meta[buf][warp][q];
+                v.x += gc.csf[0] * (float)((meta & 255) - 128);
+                v.y += gc.csf[1] * (float)(((meta >> 8) & 255) - 128);
+                v.z += gc.csf[2] * (float)(((meta >> 16) & 255) - 128);
+              }
+              if (idx_rule) {
+                const int c = __float_as_int(v.w);
+                v.w = __int_as_float(c ^ (c >> 31));
+              }
               s_pf[buf][warp][q] = v;
             }
             __syncwarp();
           }
           if (rb + JR < total) stage(rb + JR, buf ^ 1);  // the next round's copies overlap this round
           // ---- phase A: 32 FP32 distance tests per lane into a bit mask (with the index rule of
-          // triclinic self pairs, so that the mirrored visit of a pair never enters the queue)
+          // triclinic self pairs, so that the mirrored visit of a pair never enters the queue).  A test
+          // passes when the sign bit of d2 - thr (and of index_i - index_j) is set; the sign bits are
+          // shifted into the mask, candidate b landing on bit b.  thr carries a 2^-13 relative margin, far
+          // above the FP32 rounding of dx^2 - thr + dy^2 + dz^2, so the strict comparison keeps every pair
+          // the exact test can accept.
           unsigned mask = 0u;
           {
-            const float4* pp = &s_pf[buf][warp][grp];
-            if (idx_rule) {
+            const float thr = g.thr_hi;
+            // the lane's 32 candidates are grp, grp + G, ...: G fixed at compile time per variant, so that
+            // every record is read at a constant offset
+            auto test32 = [&](auto g_const) {
+              constexpr int GG = decltype(g_const)::value;
+              const float4* pp = &s_pf[buf][warp][grp];
+              if (idx_rule) {
 #pragma unroll
-              for (int b = 0; b < 32; b++) {
-                const float4 p = pp[b * G];
-                const float dx = pi[0] - p.x, dy = pi[1] - p.y, dz = (N == 3) ? pi[2] - p.z : 0.f;
-                const float d2f = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                const int cj = __float_as_int(p.w);  // particle code: index, or -index-1 for a ghost
-                mask |= (d2f <= g.thr_hi && idx_i < (cj ^ (cj >> 31))) ? (1u << b) : 0u;
-              }
-            } else {
+                for (int b = 31; b >= 0; b--) {
+                  const float4 p = pp[b * GG];
+                  const float dx = pi[0] - p.x, dy = pi[1] - p.y, dz = (N == 3) ? pi[2] - p.z : 0.f;
+                  const float e = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, -thr)));  // d2 - thr
+                  const int v = __float_as_int(e) & (idx_i - __float_as_int(p.w));  // .w: index
+                  mask = __funnelshift_l((unsigned)v, mask, 1);  // (mask << 1) | sign bit of v
+                }
+              } else {
 #pragma unroll
-              for (int b = 0; b < 32; b++) {
-                const float4 p = pp[b * G];
-                const float dx = pi[0] - p.x, dy = pi[1] - p.y, dz = (N == 3) ? pi[2] - p.z : 0.f;
-                const float d2f = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                mask |= (d2f <= g.thr_hi) ? (1u << b) : 0u;
+                for (int b = 31; b >= 0; b--) {
+                  const float4 p = pp[b * GG];
+                  const float dx = pi[0] - p.x, dy = pi[1] - p.y, dz = (N == 3) ? pi[2] - p.z : 0.f;
+                  const float e = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, -thr)));  // d2 - thr
+                  mask = __funnelshift_l(__float_as_uint(e), mask, 1);
+                }
               }
-            }
+            };
+            if (G == 2) test32(std::integral_constant<int, 2>());
+            else if (G == 1) test32(std::integral_constant<int, 1>());
+            else test32(std::integral_constant<int, 4>());
           }
           if (!act_i) mask = 0u;
           // ---- phase B: compact the candidates of all lanes into a queue and process them with every lane
@@ -678,6 +713,18 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                 }
               }
             } else if constexpr (IS_F) {
+              // `cur` follows every queue entry (hit or not), so the lanes holding a particle are exactly
+              // the lanes whose runs cover its entries: adjacent, and only the last one moves past it inside
+              // its run; no other lane updates that particle's sums during the loop
+              if (has && ie != cur) {
+                if (cur >= 0) {
+#pragma unroll
+                  for (int d = 0; d < N; d++) s_if[warp][d][cur] += acc[d];
+                }
+                cur = ie;
+#pragma unroll
+                for (int d = 0; d < N; d++) acc[d] = FA(0);
+              }
               if (hit) {
                 FA uu, gg;
                 FA df[3] = {0, 0, 0};
@@ -708,15 +755,15 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                     adj[3] += gg * dv[0] * dv[1];
                     adj[4] += gg * dv[0] * dv[2];
                     adj[5] += gg * dv[1] * dv[2];
-                    FA eps = (FA)A.p[0], sig = (FA)A.p[1];
+                    FA eps = par<FA>(A, 0), sig = par<FA>(A, 1);
                     int cls = 0;
                     if (A.ntypes > 0) {
                       const int ti = A.tx[idx_i], tj = A.tx[idx_j];
-                      eps = (FA)A.eps_t[ti * A.ntypes + tj];
-                      sig = (FA)A.sig_t[ti * A.ntypes + tj];
+                      eps = eps_tab<FA>(A, ti * A.ntypes + tj);
+                      sig = sig_tab<FA>(A, ti * A.ntypes + tj);
                       cls = ti + tj;  // 2 types: AA = 0, AB = 1, BB = 2
                     }
-                    const FA c12 = (FA)A.p[2], c6 = (FA)A.p[3];
+                    const FA c12 = par<FA>(A, 2), c6 = par<FA>(A, 3);
                     const FA dd2 = sure ? (FA)d2f : (FA)d2;
                     const FA sr2 = sig * sig * vrcp(dd2);
                     const FA sr6 = sr2 * sr2 * sr2;
@@ -729,15 +776,6 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                       adj[9 + k] += (cls == k) ? dsg : FA(0);
                     }
                   }
-                }
-                if (ie != cur) {
-                  if (cur >= 0) {
-#pragma unroll
-                    for (int d = 0; d < N; d++) atomicAdd(&s_if[warp][d][cur], acc[d]);
-                  }
-                  cur = ie;
-#pragma unroll
-                  for (int d = 0; d < N; d++) acc[d] = FA(0);
                 }
 #pragma unroll
                 for (int d = 0; d < N; d++) acc[d] -= df[d];
@@ -859,9 +897,24 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
             }
           }
           if constexpr (IS_F) {
-            if (cur >= 0) {
+            // lanes ending on the same particle are adjacent: sum each run of equal `cur` into its first
+            // lane, which alone adds it to the particle's sums
+            __syncwarp();
 #pragma unroll
-              for (int d = 0; d < N; d++) atomicAdd(&s_if[warp][d][cur], acc[d]);
+            for (int off = 1; off < 32; off <<= 1) {
+              const int co = __shfl_down_sync(FULL, cur, off);
+              FA t[3];
+#pragma unroll
+              for (int d = 0; d < N; d++) t[d] = __shfl_down_sync(FULL, acc[d], off);
+              if (lane + off < 32 && co == cur) {
+#pragma unroll
+                for (int d = 0; d < N; d++) acc[d] += t[d];
+              }
+            }
+            const int cprev = __shfl_up_sync(FULL, cur, 1);
+            if (cur >= 0 && (lane == 0 || cprev != cur)) {
+#pragma unroll
+              for (int d = 0; d < N; d++) s_if[warp][d][cur] += acc[d];
             }
           }
           if constexpr (OPK == OPK_HIST) {
