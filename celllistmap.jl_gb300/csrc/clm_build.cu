@@ -39,6 +39,106 @@ constexpr int kBlock = 256;
 constexpr int SCAN_IPT = 8;
 constexpr int SCAN_TILE = kBlock * SCAN_IPT;
 
+// Single-pass exclusive scan with decoupled look-back: tiles take increasing tickets, publish their
+// aggregate, then one warp reads the published words of the 32 preceding tiles at a time (aggregate or
+// inclusive prefix) and sums back to the nearest inclusive prefix.  A tile only waits on tiles that took their tickets before it (and
+// so are running); every wait is bounded, and a tile that gives up sets DERR_SCAN and carries on.
+// status[t]: (state << 32) | value, state 1 = aggregate, 2 = inclusive prefix; zeroed before the launch
+// together with the ticket counter.  In-place use (in == out) is safe: a tile reads only its own inputs.
+constexpr unsigned long long kScanAgg = 1ull << 32, kScanPrefix = 2ull << 32;
+constexpr int kScanSpinLimit = 1 << 20;
+
+__global__ void __launch_bounds__(kBlock) k_scan_1pass(const int* in, int* out, int64_t m, int* __restrict__ total,
+                                                       unsigned long long* __restrict__ status,
+                                                       unsigned* __restrict__ ticket, int64_t ntiles,
+                                                       int* __restrict__ err) {
+  __shared__ int wsum[kBlock / 32];
+  __shared__ int s_tile, s_excl;
+  if (threadIdx.x == 0) s_tile = (int)atomicAdd(ticket, 1u);
+  __syncthreads();
+  const int tile = s_tile;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t base = (int64_t)tile * SCAN_TILE + (int64_t)threadIdx.x * SCAN_IPT;
+  int v[SCAN_IPT];
+  int s = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_IPT; k++) {
+    int64_t idx = base + k;
+    int t = (idx < m) ? in[idx] : 0;
+    v[k] = s;
+    s += t;
+  }
+  int incl = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int w = (lane < kBlock / 32) ? wsum[lane] : 0;
+    int wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    if (lane < kBlock / 32) wsum[lane] = wi - w;
+    const int agg = __shfl_sync(0xffffffffu, wi, kBlock / 32 - 1);  // the block aggregate
+    int excl = 0;
+    if (tile == 0) {
+      if (lane == 0) atomicExch(&status[0], kScanPrefix | (unsigned)agg);
+    } else {
+      if (lane == 0) atomicExch(&status[tile], kScanAgg | (unsigned)agg);
+      // look back over windows of 32 earlier tiles (lane k reads tile top - k; below tile 0 reads as a
+      // zero prefix) until a window holds an inclusive prefix with every nearer tile published
+      int top = tile - 1;
+      int spins = 0;
+      bool gave_up = false;
+      while (true) {
+        const int jj = top - lane;
+        unsigned long long wd = 2ull << 32;  // a zero inclusive prefix below tile 0
+        if (jj >= 0) wd = *(volatile unsigned long long*)&status[jj];
+        const unsigned long long state = wd & ~0xffffffffull;
+        const unsigned pend = __ballot_sync(0xffffffffu, state == 0ull);
+        const unsigned pref = __ballot_sync(0xffffffffu, state == kScanPrefix);
+        const int first = pref ? __ffs(pref) - 1 : 31;          // nearest prefix, or the whole window
+        const unsigned need = (first == 31) ? 0xffffffffu : ((2u << first) - 1u);
+        if (pend & need) {
+          if (++spins > kScanSpinLimit) {
+            gave_up = true;
+            break;
+          }
+          __nanosleep(32);
+          continue;
+        }
+        int val = (lane <= first) ? (int)(unsigned)(wd & 0xffffffffull) : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+        excl += val;
+        if (pref & need) break;
+        top -= 32;
+      }
+      if (lane == 0) {
+        if (gave_up) atomicOr(err, DERR_SCAN);
+        atomicExch(&status[tile], kScanPrefix | (unsigned)(excl + agg));
+      }
+    }
+    if (lane == 0) {
+      s_excl = excl;
+      if (total && tile == ntiles - 1) *total = excl + agg;
+    }
+  }
+  __syncthreads();
+  const int off = (incl - s) + wsum[warp] + s_excl;
+#pragma unroll
+  for (int k = 0; k < SCAN_IPT; k++) {
+    int64_t idx = base + k;
+    if (idx < m) out[idx] = v[k] + off;
+  }
+}
+
 __global__ void __launch_bounds__(kBlock) k_scan_tiles(const int* __restrict__ in, int* __restrict__ out, int64_t m,
                                                        int* __restrict__ tile_sums) {
   __shared__ int wsum[kBlock / 32];
@@ -79,16 +179,6 @@ __global__ void __launch_bounds__(kBlock) k_scan_tiles(const int* __restrict__ i
     if (idx < m) out[idx] = v[k] + off;
   }
   if (threadIdx.x == kBlock - 1) tile_sums[blockIdx.x] = off + s;
-}
-
-__global__ void __launch_bounds__(kBlock) k_scan_add(int* __restrict__ out, int64_t m, const int* __restrict__ offs) {
-  const int add = offs[blockIdx.x];
-  const int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
-#pragma unroll
-  for (int k = 0; k < SCAN_IPT; k++) {
-    int64_t idx = base + (int64_t)k * kBlock + threadIdx.x;
-    if (idx < m) out[idx] += add;
-  }
 }
 
 // ------------------------------------------------------------------ radix sort (8-bit digits)
@@ -496,8 +586,8 @@ int scan_exclusive(Handle& h, const int* in, int* out, int64_t m, int* total, in
     if (total) CLM_CUDA_TRY(h, cudaMemsetAsync(total, 0, sizeof(int), h.stream));
     return OK;
   }
-  if (depth >= 4) {
-    h.last_error = "scan too deep";
+  if (depth < 0 || depth >= 4) {
+    h.last_error = "scan buffer index out of range";
     return ERR_INTERNAL;
   }
   int64_t ntiles = (m + SCAN_TILE - 1) / SCAN_TILE;
@@ -507,18 +597,16 @@ int scan_exclusive(Handle& h, const int* in, int* out, int64_t m, int* total, in
     h.launches++;
     return OK;
   }
-  DevBuf& lv = h.scan.level[depth];
-  if (!lv.reserve((size_t)(ntiles + 1) * sizeof(int) * 2)) return ERR_NOMEM;
-  int* sums = lv.as<int>();
-  int* sums_scan = sums + ntiles;
-  k_scan_tiles<<<(unsigned)ntiles, kBlock, 0, h.stream>>>(in, out, m, sums);
+  // one launch: tile status words and the ticket counter, zeroed first
+  DevBuf& sb = h.scan.level[depth];
+  if (!sb.reserve((size_t)(ntiles + 2) * sizeof(unsigned long long))) return ERR_NOMEM;
+  unsigned long long* status = sb.as<unsigned long long>();
+  unsigned* ticket = reinterpret_cast<unsigned*>(status + ntiles);
+  CLM_CUDA_TRY(h, cudaMemsetAsync(status, 0, (size_t)(ntiles + 1) * sizeof(unsigned long long), h.stream));
+  k_scan_1pass<<<(unsigned)ntiles, kBlock, 0, h.stream>>>(in, out, m, total, status, ticket, ntiles,
+                                                         h.err.as<int>());
   CLM_CUDA_TRY(h, cudaGetLastError());
-    h.launches++;
-  int st = scan_exclusive(h, sums, sums_scan, ntiles, total, depth + 1);
-  if (st) return st;
-  k_scan_add<<<(unsigned)ntiles, kBlock, 0, h.stream>>>(out, m, sums_scan);
-  CLM_CUDA_TRY(h, cudaGetLastError());
-    h.launches++;
+  h.launches++;
   return OK;
 }
 
@@ -822,6 +910,10 @@ int check_build_totals(Handle& h, bool* overflow) {
     } else if (S.n_copies > S.copy_cap) {
       S.copy_cap = S.n_copies;
     }
+  }
+  if (errw & DERR_SCAN) {
+    h.last_error = "cell-list build: a scan tile gave up waiting for an earlier tile";
+    return ERR_INTERNAL;
   }
   if (!*overflow && (errw & DERR_CELL_RANGE)) {
     h.last_error = "cell-list build consistency check failed (particle outside the computing box)";

@@ -147,6 +147,7 @@ enum DevError : int {
   DERR_CELL_RANGE = 2,
   DERR_COPY_OVERFLOW = 4,
   DERR_NL_OVERFLOW = 8,
+  DERR_SCAN = 16,  // a single-pass scan gave up waiting for the prefix of an earlier tile
 };
 
 }  // namespace clm
