@@ -445,25 +445,28 @@ __device__ __forceinline__ void gather_at(const DevGeom<T>& g, const T* __restri
     T w = wrapped[(int64_t)p * N + d];
     q[d] = (k == g.zero_code) ? w : xadd(w, g.shift[k][d]);
   }
-  int c[3];
-  cart_of(li, g.nc, N, c);
-  float o[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-  for (int d = 0; d < N; d++) {
-    // FP32 offset of the copy from its cell origin, all in float pairs: (qh + ql) - (oh + ol)
-    float oh, ol;
-    origin_ff(g.cbf_hi[d], g.cbf_lo[d], g.csf[d], g.csf_lo[d], c[d] - 1, oh, ol);
-    const float qh = (float)q[d];
-    const float ql = (float)(q[d] - (T)qh);
-    o[d] = (qh - oh) + (ql - ol);
-  }
   const int pc = (k == g.zero_code) ? p : -(p + 1);
   px[t] = q[0];
   py[t] = q[1];
   if (N == 3) pz[t] = q[N - 1];
-  off[t] = make_float4(o[0], o[1], o[2], __int_as_float(pc));
-  if constexpr (std::is_same<T, float>::value)
+  if constexpr (std::is_same<T, float>::value) {
+    // Float32 handles test the coordinates themselves (no cell-relative offsets are read)
     xq[t] = make_float4((float)q[0], (float)q[1], N == 3 ? (float)q[N - 1] : 0.f, __int_as_float(pc));
+  } else {
+    int c[3];
+    cart_of(li, g.nc, N, c);
+    float o[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int d = 0; d < N; d++) {
+      // FP32 offset of the copy from its cell origin, all in float pairs: (qh + ql) - (oh + ol)
+      float oh, ol;
+      origin_ff(g.cbf_hi[d], g.cbf_lo[d], g.csf[d], g.csf_lo[d], c[d] - 1, oh, ol);
+      const float qh = (float)q[d];
+      const float ql = (float)(q[d] - (T)qh);
+      o[d] = (qh - oh) + (ql - ol);
+    }
+    off[t] = make_float4(o[0], o[1], o[2], __int_as_float(pc));
+  }
   code[t] = pc;
   if (k == g.zero_code) cell_flags[cb + li] = 1;  // the cell holds a real particle
 }
@@ -769,7 +772,7 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
       !S.ncopy.reserve(sizeof(int) * (n + 1)) || !S.keys[0].reserve(sizeof(uint32_t) * cap) ||
       !S.keys[1].reserve(sizeof(uint32_t) * cap) || !S.vals[0].reserve(sizeof(uint32_t) * cap) ||
       !S.vals[1].reserve(sizeof(uint32_t) * cap) || !S.px.reserve(sizeof(T) * cap) || !S.py.reserve(sizeof(T) * cap) ||
-      !S.pz.reserve(sizeof(T) * cap) || !S.off.reserve(sizeof(float4) * cap) || !S.code.reserve(sizeof(int) * cap) ||
+      !S.pz.reserve(sizeof(T) * cap) || !S.off.reserve(std::is_same<T, float>::value ? 16 : sizeof(float4) * cap) || !S.code.reserve(sizeof(int) * cap) ||
       !S.xq.reserve(std::is_same<T, float>::value ? sizeof(float4) * cap : 16) ||
       !S.rs_hist.reserve(sizeof(int) * (1024 * (int64_t)ntiles + 1)))
     return ERR_NOMEM;

@@ -138,7 +138,7 @@ __device__ __forceinline__ void cart_of(int li, const int* nc, int dim, int* c) 
 template <class T, int N>
 __device__ __forceinline__ void cell_center(const DevGeom<T>& g, const int* c, T* ctr) {
 #pragma unroll
-  for (int i = 0; i < N; i++) ctr[i] = xsub(xadd(g.cbmin[i], xmul(g.cs[i], (T)c[i])), xdiv(g.cs[i], T(2)));
+  for (int i = 0; i < N; i++) ctr[i] = xsub(xadd(g.cbmin[i], xmul(g.cs[i], (T)c[i])), xmul(g.cs[i], T(0.5)));  // cs/2 exactly
 }
 
 // Device error bits (OR-ed into the handle's error word).

@@ -19,7 +19,9 @@
 namespace clm {
 namespace pk {
 
-__device__ __forceinline__ void stencil_offset(bool forward, int l, int dim, int k, int* o) {
+template <int LC = 0>
+__device__ __forceinline__ void stencil_offset(bool forward, int l_rt, int dim, int k, int* o) {
+  const int l = LC ? LC : l_rt;  // LC: lcell fixed at compile time (constant divisors)
   const int w = 2 * l + 1;
   o[2] = 0;
   if (forward) {
@@ -426,7 +428,10 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
           int cnt = 0, start = 0, meta = 0;
           if (kk < nent) {
             int o[3] = {0, 0, 0};
-            if (kk > 0) stencil_offset(!full, l, N, kk - 1, o);
+            if (kk > 0) {
+              if (l == 1) stencil_offset<1>(!full, l, N, kk - 1, o);
+              else stencil_offset(!full, l, N, kk - 1, o);
+            }
             int cj[3] = {1, 1, 1};
             bool inr = true;
 #pragma unroll
