@@ -32,6 +32,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "within-cutoff pairs/s (cell-list build + pair map, LJ energy+forces)"
+NCU_TRAFFIC_BYTES = 56_836_352 + 319_232  # DRAM bytes per launch of the headline pair kernel (ncu)
 WORKLOAD = "fcc1M_f32_triclinic_lj_rc2.5"
 CUTOFF = 2.5
 
@@ -585,10 +586,10 @@ def main():
                   "frac": (build_gbs / hbm_peak) if (build_gbs and hbm_peak) else None,
                   "bytes_per_build": build_bytes, "copies": copies, "cells": ncells, "build_ms": build_ms,
                   "note": "cell-list build (K1-K4, sort, scans) as a whole; launch- and latency-bound at this size"}
-    traffic = None
-    tj = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tj):
-        traffic = json.load(open(tj)).get("k_pairs_lj_forces_f32_per_launch_bytes")
+    # dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel on this workload, from one
+    # ncu capture (profiles/k_pairs_lj_forces_f32_fcc1M_triclinic.md); a profiler cannot run inside the
+    # timed region, so the figure is recorded rather than measured here
+    traffic = NCU_TRAFFIC_BYTES
 
     peaks.clm_peak_fp64_gflops.restype = C.c_double
     peaks.clm_peak_fp64_gflops.argtypes = [C.c_int]
