@@ -294,7 +294,46 @@ __device__ __forceinline__ bool wrap_count_at(const DevGeom<T>& g, const T* __re
   for (int k = 0; k < N; k++) wrapped[(int64_t)i * N + k] = p[k];
   uint32_t m = 0;
   int cnt = 1;
-  if (g.kind != NONPERIODIC) {
+  if (g.kind != NONPERIODIC && g.img_tree) {
+    // image k = (s0+1) + 3(s1+1) [+ 9(s2+1)]: the last component is tested once per s_last, the next
+    // once per (s_mid, s_last), the first per image; each test uses the shift of the image itself
+    // (equal, for the components tested early, across the images that share their s values)
+#pragma unroll
+    for (int sl = -1; sl <= 1; sl++) {
+      const int kl = (N == 3) ? 9 * (sl + 1) + 4 : 3 * (sl + 1) + 1;
+      const T ql = xadd(p[N - 1], g.shift[kl][N - 1]);
+      if (!(g.cbmin[N - 1] <= ql && ql < g.cbmax[N - 1])) continue;
+      if (N == 3) {
+#pragma unroll
+        for (int sm = -1; sm <= 1; sm++) {
+          const int km = 9 * (sl + 1) + 3 * (sm + 1) + 1;
+          const T qm = xadd(p[1], g.shift[km][1]);
+          if (!(g.cbmin[1] <= qm && qm < g.cbmax[1])) continue;
+#pragma unroll
+          for (int s0 = -1; s0 <= 1; s0++) {
+            const int k = 9 * (sl + 1) + 3 * (sm + 1) + (s0 + 1);
+            if (k == g.zero_code) continue;
+            const T q0 = xadd(p[0], g.shift[k][0]);
+            if (g.cbmin[0] <= q0 && q0 < g.cbmax[0]) {
+              m |= 1u << k;
+              cnt++;
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int s0 = -1; s0 <= 1; s0++) {
+          const int k = 3 * (sl + 1) + (s0 + 1);
+          if (k == g.zero_code) continue;
+          const T q0 = xadd(p[0], g.shift[k][0]);
+          if (g.cbmin[0] <= q0 && q0 < g.cbmax[0]) {
+            m |= 1u << k;
+            cnt++;
+          }
+        }
+      }
+    }
+  } else if (g.kind != NONPERIODIC) {
     for (int k = 0; k < g.nimg; k++) {
       if (k == g.zero_code) continue;
       T q[N];
@@ -640,6 +679,12 @@ template <class T> void fill_devgeom(const Geometry<T>& g, int precision, DevGeo
   d.cutoff_sqr = g.cutoff_sqr;
   d.margin_wide = (double)g.cutoff * (1.0 + std::sqrt((double)g.dim) / 2.0);
   d.nimg = (g.dim == 3) ? 27 : 9;
+  // with exact zeros below the diagonal, component i of an image shift depends only on s_i..s_dim-1, so
+  // the image tests can run dimension by dimension from the last one (same values, fewer tests)
+  d.img_tree = 1;
+  for (int i = 0; i < g.dim; i++)
+    for (int j = 0; j < i; j++)
+      if (g.Mal[i][j] != T(0)) d.img_tree = 0;
   d.zero_code = (g.dim == 3) ? 13 : 4;
   // translation_image: x + Mal * s, s in {-1,0,1}^N with the first index fastest
   for (int k = 0; k < d.nimg; k++) {

@@ -44,6 +44,7 @@ template <class T> struct DevGeom {
   float thr_hi, thr_lo; // FP32 prefilter bounds on d2 (maybe-inside / surely-inside)
   int zero_code;        // image code of the zero shift (13 in 3D, 4 in 2D)
   int nimg;             // 3^dim
+  int img_tree;         // aligned cell exactly upper triangular: image tests can be pruned per dimension
 };
 
 // StaticArrays solve (Cramer form), then fastmod1, boundary -> 0, then M*p and R*(.)
