@@ -360,3 +360,28 @@ def test_copy_capacity_overflow_rebuilds(clm, orc, via_run):
     assert_same_pairs(orc, got, ref)
     assert s.celllist_info()["n_particles"] == 8 * len(x)
     s.close()
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_many_scan_tiles(clm, orc, dtype):
+    """~200k particles of the headline geometry: the build's scans run over ~100 tiles (copy offsets) and
+    ~170 tiles x 512 digits (radix histograms), so the single-pass look-back is exercised across many
+    tiles; the cell list (copy by copy), the neighbour list, the LJ energy and forces match the oracle."""
+    x, M = clm.workloads.cfg2(ncell=37)
+    x = x.astype(dtype)
+    kw = dict(kind="tri", unitcell=M, cutoff=2.5, dtype=dtype)
+    s = clm.ParticleSystem(xpositions=x, unitcell=M, cutoff=2.5, dtype=dtype)
+    got = clm.pairwise(clm.NeighborList(), s)
+    assert_same_pairs(orc, got, orc.run("nl", x, **kw))
+    cl = s.fetch_celllist(0)
+    oc = orc.celllist(x, **kw)
+    np.testing.assert_array_equal(cl["cell"], oc["cell"])
+    np.testing.assert_array_equal(cl["index"], oc["index"])
+    np.testing.assert_array_equal(cl["coords"].astype(np.float64), oc["coords"])
+    ef = clm.pairwise(clm.LennardJonesForces(1.0, 1.0, 4.0, 4.0), s)
+    r = orc.run("lj_forces", x, params=[1.0, 1.0, 4.0, 4.0], **kw)
+    tol = TOL[dtype]
+    assert abs(ef.energy - r["scalar"]) <= tol * abs(r["scalar"])
+    fx = np.asarray(ef.forces, np.float64)
+    assert np.abs(fx - r["forces_x"]).max() <= tol * np.abs(r["forces_x"]).max()
+    s.close()
