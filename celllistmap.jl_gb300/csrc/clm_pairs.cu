@@ -27,7 +27,9 @@
 // reference's arithmetic in the input dtype, so the pair set and d are bit-exact.
 // Split form (CLM_PREC_SPLIT): pairs certainly inside are accepted from the
 // FP32 test and evaluated in FP32; only the band is re-tested in the input
-// dtype.  Sums are accumulated in FP64 (Kahan-compensated FP32 per lane).
+// dtype.  Energies are summed per lane in the pair-value precision over one
+// particle chunk, then in FP64; forces are summed with atomics (16-byte FP32
+// records, or FP64 components) and converted to the output dtype afterwards.
 //
 // Cells holding many particles are split into parts (interleaved chunks of 32
 // particles) so that every resident warp has work; batches of independent

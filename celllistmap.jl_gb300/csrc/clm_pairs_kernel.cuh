@@ -286,8 +286,9 @@ __device__ __forceinline__ void force_add(const PairArgs<T>& A, bool ys, int idx
 // evaluated only for pairs with d2 > cutoff^2 (1 - 2^-13): any pair further inside passes it (the
 // projection of the separation on a unit vector cannot exceed the separation, and the margin covers the
 // half cell), so skipping it elsewhere leaves the pair set unchanged.
-// Resident blocks per SM (6 for Float32, 3 for Float64: 85 / 170 registers per thread) were picked by
-// timing 4..8 and 3..4 on GB300; fewer registers spill in the pair epilogues.
+// Resident blocks per SM (6 for Float32, 3 for Float64: at most 85 / 170 registers per thread; the
+// kernels use 64-80 / 113-152) were picked by timing 4..8 and 3..4 on GB300; fewer registers spill in the
+// pair epilogues.
 // OPC: the operator id when fixed at compile time (the LJ force loop), 0 = read from the arguments.
 template <class T, int N, int OPK, bool SPLIT, bool CROSS, bool BATCH, int OPC = 0>
 __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(const PairArgs<T> A) {
