@@ -66,23 +66,6 @@ template <class T> __device__ __forceinline__ T pos_of(const SetView<T>& S, int 
   return d == 0 ? S.px[t] : (d == 1 ? S.py[t] : S.pz[t]);
 }
 
-// Kahan-compensated accumulator (FP32) or plain FP64
-template <class A> struct Acc {
-  A s = 0, c = 0;
-  __device__ __forceinline__ void add(A v) {
-    if (std::is_same<A, float>::value) {
-      A y = v - c;
-      A t = s + y;
-      c = (t - s) - y;
-      s = t;
-    } else {
-      s += v;
-    }
-  }
-  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
-};
-
-
 // Reciprocal and reciprocal square root for pair VALUES (energies, forces), which are checked against
 // tolerances, never used for pair membership or neighbour-list distances.
 //  FP32: hardware approximations (rcp.approx / rsqrt.approx, a couple of ulp).
