@@ -663,12 +663,38 @@ struct Acc {  // Neumaier-compensated or plain double accumulator
   double value() const { return s + c; }
 };
 
+// Per-thread force sums: compensated accumulators, or plain doubles (the reference's per-batch output
+// copies) when compensation is off.
+struct FSum {
+  bool comp = true;
+  std::vector<Acc> a;
+  std::vector<double> p;
+  void assign(size_t n, bool c) {
+    comp = c;
+    if (c) {
+      Acc z;
+      a.assign(n, z);
+      p.clear();
+    } else {
+      p.assign(n, 0.0);
+      a.clear();
+    }
+  }
+  inline void add(size_t q, double v) {
+    if (comp) a[q].add(v);
+    else p[q] += v;
+  }
+  double value(size_t q) const { return comp ? a[q].value() : p[q]; }
+  bool empty() const { return a.empty() && p.empty(); }
+};
+
 struct Local {
+  bool used = false;  // set by the thread that owns it
   std::vector<int64_t> ni, nj;
   std::vector<double> nd;
   Acc energy;
   int64_t count = 0;
-  std::vector<Acc> fx, fy;   // per particle per component
+  FSum fx, fy;   // per particle per component
   double min_d = std::numeric_limits<double>::infinity();
   int64_t min_i = -1, min_j = -1;
   std::vector<int64_t> hc;
@@ -684,7 +710,7 @@ template <class T, int N> struct OpCtx {
 };
 
 template <class T, int N>
-inline void apply_op(const OpCtx<T, N>& ctx, Local& L, int64_t i, int64_t j, const T* xi, const T* xj, T d2,
+__attribute__((always_inline)) inline void apply_op(const OpCtx<T, N>& ctx, Local& L, int64_t i, int64_t j, const T* xi, const T* xj, T d2,
                      const Mat<T, N>* rinv = nullptr) {
   const orc_op* op = ctx.op;
   const int code = op->op;
@@ -727,8 +753,8 @@ inline void apply_op(const OpCtx<T, N>& ctx, Local& L, int64_t i, int64_t j, con
         double g = dudr / dd;
         for (int k = 0; k < N; k++) {
           double df = g * dv[k];
-          L.fx[i * N + k].add(-df);
-          if (ctx.cross) L.fy[j * N + k].add(df); else L.fx[j * N + k].add(df);
+          L.fx.add((size_t)(i * N + k), -df);
+          if (ctx.cross) L.fy.add((size_t)(j * N + k), df); else L.fx.add((size_t)(j * N + k), df);
         }
       }
       break;
@@ -767,8 +793,8 @@ inline void apply_op(const OpCtx<T, N>& ctx, Local& L, int64_t i, int64_t j, con
         double g = eps * (-12.0 * c12 * sr12 + 6.0 * c6 * sr6) / dd2;  // (du/dr)/r
         for (int k = 0; k < N; k++) {
           double df = g * dv[k];
-          L.fx[i * N + k].add(-df);
-          if (ctx.cross) L.fy[j * N + k].add(df); else L.fx[j * N + k].add(df);
+          L.fx.add((size_t)(i * N + k), -df);
+          if (ctx.cross) L.fy.add((size_t)(j * N + k), df); else L.fx.add((size_t)(j * N + k), df);
         }
       }
       break;
@@ -779,8 +805,8 @@ inline void apply_op(const OpCtx<T, N>& ctx, Local& L, int64_t i, int64_t j, con
       double g = 1.0 / dd2 / dd;
       for (int k = 0; k < N; k++) {
         double df = g * (-dv[k]);  // (1/d2)*(1/d)*(y - x)
-        L.fx[i * N + k].add(df);
-        if (ctx.cross) L.fy[j * N + k].add(-df); else L.fx[j * N + k].add(-df);
+        L.fx.add((size_t)(i * N + k), df);
+        if (ctx.cross) L.fy.add((size_t)(j * N + k), -df); else L.fx.add((size_t)(j * N + k), -df);
       }
       break;
     }
@@ -809,6 +835,44 @@ inline void apply_op(const OpCtx<T, N>& ctx, Local& L, int64_t i, int64_t j, con
 // ----------------------------------------------------------------------------
 // Map (serial structure of self.jl / cross.jl / vicinal_cells.jl)
 // ----------------------------------------------------------------------------
+// Per-thread scratch: the projected particles of a vicinal cell (project_particles!), the candidates'
+// coordinates as separate arrays, one row of squared distances, pass flags and the passing positions.
+// The inner loops first compute the squared distances of one particle to all its candidates and the
+// tests in a branch-free pass (each d2 is computed exactly as dist2 computes it), then visit the
+// candidates that passed every test in their original order: the pairs found, their order and their d2
+// are those of the plain loop.
+template <class T, int N> struct Scratch {
+  std::vector<Particle<T, N>> pp;
+  std::vector<T> ppx;
+  std::vector<T> c[N];
+  std::vector<T> d2;
+  std::vector<unsigned char> ok;
+  std::vector<int32_t> sel;
+  void coords_of(const Particle<T, N>* p, int64_t n) {
+    for (int k = 0; k < N; k++) c[k].resize((size_t)n);
+    for (int64_t q = 0; q < n; q++)
+      for (int k = 0; k < N; k++) c[k][(size_t)q] = p[q].x[k];
+    if ((int64_t)d2.size() < n) {
+      d2.resize((size_t)n);
+      ok.resize((size_t)n);
+      sel.resize((size_t)n);
+    }
+  }
+};
+
+// d2 of x to the candidates q in [q0, q1) (coordinates by component), same operation order as dist2
+template <class T, int N>
+inline void d2_row(const T* x, const std::vector<T>* c, int64_t q0, int64_t q1, T* out) {
+  const T x0 = x[0];
+  const T* c0 = c[0].data();
+  for (int64_t q = q0; q < q1; q++) out[q] = (x0 - c0[q]) * (x0 - c0[q]);
+  for (int k = 1; k < N; k++) {
+    const T xk = x[k];
+    const T* ck = c[k].data();
+    for (int64_t q = q0; q < q1; q++) out[q] = out[q] + (xk - ck[q]) * (xk - ck[q]);
+  }
+}
+
 template <class T, int N> struct Mapper {
   const Box<T, N>& B;
   const OpCtx<T, N>& ctx;
@@ -833,46 +897,55 @@ template <class T, int N> struct Mapper {
   }
 
   // same-cell, self
-  void current_self(Local& L, const Span<Particle<T, N>>& cell) const {
+  void current_self(Local& L, const Span<Particle<T, N>>& cell, Scratch<T, N>& S) const {
     const int64_t n = (int64_t)cell.size();
+    S.coords_of(cell.b, n);
+    T* d2 = S.d2.data();
     if (!tri) {
       for (int64_t a = 0; a + 1 < n; a++) {
         const auto& pi = cell[a];
+        d2_row<T, N>(pi.x, S.c, a + 1, n, d2);
         for (int64_t b = a + 1; b < n; b++) {
+          if (!(d2[b] <= B.cutoff_sqr)) continue;
           const auto& pj = cell[b];
           if (!nonper && !(pi.real || pj.real)) continue;
-          T d2 = dist2(pi.x, pj.x);
-          if (d2 <= B.cutoff_sqr) emit(L, pi, pj, d2);
+          emit(L, pi, pj, d2[b]);
         }
       }
     } else {
       for (int64_t a = 0; a < n; a++) {
         const auto& pi = cell[a];
         if (!pi.real) continue;
+        d2_row<T, N>(pi.x, S.c, 0, n, d2);
         for (int64_t b = 0; b < n; b++) {
+          if (!(d2[b] <= B.cutoff_sqr)) continue;
           const auto& pj = cell[b];
           if (pi.index >= pj.index) continue;
-          T d2 = dist2(pi.x, pj.x);
-          if (d2 <= B.cutoff_sqr) emit(L, pi, pj, d2);
+          emit(L, pi, pj, d2[b]);
         }
       }
     }
   }
 
   // same-cell, cross
-  void current_cross(Local& L, const Span<Particle<T, N>>& ci, const Span<Particle<T, N>>& cj) const {
+  void current_cross(Local& L, const Span<Particle<T, N>>& ci, const Span<Particle<T, N>>& cj,
+                     Scratch<T, N>& S) const {
+    const int64_t n = (int64_t)cj.size();
+    S.coords_of(cj.b, n);
+    T* d2 = S.d2.data();
     for (const auto& pi : ci) {
       if (!nonper && !pi.real) continue;
-      for (const auto& pj : cj) {
-        T d2 = dist2(pi.x, pj.x);
-        if (d2 <= B.cutoff_sqr) emit(L, pi, pj, d2);
-      }
+      d2_row<T, N>(pi.x, S.c, 0, n, d2);
+      for (int64_t b = 0; b < n; b++)
+        if (d2[b] <= B.cutoff_sqr) emit(L, pi, cj[b], d2[b]);
     }
   }
 
   // vicinal cells with projection culling; skip = index rule for triclinic self
   void vicinal(Local& L, const Span<Particle<T, N>>& ci, const int64_t* cci, const Span<Particle<T, N>>& cj,
-               const int64_t* ccj, bool skip, std::vector<Particle<T, N>>& pp, std::vector<T>& ppx) const {
+               const int64_t* ccj, bool skip, Scratch<T, N>& S) const {
+    std::vector<Particle<T, N>>& pp = S.pp;
+    std::vector<T>& ppx = S.ppx;
     T ctr_i[N], ctr_j[N], dc[N];
     cell_center(B, cci, ctr_i);
     cell_center(B, ccj, ctr_j);
@@ -895,21 +968,46 @@ template <class T, int N> struct Mapper {
       if (keep) { pp.push_back(pj); ppx.push_back(xp); }
     }
     if (pp.empty()) return;
+    const int64_t np = (int64_t)pp.size();
+    S.coords_of(pp.data(), np);
+    T* d2 = S.d2.data();
+    unsigned char* ok = S.ok.data();
+    const T* px = ppx.data();
     for (const auto& pi : ci) {
       if (tri && !pi.real) continue;
       T v[N];
       for (int k = 0; k < N; k++) v[k] = pi.x[k] - ctr_i[k];
       T xpi = dotN<T, N>(v, dc);
-      for (size_t q = 0; q < pp.size(); q++) {
-        if (!(std::fabs(ppx[q] - xpi) <= B.cutoff)) continue;  // partition!
-        const auto& pj = pp[q];
+      // d2 (as dist2 computes it), partition! (|xproj_j - xproj_i| <= cutoff) and the cutoff test, in one
+      // branch-free pass
+      const T* c0 = S.c[0].data();
+      const T* c1 = S.c[1].data();
+      const T* c2 = S.c[N - 1].data();
+      const T x0 = pi.x[0], x1 = pi.x[1], x2 = pi.x[N - 1];
+      const T cut = B.cutoff, cut2 = B.cutoff_sqr;
+      for (int64_t q = 0; q < np; q++) {
+        T e = (x0 - c0[q]) * (x0 - c0[q]);
+        e = e + (x1 - c1[q]) * (x1 - c1[q]);
+        if (N == 3) e = e + (x2 - c2[q]) * (x2 - c2[q]);
+        d2[q] = e;
+        ok[q] = (unsigned char)((std::fabs(px[q] - xpi) <= cut) & (e <= cut2));
+      }
+      // the candidates that passed, in their order (branch-free compaction)
+      int32_t* sel = S.sel.data();
+      int64_t m = 0;
+      for (int64_t q = 0; q < np; q++) {
+        sel[m] = (int32_t)q;
+        m += ok[q];
+      }
+      for (int64_t t = 0; t < m; t++) {
+        const int64_t q = sel[t];
+        const auto& pj = pp[(size_t)q];
         if (tri) {
           if (skip && pi.index >= pj.index) continue;
         } else if (!nonper) {
           if (!(pi.real || pj.real)) continue;
         }
-        T d2 = dist2(pi.x, pj.x);
-        if (d2 <= B.cutoff_sqr) emit(L, pi, pj, d2);
+        emit(L, pi, pj, d2[q]);
       }
     }
   }
@@ -946,9 +1044,8 @@ template <class T, int N> void alloc_local(Local& L, const orc_op* op, int64_t n
   L.energy.comp = op->compensated != 0;
   for (auto& a : L.adj) a.comp = op->compensated != 0;
   if (op->op == OP_SOFT_FORCES || op->op == OP_LJ_FORCES || op->op == OP_INV_D_FORCES || op->op == OP_LJ_ADJOINT) {
-    Acc z; z.comp = op->compensated != 0;
-    L.fx.assign((size_t)(nx * N), z);
-    if (cross) L.fy.assign((size_t)(ny * N), z);
+    L.fx.assign((size_t)(nx * N), op->compensated != 0);
+    if (cross) L.fy.assign((size_t)(ny * N), op->compensated != 0);
   }
   if (op->op == OP_RHIST) {
     Acc z; z.comp = op->compensated != 0;
@@ -987,7 +1084,6 @@ int run_map(const orc_spec* s, const T* x, int64_t nx, const T* y, int64_t ny, c
   nth = 1;
 #endif
   std::vector<Local> locals((size_t)nth);
-  for (auto& L : locals) alloc_local<T, N>(L, op, nx, ny, cross);
   const int64_t nreal = (int64_t)clx.real_cells.size();
 #ifdef _OPENMP
 #pragma omp parallel num_threads(nth)
@@ -999,8 +1095,9 @@ int run_map(const orc_spec* s, const T* x, int64_t nx, const T* y, int64_t ny, c
     int tid = 0;
 #endif
     Local& L = locals[(size_t)tid];
-    std::vector<Particle<T, N>> pp;
-    std::vector<T> ppx;
+    alloc_local<T, N>(L, op, nx, ny, cross);  // each thread fills its own sums (in parallel)
+    L.used = true;
+    Scratch<T, N> scr;
 #ifdef _OPENMP
 #pragma omp for schedule(dynamic, 8)
 #endif
@@ -1010,24 +1107,24 @@ int run_map(const orc_spec* s, const T* x, int64_t nx, const T* y, int64_t ny, c
       int64_t cc[N];
       cart_from_linear(B, li, cc);
       if (!cross) {
-        mp.current_self(L, cell);
+        mp.current_self(L, cell, scr);
         const auto& sten = (tri ? st_all : st_fw);
         for (const auto& o : sten) {
           int64_t cj[N];
           for (int k = 0; k < N; k++) cj[k] = cc[k] + o[k];
           const auto other = clx.cell(linear_index(B, cj));
           if (other.empty()) continue;
-          mp.vicinal(L, cell, cc, other, cj, true, pp, ppx);
+          mp.vicinal(L, cell, cc, other, cj, true, scr);
         }
       } else {
         const auto same = cly.cell(li);
-        if (!same.empty()) mp.current_cross(L, cell, same);
+        if (!same.empty()) mp.current_cross(L, cell, same, scr);
         for (const auto& o : st_all) {
           int64_t cj[N];
           for (int k = 0; k < N; k++) cj[k] = cc[k] + o[k];
           const auto other = cly.cell(linear_index(B, cj));
           if (other.empty()) continue;
-          mp.vicinal(L, cell, cc, other, cj, false, pp, ppx);
+          mp.vicinal(L, cell, cc, other, cj, false, scr);
         }
       }
     }
@@ -1063,17 +1160,23 @@ int run_map(const orc_spec* s, const T* x, int64_t nx, const T* y, int64_t ny, c
     for (auto& L : locals) a.add(L.adj[k].value());
     res->adj[k] = a.value();
   }
-  if (!locals[0].fx.empty()) {
-    for (int64_t q = 0; q < nx * N; q++) {
+  std::vector<const Local*> used;
+  for (auto& L : locals)
+    if (L.used) used.push_back(&L);
+  if (!used.empty() && !used[0]->fx.empty()) {
+    // element-wise sum of the threads' copies in thread order (parallel over elements)
+    const int64_t mx = nx * N, my = (cross && res->forces_y) ? ny * N : 0;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nth) schedule(static)
+#endif
+    for (int64_t q = 0; q < mx + my; q++) {
       Acc a; a.comp = op->compensated != 0;
-      for (auto& L : locals) a.add(L.fx[(size_t)q].value());
-      res->forces_x[q] = a.value();
-    }
-    if (cross && res->forces_y) {
-      for (int64_t q = 0; q < ny * N; q++) {
-        Acc a; a.comp = op->compensated != 0;
-        for (auto& L : locals) a.add(L.fy[(size_t)q].value());
-        res->forces_y[q] = a.value();
+      if (q < mx) {
+        for (const Local* L : used) a.add(L->fx.value((size_t)q));
+        res->forces_x[q] = a.value();
+      } else {
+        for (const Local* L : used) a.add(L->fy.value((size_t)(q - mx)));
+        res->forces_y[q - mx] = a.value();
       }
     }
   }
@@ -1081,7 +1184,11 @@ int run_map(const orc_spec* s, const T* x, int64_t nx, const T* y, int64_t ny, c
     for (int b = 0; b < op->nbins; b++) {
       int64_t c = 0;
       Acc a; a.comp = op->compensated != 0;
-      for (auto& L : locals) { c += L.hc[(size_t)b]; a.add(L.hs[(size_t)b].value()); }
+      for (auto& L : locals) {
+        if (!L.used) continue;
+        c += L.hc[(size_t)b];
+        a.add(L.hs[(size_t)b].value());
+      }
       res->hist_count[b] = c;
       res->hist_sum[b] = a.value();
     }
@@ -1156,9 +1263,9 @@ int run_naive(const orc_spec* s, const T* x, int64_t nx, const T* y, int64_t ny,
   }
   res->min_d = L.min_d; res->min_i = L.min_i; res->min_j = L.min_j;
   if (!L.fx.empty()) {
-    for (int64_t q = 0; q < nx * N; q++) res->forces_x[q] = L.fx[(size_t)q].value();
+    for (int64_t q = 0; q < nx * N; q++) res->forces_x[q] = L.fx.value((size_t)q);
     if (cross && res->forces_y)
-      for (int64_t q = 0; q < ny * N; q++) res->forces_y[q] = L.fy[(size_t)q].value();
+      for (int64_t q = 0; q < ny * N; q++) res->forces_y[q] = L.fy.value((size_t)q);
   }
   if (op->op == OP_RHIST)
     for (int b = 0; b < op->nbins; b++) { res->hist_count[b] = L.hc[(size_t)b]; res->hist_sum[b] = L.hs[(size_t)b].value(); }
