@@ -86,7 +86,15 @@ def _xtc_frame(xyz_nm, box_nm, precision, runs=(), smallidx=20):
     mn, mx = q.min(axis=0), q.max(axis=0)
     radix = [int(mx[k] - mn[k] + 1) for k in range(3)]
     nbits = (radix[0] * radix[1] * radix[2]).bit_length()
+    large = any(r > 0xFFFFFF for r in radix)  # then each component is stored with its own width
     w = _BitWriter()
+
+    def first(digits):
+        if large:
+            for k in range(3):
+                w.put(digits[k], radix[k].bit_length())
+        else:
+            w.triplet(digits, radix, nbits)
     run_at = dict(runs)
     i, current = 0, 0
 
@@ -103,14 +111,14 @@ def _xtc_frame(xyz_nm, box_nm, precision, runs=(), smallidx=20):
     while i < n:
         length = run_at.get(i, 0)
         if length == 0:
-            w.triplet([int(q[i, k] - mn[k]) for k in range(3)], radix, nbits)
+            first([int(q[i, k] - mn[k]) for k in range(3)])
             run_flag(0)
             i += 1
             continue
         # output order a_i, a_{i+1}, ...: the full triplet carries a_{i+1}, the first small difference a_i
         size = _MAGIC[smallidx]
         half = size // 2
-        w.triplet([int(q[i + 1, k] - mn[k]) for k in range(3)], radix, nbits)
+        first([int(q[i + 1, k] - mn[k]) for k in range(3)])
         run_flag(length)
         prev = q[i + 1]
         for k, a in enumerate([i] + list(range(i + 2, i + 1 + length))):
@@ -161,6 +169,21 @@ def test_xtc_synthetic_frames(clm, tmp_path, runs):
         f.write(b"\0\0\0\1" + data[4:])
     with pytest.raises(ValueError):
         clm.trajectory.read_xtc(p)
+
+
+def test_xtc_large_coordinate_range(clm, tmp_path):
+    # a range above 2^24 stored integers (here 40,000 nm at precision 1000) switches the format to one
+    # field per component
+    rng = np.random.default_rng(10)
+    x = rng.random((30, 3)) * np.array([40000.0, 3.0, 20000.0])
+    x[4] = x[5] + rng.uniform(-0.03, 0.03, 3)  # atom 4 is packed as a small difference from atom 5
+    box = np.diag([40000.0, 3.0, 20000.0])
+    p = os.path.join(tmp_path, "big.xtc")
+    with open(p, "wb") as f:
+        f.write(_xtc_frame(x, box, 1000.0, ((4, 1),)))
+    (fr,) = clm.trajectory.read_xtc(p)
+    want = (np.rint(x * 1000).astype(np.float32) * np.float32(1.0 / 1000)).astype(np.float64) * 10
+    np.testing.assert_allclose(fr.positions, want, rtol=1e-6, atol=0)
 
 
 def test_xtc_small_frame_uncompressed(clm, tmp_path):
