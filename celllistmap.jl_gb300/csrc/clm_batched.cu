@@ -235,7 +235,6 @@ template <class T> int enqueue_op(Handle& h, int slot, int op, const clm_op_para
   A.X = view_of<T>(X);
   A.Y = A.X;
   A.real_list = X.real_list.as<int>();
-  A.xflags = X.cell_flags.as<int>();
   A.n_real_dev = X.real_scan.as<int>() + X.ncells;
   A.self = 1;
   A.split = (h.precision == CLM_PREC_SPLIT) && sizeof(T) == 8;  // Float32: the split form is the exact form

@@ -208,7 +208,6 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
   A.X = view_of<T>(X);
   A.Y = view_of<T>(Y);
   A.real_list = X.real_list.as<int>();
-  A.xflags = X.cell_flags.as<int>();
   A.n_real_dev = X.real_scan.as<int>() + X.ncells;
   A.self = (h.nsets == 1);
   A.split = (h.precision == 1) && sizeof(T) == 8;  // Float32 inputs: the split form is the exact form
@@ -578,7 +577,6 @@ int run_pairs_scalar_scratch(Handle& h, const Geometry<T>& g, int op, const void
   A.X = view_of<T>(X);
   A.Y = view_of<T>(Y);
   A.real_list = X.real_list.as<int>();
-  A.xflags = X.cell_flags.as<int>();
   A.n_real_dev = X.real_scan.as<int>() + X.ncells;
   A.self = (h.nsets == 1);
   A.split = (h.precision == 1) && sizeof(T) == 8;  // Float32 inputs: the split form is the exact form

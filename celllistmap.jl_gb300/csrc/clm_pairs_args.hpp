@@ -28,7 +28,6 @@ template <class T> struct PairArgs {
   DevGeom<T> g;
   SetView<T> X, Y;
   const int* real_list;
-  const int* xflags;  // per cell of set x: contains real particles
   const int* n_real_dev;  // number of cells with real particles (device)
   int self;
   int split;
