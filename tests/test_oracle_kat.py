@@ -171,6 +171,37 @@ def test_box_docstring_examples(orc):
     assert list(orc.box_info(unitcell=[120, 150, 100], cutoff=10.0)["nc"]) == [15, 18, 13]
 
 
+def test_align_cell_and_cell_limits(orc):
+    # test/internals/CellOperations.jl:109-190: align_cell of 2D cells and cell_limits of aligned cells.
+    # box_info gives the aligned cell, the rotation and the computing box, which is cell_limits widened by
+    # lcell cells on each side.
+    l = np.sqrt(2) / 2
+    for m, mt, R in [([[l, 0], [l, 1]], [[1, l], [0, l]], [[l, l], [-l, l]]),
+                     ([[-l, 0], [l, 1]], [[1, l], [0, -l]], [[-l, l], [-l, -l]])]:
+        b = orc.box_info(dim=2, kind="tri", unitcell=m, cutoff=0.05)
+        np.testing.assert_allclose(b["aligned_unit_cell"], mt, atol=1e-12)
+        np.testing.assert_allclose(b["rotation"], R, atol=1e-12)
+    for m, lo, hi in [([[10, 5], [5, 10]], [0.0, 0.0], [20.12461179749811, 6.708203932499369]),
+                      ([[10, 5], [0, 10]], [0.0, -8.94427190999916], [15.652475842498529, 0.0]),
+                      ([[1, 0, 0], [0, 2, 0], [0, 0, 1]], [0.0, -1.0, 0.0], [2.0, 0.0, 1.0]),
+                      ([[1, 0, 0], [0, 2, 0], [0, 0, 3]], [0.0, 0.0, -1.0], [3.0, 2.0, 0.0])]:
+        b = orc.box_info(dim=len(lo), kind="tri", unitcell=m, cutoff=0.1)
+        h = b["cell_size"]
+        np.testing.assert_allclose(b["computing_box"][0] + h, lo, atol=1e-10)
+        np.testing.assert_allclose(b["computing_box"][1] - h, hi, atol=1e-10)
+    # a rotated diag(3, 2, 1): the longest vector goes back onto x, the other two into the y-z plane
+    rng = np.random.default_rng(5)
+    for _ in range(5):
+        q, r = np.linalg.qr(rng.normal(size=(3, 3)))
+        R = q * np.sign(np.diag(r))
+        if np.linalg.det(R) < 0:  # a proper rotation
+            R[:, 0] = -R[:, 0]
+        b = orc.box_info(dim=3, kind="tri", unitcell=R @ np.diag([3.0, 2.0, 1.0]), cutoff=0.1)
+        ma = b["aligned_unit_cell"]
+        np.testing.assert_allclose(ma[:, 0], [3.0, 0.0, 0.0], atol=1e-12)
+        np.testing.assert_allclose(np.cross([1.0, 0.0, 0.0], np.cross(ma[:, 1], ma[:, 2])), 0.0, atol=1e-10)
+
+
 def test_cell_too_small_and_lcell(orc):
     # src/internals/Box.jl:192, 243
     with pytest.raises(orc.OracleError) as e:
