@@ -197,19 +197,3 @@ def test_xtc_small_frame_uncompressed(clm, tmp_path):
     (fr,) = clm.trajectory.read_xtc(p)
     np.testing.assert_array_equal(fr.positions, x.astype(np.float64) * 10)
     np.testing.assert_array_equal(fr.unitcell, np.diag([20.0, 20.0, 20.0]))
-
-
-@pytest.mark.skipif(not os.path.isdir("/root/reference/test/applications/gromacs/argon"),
-                    reason="the reference's GROMACS files are not on this machine")
-@pytest.mark.parametrize("name", ["minimal", "cubic", "dodecahedron", "octahedron"])
-def test_xtc_reference_files(clm, golden_dir, name):
-    # the decoded frame is the PDB the run started from, up to lattice translations (GROMACS puts atoms
-    # in the box), and it is the committed fixture
-    base = os.path.join("/root/reference/test/applications/gromacs/argon", name)
-    (fr,) = clm.trajectory.read_xtc(base + ".xtc")
-    pdb, _ = clm.trajectory.read_pdb(base + ".pdb")
-    d = np.linalg.solve(fr.unitcell, (fr.positions - pdb).T).T
-    assert np.abs(d - np.rint(d)).max() < 1e-6
-    g = np.load(os.path.join(golden_dir, "gromacs_argon.npz"))
-    np.testing.assert_array_equal(fr.positions, g[name + "_x"])
-    np.testing.assert_array_equal(fr.unitcell, g[name + "_cell"])
