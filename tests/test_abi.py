@@ -59,3 +59,34 @@ def test_dimension_and_argument_checks_happen_on_the_host(clm):
     assert api._promote_dtype([1, 1, 1], 2, None) == "float64"
     import numpy as np
     assert api._promote_dtype(np.array([1.0, 1.0], np.float32), np.float32(0.1), None) == np.float32
+
+
+def _build_c_driver(clm, tmp_path):
+    """Compile tests/abi_driver.c (plain C99 against the header) and link it to the library."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    libdir = os.path.dirname(clm._abi.lib_path())
+    exe = str(tmp_path / "abi_driver")
+    cmd = [cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "abi_driver.c"), "-L", libdir, "-lcelllist_cuda", "-Wl,-rpath," + libdir,
+           "-lm", "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_c_client_compiles_and_links(clm, tmp_path):
+    # the header is plain C and every entry point the driver calls resolves in the shared library
+    assert os.path.exists(_build_c_driver(clm, tmp_path))
+
+
+@pytest.mark.gpu
+def test_c_client_known_answers(clm, tmp_path):
+    import subprocess
+    exe = _build_c_driver(clm, tmp_path)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "abi driver ok" in r.stdout
