@@ -28,6 +28,7 @@ LennardJones = _api.LennardJones
 LennardJonesForces = _api.LennardJonesForces
 LennardJonesAdjoint = _api.LennardJonesAdjoint
 InverseDistanceForces = _api.InverseDistanceForces
+WeightedInverseDistance = _api.WeightedInverseDistance
 MinimumDistance = _api.MinimumDistance
 RadialHistogram = _api.RadialHistogram
 NeighborList = _api.NeighborList
@@ -36,7 +37,7 @@ __all__ = [
     "ArgumentError", "BatchedSystems", "Box", "CUDAError", "DimensionMismatch", "EnergyAndForces", "InPlaceNeighborList",
     "ParticleSystem", "device_allocations", "neighborlist", "neighborlist_", "pairwise", "pairwise_", "update", "version", "ops",
     "Count", "SumD2", "SumD", "SumInvD", "SoftEnergy", "SoftForces", "LennardJones", "LennardJonesForces", "LennardJonesAdjoint",
-    "InverseDistanceForces", "MinimumDistance", "RadialHistogram", "NeighborList",
+    "InverseDistanceForces", "WeightedInverseDistance", "MinimumDistance", "RadialHistogram", "NeighborList",
 ]
 
 

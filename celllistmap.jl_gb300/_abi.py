@@ -19,6 +19,7 @@ CLM_PREC_EXACT, CLM_PREC_SPLIT = 0, 1
 OP = {
     "nl": 1, "count": 2, "sum_d2": 3, "sum_d": 4, "sum_inv_d": 5, "soft_energy": 6, "soft_forces": 7,
     "lj_energy": 8, "lj_forces": 9, "mindist": 10, "rhist": 11, "inv_d_forces": 12, "lj_adjoint": 13,
+    "weighted_inv_d": 14,
 }
 STATUS = {
     0: "CLM_OK", 1: "CLM_ERR_ARG", 2: "CLM_ERR_CELL_TOO_SMALL", 3: "CLM_ERR_NAN", 4: "CLM_ERR_DIM",
@@ -41,7 +42,8 @@ class OpParams(C.Structure):
     _fields_ = [("p", C.c_double * 8), ("ntypes", C.c_int32), ("nbins", C.c_int32), ("types_x", C.c_void_p),
                 ("types_y", C.c_void_p), ("eps_table", C.c_void_p), ("sig_table", C.c_void_p),
                 ("vel_x", C.c_void_p), ("vel_y", C.c_void_p), ("bins", C.c_void_p),
-                ("params_on_device", C.c_int32), ("reserved", C.c_int32)]
+                ("params_on_device", C.c_int32), ("reserved", C.c_int32),
+                ("weights_x", C.c_void_p), ("weights_y", C.c_void_p)]
 
 
 class Outputs(C.Structure):

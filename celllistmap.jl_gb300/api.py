@@ -237,6 +237,35 @@ class InverseDistanceForces(_ForcesOp):
     op = "inv_d_forces"
 
 
+class WeightedInverseDistance(_ForcesOp):
+    """Per-particle weights w (masses, charges): energy u -= c w_i w_j / d and forces
+    df = (c w_i w_j / d^2 / d) (x_i - x_j), f[i] -= df, f[j] += df — the gravitational potential and force
+    examples with w = mass and c = 9.8 (test/examples/gravitational_potential.jl:30-33,
+    test/examples/gravitational_force.jl:37-46).  `weights_y` for two sets."""
+    op = "weighted_inv_d"
+
+    def __init__(self, weights_x, c=9.8, weights_y=None):
+        self.weights_x, self.weights_y, self.c = weights_x, weights_y, c
+
+    def params(self, system):
+        p = _abi.OpParams()
+        p.p[0] = float(self.c)
+        wx = np.ascontiguousarray(self.weights_x, dtype=np.float64).reshape(-1)
+        if wx.shape[0] != system.n_x:
+            raise DimensionMismatch("weights_x does not match the first set")
+        p.weights_x = wx.ctypes.data
+        keep = [wx]
+        if system.nsets == 2:
+            if self.weights_y is None:
+                raise ArgumentError("weights_y is required for two sets")
+            wy = np.ascontiguousarray(self.weights_y, dtype=np.float64).reshape(-1)
+            if wy.shape[0] != system.n_y:
+                raise DimensionMismatch("weights_y does not match the second set")
+            p.weights_y = wy.ctypes.data
+            keep.append(wy)
+        return p, keep
+
+
 class MinimumDistance(Operator):
     """Pair with the smallest distance (test/examples/nearest_neighbor.jl:9-16,43); returns (i, j, d),
     (-1, -1, inf) when no pair is within the cutoff."""

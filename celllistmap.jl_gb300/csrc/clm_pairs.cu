@@ -228,6 +228,7 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
   const int64_t nx = X.n, ny = (h.nsets == 2) ? Y.n : 0;
   const bool types = P && (op == 8 || op == 9 || op == 13) && P->ntypes > 0;
   const bool hist = (op == 11);
+  const bool weights = (op == 14);
   if (opk == OPK_ADJ) {
     if (h.nsets != 1) {
       h.last_error = "the LJ adjoint is defined for a single set of particles";
@@ -249,6 +250,14 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
     }
     need += align(sizeof(int) * nx) + align(sizeof(int) * ny) + 2 * align(sizeof(double) * P->ntypes * P->ntypes) +
             2 * align(sizeof(float) * P->ntypes * P->ntypes);
+  }
+  if (weights) {
+    if (!P || !P->weights_x || (h.nsets == 2 && !P->weights_y)) {
+      h.last_error = "WEIGHTED_INV_D needs weights_x (and weights_y for two sets)";
+      return ERR_ARG;
+    }
+    need += align(sizeof(double) * nx) + align(sizeof(double) * ny) + align(sizeof(float) * nx) +
+            align(sizeof(float) * ny);
   }
   if (hist) {
     if (!P || P->nbins < 1 || P->nbins > 256 || !P->bins || !P->vel_x || (h.nsets == 2 && !P->vel_y)) {
@@ -291,6 +300,26 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
     A.sig_t = stb;
     A.eps_tf = etf;
     A.sig_tf = stf;
+  }
+  if (weights) {
+    double* wx = (double*)(ob + at);
+    at += align(sizeof(double) * nx);
+    double* wy = (double*)(ob + at);
+    at += align(sizeof(double) * ny);
+    float* wxf = (float*)(ob + at);
+    at += align(sizeof(float) * nx);
+    float* wyf = (float*)(ob + at);
+    at += align(sizeof(float) * ny);
+    if (nx) CLM_CUDA_TRY(h, cudaMemcpyAsync(wx, P->weights_x, sizeof(double) * nx, k_in, h.stream));
+    if (ny) CLM_CUDA_TRY(h, cudaMemcpyAsync(wy, P->weights_y, sizeof(double) * ny, k_in, h.stream));
+    if (nx) k_to_f32<double><<<(unsigned)((nx + 255) / 256), 256, 0, h.stream>>>(wx, nx, wxf);
+    if (ny) k_to_f32<double><<<(unsigned)((ny + 255) / 256), 256, 0, h.stream>>>(wy, ny, wyf);
+    CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches += (nx > 0) + (ny > 0);
+    A.wx = wx;
+    A.wy = wy;
+    A.wxf = wxf;
+    A.wyf = wyf;
   }
   if (hist) {
     A.nbins = P->nbins;

@@ -49,6 +49,10 @@ template <class T> struct PairArgs {
   int nbins;
   const float* vxf;  // velocities in FP32 (pair values of the FP32 forms)
   const float* vyf;
+  const double* wx;   // per-particle weights (WEIGHTED_INV_D) of x and y, and FP32 copies
+  const double* wy;
+  const float* wxf;
+  const float* wyf;
   // outputs
   int* nl_i;
   int* nl_j;
@@ -138,7 +142,7 @@ inline int opkind_of(int op) {
   switch (op) {
     case 1: return OPK_NL;
     case 2: case 3: case 4: case 5: case 6: case 8: return OPK_SCALAR;
-    case 7: case 9: case 12: return OPK_FORCES;
+    case 7: case 9: case 12: case 14: return OPK_FORCES;
     case 13: return OPK_ADJ;
     case 10: return OPK_MIN;
     case 11: return OPK_HIST;

@@ -109,6 +109,11 @@ template <class V, class T> __device__ __forceinline__ V sig_tab(const PairArgs<
   if constexpr (std::is_same<V, float>::value) return A.sig_tf[k];
   else return (V)A.sig_t[k];
 }
+// Per-particle weight of particle k of set x (or y when ys).
+template <class V, class T> __device__ __forceinline__ V weight(const PairArgs<T>& A, bool ys, int k) {
+  if constexpr (std::is_same<V, float>::value) return (ys ? A.wyf : A.wxf)[k];
+  else return (V)(ys ? A.wy : A.wx)[k];
+}
 
 // Per-pair energy u and g = (du/dr)/r (force contribution df = g*(x_i - x_j)).
 template <class V, class T>
@@ -156,6 +161,13 @@ __device__ __forceinline__ void pair_value(const PairArgs<T>& A, int op, V d2, i
       V sr12 = sr6 * sr6;
       u = eps * (c12 * sr12 - c6 * sr6);
       g = eps * (V(-12) * c12 * sr12 + V(6) * c6 * sr6) * r2i;
+      break;
+    }
+    case 14: {  // weighted 1/d: u = -c w_i w_j / d, g = (c w_i w_j / d^2) / d
+      const V cw = par<V>(A, 0) * weight<V>(A, false, i) * weight<V>(A, A.self == 0, j);
+      const V ri = vrsqrt(d2);
+      u = -(cw * ri);
+      g = cw * (ri * ri * ri);
       break;
     }
     case 12: {  // 1/d with gradient accumulation

@@ -67,9 +67,13 @@ enum clm_op_id {
   CLM_OP_MINDIST = 10,       /* argmin d, test/examples/nearest_neighbor.jl:9-16,43 */
   CLM_OP_RHIST = 11,         /* radial histogram with per-bin velocity accumulator, test/examples/pairwise_velocities.jl:17-24 */
   CLM_OP_INV_D_FORCES = 12,  /* energy 1/d with gradient accumulation, docs/src/ParticleSystem/single_set_compound.md:79-86 */
-  CLM_OP_LJ_ADJOINT = 13     /* LJ energy, forces and the adjoint of the energy w.r.t. the cell and the per-type
+  CLM_OP_LJ_ADJOINT = 13,    /* LJ energy, forces and the adjoint of the energy w.r.t. the cell and the per-type
                                 eps/sigma (no reference counterpart: the reference differentiates closures with
                                 ForwardDiff, test/examples/generic_types.jl:10-20,102) */
+  CLM_OP_WEIGHTED_INV_D = 14 /* u -= c w_i w_j / d and forces df = (c w_i w_j / d^2 / d)(x_i - x_j), f_i -= df,
+                                f_j += df: the gravitational potential and force examples with w = mass,
+                                c = 9.8 (test/examples/gravitational_potential.jl:30-33,
+                                test/examples/gravitational_force.jl:37-46); Coulomb sums with w = charge */
 };
 
 /* Precision forms of the map (see clm_set_precision). */
@@ -92,6 +96,8 @@ typedef struct {
   const double* bins;        /* RHIST: nbins+1 ascending edges */
   int32_t params_on_device;  /* 1 if the pointers above are device pointers */
   int32_t reserved;
+  const double* weights_x;   /* WEIGHTED_INV_D: weight of each x particle (p[0] = c) */
+  const double* weights_y;   /* WEIGHTED_INV_D cross: weight of each y particle */
 } clm_op_params;
 
 /* Outputs of clm_run.  Pointers may be host or device (out_on_device).  Only

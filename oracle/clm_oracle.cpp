@@ -84,6 +84,8 @@ typedef struct {
   const double* bins;
   int32_t nbins;
   int32_t pad_;
+  const double* weights_x;  // WEIGHTED_INV_D: per-particle weights (masses, charges) of x and y
+  const double* weights_y;
 } orc_op;
 
 typedef struct {
@@ -112,7 +114,7 @@ enum { KIND_ORTHO = 0, KIND_TRI = 1, KIND_NONPER = 2 };
 enum {
   OP_NL = 1, OP_COUNT = 2, OP_SUM_D2 = 3, OP_SUM_D = 4, OP_SUM_INV_D = 5,
   OP_SOFT_ENERGY = 6, OP_SOFT_FORCES = 7, OP_LJ_ENERGY = 8, OP_LJ_FORCES = 9,
-  OP_MINDIST = 10, OP_RHIST = 11, OP_INV_D_FORCES = 12, OP_LJ_ADJOINT = 13
+  OP_MINDIST = 10, OP_RHIST = 11, OP_INV_D_FORCES = 12, OP_LJ_ADJOINT = 13, OP_WEIGHTED_INV_D = 14
 };
 enum {
   ERR_OK = 0, ERR_ARG = 1, ERR_CELL_TOO_SMALL = 2, ERR_NAN = 3, ERR_DIM = 4,
@@ -799,6 +801,21 @@ __attribute__((always_inline)) inline void apply_op(const OpCtx<T, N>& ctx, Loca
       }
       break;
     }
+    case OP_WEIGHTED_INV_D: {
+      // u -= c w_i w_j / d (test/examples/gravitational_potential.jl:30-33, c = 9.8, w = mass);
+      // df = ((c w_i w_j) / d2 / d) (x - y), f[i] -= df, f[j] += df (gravitational_force.jl:37-46)
+      const double wi = op->weights_x[i];
+      const double wj = ctx.cross ? op->weights_y[j] : op->weights_x[j];
+      const double cw = op->p[0] * wi * wj;
+      L.energy.add(-(cw / dd));
+      const double g = cw / dd2 / dd;
+      for (int k = 0; k < N; k++) {
+        double df = g * dv[k];
+        L.fx.add((size_t)(i * N + k), -df);
+        if (ctx.cross) L.fy.add((size_t)(j * N + k), df); else L.fx.add((size_t)(j * N + k), df);
+      }
+      break;
+    }
     case OP_INV_D_FORCES: {
       // energy += 1/d; forces accumulate the gradient (single_set_compound.md:79-86)
       L.energy.add(1.0 / dd);
@@ -1043,7 +1060,8 @@ template <class T, int N> void stencil(const Box<T, N>& B, bool forward, std::ve
 template <class T, int N> void alloc_local(Local& L, const orc_op* op, int64_t nx, int64_t ny, bool cross) {
   L.energy.comp = op->compensated != 0;
   for (auto& a : L.adj) a.comp = op->compensated != 0;
-  if (op->op == OP_SOFT_FORCES || op->op == OP_LJ_FORCES || op->op == OP_INV_D_FORCES || op->op == OP_LJ_ADJOINT) {
+  if (op->op == OP_SOFT_FORCES || op->op == OP_LJ_FORCES || op->op == OP_INV_D_FORCES || op->op == OP_LJ_ADJOINT ||
+      op->op == OP_WEIGHTED_INV_D) {
     L.fx.assign((size_t)(nx * N), op->compensated != 0);
     if (cross) L.fy.assign((size_t)(ny * N), op->compensated != 0);
   }

@@ -25,7 +25,7 @@ KIND = {"ortho": 0, "orthorhombic": 0, "tri": 1, "triclinic": 1, "nonperiodic": 
 OPS = {
     "nl": 1, "count": 2, "sum_d2": 3, "sum_d": 4, "sum_inv_d": 5,
     "soft_energy": 6, "soft_forces": 7, "lj_energy": 8, "lj_forces": 9,
-    "mindist": 10, "rhist": 11, "inv_d_forces": 12, "lj_adjoint": 13,
+    "mindist": 10, "rhist": 11, "inv_d_forces": 12, "lj_adjoint": 13, "weighted_inv_d": 14,
 }
 ERRORS = {1: "invalid argument", 2: "unit cell too small for cutoff", 3: "invalid (NaN) coordinates",
           4: "dimension mismatch", 6: "capacity", 10: "lcell must be >= 1"}
@@ -53,7 +53,8 @@ class _Op(C.Structure):
     _fields_ = [("op", C.c_int32), ("nthreads", C.c_int32), ("compensated", C.c_int32), ("ntypes", C.c_int32),
                 ("types_x", C.c_void_p), ("types_y", C.c_void_p), ("p", C.c_double * 8),
                 ("eps_table", C.c_void_p), ("sig_table", C.c_void_p), ("vel_x", C.c_void_p),
-                ("vel_y", C.c_void_p), ("bins", C.c_void_p), ("nbins", C.c_int32), ("pad_", C.c_int32)]
+                ("vel_y", C.c_void_p), ("bins", C.c_void_p), ("nbins", C.c_int32), ("pad_", C.c_int32),
+                ("weights_x", C.c_void_p), ("weights_y", C.c_void_p)]
 
 
 class _Result(C.Structure):
@@ -169,7 +170,7 @@ def celllist(x, *, dim=3, kind="ortho", unitcell=None, cutoff, lcell=1, dtype=np
 
 def run(op, x, y=None, *, dim=3, kind="ortho", unitcell=None, cutoff, lcell=1, dtype=np.float64,
         params=(), types_x=None, types_y=None, eps_table=None, sig_table=None, vel_x=None, vel_y=None,
-        bins=None, nthreads=1, compensated=True, naive=False, nl_cap=None):
+        bins=None, nthreads=1, compensated=True, naive=False, nl_cap=None, weights_x=None, weights_y=None):
     """Run one operator over all pairs within the cutoff; returns a dict of outputs."""
     s = _spec(dtype, dim, kind, unitcell, cutoff, lcell)
     xa, nx = _pos(x, dtype, dim)
@@ -206,6 +207,14 @@ def run(op, x, y=None, *, dim=3, kind="ortho", unitcell=None, cutoff, lcell=1, d
             vy = np.ascontiguousarray(vel_y, dtype=np.float64).reshape(-1, dim)
             keep.append(vy)
             o.vel_y = vy.ctypes.data
+    if weights_x is not None:
+        wx = np.ascontiguousarray(weights_x, dtype=np.float64).reshape(-1)
+        keep.append(wx)
+        o.weights_x = wx.ctypes.data
+        if weights_y is not None:
+            wy = np.ascontiguousarray(weights_y, dtype=np.float64).reshape(-1)
+            keep.append(wy)
+            o.weights_y = wy.ctypes.data
     if bins is not None:
         b = np.ascontiguousarray(bins, dtype=np.float64)
         keep.append(b)
@@ -231,7 +240,7 @@ def run(op, x, y=None, *, dim=3, kind="ortho", unitcell=None, cutoff, lcell=1, d
             n = r.nl_n
             return {"i": ni[:n].copy(), "j": nj[:n].copy(), "d": nd[:n].copy()}
     fx = fy = hc = hs = None
-    if o.op in (OPS["soft_forces"], OPS["lj_forces"], OPS["inv_d_forces"], OPS["lj_adjoint"]):
+    if o.op in (OPS["soft_forces"], OPS["lj_forces"], OPS["inv_d_forces"], OPS["lj_adjoint"], OPS["weighted_inv_d"]):
         fx = np.zeros((nx, dim), np.float64)
         r.forces_x = fx.ctypes.data
         if ya is not None:

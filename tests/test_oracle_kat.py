@@ -285,3 +285,50 @@ def test_pathological_coordinates(orc):
         cl = orc.run("count", x, unitcell=sides, cutoff=10.0, lcell=lcell)
         nv = orc.run("count", x, unitcell=sides, cutoff=10.0, naive=True)
         assert cl["count"] == nv["count"]
+
+
+def _gravity_brute_force(x, side, cutoff, m, c=9.8):
+    """test/examples/gravitational_potential.jl:30-33 and gravitational_force.jl:37-46 written out over
+    all pairs with the minimum image in a cubic box."""
+    n = len(x)
+    u = 0.0
+    f = np.zeros_like(x)
+    for i in range(n - 1):
+        dx = x[i] - x[i + 1:]
+        dx -= side * np.rint(dx / side)
+        d2 = np.sum(dx * dx, axis=1)
+        sel = np.nonzero(d2 <= cutoff * cutoff)[0]
+        for k in sel:
+            j = i + 1 + k
+            d = np.sqrt(d2[k])
+            u -= c * m[i] * m[j] / d
+            df = (c * m[i] * m[j] / d2[k] / d) * dx[k]
+            f[i] -= df
+            f[j] += df
+    return u, f
+
+
+@pytest.mark.parametrize("kind", ["ortho", "tri"])
+def test_weighted_inverse_distance(orc, kind):
+    # the gravitational examples' closures, with masses m = 5 x_1 as in the reference's examples
+    rng = np.random.default_rng(21)
+    side = 60.0
+    x = rng.random((1500, 3)) * side
+    m = 5 * x[:, 0]
+    uc = [side] * 3 if kind == "ortho" else np.diag([side] * 3)
+    r = orc.run("weighted_inv_d", x, kind=kind, unitcell=uc, cutoff=10.0, params=[9.8], weights_x=m)
+    rn = orc.run("weighted_inv_d", x, kind=kind, unitcell=uc, cutoff=10.0, params=[9.8], weights_x=m, naive=True)
+    assert r["scalar"] == pytest.approx(rn["scalar"], rel=1e-12)
+    np.testing.assert_allclose(r["forces_x"], rn["forces_x"], rtol=0, atol=1e-12 * np.abs(rn["forces_x"]).max())
+    u, f = _gravity_brute_force(x, side, 10.0, m)
+    assert r["scalar"] == pytest.approx(u, rel=1e-12)
+    np.testing.assert_allclose(r["forces_x"], f, rtol=0, atol=1e-12 * np.abs(f).max())
+    # two sets: weights of y apply to the partner
+    y = rng.random((700, 3)) * side
+    my = 5 * y[:, 0]
+    rc = orc.run("weighted_inv_d", x, y, kind=kind, unitcell=uc, cutoff=10.0, params=[9.8], weights_x=m,
+                 weights_y=my)
+    rcn = orc.run("weighted_inv_d", x, y, kind=kind, unitcell=uc, cutoff=10.0, params=[9.8], weights_x=m,
+                  weights_y=my, naive=True)
+    assert rc["scalar"] == pytest.approx(rcn["scalar"], rel=1e-12)
+    np.testing.assert_allclose(rc["forces_y"], rcn["forces_y"], rtol=0, atol=1e-12 * np.abs(rcn["forces_y"]).max())
