@@ -90,3 +90,29 @@ def test_c_client_known_answers(clm, tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "abi driver ok" in r.stdout
+
+
+def test_operator_parameters_are_checked_on_the_host(clm):
+    """Operator arguments are validated before any device work (stand-in system: sizes only)."""
+    import numpy as np
+
+    class Sys:
+        n_x, n_y, nsets, dim, dtype = 5, 3, 1, 3, np.float64
+
+    p, keep = clm.WeightedInverseDistance(np.ones(5), 9.8).params(Sys)
+    assert p.p[0] == 9.8 and p.weights_x == keep[0].ctypes.data and not p.weights_y
+    with pytest.raises(clm.DimensionMismatch):
+        clm.WeightedInverseDistance(np.ones(4)).params(Sys)
+    Sys.nsets = 2
+    with pytest.raises(clm.ArgumentError):
+        clm.WeightedInverseDistance(np.ones(5)).params(Sys)  # two sets need weights_y
+    with pytest.raises(clm.DimensionMismatch):
+        clm.WeightedInverseDistance(np.ones(5), weights_y=np.ones(2)).params(Sys)
+    p, keep = clm.WeightedInverseDistance(np.ones(5), 1.0, np.ones(3)).params(Sys)
+    assert p.weights_y == keep[1].ctypes.data
+    Sys.nsets = 1
+    eps = np.ones((2, 2))
+    with pytest.raises(clm.ArgumentError):  # type index outside the tables
+        clm.LennardJones(types_x=np.array([0, 1, 2, 0, 1]), eps_table=eps, sig_table=eps).params(Sys)
+    with pytest.raises(clm.DimensionMismatch):
+        clm.LennardJones(types_x=np.array([0, 1]), eps_table=eps, sig_table=eps).params(Sys)
