@@ -84,7 +84,8 @@ enum clm_precision {
 
 /* Operator parameters (clm_run's op_params).  Unused fields are ignored. */
 typedef struct {
-  double p[8];               /* SOFT: p[0] = c (0 => cutoff).  LJ: p[0] = eps, p[1] = sigma, p[2] = c12, p[3] = c6 */
+  double p[8];               /* SOFT: p[0] = c (0 => cutoff).  LJ: p[0] = eps, p[1] = sigma, p[2] = c12, p[3] = c6.
+                                WEIGHTED_INV_D: p[0] = c */
   int32_t ntypes;            /* LJ: number of particle types (0 => single eps/sigma) */
   int32_t nbins;             /* RHIST: number of bins */
   const int32_t* types_x;    /* LJ: type of each x particle (host or device, see params_on_device) */
