@@ -116,3 +116,12 @@ def test_operator_parameters_are_checked_on_the_host(clm):
         clm.LennardJones(types_x=np.array([0, 1, 2, 0, 1]), eps_table=eps, sig_table=eps).params(Sys)
     with pytest.raises(clm.DimensionMismatch):
         clm.LennardJones(types_x=np.array([0, 1]), eps_table=eps, sig_table=eps).params(Sys)
+
+
+def test_operator_ids_agree_across_header_python_and_oracle(clm, orc):
+    """The operator ids of include/celllistmap_gb300.h, the Python binding table and the oracle's table
+    are the same numbers."""
+    src = open(os.path.join(ROOT, "include", "celllistmap_gb300.h")).read()
+    ids = {name.lower(): int(v) for name, v in re.findall(r"CLM_OP_([A-Z0-9_]+)\s*=\s*(\d+)", src)}
+    assert ids and ids == {k: v for k, v in clm._abi.OP.items()}
+    assert {k: v for k, v in orc.OPS.items()} == ids
