@@ -332,3 +332,25 @@ def test_weighted_inverse_distance(orc, kind):
                   weights_y=my, naive=True)
     assert rc["scalar"] == pytest.approx(rcn["scalar"], rel=1e-12)
     np.testing.assert_allclose(rc["forces_y"], rcn["forces_y"], rtol=0, atol=1e-12 * np.abs(rcn["forces_y"]).max())
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_neighborlists_vs_kdtree(orc, dim):
+    # test/API/neighborlists.jl:1-45: non-periodic self and cross lists against a tree-based search
+    # (NearestNeighbors.jl there, scipy's cKDTree here), for two cutoffs
+    spatial = pytest.importorskip("scipy.spatial")
+    rng = np.random.default_rng(40 + dim)
+    for n, m, r in [(500, 1000, 0.1), (450, 831, 0.05)]:
+        x = rng.random((n, dim))
+        y = rng.random((m, dim))
+        got = orc.run("nl", x, dim=dim, kind="nonperiodic", cutoff=r)
+        a, b = np.minimum(got["i"], got["j"]), np.maximum(got["i"], got["j"])
+        assert len(set(zip(a.tolist(), b.tolist()))) == len(a)  # each pair once
+        ref = spatial.cKDTree(x).query_pairs(r, output_type="ndarray")
+        assert set(zip(a.tolist(), b.tolist())) == set(map(tuple, ref.tolist()))
+        np.testing.assert_allclose(got["d"], np.linalg.norm(x[got["i"]] - x[got["j"]], axis=1), rtol=1e-12)
+        got = orc.run("nl", x, y, dim=dim, kind="nonperiodic", cutoff=r)
+        pairs = set(zip(got["i"].tolist(), got["j"].tolist()))
+        assert len(pairs) == len(got["i"])
+        sm = spatial.cKDTree(x).sparse_distance_matrix(spatial.cKDTree(y), r, output_type="ndarray")
+        assert pairs == set(zip(sm["i"].tolist(), sm["j"].tolist()))
