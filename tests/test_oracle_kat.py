@@ -354,3 +354,54 @@ def test_neighborlists_vs_kdtree(orc, dim):
         assert len(pairs) == len(got["i"])
         sm = spatial.cKDTree(x).sparse_distance_matrix(spatial.cKDTree(y), r, output_type="ndarray")
         assert pairs == set(zip(sm["i"].tolist(), sm["j"].tolist()))
+
+
+def test_images_counted_once(orc):
+    # test/internals/tests.jl:490-593: pairs through the periodic boundary, triclinic wrapping and a dense
+    # cluster at the boundaries, each pair counted once (cell lists against the naive loop)
+    x = np.array([[0.5, 5.0, 5.0], [9.6, 5.0, 5.0]])
+    assert orc.run("count", x, unitcell=[10.0] * 3, cutoff=2.0)["count"] == 1
+    uc = np.array([[10.0, 3.0, 0.0], [0.0, 10.0, 2.0], [0.0, 0.0, 10.0]])
+    x = np.array([[0.5, 0.5, 0.5], [2.0, 1.0, 1.0], [9.5, 9.5, 9.5], [8.5, 9.0, 9.0]])
+    kw = dict(kind="tri", unitcell=uc, cutoff=2.5)
+    assert orc.run("count", x, **kw)["count"] == orc.run("count", x, naive=True, **kw)["count"]
+    g = np.array([[0.3 * i, 0.3 * j, 0.3 * k] for i in range(1, 6) for j in range(1, 6) for k in range(1, 6)])
+    x = np.concatenate([g, 15.0 - g])
+    kw = dict(unitcell=[15.0] * 3, cutoff=2.5)
+    n = orc.run("count", x, **kw)["count"]
+    assert n == orc.run("count", x, naive=True, **kw)["count"]
+    nl = orc.run("nl", x, **kw)
+    a, b = np.minimum(nl["i"], nl["j"]), np.maximum(nl["i"], nl["j"])
+    assert len(set(zip(a.tolist(), b.tolist()))) == len(a) == n
+
+
+def test_margins_with_large_lcell(orc):
+    # test/internals/tests.jl:595-684: particles at cell corners with lcell up to 5, triclinic cells with
+    # lcell up to 3, and pairs just inside the cutoff across cell boundaries
+    rng = np.random.default_rng(55)
+    for lcell in [1, 2, 3, 5]:
+        sides = np.array([20.0] * 3)
+        x = list(rng.random((200, 3)) * sides)
+        cs = sides / (2 * lcell + 1)
+        for i in range(1, lcell + 2):
+            for j in range(1, lcell + 2):
+                for k in range(1, lcell + 2):
+                    c = np.array([cs[0] * i + 0.1, cs[1] * j + 0.1, cs[2] * k + 0.1])
+                    if np.all(c < sides):
+                        x.append(c)
+        x = np.array(x)
+        kw = dict(unitcell=list(sides), cutoff=2.5, lcell=lcell)
+        assert orc.run("sum_d", x, **kw)["scalar"] == pytest.approx(orc.run("sum_d", x, naive=True, **kw)["scalar"],
+                                                                    rel=1e-10)
+    uc = np.array([[15.0, 5.0, 0.0], [0.0, 15.0, 3.0], [0.0, 0.0, 15.0]])
+    for lcell in [1, 2, 3]:
+        x = rng.random((150, 3)) @ uc.T
+        kw = dict(kind="tri", unitcell=uc, cutoff=2.0, lcell=lcell)
+        assert orc.run("sum_d", x, **kw)["scalar"] == pytest.approx(orc.run("sum_d", x, naive=True, **kw)["scalar"],
+                                                                    rel=1e-10)
+    c = 3.0 - 0.001
+    x = np.array([[5.0, 5.0, 5.0], [5.0 + c, 5.0, 5.0], [10.0, 10.0, 10.0], [10.0, 10.0 + c, 10.0],
+                  [15.0, 15.0, 15.0], [15.0, 15.0, 15.0 + c]])
+    kw = dict(unitcell=[30.0] * 3, cutoff=3.0, lcell=3)
+    n = orc.run("count", x, **kw)["count"]
+    assert n == orc.run("count", x, naive=True, **kw)["count"] and n >= 3
