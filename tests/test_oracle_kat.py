@@ -264,11 +264,9 @@ def test_celllist_matches_naive(orc, dim, kind, uc, cut, lcell, n, cross):
     np.testing.assert_allclose(e1["forces_x"], e2["forces_x"], atol=1e-11 * max(1.0, np.abs(e2["forces_x"]).max()))
 
 
-def test_pathological_coordinates(orc):
+def _pathological(rng, n, sides):
     """test/modules/Testing.jl:36-60: points on faces, +-nextfloat(0), outside the box."""
-    rng = np.random.default_rng(5)
-    sides = np.array([250.0, 250.0, 250.0])
-    x = sides * rng.random((200, 3))
+    x = sides * rng.random((n, 3))
     x[0] = -sides / 2
     x[1] = -sides / 2 + [np.nextafter(0, 1), np.nextafter(0, 1), sides[2] * rng.random()]
     x[2] = -sides / 2 + [np.nextafter(0, -1), np.nextafter(0, -1), sides[2] * rng.random()]
@@ -281,6 +279,14 @@ def test_pathological_coordinates(orc):
     x[13] = [np.nextafter(0, -1), np.nextafter(0, -1), sides[2] * rng.random()]
     x[14] = 0.0
     x[99] = [sides[0] / 2, -sides[1] / 2, 2 * sides[2]]
+    return x
+
+
+def test_pathological_coordinates(orc):
+    """test/modules/Testing.jl:36-60: points on faces, +-nextfloat(0), outside the box."""
+    rng = np.random.default_rng(5)
+    sides = np.array([250.0, 250.0, 250.0])
+    x = _pathological(rng, 200, sides)
     for lcell in (1, 2):
         cl = orc.run("count", x, unitcell=sides, cutoff=10.0, lcell=lcell)
         nv = orc.run("count", x, unitcell=sides, cutoff=10.0, naive=True)
@@ -405,3 +411,17 @@ def test_margins_with_large_lcell(orc):
     kw = dict(unitcell=[30.0] * 3, cutoff=3.0, lcell=3)
     n = orc.run("count", x, **kw)["count"]
     assert n == orc.run("count", x, naive=True, **kw)["count"] and n >= 3
+
+
+def test_disjoint_sets_gravitational_potential(orc):
+    # test/internals/tests.jl:1-33: the gravitational potential between two pathological sets (masses
+    # indexed by each set's own index), lcell 1 and 3, against the naive loop
+    rng = np.random.default_rng(6)
+    sides = np.array([250.0, 250.0, 250.0])
+    x = _pathological(rng, 2000, sides)
+    y = _pathological(rng, 2000, sides) + 0.25  # no point of y on a point of x (1/d finite)
+    mass = rng.random(2000)
+    kw = dict(unitcell=sides, cutoff=10.0, params=[9.8], weights_x=mass, weights_y=mass)
+    naive = orc.run("weighted_inv_d", x, y, naive=True, **kw)["scalar"]
+    for lcell in (1, 3):
+        assert orc.run("weighted_inv_d", x, y, lcell=lcell, **kw)["scalar"] == pytest.approx(naive, rel=1e-12)
