@@ -425,3 +425,20 @@ def test_disjoint_sets_gravitational_potential(orc):
     naive = orc.run("weighted_inv_d", x, y, naive=True, **kw)["scalar"]
     for lcell in (1, 3):
         assert orc.run("weighted_inv_d", x, y, lcell=lcell, **kw)["scalar"] == pytest.approx(naive, rel=1e-12)
+
+
+def test_pathological_2d_cells(orc):
+    # test/modules/Testing.jl:563-599 (test_pathological2D, test/internals/tests.jl:700-702): two random
+    # points in 11 awkward 2D cells (sheared, rotated, negative determinant) for lcell 1..5, cell lists
+    # against the naive loop
+    l = np.sqrt(2) / 2
+    mats = [[[1, 0], [0, 1]], [[l, 0], [l, 1]], [[1.1, 0], [0, 1]], [[1.2, 0], [0, 1]], [[1, 0], [0, 1.1]],
+            [[1, 0], [0, 1.2]], [[1, 0.2], [0, 1.2]], [[1, 0.2], [0.2, 1.2]], [[1.2, 0.2], [0.2, 1.2]],
+            [[-1.2, 0.2], [0.2, 1.2]], [[-1.2, 0.2], [0.2, -1.2]]]
+    rng = np.random.default_rng(7)
+    for _ in range(200):
+        for M in mats:
+            for lcell in range(1, 6):
+                x = rng.random((2, 2))
+                kw = dict(dim=2, kind="tri", unitcell=M, cutoff=0.2, lcell=lcell)
+                assert orc.run("count", x, **kw)["count"] == orc.run("count", x, naive=True, **kw)["count"], (M, lcell, x)
