@@ -442,3 +442,33 @@ def test_pathological_2d_cells(orc):
                 x = rng.random((2, 2))
                 kw = dict(dim=2, kind="tri", unitcell=M, cutoff=0.2, lcell=lcell)
                 assert orc.run("count", x, **kw)["count"] == orc.run("count", x, naive=True, **kw)["count"], (M, lcell, x)
+
+
+@pytest.mark.parametrize("kind", ["ortho", "tri"])
+def test_random_cells_sweep(orc, kind):
+    # test/modules/Testing.jl:162-257 (test_random_cells, test/internals/tests.jl:686-698): random cells with
+    # entries in [-10, 10] (orthorhombic: the diagonal), cutoff in [1, 2], lcell 1..3, kept when they pass the
+    # unit-cell check; 10-20 points far outside the cell (wrapped in); cell lists against the naive loop
+    rng = np.random.default_rng(3 if kind == "ortho" else 4)
+    for dim in (2, 3):
+        for lcell in (1, 2, 3):
+            done = trials = 0
+            while done < 40 and trials < 3000:
+                trials += 1
+                M = np.diag(-10 + 20 * rng.random(dim)) if kind == "ortho" else -10 + 20 * rng.random((dim, dim))
+                uc = np.diag(M) if kind == "ortho" else M
+                cut = 1 + rng.random()
+                try:
+                    b = orc.box_info(dim=dim, kind=kind, unitcell=uc, cutoff=cut, lcell=lcell)
+                except orc.OracleError as e:
+                    assert e.code == 2  # only the unit-cell check may refuse a cell
+                    continue
+                if np.prod(b["nc"]) > 100000:
+                    continue
+                x = 10 * rng.random((int(rng.integers(10, 21)), dim)) - 50
+                kw = dict(dim=dim, kind=kind, unitcell=uc, cutoff=cut, lcell=lcell)
+                assert orc.run("count", x, **kw)["count"] == orc.run("count", x, naive=True, **kw)["count"]
+                assert orc.run("sum_d2", x, **kw)["scalar"] == pytest.approx(
+                    orc.run("sum_d2", x, naive=True, **kw)["scalar"], rel=1e-10, abs=1e-10)
+                done += 1
+            assert done == 40
