@@ -84,3 +84,34 @@ def test_host_geometry_matches_oracle(probe, orc, f64, dim, kind):
             np.testing.assert_array_equal(rinv.reshape(dim, dim, order="F"), b["inv_rotation"])
         checked += 1
     assert checked >= 20
+
+
+@pytest.mark.parametrize("f64", [True, False])
+@pytest.mark.parametrize("kind", ["ortho", "tri"])
+def test_host_geometry_random_sweep(probe, orc, f64, kind):
+    # the reference's random-cell sweep (test/modules/Testing.jl:162-257): entries in [-10, 10] (negative
+    # sides and left-handed cells included), cutoff in [1, 2]; accepted and refused cells and every field agree
+    rng = np.random.default_rng(60 + (1 if f64 else 0) + (2 if kind == "tri" else 0))
+    dtype = np.float64 if f64 else np.float32
+    accepted = 0
+    for _ in range(300):
+        dim = int(rng.integers(2, 4))
+        M = np.diag(-10 + 20 * rng.random(dim)) if kind == "ortho" else -10 + 20 * rng.random((dim, dim))
+        cutoff, lcell = float(1 + rng.random()), int(rng.integers(1, 4))
+        st, nc, (cs, lo, hi, mal, rot, rinv) = product_box(probe, M, dim, kind, cutoff, lcell, f64)
+        try:
+            b = orc.box_info(dim=dim, kind=kind, unitcell=np.diag(M) if kind == "ortho" else M, cutoff=cutoff,
+                             lcell=lcell, dtype=dtype)
+        except orc.OracleError as e:
+            assert st == e.code
+            continue
+        assert st == 0
+        np.testing.assert_array_equal(nc, b["nc"])
+        np.testing.assert_array_equal(cs, b["cell_size"])
+        np.testing.assert_array_equal(lo, b["computing_box"][0])
+        np.testing.assert_array_equal(hi, b["computing_box"][1])
+        if kind == "tri":
+            np.testing.assert_array_equal(mal.reshape(dim, dim, order="F"), b["aligned_unit_cell"])
+            np.testing.assert_array_equal(rot.reshape(dim, dim, order="F"), b["rotation"])
+        accepted += 1
+    assert accepted >= 50
