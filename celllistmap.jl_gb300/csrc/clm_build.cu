@@ -27,6 +27,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "clm_build_steps.cuh"
 #include "clm_internal.hpp"
 
 namespace clm {
@@ -264,92 +265,7 @@ __global__ void __launch_bounds__(kBlock) k_rs_scatter(const uint32_t* __restric
 }
 
 // ------------------------------------------------------------------ K1: wrap, images, copy count
-// Returns false if the particle has a NaN coordinate (it then gets no copy).
-template <class T, int N>
-__device__ __forceinline__ bool wrap_count_at(const DevGeom<T>& g, const T* __restrict__ x, int i,
-                                              T* __restrict__ wrapped, uint32_t* __restrict__ mask,
-                                              int* __restrict__ ncopy) {
-  T xi[N];
-  bool bad = false;
-#pragma unroll
-  for (int k = 0; k < N; k++) {
-    xi[k] = x[(int64_t)i * N + k];
-    bad = bad || isnan(xi[k]);
-  }
-  if (bad) {
-#pragma unroll
-    for (int k = 0; k < N; k++) wrapped[(int64_t)i * N + k] = T(0);
-    mask[i] = 0;
-    ncopy[i] = 0;
-    return false;
-  }
-  T p[N];
-  if (g.kind == NONPERIODIC) {
-#pragma unroll
-    for (int k = 0; k < N; k++) p[k] = xi[k];
-  } else {
-    wrap_point<T, N>(g, xi, p);
-  }
-#pragma unroll
-  for (int k = 0; k < N; k++) wrapped[(int64_t)i * N + k] = p[k];
-  uint32_t m = 0;
-  int cnt = 1;
-  if (g.kind != NONPERIODIC && g.img_tree) {
-    // image k = (s0+1) + 3(s1+1) [+ 9(s2+1)]: the last component is tested once per s_last, the next
-    // once per (s_mid, s_last), the first per image; each test uses the shift of the image itself
-    // (equal, for the components tested early, across the images that share their s values)
-#pragma unroll
-    for (int sl = -1; sl <= 1; sl++) {
-      const int kl = (N == 3) ? 9 * (sl + 1) + 4 : 3 * (sl + 1) + 1;
-      const T ql = xadd(p[N - 1], g.shift[kl][N - 1]);
-      if (!(g.cbmin[N - 1] <= ql && ql < g.cbmax[N - 1])) continue;
-      if (N == 3) {
-#pragma unroll
-        for (int sm = -1; sm <= 1; sm++) {
-          const int km = 9 * (sl + 1) + 3 * (sm + 1) + 1;
-          const T qm = xadd(p[1], g.shift[km][1]);
-          if (!(g.cbmin[1] <= qm && qm < g.cbmax[1])) continue;
-#pragma unroll
-          for (int s0 = -1; s0 <= 1; s0++) {
-            const int k = 9 * (sl + 1) + 3 * (sm + 1) + (s0 + 1);
-            if (k == g.zero_code) continue;
-            const T q0 = xadd(p[0], g.shift[k][0]);
-            if (g.cbmin[0] <= q0 && q0 < g.cbmax[0]) {
-              m |= 1u << k;
-              cnt++;
-            }
-          }
-        }
-      } else {
-#pragma unroll
-        for (int s0 = -1; s0 <= 1; s0++) {
-          const int k = 3 * (sl + 1) + (s0 + 1);
-          if (k == g.zero_code) continue;
-          const T q0 = xadd(p[0], g.shift[k][0]);
-          if (g.cbmin[0] <= q0 && q0 < g.cbmax[0]) {
-            m |= 1u << k;
-            cnt++;
-          }
-        }
-      }
-    }
-  } else if (g.kind != NONPERIODIC) {
-    for (int k = 0; k < g.nimg; k++) {
-      if (k == g.zero_code) continue;
-      T q[N];
-#pragma unroll
-      for (int d = 0; d < N; d++) q[d] = xadd(p[d], g.shift[k][d]);
-      if (in_box<T, N>(g, q)) {
-        m |= 1u << k;
-        cnt++;
-      }
-    }
-  }
-  mask[i] = m;
-  ncopy[i] = cnt;
-  return true;
-}
-
+// (the per-particle step, wrap_count_at, is in clm_build_steps.cuh)
 template <class T, int N>
 __global__ void __launch_bounds__(kBlock) k_wrap_count(DevGeom<T> g, const T* __restrict__ x, int n,
                                                        T* __restrict__ wrapped, uint32_t* __restrict__ mask,
@@ -381,49 +297,6 @@ __global__ void __launch_bounds__(kBlock) k_wrap_count_b(const DevGeom<T>* __res
 }
 
 // ------------------------------------------------------------------ K2: keys, histogram, real flags
-// `cb` is the first global cell of the particle's system (0 for one system).
-template <class T, int N>
-__device__ __forceinline__ void emit_at(const DevGeom<T>& g, int cb, const T* __restrict__ wrapped,
-                                        const uint32_t* __restrict__ mask, const int* __restrict__ ncopy,
-                                        const int* __restrict__ copy_off, int i, int cap, uint32_t* __restrict__ keys,
-                                        uint32_t* __restrict__ vals, int* __restrict__ err) {
-  if (ncopy[i] == 0) return;
-  int base = copy_off[i];
-  if (base < 0 || base + ncopy[i] > cap) {
-    atomicOr(err, DERR_COPY_OVERFLOW);
-    return;
-  }
-  T p[N];
-#pragma unroll
-  for (int k = 0; k < N; k++) p[k] = wrapped[(int64_t)i * N + k];
-  int li = cell_of<T, N>(g, p, true);
-  if (li < 0) {
-    atomicOr(err, DERR_CELL_RANGE);
-    li = 0;
-  }
-  li += cb;
-  keys[base] = (uint32_t)li;
-  vals[base] = ((uint32_t)i << 5) | (uint32_t)g.zero_code;
-  int t = 1;
-  uint32_t m = mask[i];
-  while (m) {
-    int k = __ffs(m) - 1;
-    m &= m - 1;
-    T q[N];
-#pragma unroll
-    for (int d = 0; d < N; d++) q[d] = xadd(p[d], g.shift[k][d]);
-    int lk = cell_of<T, N>(g, q, false);
-    if (lk < 0) {
-      atomicOr(err, DERR_CELL_RANGE);
-      lk = 0;
-    }
-    lk += cb;
-    keys[base + t] = (uint32_t)lk;
-    vals[base + t] = ((uint32_t)i << 5) | (uint32_t)k;
-    t++;
-  }
-}
-
 template <class T, int N>
 __global__ void __launch_bounds__(kBlock) k_emit(DevGeom<T> g, const T* __restrict__ wrapped,
                                                  const uint32_t* __restrict__ mask, const int* __restrict__ ncopy,
@@ -449,67 +322,6 @@ __global__ void __launch_bounds__(kBlock) k_emit_b(const DevGeom<T>* __restrict_
 }
 
 // ------------------------------------------------------------------ K4: gather in cell order
-// origin of cell c along one axis as an unevaluated float pair (hi + lo): cbmin + cs*(c-1) with the
-// product and the sum carried exactly (TwoProduct with an FMA, TwoSum)
-__device__ __forceinline__ void origin_ff(float cb_hi, float cb_lo, float cs_hi, float cs_lo, int c1, float& hi,
-                                          float& lo) {
-  const float k = (float)c1;
-  const float p = cs_hi * k;
-  const float pe = fmaf(cs_hi, k, -p) + cs_lo * k;
-  const float s = cb_hi + p;
-  const float bb = s - cb_hi;
-  const float se = (cb_hi - (s - bb)) + (p - bb);
-  hi = s;
-  lo = se + pe + cb_lo;
-}
-
-// cell_start from the keys sorted by cell: copy t writes the starts of the cells between the previous
-// copy's cell (exclusive) and its own (inclusive); t = n closes the list up to ncells.
-__device__ __forceinline__ void cell_starts_at(const uint32_t* __restrict__ skeys, int t, int n, int ncells,
-                                               int* __restrict__ cell_start) {
-  const int lo = (t == 0) ? 0 : (int)skeys[t - 1] + 1;
-  const int hi = (t == n) ? ncells : (int)skeys[t];
-  for (int c = lo; c <= hi && c <= ncells; c++) cell_start[c] = t;
-}
-
-// Copy t of the sorted list: particle p, image k, in the cell `li` (local index of its system).
-template <class T, int N>
-__device__ __forceinline__ void gather_at(const DevGeom<T>& g, const T* __restrict__ wrapped, int t, int p, int k,
-                                          int li, T* __restrict__ px, T* __restrict__ py, T* __restrict__ pz,
-                                          float4* __restrict__ off, float4* __restrict__ xq,
-                                          int* __restrict__ code, int* __restrict__ cell_flags, int cb) {
-  T q[N];
-#pragma unroll
-  for (int d = 0; d < N; d++) {
-    T w = wrapped[(int64_t)p * N + d];
-    q[d] = (k == g.zero_code) ? w : xadd(w, g.shift[k][d]);
-  }
-  const int pc = (k == g.zero_code) ? p : -(p + 1);
-  px[t] = q[0];
-  py[t] = q[1];
-  if (N == 3) pz[t] = q[N - 1];
-  if constexpr (std::is_same<T, float>::value) {
-    // Float32 handles test the coordinates themselves (no cell-relative offsets are read)
-    xq[t] = make_float4((float)q[0], (float)q[1], N == 3 ? (float)q[N - 1] : 0.f, __int_as_float(pc));
-  } else {
-    int c[3];
-    cart_of(li, g.nc, N, c);
-    float o[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-    for (int d = 0; d < N; d++) {
-      // FP32 offset of the copy from its cell origin, all in float pairs: (qh + ql) - (oh + ol)
-      float oh, ol;
-      origin_ff(g.cbf_hi[d], g.cbf_lo[d], g.csf[d], g.csf_lo[d], c[d] - 1, oh, ol);
-      const float qh = (float)q[d];
-      const float ql = (float)(q[d] - (T)qh);
-      o[d] = (qh - oh) + (ql - ol);
-    }
-    off[t] = make_float4(o[0], o[1], o[2], __int_as_float(pc));
-  }
-  code[t] = pc;
-  if (k == g.zero_code) cell_flags[cb + li] = 1;  // the cell holds a real particle
-}
-
 template <class T, int N>
 __global__ void __launch_bounds__(kBlock) k_gather(DevGeom<T> g, const T* __restrict__ wrapped,
                                                    const uint32_t* __restrict__ skeys,
@@ -650,60 +462,6 @@ int scan_exclusive(Handle& h, const int* in, int* out, int64_t m, int* total, in
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
   return OK;
-}
-
-template <class T> void fill_devgeom(const Geometry<T>& g, int precision, DevGeom<T>& d) {
-  std::memset(&d, 0, sizeof(d));
-  (void)precision;
-  d.dim = g.dim;
-  d.kind = g.kind;
-  d.lcell = g.lcell;
-  d.ncells = (int)g.ncells();
-  for (int i = 0; i < 3; i++) {
-    d.nc[i] = (int)g.nc[i];
-    d.cbmin[i] = g.cbmin[i];
-    d.cbmax[i] = g.cbmax[i];
-    d.cs[i] = g.cs[i];
-    d.csf[i] = (float)g.cs[i];
-    d.csf_lo[i] = (float)((double)g.cs[i] - (double)d.csf[i]);
-    d.cbf_hi[i] = (float)g.cbmin[i];
-    d.cbf_lo[i] = (float)((double)g.cbmin[i] - (double)d.cbf_hi[i]);
-    for (int j = 0; j < 3; j++) {
-      d.Min[i][j] = g.Min[i][j];
-      d.R[i][j] = g.R[i][j];
-      d.Rinv[i][j] = g.Rinv[i][j];
-    }
-  }
-  d.det_in = g.det_in;
-  d.cutoff = g.cutoff;
-  d.cutoff_sqr = g.cutoff_sqr;
-  d.margin_wide = (double)g.cutoff * (1.0 + std::sqrt((double)g.dim) / 2.0);
-  d.nimg = (g.dim == 3) ? 27 : 9;
-  // with exact zeros below the diagonal, component i of an image shift depends only on s_i..s_dim-1, so
-  // the image tests can run dimension by dimension from the last one (same values, fewer tests)
-  d.img_tree = 1;
-  for (int i = 0; i < g.dim; i++)
-    for (int j = 0; j < i; j++)
-      if (g.Mal[i][j] != T(0)) d.img_tree = 0;
-  d.zero_code = (g.dim == 3) ? 13 : 4;
-  // translation_image: x + Mal * s, s in {-1,0,1}^N with the first index fastest
-  for (int k = 0; k < d.nimg; k++) {
-    int s[3], kk = k;
-    for (int i = 0; i < g.dim; i++) {
-      s[i] = kk % 3 - 1;
-      kk /= 3;
-    }
-    for (int i = 0; i < g.dim; i++) {
-      T acc = g.Mal[i][0] * T(s[0]);
-      for (int j = 1; j < g.dim; j++) acc = acc + g.Mal[i][j] * T(s[j]);
-      d.shift[k][i] = acc;
-    }
-  }
-  // FP32 prefilter band around cutoff^2 (relative 2^-13, far above the FP32
-  // error of d2 computed from cell-relative offsets, ~2^-18 relative).
-  double c2 = (double)g.cutoff_sqr;
-  d.thr_hi = std::nextafter((float)(c2 * (1.0 + std::ldexp(1.0, -13))), INFINITY);
-  d.thr_lo = std::nextafter((float)(c2 * (1.0 - std::ldexp(1.0, -13))), 0.0f);
 }
 
 template <class T> int set_limits(Handle& h, T* lo, T* hi) {

@@ -6,22 +6,40 @@
 // (Julia does not contract a*b+c).  The FP32 prefilter in the pair kernels is
 // free to use FMAs: it only decides which pairs get an exact re-test.
 #pragma once
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 
 namespace clm {
 
 // ---------------------------------------------------------------- exact arithmetic
-__device__ __forceinline__ double xadd(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ double xsub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double xmul(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ double xdiv(double a, double b) { return __ddiv_rn(a, b); }
-__device__ __forceinline__ double xsqrt(double a) { return __dsqrt_rn(a); }
-__device__ __forceinline__ float xadd(float a, float b) { return __fadd_rn(a, b); }
-__device__ __forceinline__ float xsub(float a, float b) { return __fsub_rn(a, b); }
-__device__ __forceinline__ float xmul(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ float xdiv(float a, float b) { return __fdiv_rn(a, b); }
-__device__ __forceinline__ float xsqrt(float a) { return __fsqrt_rn(a); }
+// On the device the _rn intrinsics; on the host (the CPU tests compile the geometry helpers below with
+// -ffp-contract=off) the plain IEEE operations, which round the same way.
+#ifdef __CUDA_ARCH__
+#define CLM_XOP(name, T, expr_dev, expr_host) \
+  __host__ __device__ __forceinline__ T name(T a, T b) { return expr_dev; }
+#else
+#define CLM_XOP(name, T, expr_dev, expr_host) \
+  __host__ __device__ __forceinline__ T name(T a, T b) { return expr_host; }
+#endif
+CLM_XOP(xadd, double, __dadd_rn(a, b), a + b)
+CLM_XOP(xsub, double, __dsub_rn(a, b), a - b)
+CLM_XOP(xmul, double, __dmul_rn(a, b), a * b)
+CLM_XOP(xdiv, double, __ddiv_rn(a, b), a / b)
+CLM_XOP(xadd, float, __fadd_rn(a, b), a + b)
+CLM_XOP(xsub, float, __fsub_rn(a, b), a - b)
+CLM_XOP(xmul, float, __fmul_rn(a, b), a * b)
+CLM_XOP(xdiv, float, __fdiv_rn(a, b), a / b)
+#undef CLM_XOP
+#ifdef __CUDA_ARCH__
+__host__ __device__ __forceinline__ double xsqrt(double a) { return __dsqrt_rn(a); }
+__host__ __device__ __forceinline__ float xsqrt(float a) { return __fsqrt_rn(a); }
+template <class T> __host__ __device__ __forceinline__ T xfloor(T a) { return floor(a); }
+#else
+__host__ __device__ __forceinline__ double xsqrt(double a) { return std::sqrt(a); }
+__host__ __device__ __forceinline__ float xsqrt(float a) { return std::sqrt(a); }
+template <class T> __host__ __device__ __forceinline__ T xfloor(T a) { return std::floor(a); }
+#endif
 
 // ---------------------------------------------------------------- geometry on device
 constexpr int kMaxDim = 3;
@@ -49,7 +67,7 @@ template <class T> struct DevGeom {
 
 // StaticArrays solve (Cramer form), then fastmod1, boundary -> 0, then M*p and R*(.)
 template <class T, int N>
-__device__ __forceinline__ void wrap_point(const DevGeom<T>& g, const T* x, T* out) {
+__host__ __device__ __forceinline__ void wrap_point(const DevGeom<T>& g, const T* x, T* out) {
   T p[N];
   const auto& a = g.Min;
   if constexpr (N == 3) {
@@ -71,7 +89,7 @@ __device__ __forceinline__ void wrap_point(const DevGeom<T>& g, const T* x, T* o
   }
 #pragma unroll
   for (int i = 0; i < N; i++) {
-    p[i] = xsub(p[i], floor(p[i]));
+    p[i] = xsub(p[i], xfloor(p[i]));
     if (p[i] == T(1)) p[i] = T(0);
   }
   T w[N];
@@ -92,7 +110,7 @@ __device__ __forceinline__ void wrap_point(const DevGeom<T>& g, const T* x, T* o
 }
 
 template <class T, int N>
-__device__ __forceinline__ bool in_box(const DevGeom<T>& g, const T* x) {
+__host__ __device__ __forceinline__ bool in_box(const DevGeom<T>& g, const T* x) {
   bool ok = true;
 #pragma unroll
   for (int i = 0; i < N; i++) ok = ok && (g.cbmin[i] <= x[i]) && (x[i] < g.cbmax[i]);
@@ -103,14 +121,14 @@ __device__ __forceinline__ bool in_box(const DevGeom<T>& g, const T* x) {
 // (src/internals/Box.jl:499-508, src/internals/CellLists.jl:956-967).  Returns
 // the 0-based linear cell index, or -1 if the cell is outside the grid.
 template <class T, int N>
-__device__ __forceinline__ int cell_of(const DevGeom<T>& g, const T* x, bool real) {
+__host__ __device__ __forceinline__ int cell_of(const DevGeom<T>& g, const T* x, bool real) {
   int li = 0;
 #pragma unroll
   for (int i = N - 1; i >= 0; i--) {
     T q = xdiv(xsub(x[i], g.cbmin[i]), g.cs[i]);
     // floor in the handle dtype (exact; cell indices are far below 2^24), which keeps Float32 builds off
     // GB300's slow FP64 pipe
-    const T fq = floor(q);
+    const T fq = xfloor(q);
     if (!(fq >= T(-1) && fq < (T)g.nc[i])) return -1;
     int c = (int)fq + 1;
     if (real) {
@@ -123,7 +141,7 @@ __device__ __forceinline__ int cell_of(const DevGeom<T>& g, const T* x, bool rea
   return li;
 }
 
-__device__ __forceinline__ void cart_of(int li, const int* nc, int dim, int* c) {
+__host__ __device__ __forceinline__ void cart_of(int li, const int* nc, int dim, int* c) {
   c[0] = li % nc[0] + 1;
   int r = li / nc[0];
   if (dim == 3) {
@@ -137,7 +155,7 @@ __device__ __forceinline__ void cart_of(int li, const int* nc, int dim, int* c) 
 
 // cell_center (src/internals/Box.jl:517-525)
 template <class T, int N>
-__device__ __forceinline__ void cell_center(const DevGeom<T>& g, const int* c, T* ctr) {
+__host__ __device__ __forceinline__ void cell_center(const DevGeom<T>& g, const int* c, T* ctr) {
 #pragma unroll
   for (int i = 0; i < N; i++) ctr[i] = xsub(xadd(g.cbmin[i], xmul(g.cs[i], (T)c[i])), xmul(g.cs[i], T(0.5)));  // cs/2 exactly
 }

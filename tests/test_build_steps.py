@@ -1,0 +1,226 @@
+"""CPU parity of the library's cell-list build steps with the oracle's serial cell list.
+
+tests/build_probe.cpp compiles the per-particle and per-copy steps the build kernels run on the device
+(csrc/clm_build_steps.cuh: the device geometry, wrap into the first cell and image tests, the cell keys of
+each copy, the gather of the copy coordinates in cell order) for the host and drives them one particle at a
+time.  The copies, their cells (with the border-case shift of real particles), their in-cell order, realness
+and coordinates must equal the oracle's (src/internals/CellLists.jl:727-1057, Box.jl:499-566) bit for bit, in
+Float64 and Float32, for orthorhombic, triclinic and non-periodic boxes in 2D and 3D, and over the
+reference's pathological coordinates and random cells (test/modules/Testing.jl:36-60, 162-257).  These run
+without a GPU; the GPU tests check the same lists built by the kernels themselves.
+"""
+import ctypes as C
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from tests.conftest import ROOT
+
+KINDS = {"ortho": 0, "tri": 1, "nonperiodic": 2}
+DERR_NAN = 1
+
+
+@pytest.fixture(scope="module")
+def probe(tmp_path_factory):
+    cxx = shutil.which("g++") or shutil.which("c++")
+    cuda_inc = None
+    for cand in (os.environ.get("CUDA_HOME", ""), "/usr/local/cuda"):
+        if cand and os.path.exists(os.path.join(cand, "include", "cuda_runtime.h")):
+            cuda_inc = os.path.join(cand, "include")
+            break
+    if cxx is None or cuda_inc is None:
+        pytest.skip("no C++ compiler or CUDA headers")
+    out = str(tmp_path_factory.mktemp("build_steps") / "libbuild_probe.so")
+    cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-I", cuda_inc,
+           "-I", os.path.join(ROOT, "celllistmap.jl_gb300", "csrc"), os.path.join(ROOT, "tests", "build_probe.cpp"),
+           "-o", out]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lib = C.CDLL(out)
+    lib.build_probe.restype = C.c_int
+    return lib
+
+
+def kind_of(uc):
+    if uc is None:
+        return "nonperiodic"
+    return "ortho" if np.asarray(uc).ndim == 1 else "tri"
+
+
+def host_celllist(lib, x, dim, kind, unitcell, cutoff, lcell, dtype):
+    """Cell list from the library's build steps run on the host: same fields as the oracle's celllist()."""
+    x = np.ascontiguousarray(np.asarray(x, dtype).astype(np.float64)).reshape(-1, dim)
+    n = x.shape[0]
+    if unitcell is None:
+        Mc = np.zeros(dim * dim)
+    else:
+        uc = np.asarray(unitcell, np.float64)
+        M = np.diag(uc) if uc.ndim == 1 else uc.reshape(dim, dim)
+        Mc = np.ascontiguousarray(M.flatten(order="F"))
+    f64 = int(np.dtype(dtype) == np.float64)
+    ncopy, nreal, err = C.c_int64(0), C.c_int64(0), C.c_int(0)
+    vp = C.c_void_p
+
+    def call(cap, *arrs):
+        return lib.build_probe(f64, dim, KINDS[kind], Mc.ctypes.data_as(vp), C.c_double(cutoff), lcell,
+                               x.ctypes.data_as(vp), n, C.c_int64(cap), C.byref(ncopy), C.byref(nreal),
+                               *[a.ctypes.data_as(vp) if a is not None else None for a in arrs], C.byref(err))
+
+    st = call(0, None, None, None, None)
+    if st:
+        return st, None
+    m = ncopy.value
+    cell, idx = np.zeros(m, np.int64), np.zeros(m, np.int64)
+    real, coords = np.zeros(m, np.int8), np.zeros((m, dim), np.float64)
+    st = call(m, cell, idx, real, coords)
+    assert st == 0, st
+    return 0, {"cell": cell, "index": idx, "real": real.astype(bool), "coords": coords,
+               "n_cells_with_real": nreal.value, "err": err.value}
+
+
+def assert_same_celllist(got, ref):
+    assert got["err"] == 0
+    assert len(got["cell"]) == len(ref["cell"])
+    np.testing.assert_array_equal(got["cell"], ref["cell"])
+    np.testing.assert_array_equal(got["index"], ref["index"])
+    np.testing.assert_array_equal(got["real"], ref["real"])
+    np.testing.assert_array_equal(got["coords"], ref["coords"])
+    assert got["n_cells_with_real"] == ref["n_cells_with_real"]
+
+
+CASES = [
+    # dim, unitcell, cutoff, lcell, n, span, shift
+    (3, [10.0, 12.0, 11.0], 1.5, 1, 3000, 12.0, -1.0),
+    (3, [10.0, 12.0, 11.0], 1.5, 2, 3000, 12.0, -1.0),
+    (3, [10.0, 12.0, 11.0], 1.5, 3, 1000, 40.0, -20.0),
+    (3, [[10.0, 2.0, 1.0], [0.0, 11.0, 1.5], [0.0, 0.0, 12.0]], 1.5, 1, 3000, 12.0, -1.0),
+    (3, [[10.0, 2.0, 1.0], [0.0, 11.0, 1.5], [0.0, 0.0, 12.0]], 1.5, 3, 2000, 12.0, -1.0),
+    (3, [[9.0, 0.5, -1.0], [1.0, 11.0, 0.5], [-0.5, 1.5, 12.0]], 2.0, 2, 2000, 30.0, -15.0),
+    (3, None, 1.5, 1, 3000, 12.0, -1.0),
+    (3, None, 1.5, 2, 2000, 12.0, -1.0),
+    (2, [10.0, 12.0], 1.2, 1, 2000, 12.0, -1.0),
+    (2, [[10.0, 3.0], [0.0, 11.0]], 1.2, 2, 2000, 12.0, -1.0),
+    (2, [[10.0, 3.0], [1.0, 11.0]], 1.2, 1, 2000, 30.0, -15.0),
+    (2, None, 1.2, 1, 2000, 12.0, -1.0),
+]
+
+
+def case_id(c):
+    dim, uc, cut, lcell, n, span, shift = c
+    return f"{dim}d-{kind_of(uc)}-lcell{lcell}-span{span:g}"
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("case", CASES, ids=case_id)
+def test_build_steps_match_oracle(probe, orc, case, dtype):
+    dim, uc, cut, lcell, n, span, shift = case
+    rng = np.random.default_rng(11 + lcell + dim)
+    x = (rng.random((n, dim)) * span + shift).astype(dtype)
+    kw = dict(dim=dim, kind=kind_of(uc), unitcell=uc, cutoff=cut, lcell=lcell, dtype=dtype)
+    st, got = host_celllist(probe, x, dim, kind_of(uc), uc, cut, lcell, dtype)
+    assert st == 0
+    assert_same_celllist(got, orc.celllist(x, **kw))
+
+
+def _pathological(rng, n, sides):
+    # test/modules/Testing.jl:36-60: points on faces, +-nextfloat(0), outside the box
+    x = sides * rng.random((n, 3))
+    tiny, mtiny = np.nextafter(0, 1), np.nextafter(0, -1)
+    x[0] = -sides / 2
+    x[1] = -sides / 2 + [tiny, tiny, sides[2] * rng.random()]
+    x[2] = -sides / 2 + [mtiny, mtiny, sides[2] * rng.random()]
+    x[3] = sides / 2 + [tiny, tiny, sides[2] * rng.random()]
+    x[4] = sides / 2 + [mtiny, mtiny, sides[2] * rng.random()]
+    x[9] = sides
+    x[10] = sides + [tiny, tiny, sides[2] * rng.random()]
+    x[11] = sides + [mtiny, mtiny, sides[2] * rng.random()]
+    x[12] = [tiny, tiny, sides[2] * rng.random()]
+    x[13] = [mtiny, mtiny, sides[2] * rng.random()]
+    x[14] = 0.0
+    x[99] = [sides[0] / 2, -sides[1] / 2, 2 * sides[2]]
+    return x
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("lcell", [1, 2])
+def test_pathological_coordinates(probe, orc, lcell, dtype):
+    rng = np.random.default_rng(5)
+    sides = np.array([250.0, 250.0, 250.0])
+    x = _pathological(rng, 200, sides).astype(dtype)
+    for uc in (sides, np.array([[250.0, 30.0, 10.0], [0.0, 250.0, 20.0], [0.0, 0.0, 250.0]])):
+        kind = kind_of(uc)
+        st, got = host_celllist(probe, x, 3, kind, uc, 10.0, lcell, dtype)
+        assert st == 0
+        assert_same_celllist(got, orc.celllist(x, dim=3, kind=kind, unitcell=uc, cutoff=10.0, lcell=lcell,
+                                               dtype=dtype))
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_particles_on_cell_boundaries(probe, orc, dtype):
+    # every particle on a cell face, an edge or a corner of the cell grid (and on the unit-cell faces): the
+    # border cases of the cell index and of the image tests
+    side, cut = 12.0, 1.5
+    g = np.arange(0.0, side + 1e-9, cut / 2)
+    pts = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    x = np.concatenate([pts, pts - side, pts + 0.5 * side]).astype(dtype)
+    for lcell in (1, 2, 3):
+        for uc in ([side, side, side], [[side, 3.0, 0.0], [0.0, side, 3.0], [0.0, 0.0, side]]):
+            kind = kind_of(uc)
+            st, got = host_celllist(probe, x, 3, kind, uc, cut, lcell, dtype)
+            assert st == 0
+            assert_same_celllist(got, orc.celllist(x, dim=3, kind=kind, unitcell=uc, cutoff=cut, lcell=lcell,
+                                                   dtype=dtype))
+
+
+@pytest.mark.parametrize("kind", ["ortho", "tri"])
+def test_random_cells_sweep(probe, orc, kind):
+    # test/modules/Testing.jl:162-257: random cells with entries in [-10, 10] (negative sides, left-handed
+    # cells), cutoff in [1, 2], lcell 1..3, 10-20 points far outside the cell; the cells the oracle refuses the
+    # library's geometry refuses with the same code
+    rng = np.random.default_rng(21 if kind == "ortho" else 22)
+    done = 0
+    for trial in range(2000):
+        dim = int(rng.integers(2, 4))
+        lcell = int(rng.integers(1, 4))
+        M = np.diag(-10 + 20 * rng.random(dim)) if kind == "ortho" else -10 + 20 * rng.random((dim, dim))
+        uc = np.diag(M) if kind == "ortho" else M
+        cut = float(1 + rng.random())
+        dtype = np.float64 if trial % 2 == 0 else np.float32
+        x = (10 * rng.random((int(rng.integers(10, 21)), dim)) - 50).astype(dtype)
+        kw = dict(dim=dim, kind=kind, unitcell=uc, cutoff=cut, lcell=lcell, dtype=dtype)
+        try:
+            b = orc.box_info(**kw)
+        except orc.OracleError as e:
+            st, _ = host_celllist(probe, x, dim, kind, uc, cut, lcell, dtype)
+            assert st == e.code
+            continue
+        if np.prod(b["nc"]) > 200000:
+            continue
+        st, got = host_celllist(probe, x, dim, kind, uc, cut, lcell, dtype)
+        assert st == 0
+        assert_same_celllist(got, orc.celllist(x, **kw))
+        done += 1
+        if done == 150:
+            break
+    assert done == 150
+
+
+def test_nan_particle_gets_no_copy(probe):
+    # a NaN coordinate is flagged and the particle gets no copy (the library then reports the reference's
+    # "Invalid coordinates found (NaN)" error instead of returning the list)
+    rng = np.random.default_rng(2)
+    x = rng.random((50, 3)) * 10.0
+    x[7, 1] = np.nan
+    st, got = host_celllist(probe, x, 3, "ortho", [10.0, 10.0, 10.0], 1.0, 1, np.float64)
+    assert st == 0
+    assert got["err"] & DERR_NAN
+    assert 7 not in set(got["index"].tolist())
+
+
+def test_empty_set(probe):
+    st, got = host_celllist(probe, np.zeros((0, 3)), 3, "ortho", [10.0, 10.0, 10.0], 1.0, 1, np.float64)
+    assert st == 0
+    assert len(got["cell"]) == 0 and got["n_cells_with_real"] == 0
