@@ -26,6 +26,13 @@ def test_library_exports_every_declared_symbol(clm):
         assert hasattr(lib, name), name
 
 
+def test_julia_binding_covers_every_declared_symbol():
+    # the reference-side binding (ccall stubs of a Julia package extension) names every entry point
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    bound = set(re.findall(r"ccall\(\(:(clm_[a-z_0-9]+)\s*,", doc))
+    assert sorted(bound) == declared_symbols()
+
+
 def test_version_string(clm):
     lib = clm._abi.load()
     assert b"sm_103a" in lib.clm_version()
