@@ -117,7 +117,9 @@ template <class T> int build_all(Handle& h, bool sync) {
     if (st) return st;
     if (!overflow) return OK;
   }
-  return fail(&h, ERR_INTERNAL, "cell-list build did not converge on a copy capacity");
+  return fail(&h, ERR_INTERNAL,
+              "cell-list build did not converge on a copy capacity (particles and their periodic images may exceed "
+              "2^31 - 1)");
 }
 
 int build_dispatch(Handle& h, bool sync = true) {

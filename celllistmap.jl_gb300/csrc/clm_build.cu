@@ -706,6 +706,12 @@ int check_build_totals(Handle& h, bool* overflow) {
   for (int s = 0; s < h.nsets; s++) {
     SetData& S = h.sets[s];
     if (!S.pending) continue;
+    if (h.pinned[32 + 2 * s] < 0) {  // the 32-bit copy-offset scan wrapped: more than 2^31 - 1 copies
+      S.pending = false;
+      S.dirty = true;
+      h.last_error = "too many particle copies for one set (particles and their periodic images exceed 2^31 - 1)";
+      return ERR_ARG;
+    }
     S.n_copies = h.pinned[32 + 2 * s];
     S.n_real_cells = h.pinned[33 + 2 * s];
     S.pending = false;
