@@ -160,6 +160,53 @@ __host__ __device__ __forceinline__ void cell_center(const DevGeom<T>& g, const 
   for (int i = 0; i < N; i++) ctr[i] = xsub(xadd(g.cbmin[i], xmul(g.cs[i], (T)c[i])), xmul(g.cs[i], T(0.5)));  // cs/2 exactly
 }
 
+// Offset of the k-th cell of the stencil around a cell, in the reference's enumeration order: the forward
+// half stencil neighbor_cells_forward (CartesianIndices (1:l, -l:l, -l:l), then (0, 1:l, -l:l), then
+// (0, 0, 1:l), first index fastest; 2D likewise) or all neighbours neighbor_cells (-l:l in every dimension,
+// the cell itself left out), src/internals/Box.jl:436-474.
+template <int LC = 0>
+__host__ __device__ __forceinline__ void stencil_offset(bool forward, int l_rt, int dim, int k, int* o) {
+  const int l = LC ? LC : l_rt;  // LC: lcell fixed at compile time (constant divisors)
+  const int w = 2 * l + 1;
+  o[2] = 0;
+  if (forward) {
+    if (dim == 3) {
+      const int nA = l * w * w, nB = l * w;
+      if (k < nA) {
+        o[0] = 1 + k % l;
+        int r = k / l;
+        o[1] = r % w - l;
+        o[2] = r / w - l;
+      } else if (k < nA + nB) {
+        int k2 = k - nA;
+        o[0] = 0;
+        o[1] = 1 + k2 % l;
+        o[2] = k2 / l - l;
+      } else {
+        o[0] = 0;
+        o[1] = 0;
+        o[2] = 1 + (k - nA - nB);
+      }
+    } else {
+      const int nA = l * w;
+      if (k < nA) {
+        o[0] = 1 + k % l;
+        o[1] = k / l - l;
+      } else {
+        o[0] = 0;
+        o[1] = 1 + (k - nA);
+      }
+    }
+  } else {
+    int total = (dim == 3) ? w * w * w : w * w;
+    int center = (total - 1) / 2;
+    int kk = (k < center) ? k : k + 1;
+    o[0] = kk % w - l;
+    o[1] = (kk / w) % w - l;
+    if (dim == 3) o[2] = kk / (w * w) - l;
+  }
+}
+
 // Device error bits (OR-ed into the handle's error word).
 enum DevError : int {
   DERR_NAN = 1,

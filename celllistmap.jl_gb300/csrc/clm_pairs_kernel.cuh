@@ -19,49 +19,6 @@
 namespace clm {
 namespace pk {
 
-template <int LC = 0>
-__device__ __forceinline__ void stencil_offset(bool forward, int l_rt, int dim, int k, int* o) {
-  const int l = LC ? LC : l_rt;  // LC: lcell fixed at compile time (constant divisors)
-  const int w = 2 * l + 1;
-  o[2] = 0;
-  if (forward) {
-    if (dim == 3) {
-      const int nA = l * w * w, nB = l * w;
-      if (k < nA) {
-        o[0] = 1 + k % l;
-        int r = k / l;
-        o[1] = r % w - l;
-        o[2] = r / w - l;
-      } else if (k < nA + nB) {
-        int k2 = k - nA;
-        o[0] = 0;
-        o[1] = 1 + k2 % l;
-        o[2] = k2 / l - l;
-      } else {
-        o[0] = 0;
-        o[1] = 0;
-        o[2] = 1 + (k - nA - nB);
-      }
-    } else {
-      const int nA = l * w;
-      if (k < nA) {
-        o[0] = 1 + k % l;
-        o[1] = k / l - l;
-      } else {
-        o[0] = 0;
-        o[1] = 1 + (k - nA);
-      }
-    }
-  } else {
-    int total = (dim == 3) ? w * w * w : w * w;
-    int center = (total - 1) / 2;
-    int kk = (k < center) ? k : k + 1;
-    o[0] = kk % w - l;
-    o[1] = (kk / w) % w - l;
-    if (dim == 3) o[2] = kk / (w * w) - l;
-  }
-}
-
 template <class T> __device__ __forceinline__ T pos_of(const SetView<T>& S, int d, int t) {
   return d == 0 ? S.px[t] : (d == 1 ? S.py[t] : S.pz[t]);
 }

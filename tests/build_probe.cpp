@@ -110,3 +110,9 @@ extern "C" int build_probe(int f64, int dim, int kind, const double* Mcol, doubl
              : run<float, 2>(kind, Mcol, cutoff, lcell, x, n, cap, n_copies, n_real_cells, cell, idx, real, coords,
                              err);
 }
+
+// The k-th offset of the pair kernel's stencil (runtime lcell, or lcell = 1 fixed at compile time).
+extern "C" void stencil_probe(int forward, int lcell, int fixed1, int dim, int k, int* o) {
+  if (fixed1) clm::stencil_offset<1>(forward != 0, lcell, dim, k, o);
+  else clm::stencil_offset(forward != 0, lcell, dim, k, o);
+}

@@ -6,8 +6,10 @@ each copy, the gather of the copy coordinates in cell order) for the host and dr
 time.  The copies, their cells (with the border-case shift of real particles), their in-cell order, realness
 and coordinates must equal the oracle's (src/internals/CellLists.jl:727-1057, Box.jl:499-566) bit for bit, in
 Float64 and Float32, for orthorhombic, triclinic and non-periodic boxes in 2D and 3D, and over the
-reference's pathological coordinates and random cells (test/modules/Testing.jl:36-60, 162-257).  These run
-without a GPU; the GPU tests check the same lists built by the kernels themselves.
+reference's pathological coordinates and random cells (test/modules/Testing.jl:36-60, 162-257).  The pair
+kernel's stencil enumeration (csrc/clm_device.cuh stencil_offset) must list the reference's forward and full
+neighbour cells in the reference's order.  These run without a GPU; the GPU tests check the same lists built
+by the kernels themselves.
 """
 import ctypes as C
 import os
@@ -224,3 +226,32 @@ def test_empty_set(probe):
     st, got = host_celllist(probe, np.zeros((0, 3)), 3, "ortho", [10.0, 10.0, 10.0], 1.0, 1, np.float64)
     assert st == 0
     assert len(got["cell"]) == 0 and got["n_cells_with_real"] == 0
+
+
+def _cartesian(ranges):
+    # Julia's CartesianIndices order: first index fastest
+    import itertools
+    return [tuple(reversed(t)) for t in itertools.product(*reversed(ranges))]
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("lcell", [1, 2, 3, 5])
+def test_stencil_in_the_reference_order(probe, dim, lcell):
+    # neighbor_cells_forward / neighbor_cells (src/internals/Box.jl:436-474), element by element
+    l = lcell
+    full_r = range(-l, l + 1)
+    if dim == 3:
+        fwd = (_cartesian([range(1, l + 1), full_r, full_r]) + _cartesian([range(0, 1), range(1, l + 1), full_r])
+               + _cartesian([range(0, 1), range(0, 1), range(1, l + 1)]))
+    else:
+        fwd = _cartesian([range(1, l + 1), full_r]) + _cartesian([range(0, 1), range(1, l + 1)])
+    full = [t for t in _cartesian([full_r] * dim) if any(t)]
+    assert len(fwd) * 2 == len(full)
+    o = (C.c_int * 3)()
+    for forward, want in ((1, fwd), (0, full)):
+        for fixed1 in ((0, 1) if l == 1 else (0,)):
+            got = []
+            for k in range(len(want)):
+                probe.stencil_probe(forward, l, fixed1, dim, k, o)
+                got.append(tuple(o[:dim]))
+            assert got == want
