@@ -35,10 +35,12 @@ CLM_XOP(xdiv, float, __fdiv_rn(a, b), a / b)
 __host__ __device__ __forceinline__ double xsqrt(double a) { return __dsqrt_rn(a); }
 __host__ __device__ __forceinline__ float xsqrt(float a) { return __fsqrt_rn(a); }
 template <class T> __host__ __device__ __forceinline__ T xfloor(T a) { return floor(a); }
+template <class T> __host__ __device__ __forceinline__ T xabs(T a) { return fabs(a); }
 #else
 __host__ __device__ __forceinline__ double xsqrt(double a) { return std::sqrt(a); }
 __host__ __device__ __forceinline__ float xsqrt(float a) { return std::sqrt(a); }
 template <class T> __host__ __device__ __forceinline__ T xfloor(T a) { return std::floor(a); }
+template <class T> __host__ __device__ __forceinline__ T xabs(T a) { return std::fabs(a); }
 #endif
 
 // ---------------------------------------------------------------- geometry on device
@@ -205,6 +207,37 @@ __host__ __device__ __forceinline__ void stencil_offset(bool forward, int l_rt, 
     o[1] = (kk / w) % w - l;
     if (dim == 3) o[2] = kk / (w * w) - l;
   }
+}
+
+template <class T, int N>
+__host__ __device__ __forceinline__ T exact_dot_rel(const T* x, const T* c, const T* u) {
+  T s = xmul(xsub(x[0], c[0]), u[0]);
+#pragma unroll
+  for (int d = 1; d < N; d++) s = xadd(s, xmul(xsub(x[d], c[d]), u[d]));
+  return s;
+}
+
+// The reference's projection filter for a pair seen from cell `from` (center cf) towards cell `to`
+// (center ct): the particle of `to` must satisfy |proj| <= margin and |proj_to - proj_from| <= cutoff
+// (src/internals/vicinal_cells.jl:4-75, auxiliary_functions.jl:166-186).
+template <class T, int N>
+__host__ __device__ bool projection_pass(const DevGeom<T>& g, const T* cf, const T* ct, const T* x_from,
+                                         const T* x_to) {
+  T dc[3] = {0, 0, 0};
+#pragma unroll
+  for (int d = 0; d < N; d++) dc[d] = xsub(ct[d], cf[d]);
+  T s2 = xmul(dc[0], dc[0]);
+#pragma unroll
+  for (int d = 1; d < N; d++) s2 = xadd(s2, xmul(dc[d], dc[d]));
+  T dcn = xsqrt(s2);
+  T u[3] = {0, 0, 0};
+#pragma unroll
+  for (int d = 0; d < N; d++) u[d] = xdiv(dc[d], dcn);
+  T pt = exact_dot_rel<T, N>(x_to, cf, u);
+  bool keep = (g.lcell == 1) ? (xabs(pt) <= xadd(g.cutoff, xdiv(dcn, T(2)))) : ((double)xabs(pt) <= g.margin_wide);
+  if (!keep) return false;
+  T pf = exact_dot_rel<T, N>(x_from, cf, u);
+  return xabs(xsub(pt, pf)) <= g.cutoff;
 }
 
 // Device error bits (OR-ed into the handle's error word).

@@ -139,36 +139,6 @@ __device__ __forceinline__ void pair_value(const PairArgs<T>& A, int op, V d2, i
   }
 }
 
-template <class T, int N>
-__device__ __forceinline__ T exact_dot_rel(const T* x, const T* c, const T* u) {
-  T s = xmul(xsub(x[0], c[0]), u[0]);
-#pragma unroll
-  for (int d = 1; d < N; d++) s = xadd(s, xmul(xsub(x[d], c[d]), u[d]));
-  return s;
-}
-
-// The reference's projection filter for a pair seen from cell `from` (center cf) towards cell `to`
-// (center ct): the particle of `to` must satisfy |proj| <= margin and |proj_to - proj_from| <= cutoff
-// (src/internals/vicinal_cells.jl:4-75, auxiliary_functions.jl:166-186).
-template <class T, int N>
-__device__ bool projection_pass(const DevGeom<T>& g, const T* cf, const T* ct, const T* x_from, const T* x_to) {
-  T dc[3] = {0, 0, 0};
-#pragma unroll
-  for (int d = 0; d < N; d++) dc[d] = xsub(ct[d], cf[d]);
-  T s2 = xmul(dc[0], dc[0]);
-#pragma unroll
-  for (int d = 1; d < N; d++) s2 = xadd(s2, xmul(dc[d], dc[d]));
-  T dcn = xsqrt(s2);
-  T u[3] = {0, 0, 0};
-#pragma unroll
-  for (int d = 0; d < N; d++) u[d] = xdiv(dc[d], dcn);
-  T pt = exact_dot_rel<T, N>(x_to, cf, u);
-  bool keep = (g.lcell == 1) ? (fabs(pt) <= xadd(g.cutoff, xdiv(dcn, T(2)))) : ((double)fabs(pt) <= g.margin_wide);
-  if (!keep) return false;
-  T pf = exact_dot_rel<T, N>(x_from, cf, u);
-  return fabs(xsub(pt, pf)) <= g.cutoff;
-}
-
 // Sum of `v` over the lanes of a match group (`peers`: the lanes sharing this lane's key), returned in
 // the group's lowest lane.  Pairwise tree: at each step every lane at an even position of its group adds
 // the value of the next remaining peer, and the lanes at odd positions drop out, so a group of g lanes

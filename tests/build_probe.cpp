@@ -2,9 +2,12 @@
 // copy the kernels receive, K1 wrap_count_at, K2 emit_at, K4 gather_at) on the host, one particle or copy at a
 // time, so that the CPU tests can compare the copies, their cells and their coordinates with the oracle's
 // serial cell list without a GPU.  The exclusive scan and the radix sort between the steps are replaced by
-// their contracts (copy offsets in particle order; a stable sort of the copies by cell).  Built by
-// tests/test_build_steps.py with g++ -ffp-contract=off, as the library's host code is.
+// their contracts (copy offsets in particle order; a stable sort of the copies by cell).  It also exposes the
+// pair kernel's stencil enumeration and checks, over every pair of a host-built cell list, the condition under
+// which the pair kernel skips the projection filter.  Built by tests/test_build_steps.py with g++
+// -ffp-contract=off, as the library's host code is.
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <numeric>
 #include <vector>
@@ -12,10 +15,21 @@
 #include "clm_build_steps.cuh"
 
 namespace {
+
+template <class T, int N> struct HostList {
+  clm::DevGeom<T> d;
+  int err = 0;
+  int total = 0;
+  std::vector<uint32_t> skeys;  // cell of each copy, in cell order
+  std::vector<T> px, py, pz;    // coordinates of each copy
+  std::vector<int> code, flags, start;
+  T x(int t, int k) const { return k == 0 ? px[(size_t)t] : (k == 1 ? py[(size_t)t] : pz[(size_t)t]); }
+};
+
+// Geometry and cell list of one set, as clm_set_box + clm_build make them; returns a clm status (or 9x for a
+// broken cell-start table).
 template <class T, int N>
-int run(int kind, const double* Mcol, double cutoff, int lcell, const double* xin, int n, int64_t cap,
-        int64_t* n_copies, int64_t* n_real_cells, int64_t* cell, int64_t* idx, int8_t* real, double* coords,
-        int* err_out) {
+int build_host(int kind, const double* Mcol, double cutoff, int lcell, const double* xin, int n, HostList<T, N>& L) {
   std::vector<T> x((size_t)n * N), wrapped((size_t)n * N);
   for (size_t k = 0; k < x.size(); k++) x[k] = (T)xin[k];
   T M[3][3] = {}, origin[3] = {0, 0, 0};
@@ -40,61 +54,142 @@ int run(int kind, const double* Mcol, double cutoff, int lcell, const double* xi
   clm::Geometry<T> g;
   const int st = clm::make_geometry<T>(g, N, kind, M, (T)cutoff, lcell, kind == clm::NONPERIODIC ? origin : nullptr);
   if (st) return st;
-  clm::DevGeom<T> d;
+  clm::DevGeom<T>& d = L.d;
   clm::fill_devgeom<T>(g, 1, d);
   std::vector<uint32_t> mask((size_t)n);
   std::vector<int> ncopy((size_t)n), off((size_t)n + 1, 0);
-  int err = 0;
   for (int i = 0; i < n; i++)
-    if (!clm::wrap_count_at<T, N>(d, x.data(), i, wrapped.data(), mask.data(), ncopy.data())) err |= clm::DERR_NAN;
+    if (!clm::wrap_count_at<T, N>(d, x.data(), i, wrapped.data(), mask.data(), ncopy.data())) L.err |= clm::DERR_NAN;
   for (int i = 0; i < n; i++) off[(size_t)i + 1] = off[(size_t)i] + ncopy[(size_t)i];
   const int total = off[(size_t)n];
   std::vector<uint32_t> keys((size_t)total), vals((size_t)total);
   for (int i = 0; i < n; i++)
     clm::emit_at<T, N>(d, 0, wrapped.data(), mask.data(), ncopy.data(), off.data(), i, total, keys.data(),
-                       vals.data(), &err);
+                       vals.data(), &L.err);
   // the radix sort's contract: copies ordered by cell, stable (particle order inside a cell)
   std::vector<int> perm((size_t)total);
   std::iota(perm.begin(), perm.end(), 0);
   std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return keys[(size_t)a] < keys[(size_t)b]; });
-  std::vector<uint32_t> skeys((size_t)total), svals((size_t)total);
+  std::vector<uint32_t> svals((size_t)total);
+  L.skeys.resize((size_t)total);
   for (int t = 0; t < total; t++) {
-    skeys[(size_t)t] = keys[(size_t)perm[(size_t)t]];
+    L.skeys[(size_t)t] = keys[(size_t)perm[(size_t)t]];
     svals[(size_t)t] = vals[(size_t)perm[(size_t)t]];
   }
   const int ncells = d.ncells;
-  std::vector<T> px((size_t)total + 1), py((size_t)total + 1), pz((size_t)total + 1);
+  L.total = total;
+  L.px.assign((size_t)total + 1, T(0));
+  L.py.assign((size_t)total + 1, T(0));
+  L.pz.assign((size_t)total + 1, T(0));
   std::vector<float4> foff((size_t)total + 1), xq((size_t)total + 1);
-  std::vector<int> code((size_t)total + 1), flags((size_t)ncells + 1, 0), start((size_t)ncells + 1, -1);
+  L.code.assign((size_t)total + 1, 0);
+  L.flags.assign((size_t)ncells + 1, 0);
+  L.start.assign((size_t)ncells + 1, -1);
   for (int t = 0; t <= total; t++) {
-    clm::cell_starts_at(skeys.data(), t, total, ncells, start.data());
+    clm::cell_starts_at(L.skeys.data(), t, total, ncells, L.start.data());
     if (t == total) break;
     const int p = (int)(svals[(size_t)t] >> 5), k = (int)(svals[(size_t)t] & 31u);
-    clm::gather_at<T, N>(d, wrapped.data(), t, p, k, (int)skeys[(size_t)t], px.data(), py.data(), pz.data(),
-                         foff.data(), xq.data(), code.data(), flags.data(), 0);
+    clm::gather_at<T, N>(d, wrapped.data(), t, p, k, (int)L.skeys[(size_t)t], L.px.data(), L.py.data(),
+                         L.pz.data(), foff.data(), xq.data(), L.code.data(), L.flags.data(), 0);
   }
-  *err_out = err;
-  *n_copies = total;
-  *n_real_cells = 0;
-  for (int c = 0; c < ncells; c++) *n_real_cells += flags[(size_t)c] ? 1 : 0;
   // cell_start must bracket each cell's copies
   for (int c = 0; c < ncells; c++)
-    if (start[(size_t)c] < 0 || start[(size_t)c] > start[(size_t)c + 1]) return 99;
+    if (L.start[(size_t)c] < 0 || L.start[(size_t)c] > L.start[(size_t)c + 1]) return 99;
   for (int t = 0; t < total; t++)
-    if (start[skeys[(size_t)t]] > t || start[skeys[(size_t)t] + 1] <= t) return 98;
+    if (L.start[L.skeys[(size_t)t]] > t || L.start[L.skeys[(size_t)t] + 1] <= t) return 98;
+  return 0;
+}
+
+template <class T, int N>
+int run(int kind, const double* Mcol, double cutoff, int lcell, const double* xin, int n, int64_t cap,
+        int64_t* n_copies, int64_t* n_real_cells, int64_t* cell, int64_t* idx, int8_t* real, double* coords,
+        int* err_out) {
+  HostList<T, N> L;
+  const int st = build_host<T, N>(kind, Mcol, cutoff, lcell, xin, n, L);
+  if (st) return st;
+  *err_out = L.err;
+  *n_copies = L.total;
+  *n_real_cells = 0;
+  for (int c = 0; c < L.d.ncells; c++) *n_real_cells += L.flags[(size_t)c] ? 1 : 0;
   if (!cell) return 0;
-  if (cap < total) return 97;
-  for (int t = 0; t < total; t++) {
-    const int pc = code[(size_t)t];
-    cell[t] = skeys[(size_t)t];
+  if (cap < L.total) return 97;
+  for (int t = 0; t < L.total; t++) {
+    const int pc = L.code[(size_t)t];
+    cell[t] = L.skeys[(size_t)t];
     idx[t] = pc >= 0 ? pc : -(pc + 1);
     real[t] = pc >= 0 ? 1 : 0;
-    coords[(size_t)t * N + 0] = (double)px[(size_t)t];
-    coords[(size_t)t * N + 1] = (double)py[(size_t)t];
-    if (N == 3) coords[(size_t)t * N + 2] = (double)pz[(size_t)t];
+    for (int k = 0; k < N; k++) coords[(size_t)t * N + k] = (double)L.x(t, k);
   }
   return 0;
 }
+
+// Over every pair (real copy a of a cell, copy b of another cell of the full stencil): the pair kernel
+// accepts a pair without the projection filter when its exact d2 is at most the band bound thr_lo (or, for
+// Float32 handles, when the FP32 distance test of the kernel, fma(dz,dz,fma(dy,dy,dx*dx)) on the
+// coordinates, is).  Counts such pairs for which the exact d2 exceeds the cutoff or the reference's filter
+// (projection_pass) would reject the pair: out = {pairs within the cutoff, pairs accepted by the shortcut,
+// pairs in the band (filter evaluated), band pairs the filter rejects, violations}.
+template <class T, int N>
+int band(int kind, const double* Mcol, double cutoff, int lcell, const double* xin, int n, int64_t* out) {
+  HostList<T, N> L;
+  const int st = build_host<T, N>(kind, Mcol, cutoff, lcell, xin, n, L);
+  if (st) return st;
+  const clm::DevGeom<T>& g = L.d;
+  const T thr = (T)g.thr_lo;
+  const int w = 2 * g.lcell + 1;
+  const int nst = (N == 3) ? w * w * w - 1 : w * w - 1;
+  for (int k = 0; k < 5; k++) out[k] = 0;
+  for (int ci_lin = 0; ci_lin < g.ncells; ci_lin++) {
+    if (!L.flags[(size_t)ci_lin]) continue;
+    int ci[3];
+    clm::cart_of(ci_lin, g.nc, N, ci);
+    T ctr_i[3] = {0, 0, 0};
+    clm::cell_center<T, N>(g, ci, ctr_i);
+    for (int s = 0; s < nst; s++) {
+      int o[3];
+      clm::stencil_offset(false, g.lcell, N, s, o);
+      const int cj[3] = {ci[0] + o[0], ci[1] + o[1], N == 3 ? ci[2] + o[2] : 1};
+      bool inside = true;
+      for (int k = 0; k < N; k++) inside = inside && cj[k] >= 1 && cj[k] <= g.nc[k];
+      if (!inside) continue;
+      const int cj_lin = (N == 3) ? (cj[0] - 1) + g.nc[0] * ((cj[1] - 1) + g.nc[1] * (cj[2] - 1))
+                                  : (cj[0] - 1) + g.nc[0] * (cj[1] - 1);
+      T ctr_j[3] = {0, 0, 0};
+      clm::cell_center<T, N>(g, cj, ctr_j);
+      for (int a = L.start[(size_t)ci_lin]; a < L.start[(size_t)ci_lin + 1]; a++) {
+        if (L.code[(size_t)a] < 0) continue;  // the particle side is a real copy
+        T xa[3];
+        for (int k = 0; k < N; k++) xa[k] = L.x(a, k);
+        for (int b = L.start[(size_t)cj_lin]; b < L.start[(size_t)cj_lin + 1]; b++) {
+          T xb[3], dx[3];
+          for (int k = 0; k < N; k++) {
+            xb[k] = L.x(b, k);
+            dx[k] = clm::xsub(xa[k], xb[k]);
+          }
+          T d2 = clm::xmul(dx[0], dx[0]);  // the exact d2, in the reference's order
+          for (int k = 1; k < N; k++) d2 = clm::xadd(d2, clm::xmul(dx[k], dx[k]));
+          bool shortcut = d2 <= thr;
+          if constexpr (sizeof(T) == 4) {
+            const float fx = xa[0] - xb[0], fy = xa[1] - xb[1], fz = (N == 3) ? xa[N - 1] - xb[N - 1] : 0.f;
+            const float d2f = std::fmaf(fz, fz, std::fmaf(fy, fy, fx * fx));
+            if (d2f <= g.thr_lo) shortcut = true;
+          }
+          const bool within = d2 <= g.cutoff_sqr;
+          out[0] += within ? 1 : 0;
+          if (shortcut) {
+            out[1]++;
+            if (!within || !clm::projection_pass<T, N>(g, ctr_i, ctr_j, xa, xb)) out[4]++;
+          } else if (within) {
+            out[2]++;
+            if (!clm::projection_pass<T, N>(g, ctr_i, ctr_j, xa, xb)) out[3]++;
+          }
+        }
+      }
+    }
+  }
+  return 0;
+}
+
 }  // namespace
 
 extern "C" int build_probe(int f64, int dim, int kind, const double* Mcol, double cutoff, int lcell, const double* x,
@@ -109,6 +204,15 @@ extern "C" int build_probe(int f64, int dim, int kind, const double* Mcol, doubl
                               err)
              : run<float, 2>(kind, Mcol, cutoff, lcell, x, n, cap, n_copies, n_real_cells, cell, idx, real, coords,
                              err);
+}
+
+extern "C" int band_probe(int f64, int dim, int kind, const double* Mcol, double cutoff, int lcell, const double* x,
+                          int n, int64_t* out) {
+  if (dim == 3)
+    return f64 ? band<double, 3>(kind, Mcol, cutoff, lcell, x, n, out)
+               : band<float, 3>(kind, Mcol, cutoff, lcell, x, n, out);
+  return f64 ? band<double, 2>(kind, Mcol, cutoff, lcell, x, n, out)
+             : band<float, 2>(kind, Mcol, cutoff, lcell, x, n, out);
 }
 
 // The k-th offset of the pair kernel's stencil (runtime lcell, or lcell = 1 fixed at compile time).

@@ -255,3 +255,50 @@ def test_stencil_in_the_reference_order(probe, dim, lcell):
                 probe.stencil_probe(forward, l, fixed1, dim, k, o)
                 got.append(tuple(o[:dim]))
             assert got == want
+
+
+def band_counts(lib, x, dim, kind, unitcell, cutoff, lcell, dtype):
+    x = np.ascontiguousarray(np.asarray(x, dtype).astype(np.float64)).reshape(-1, dim)
+    if unitcell is None:
+        Mc = np.zeros(dim * dim)
+    else:
+        uc = np.asarray(unitcell, np.float64)
+        Mc = np.ascontiguousarray((np.diag(uc) if uc.ndim == 1 else uc.reshape(dim, dim)).flatten(order="F"))
+    out = np.zeros(5, np.int64)
+    st = lib.band_probe(int(np.dtype(dtype) == np.float64), dim, KINDS[kind], Mc.ctypes.data_as(C.c_void_p),
+                        C.c_double(cutoff), lcell, x.ctypes.data_as(C.c_void_p), x.shape[0],
+                        out.ctypes.data_as(C.c_void_p))
+    return st, out
+
+
+BAND_CELLS = [
+    (3, [20.0, 20.0, 20.0]),
+    (3, [[20.0, 4.0, 2.0], [0.0, 20.0, 3.0], [0.0, 0.0, 20.0]]),
+    (3, [[14.0, 9.0, -6.0], [1.0, 15.0, 7.0], [-2.0, 3.0, 16.0]]),
+    (3, None),
+    (2, [30.0, 25.0]),
+    (2, [[30.0, 14.0], [0.0, 25.0]]),
+    (2, [[24.0, -11.0], [5.0, 26.0]]),
+    (2, None),
+]
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("lcell", [1, 2, 3])
+@pytest.mark.parametrize("cell", BAND_CELLS, ids=lambda c: f"{c[0]}d-{kind_of(c[1])}")
+def test_projection_filter_passes_inside_the_band(probe, cell, lcell, dtype):
+    # The pair kernel evaluates the reference's projection filter (vicinal_cells.jl:4-75) only for pairs with
+    # d2 > rc^2 (1 - 2^-13) (and, for Float32 handles, accepts a pair whose FP32 fma distance test is below
+    # that bound).  The filter keeps every pair well inside the cutoff: |(x_j - x_i).u| <= d < rc, and the
+    # particle's projection on the cell-pair axis is at most half the centre distance (lcell 1) or
+    # rc sqrt(N)/2 (lcell > 1), inside the margins.  Checked over every pair of the full stencil.
+    dim, uc = cell
+    rng = np.random.default_rng(40 + lcell + dim)
+    n = 6000 if dim == 3 else 3000
+    span = 20.0 if dim == 3 else 28.0
+    x = (rng.random((n, dim)) * span - 3.0).astype(dtype)
+    st, out = band_counts(probe, x, dim, kind_of(uc), uc, 2.0, lcell, dtype)
+    assert st == 0
+    within, shortcut, banded, rejected, violations = out.tolist()
+    assert violations == 0
+    assert shortcut > 0.99 * within > 0 and banded > 0 and rejected <= banded
