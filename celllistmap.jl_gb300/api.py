@@ -345,20 +345,17 @@ OPERATORS = {c.op: c for c in [Count, SumD2, SumD, SumInvD, SoftEnergy, SoftForc
 
 # ---------------------------------------------------------------------------- helpers
 def _promote_dtype(unitcell, cutoff, dtype):
-    """_promote_types (src/internals/Box.jl:132-142): float type of unit cell and cutoff; Int -> Float64."""
+    """_promote_types (src/internals/Box.jl:132-142): the promoted element type of the unit cell and the
+    cutoff, integers yielding to any float type (Julia's promote_type(Int, Float32) is Float32) and integers
+    alone giving Float64."""
     if dtype is not None:
         return np.dtype(dtype)
-    types = []
-    if cutoff is not None:
-        types.append(np.asarray(cutoff).dtype)
-    if unitcell is not None:
-        types.append(np.asarray(unitcell).dtype)
-    t = np.result_type(*types) if types else np.dtype(np.float64)
-    if not np.issubdtype(t, np.floating):
-        t = np.dtype(np.float64)
-    if t not in (np.float32, np.float64):
-        t = np.dtype(np.float64)
-    return t
+    floats = [t for t in (np.asarray(v).dtype for v in (cutoff, unitcell) if v is not None)
+              if np.issubdtype(t, np.floating)]
+    if not floats:
+        return np.dtype(np.float64)
+    t = np.result_type(*floats)
+    return t if t in (np.float32, np.float64) else np.dtype(np.float64)
 
 
 def _as_positions(x, dim, dtype):

@@ -68,6 +68,31 @@ def test_dimension_and_argument_checks_happen_on_the_host(clm):
     assert api._promote_dtype(np.array([1.0, 1.0], np.float32), np.float32(0.1), None) == np.float32
 
 
+def test_type_promotion_like_the_reference(clm):
+    # _promote_types cases of test/internals/Box.jl:11-28,124-131 (0.1f0 -> np.float32(0.1), a Float32
+    # vector -> a float32 array, nothing -> None): integers yield to any float type, integers alone give
+    # Float64, Float32 with Float64 gives Float64
+    import numpy as np
+    api = clm._api if hasattr(clm, "_api") else clm.api
+    f32 = np.float32
+    cases = [
+        ([1, 1, 1], 0.1, np.float64),
+        ([1, 1, 1], f32(0.1), np.float32),
+        ([1.0, 1, 1], f32(0.1), np.float64),
+        (np.array([1, 1, 1], f32), f32(0.1), np.float32),
+        ([10, 10, 10.0], 1, np.float64),
+        (np.array([10, 10, 10], f32), 1, np.float32),
+        ([10, 10, 10], 1, np.float64),
+        (None, f32(1.0), np.float32),
+        (np.array([1, 1, 1], f32), None, np.float32),
+        (np.array([1, 1, 1], f32), 1.0, np.float64),
+        ([1.0, 1.0, 1.0], f32(1.0), np.float64),
+        ([1, 1, 1], 1, np.float64),
+    ]
+    for unitcell, cutoff, want in cases:
+        assert api._promote_dtype(unitcell, cutoff, None) == want, (unitcell, cutoff)
+
+
 def _build_c_driver(clm, tmp_path):
     """Compile tests/abi_driver.c (plain C99 against the header) and link it to the library."""
     import shutil
