@@ -220,3 +220,21 @@ extern "C" void stencil_probe(int forward, int lcell, int fixed1, int dim, int k
   if (fixed1) clm::stencil_offset<1>(forward != 0, lcell, dim, k, o);
   else clm::stencil_offset(forward != 0, lcell, dim, k, o);
 }
+
+// The library's cell of one point (cell_of, with the border-case shift when `real`), as 1-based cartesian
+// indices; returns the linear index or -1, or a clm status (> 0 is returned as -2 - status).
+extern "C" int cell_probe(int dim, int kind, const double* Mcol, double cutoff, int lcell, const double* x, int real,
+                          int* cart, int* nc) {
+  double M[3][3] = {};
+  for (int i = 0; i < dim; i++)
+    for (int j = 0; j < dim; j++) M[i][j] = (kind == clm::ORTHO && i != j) ? 0.0 : Mcol[j * dim + i];
+  clm::Geometry<double> g;
+  const int st = clm::make_geometry<double>(g, dim, kind, M, cutoff, lcell, nullptr);
+  if (st) return -2 - st;
+  clm::DevGeom<double> d;
+  clm::fill_devgeom<double>(g, 1, d);
+  for (int k = 0; k < 3; k++) nc[k] = d.nc[k];
+  const int li = (dim == 3) ? clm::cell_of<double, 3>(d, x, real != 0) : clm::cell_of<double, 2>(d, x, real != 0);
+  if (li >= 0) clm::cart_of(li, d.nc, dim, cart);
+  return li;
+}

@@ -68,6 +68,24 @@ def test_dimension_and_argument_checks_happen_on_the_host(clm):
     assert api._promote_dtype(np.array([1.0, 1.0], np.float32), np.float32(0.1), None) == np.float32
 
 
+def test_dimension_inference_like_the_reference(clm):
+    # get_dim cases of test/internals/auxiliary_functions.jl:12-31 (positions as lists of points; the
+    # untyped-empty-vector case has no Python counterpart: [] and an empty (0, dim) array are both accepted)
+    import numpy as np
+    api = clm._api if hasattr(clm, "_api") else clm.api
+    assert api._get_dim([1, 2], [[1, 2], [3, 4]]) == 2
+    assert api._get_dim([1, 2], [[1, 2], [3, 4]], [[1, 2], [3, 4]]) == 2
+    assert api._get_dim([1, 2, 3], [[1, 2, 3], [3, 4, 5]]) == 3
+    assert api._get_dim([1, 2, 3], [[1, 2, 3], [3, 4, 5]], [[1, 2, 3], [3, 4, 5]]) == 3
+    assert api._get_dim([1, 2], np.zeros((0, 2))) == 2
+    assert api._get_dim([], [[1.0, 2.0]]) == 2
+    assert api._get_dim(None, [[1.0, 2.0]]) == 2
+    for args, msg in ((([1, 2], [[1, 2, 3]]), "Incompatible dimensions"), (([1, 2, 3, 4], [[1, 2, 3, 4]]), "2 or 3"),
+                      ((None, [[]]), "Could not infer")):
+        with pytest.raises(clm.ArgumentError, match=msg):
+            api._get_dim(*args)
+
+
 def test_type_promotion_like_the_reference(clm):
     # _promote_types cases of test/internals/Box.jl:11-28,124-131 (0.1f0 -> np.float32(0.1), a Float32
     # vector -> a float32 array, nothing -> None): integers yield to any float type, integers alone give

@@ -302,3 +302,29 @@ def test_projection_filter_passes_inside_the_band(probe, cell, lcell, dtype):
     within, shortcut, banded, rejected, violations = out.tolist()
     assert violations == 0
     assert shortcut > 0.99 * within > 0 and banded > 0 and rejected <= banded
+
+
+def test_real_particle_border_case(probe):
+    # test/internals/CellLists.jl:161-190: Box([1, 1, 1], 0.1, lcell=1); a real particle in cell lcell moves
+    # to lcell + 1, one in cell nc - lcell + 1 moves to nc - lcell, per dimension; an image is not moved
+    M = np.ascontiguousarray(np.eye(3).flatten(order="F"))
+    cart, nc = (C.c_int * 3)(), (C.c_int * 3)()
+
+    def cell(x, real, lcell=1):
+        xa = np.ascontiguousarray(x, np.float64)
+        li = probe.cell_probe(3, KINDS["ortho"], M.ctypes.data_as(C.c_void_p), C.c_double(0.1), lcell,
+                              xa.ctypes.data_as(C.c_void_p), int(real), cart, nc)
+        assert li >= 0
+        return tuple(cart), tuple(nc)
+
+    h = 0.1  # cell side; cell c (1-based) spans [-0.1 + (c - 1) h, -0.1 + c h)
+    centre = lambda c: -0.1 + (c - 0.5) * h  # noqa: E731
+    (c1, n1) = cell([centre(1), centre(2), centre(3)], True)
+    assert n1 == (13, 13, 13)  # floor(1 / 0.1) + 2 lcell + 1
+    assert c1 == (2, 2, 3)
+    c2, _ = cell([centre(13), centre(2), centre(3)], True)
+    assert c2 == (12, 2, 3)
+    c3, _ = cell([centre(1), centre(13), centre(6)], True)
+    assert c3 == (2, 12, 6)
+    c4, _ = cell([centre(1), centre(13), centre(6)], False)  # images keep their cell
+    assert c4 == (1, 13, 6)
