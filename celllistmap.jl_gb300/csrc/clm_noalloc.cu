@@ -4,7 +4,7 @@
 // code running inside a CUDA stream capture (allocation calls synchronize the device and break the
 // capture), applications whose device memory is entirely owned by their own pool allocator (a Julia
 // CUDA.jl or PyTorch caching pool, an MD engine with a fixed arena), and real-time loops that must not
-// hit the driver's allocator.  They build the cell lists once with the ordinary entry points (which do
+// call into the CUDA allocator.  They build the cell lists once with the ordinary entry points (which do
 // allocate), then evaluate scalar reductions of the pair map any number of times through this entry
 // point.
 //

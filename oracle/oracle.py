@@ -1,8 +1,8 @@
 """ctypes front end of the CPU oracle (``oracle/clm_oracle.cpp``).
 
 TEST INFRASTRUCTURE ONLY: imported by ``tests/``, ``__graft_entry__.smoke()``
-and ``bench.py``'s CPU-baseline leg as the checker.  The shipped package never
-imports this module.
+and ``bench.py``'s CPU-baseline leg, to check results and to time the CPU baseline.  The shipped
+package never imports this module.
 
 The oracle restates CellListMap.jl's serial cell-list build and pair map
 (``src/internals/CellLists.jl:940-1057``, ``src/internals/self.jl:106-184``,

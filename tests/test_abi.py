@@ -129,7 +129,7 @@ def _build_c_driver(clm, tmp_path):
 
 
 def test_c_client_compiles_and_links(clm, tmp_path):
-    # the header is plain C and every entry point the driver calls resolves in the shared library
+    # the header is plain C and every entry point the C client calls resolves in the shared library
     assert os.path.exists(_build_c_driver(clm, tmp_path))
 
 
