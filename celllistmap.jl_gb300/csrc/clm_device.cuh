@@ -209,6 +209,26 @@ __host__ __device__ __forceinline__ void stencil_offset(bool forward, int l_rt, 
   }
 }
 
+// Which visits of a candidate pair the map keeps (src/internals/self.jl:143-184, cross.jl:111-129), for a
+// particle copy i (slot ii of its cell) and a candidate copy j (slot slot_j; `same`: the same cell).
+// Self pairs: orthorhombic cells keep a pair once (j after i in the same cell; any cell of the forward half
+// stencil) when one of the copies is real; triclinic cells keep index_i < index_j (i real, full stencil);
+// non-periodic systems have no images.  Cross pairs in orthorhombic cells: the particle copy must be real
+// for a candidate of its own cell, and one of the two copies for a candidate of another cell; triclinic and
+// non-periodic cross pairs keep every visit.
+__host__ __device__ __forceinline__ bool pair_rule(bool cross, bool tri, bool nonper, bool same, int slot_j, int ii,
+                                                   bool real_i, bool real_j, int idx_i, int idx_j) {
+  bool cand = true;
+  if (!cross) {
+    if (tri) cand = idx_i < idx_j;
+    else if (same) cand = (slot_j > ii) && (nonper || real_i || real_j);
+    else cand = nonper || real_i || real_j;
+  } else {
+    if (!tri && !nonper) cand = same ? real_i : (real_i || real_j);
+  }
+  return cand;
+}
+
 template <class T, int N>
 __host__ __device__ __forceinline__ T exact_dot_rel(const T* x, const T* c, const T* u) {
   T s = xmul(xsub(x[0], c[0]), u[0]);

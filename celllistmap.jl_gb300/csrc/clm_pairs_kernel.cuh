@@ -550,14 +550,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
               if constexpr (!ABS_PF) tjj = s_tj[buf][warp][j];
               const bool same = (meta & F_SAME) != 0;
               const int slot_j = rb + j;  // position inside the cell when same
-              bool cand = true;
-              if (!CROSS) {
-                if (tri) cand = idx_i < idx_j;
-                else if (same) cand = (slot_j > ii) && (nonper || real_i || real_j);
-                else cand = nonper || real_i || real_j;
-              } else {
-                if (!tri && !nonper) cand = same ? real_i : (real_i || real_j);
-              }
+              const bool cand = pair_rule(CROSS, tri, nonper, same, slot_j, ii, real_i, real_j, idx_i, idx_j);
               if (cand) {
                 dvf[0] = pi[0] - p.x;
                 dvf[1] = pi[1] - p.y;

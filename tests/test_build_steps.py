@@ -328,3 +328,87 @@ def test_real_particle_border_case(probe):
     assert c3 == (2, 12, 6)
     c4, _ = cell([centre(1), centre(13), centre(6)], False)  # images keep their cell
     assert c4 == (1, 13, 6)
+
+
+def host_map_nl(lib, x, dim, kind, unitcell, cutoff, lcell, dtype):
+    """Self-pair neighbour list of the pair kernel's logic emulated on the host (tests/build_probe.cpp
+    map_nl): returns (status, i, j, d, lost), `lost` counting exact hits the FP32 pass would drop."""
+    x = np.ascontiguousarray(np.asarray(x, dtype).astype(np.float64)).reshape(-1, dim)
+    if unitcell is None:
+        Mc = np.zeros(dim * dim)
+    else:
+        uc = np.asarray(unitcell, np.float64)
+        Mc = np.ascontiguousarray((np.diag(uc) if uc.ndim == 1 else uc.reshape(dim, dim)).flatten(order="F"))
+    lib.map_nl_probe.restype = C.c_int64
+    lost, st = C.c_int64(0), C.c_int(0)
+    vp = C.c_void_p
+
+    def call(cap, i, j, d):
+        return lib.map_nl_probe(int(np.dtype(dtype) == np.float64), dim, KINDS[kind], Mc.ctypes.data_as(vp),
+                                C.c_double(cutoff), lcell, x.ctypes.data_as(vp), x.shape[0], C.c_int64(cap),
+                                i.ctypes.data_as(vp), j.ctypes.data_as(vp), d.ctypes.data_as(vp), C.byref(lost),
+                                C.byref(st))
+
+    e = np.zeros(1, np.int64)
+    m = call(0, e, e, e.astype(np.float64))
+    if st.value:
+        return st.value, None, None, None, None
+    i, j, d = np.zeros(m, np.int64), np.zeros(m, np.int64), np.zeros(m, np.float64)
+    assert call(m, i, j, d) == m
+    return 0, i, j, d, lost.value
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("case", CASES, ids=case_id)
+def test_emulated_map_matches_oracle_neighbor_list(probe, orc, case, dtype):
+    # The pair kernel's self-pair logic (cells with real particles, stencil, pair rule, exact test, band and
+    # projection filter) driven on the host over the host-built cell list: the same pairs and bit-identical
+    # distances as the oracle (src/internals/self.jl:106-184), and no exact hit the FP32 pass would drop.
+    dim, uc, cut, lcell, n, span, shift = case
+    rng = np.random.default_rng(21 + lcell + dim)
+    x = (rng.random((n, dim)) * span + shift).astype(dtype)
+    st, i, j, d, lost = host_map_nl(probe, x, dim, kind_of(uc), uc, cut, lcell, dtype)
+    assert st == 0 and lost == 0
+    ref = orc.run("nl", x, dim=dim, kind=kind_of(uc), unitcell=uc, cutoff=cut, lcell=lcell, dtype=dtype)
+    A, B = orc.canonical_pairs(i, j, d), orc.canonical_pairs(ref["i"], ref["j"], ref["d"])
+    assert len(A[0]) == len(B[0]) > 0
+    for u, v in zip(A, B):
+        np.testing.assert_array_equal(u, np.asarray(v, u.dtype))
+
+
+def test_emulated_map_pathological_and_random_cells(probe, orc):
+    # the same emulation over the reference's pathological coordinates (test/modules/Testing.jl:36-60) and
+    # its random-cell sweep (test/modules/Testing.jl:162-257: entries in [-10, 10], points far outside)
+    rng = np.random.default_rng(8)
+    sides = np.array([250.0, 250.0, 250.0])
+    xp = _pathological(rng, 500, sides)
+    checks = [(xp, 3, uc, 10.0, lcell) for lcell in (1, 2)
+              for uc in (sides, np.array([[250.0, 30.0, 10.0], [0.0, 250.0, 20.0], [0.0, 0.0, 250.0]]))]
+    done = 0
+    for _ in range(600):
+        dim = int(rng.integers(2, 4))
+        kind = "ortho" if rng.random() < 0.3 else "tri"
+        M = np.diag(-10 + 20 * rng.random(dim)) if kind == "ortho" else -10 + 20 * rng.random((dim, dim))
+        uc = np.diag(M) if kind == "ortho" else M
+        cut, lcell = float(1 + rng.random()), int(rng.integers(1, 4))
+        try:
+            b = orc.box_info(dim=dim, kind=kind, unitcell=uc, cutoff=cut, lcell=lcell)
+        except orc.OracleError:
+            continue
+        if np.prod(b["nc"]) > 100000:
+            continue
+        checks.append((10 * rng.random((int(rng.integers(10, 60)), dim)) - 50, dim, uc, cut, lcell))
+        done += 1
+        if done == 80:
+            break
+    assert done == 80
+    for x, dim, uc, cut, lcell in checks:
+        for dtype in (np.float64, np.float32):
+            kind = kind_of(uc)
+            st, i, j, d, lost = host_map_nl(probe, x, dim, kind, uc, cut, lcell, dtype)
+            assert st == 0 and lost == 0
+            ref = orc.run("nl", x, dim=dim, kind=kind, unitcell=uc, cutoff=cut, lcell=lcell, dtype=dtype)
+            A, B = orc.canonical_pairs(i, j, d), orc.canonical_pairs(ref["i"], ref["j"], ref["d"])
+            assert len(A[0]) == len(B[0])
+            for u, v in zip(A, B):
+                np.testing.assert_array_equal(u, np.asarray(v, u.dtype))
