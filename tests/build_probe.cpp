@@ -240,6 +240,56 @@ extern "C" int cell_probe(int dim, int kind, const double* Mcol, double cutoff, 
 }
 
 namespace {
+// FP32 prefilter coordinates of a cell list's copies for Float64 handles, as the gather writes them: the
+// FP32 offset of each copy from its cell origin, in float pairs.
+template <class T, int N> std::vector<float4> fp32_offsets(const HostList<T, N>& L) {
+  const clm::DevGeom<T>& g = L.d;
+  std::vector<float4> foff((size_t)L.total + 1);
+  if (sizeof(T) == 8) {
+    for (int t = 0; t < L.total; t++) {
+      int c[3];
+      clm::cart_of((int)L.skeys[(size_t)t], g.nc, N, c);
+      float o[3] = {0.f, 0.f, 0.f};
+      for (int d = 0; d < N; d++) {
+        float oh, ol;
+        clm::origin_ff(g.cbf_hi[d], g.cbf_lo[d], g.csf[d], g.csf_lo[d], c[d] - 1, oh, ol);
+        const float qh = (float)L.x(t, d);
+        const float ql = (float)(L.x(t, d) - (T)qh);
+        o[d] = (qh - oh) + (ql - ol);
+      }
+      foff[(size_t)t] = make_float4(o[0], o[1], o[2], 0.f);
+    }
+  }
+  return foff;
+}
+
+// The FP32 distance pass of the kernel for copy a of list La against copy b of list Lb in a cell displaced
+// by o: true when it keeps the pair (d2 - thr_hi < 0) with the displacement shift of the offsets both
+// fused and unfused.
+template <class T, int N>
+bool fp32_keeps(const HostList<T, N>& La, const std::vector<float4>& fa, int a, const HostList<T, N>& Lb,
+                const std::vector<float4>& fb, int b, const int* o) {
+  const clm::DevGeom<T>& g = La.d;
+  for (int fused = 0; fused < 2; fused++) {
+    float p[3] = {0.f, 0.f, 0.f}, q[3] = {0.f, 0.f, 0.f};
+    for (int k = 0; k < N; k++) {
+      if (sizeof(T) == 4) {
+        p[k] = (float)La.x(a, k);
+        q[k] = (float)Lb.x(b, k);
+      } else {
+        const float offk = k == 0 ? fb[(size_t)b].x : (k == 1 ? fb[(size_t)b].y : fb[(size_t)b].z);
+        const float sh = (float)o[k];
+        q[k] = fused ? std::fmaf(g.csf[k], sh, offk) : offk + g.csf[k] * sh;
+        p[k] = k == 0 ? fa[(size_t)a].x : (k == 1 ? fa[(size_t)a].y : fa[(size_t)a].z);
+      }
+    }
+    const float fx = p[0] - q[0], fy = p[1] - q[1], fz = p[2] - q[2];
+    const float ef = std::fmaf(fz, fz, std::fmaf(fy, fy, std::fmaf(fx, fx, -g.thr_hi)));
+    if (!(ef < 0.f)) return false;
+  }
+  return true;
+}
+
 // The self-pair map of the pair kernel, emulated on the host from the library's own pieces: the cells with
 // real particles, every copy of such a cell as the particle side (real copies only in triclinic cells),
 // stencil entry 0 (the cell itself) then the forward half stencil (orthorhombic, non-periodic) or all
@@ -259,24 +309,7 @@ int64_t map_nl(int kind, const double* Mcol, double cutoff, int lcell, const dou
   const int wN = (N == 3) ? w * w * w : w * w;
   const int nent = (tri ? wN - 1 : (wN - 1) / 2) + 1;
   const T band = (T)g.thr_lo;
-  // FP32 prefilter coordinates as the gather writes them: the Float32 coordinates, or (Float64) the FP32
-  // offsets of each copy from its cell origin
-  std::vector<float4> foff((size_t)L.total + 1);
-  if (sizeof(T) == 8) {
-    for (int t = 0; t < L.total; t++) {
-      int c[3];
-      clm::cart_of((int)L.skeys[(size_t)t], g.nc, N, c);
-      float o[3] = {0.f, 0.f, 0.f};
-      for (int d = 0; d < N; d++) {
-        float oh, ol;
-        clm::origin_ff(g.cbf_hi[d], g.cbf_lo[d], g.csf[d], g.csf_lo[d], c[d] - 1, oh, ol);
-        const float qh = (float)L.x(t, d);
-        const float ql = (float)(L.x(t, d) - (T)qh);
-        o[d] = (qh - oh) + (ql - ol);
-      }
-      foff[(size_t)t] = make_float4(o[0], o[1], o[2], 0.f);
-    }
-  }
+  const std::vector<float4> foff = fp32_offsets(L);
   int64_t np = 0;
   *lost = 0;
   for (int ci_lin = 0; ci_lin < g.ncells; ci_lin++) {
@@ -322,28 +355,8 @@ int64_t map_nl(int kind, const double* Mcol, double cutoff, int lcell, const dou
           bool hit = d2 <= g.cutoff_sqr;
           if (hit && d2 > band && e > 0) hit = clm::projection_pass<T, N>(g, ctr_i, ctr_j, xa, xb);
           if (!hit) continue;
-          // the FP32 distance pass must keep this pair (d2 - thr_hi < 0), whichever way the shift rounds
-          for (int fused = 0; fused < 2; fused++) {
-            float p[3], q[3];
-            for (int k = 0; k < 3; k++) p[k] = q[k] = 0.f;
-            for (int k = 0; k < N; k++) {
-              if (sizeof(T) == 4) {
-                p[k] = (float)xa[k];
-                q[k] = (float)xb[k];
-              } else {
-                const float offk = k == 0 ? foff[(size_t)b].x : (k == 1 ? foff[(size_t)b].y : foff[(size_t)b].z);
-                const float sh = (float)o[k];
-                q[k] = fused ? std::fmaf(g.csf[k], sh, offk) : offk + g.csf[k] * sh;
-                p[k] = k == 0 ? foff[(size_t)a].x : (k == 1 ? foff[(size_t)a].y : foff[(size_t)a].z);
-              }
-            }
-            const float fx = p[0] - q[0], fy = p[1] - q[1], fz = p[2] - q[2];
-            const float ef = std::fmaf(fz, fz, std::fmaf(fy, fy, std::fmaf(fx, fx, -g.thr_hi)));
-            if (!(ef < 0.f)) {
-              (*lost)++;
-              break;
-            }
-          }
+          // the FP32 distance pass must keep this pair, whichever way the shift rounds
+          if (!fp32_keeps(L, foff, a, L, foff, b, o)) (*lost)++;
           if (np < cap) {
             pi_out[np] = idx_i;
             pj_out[np] = idx_j;
@@ -366,4 +379,95 @@ extern "C" int64_t map_nl_probe(int f64, int dim, int kind, const double* Mcol, 
                : map_nl<float, 3>(kind, Mcol, cutoff, lcell, x, n, cap, pi, pj, d, lost, st);
   return f64 ? map_nl<double, 2>(kind, Mcol, cutoff, lcell, x, n, cap, pi, pj, d, lost, st)
              : map_nl<float, 2>(kind, Mcol, cutoff, lcell, x, n, cap, pi, pj, d, lost, st);
+}
+
+namespace {
+// The x-y (cross) map of the pair kernel emulated on the host, periodic cells: the cells with real x
+// particles, every x copy of such a cell as the particle side (real copies only in triclinic cells), the y
+// copies of the cell itself and of all its neighbours as candidates, the kernel's pair rule, the exact test,
+// the band and the projection filter; the FP32 pass is checked as for self pairs.
+template <class T, int N>
+int64_t map_cross(int kind, const double* Mcol, double cutoff, int lcell, const double* xin, int nx,
+                  const double* yin, int ny, int64_t cap, int64_t* pi_out, int64_t* pj_out, double* d_out,
+                  int64_t* lost, int* st_out) {
+  *st_out = (kind == clm::NONPERIODIC) ? 77 : 0;  // non-periodic cross boxes span both sets: not emulated
+  if (*st_out) return -1;
+  HostList<T, N> X, Y;
+  *st_out = build_host<T, N>(kind, Mcol, cutoff, lcell, xin, nx, X);
+  if (!*st_out) *st_out = build_host<T, N>(kind, Mcol, cutoff, lcell, yin, ny, Y);
+  if (*st_out) return -1;
+  const clm::DevGeom<T>& g = X.d;
+  const bool tri = g.kind == clm::TRICLINIC;
+  const int w = 2 * g.lcell + 1;
+  const int nent = ((N == 3) ? w * w * w : w * w);  // the cell itself, then all neighbours
+  const T band = (T)g.thr_lo;
+  const std::vector<float4> fx = fp32_offsets(X), fy = fp32_offsets(Y);
+  int64_t np = 0;
+  *lost = 0;
+  for (int ci_lin = 0; ci_lin < g.ncells; ci_lin++) {
+    if (!X.flags[(size_t)ci_lin]) continue;
+    int ci[3];
+    clm::cart_of(ci_lin, g.nc, N, ci);
+    T ctr_i[3] = {0, 0, 0};
+    clm::cell_center<T, N>(g, ci, ctr_i);
+    const int si = X.start[(size_t)ci_lin], ni = X.start[(size_t)ci_lin + 1] - si;
+    for (int ii = 0; ii < ni; ii++) {
+      const int a = si + ii;
+      const int code_i = X.code[(size_t)a];
+      const bool real_i = code_i >= 0;
+      const int idx_i = real_i ? code_i : -code_i - 1;
+      if (tri && !real_i) continue;
+      T xa[3];
+      for (int k = 0; k < N; k++) xa[k] = X.x(a, k);
+      for (int e = 0; e < nent; e++) {
+        int o[3] = {0, 0, 0};
+        if (e > 0) clm::stencil_offset(false, g.lcell, N, e - 1, o);
+        const int cj[3] = {ci[0] + o[0], ci[1] + o[1], N == 3 ? ci[2] + o[2] : 1};
+        bool inside = true;
+        for (int k = 0; k < N; k++) inside = inside && cj[k] >= 1 && cj[k] <= g.nc[k];
+        if (!inside) continue;
+        const int cj_lin = (N == 3) ? (cj[0] - 1) + g.nc[0] * ((cj[1] - 1) + g.nc[1] * (cj[2] - 1))
+                                    : (cj[0] - 1) + g.nc[0] * (cj[1] - 1);
+        const int sj = Y.start[(size_t)cj_lin], nj = Y.start[(size_t)cj_lin + 1] - sj;
+        T ctr_j[3] = {0, 0, 0};
+        if (e > 0) clm::cell_center<T, N>(g, cj, ctr_j);
+        for (int jj = 0; jj < nj; jj++) {
+          const int b = sj + jj;
+          const int code_j = Y.code[(size_t)b];
+          const bool real_j = code_j >= 0;
+          const int idx_j = real_j ? code_j : -code_j - 1;
+          if (!clm::pair_rule(true, tri, false, e == 0, jj, ii, real_i, real_j, idx_i, idx_j)) continue;
+          T xb[3], dx[3];
+          for (int k = 0; k < N; k++) {
+            xb[k] = Y.x(b, k);
+            dx[k] = clm::xsub(xa[k], xb[k]);
+          }
+          T d2 = clm::xmul(dx[0], dx[0]);
+          for (int k = 1; k < N; k++) d2 = clm::xadd(d2, clm::xmul(dx[k], dx[k]));
+          bool hit = d2 <= g.cutoff_sqr;
+          if (hit && d2 > band && e > 0) hit = clm::projection_pass<T, N>(g, ctr_i, ctr_j, xa, xb);
+          if (!hit) continue;
+          if (!fp32_keeps(X, fx, a, Y, fy, b, o)) (*lost)++;
+          if (np < cap) {
+            pi_out[np] = idx_i;
+            pj_out[np] = idx_j;
+            d_out[np] = (double)clm::xsqrt(d2);
+          }
+          np++;
+        }
+      }
+    }
+  }
+  return np;
+}
+}  // namespace
+
+extern "C" int64_t map_cross_probe(int f64, int dim, int kind, const double* Mcol, double cutoff, int lcell,
+                                   const double* x, int nx, const double* y, int ny, int64_t cap, int64_t* pi,
+                                   int64_t* pj, double* d, int64_t* lost, int* st) {
+  if (dim == 3)
+    return f64 ? map_cross<double, 3>(kind, Mcol, cutoff, lcell, x, nx, y, ny, cap, pi, pj, d, lost, st)
+               : map_cross<float, 3>(kind, Mcol, cutoff, lcell, x, nx, y, ny, cap, pi, pj, d, lost, st);
+  return f64 ? map_cross<double, 2>(kind, Mcol, cutoff, lcell, x, nx, y, ny, cap, pi, pj, d, lost, st)
+             : map_cross<float, 2>(kind, Mcol, cutoff, lcell, x, nx, y, ny, cap, pi, pj, d, lost, st);
 }

@@ -412,3 +412,37 @@ def test_emulated_map_pathological_and_random_cells(probe, orc):
             assert len(A[0]) == len(B[0])
             for u, v in zip(A, B):
                 np.testing.assert_array_equal(u, np.asarray(v, u.dtype))
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("case", [c for c in CASES if c[1] is not None], ids=case_id)
+def test_emulated_cross_map_matches_oracle(probe, orc, case, dtype):
+    # the kernel's x-y pair logic emulated on the host (tests/build_probe.cpp map_cross) against the oracle's
+    # two-set neighbour list (src/internals/cross.jl:8-129): same (i, j) pairs, bit-identical distances
+    dim, uc, cut, lcell, n, span, shift = case
+    rng = np.random.default_rng(31 + lcell + dim)
+    x = (rng.random((n, dim)) * span + shift).astype(dtype)
+    y = (rng.random((n // 2 + 7, dim)) * span + shift).astype(dtype)
+    u = np.asarray(uc, np.float64)
+    Mc = np.ascontiguousarray((np.diag(u) if u.ndim == 1 else u).flatten(order="F"))
+    xd, yd = (np.ascontiguousarray(a.astype(np.float64)) for a in (x, y))
+    probe.map_cross_probe.restype = C.c_int64
+    lost, st = C.c_int64(0), C.c_int(0)
+    vp = C.c_void_p
+
+    def call(cap, i, j, d):
+        return probe.map_cross_probe(int(np.dtype(dtype) == np.float64), dim, KINDS[kind_of(uc)],
+                                     Mc.ctypes.data_as(vp), C.c_double(cut), lcell, xd.ctypes.data_as(vp), len(x),
+                                     yd.ctypes.data_as(vp), len(y), C.c_int64(cap), i.ctypes.data_as(vp),
+                                     j.ctypes.data_as(vp), d.ctypes.data_as(vp), C.byref(lost), C.byref(st))
+
+    e = np.zeros(1, np.int64)
+    m = call(0, e, e, e.astype(np.float64))
+    assert st.value == 0 and m > 0
+    i, j, d = np.zeros(m, np.int64), np.zeros(m, np.int64), np.zeros(m, np.float64)
+    assert call(m, i, j, d) == m and lost.value == 0
+    ref = orc.run("nl", x, y, dim=dim, kind=kind_of(uc), unitcell=uc, cutoff=cut, lcell=lcell, dtype=dtype)
+    a, b = np.lexsort((j, i)), np.lexsort((ref["j"], ref["i"]))
+    np.testing.assert_array_equal(i[a], ref["i"][b])
+    np.testing.assert_array_equal(j[a], ref["j"][b])
+    np.testing.assert_array_equal(d[a], np.asarray(ref["d"][b], np.float64))
