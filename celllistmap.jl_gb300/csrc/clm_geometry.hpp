@@ -13,6 +13,7 @@
 //
 // The host compiler must not contract a*b+c (built with -ffp-contract=off).
 #pragma once
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -315,6 +316,28 @@ template <class T> void nonperiodic_cell(int dim, const T* lo, const T* hi, T cu
     M[i][i] = (hi[i] - lo[i]) + pad;
     origin[i] = lo[i];
   }
+}
+
+// Bound on the error of the FP32 pair distance of the split form (Float64 handles): the offsets of the
+// copies from their cell origins (at most a cell side, within 2^-23 relative), the cell displacement added
+// to the candidate's offset (at most lcell cells, the FP32 cell side within 2^-24), and the subtraction give
+// each component an absolute error below (3 lcell + 5) cell_side 2^-24, the distance below sqrt(dim) times
+// that, plus its own few-ulp rounding.
+template <class T> double split_distance_error(const Geometry<T>& g) {
+  double cs = 0.0;
+  for (int i = 0; i < g.dim; i++) cs = std::max(cs, (double)g.cs[i]);
+  return std::sqrt((double)g.dim) * (3.0 * g.lcell + 5.0) * cs * std::ldexp(1.0, -24);
+}
+
+// The split-form radial histogram decides bins from that FP32 distance and re-decides exactly within 2^-12
+// (relative) of an edge, which covers the error for every edge above split_distance_error * 2^12.  True when
+// all positive edges are above it (the bins then equal the exact form's).  An edge at 0 only separates
+// pairs at distance 0, which the FP32 distance also gives as 0 for copies of the same cell.
+template <class T> bool split_bins_exact(const Geometry<T>& g, const double* edges, int nedges) {
+  const double rmin = split_distance_error(g) * 4096.0;
+  for (int k = 0; k < nedges; k++)
+    if (edges[k] > 0.0 && edges[k] < rmin) return false;
+  return true;
 }
 
 }  // namespace clm

@@ -211,6 +211,16 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
   A.n_real_dev = X.real_scan.as<int>() + X.ncells;
   A.self = (h.nsets == 1);
   A.split = (h.precision == 1) && sizeof(T) == 8;  // Float32 inputs: the split form is the exact form
+  if (op == 11 && A.split && P && P->bins && P->nbins >= 1 && P->nbins <= 256) {
+    // histogram edges finer than the split form's FP32 distance error: run the exact form, so that the
+    // bins stay those of the reference
+    std::vector<double> edges((size_t)P->nbins + 1);
+    if (P->params_on_device)
+      CLM_CUDA_TRY(h, cudaMemcpy(edges.data(), P->bins, sizeof(double) * edges.size(), cudaMemcpyDeviceToHost));
+    else
+      std::copy(P->bins, P->bins + edges.size(), edges.begin());
+    if (!split_bins_exact(g, edges.data(), (int)edges.size())) A.split = false;
+  }
   A.op = op;
   A.err = h.err.as<int>();
   A.cell_split = cell_split_for(h, g, opk);

@@ -471,3 +471,76 @@ extern "C" int64_t map_cross_probe(int f64, int dim, int kind, const double* Mco
   return f64 ? map_cross<double, 2>(kind, Mcol, cutoff, lcell, x, nx, y, ny, cap, pi, pj, d, lost, st)
              : map_cross<float, 2>(kind, Mcol, cutoff, lcell, x, nx, y, ny, cap, pi, pj, d, lost, st);
 }
+
+// Largest |r_fp32 - r| over the pairs within the cutoff (real copy of a cell against every copy of the
+// full stencil), divided by the library's bound split_distance_error: r_fp32 is the split form's FP32
+// distance of cell-relative offsets (shift fused and unfused), r the exact distance.  Float64 handles.
+extern "C" int split_error_probe(int dim, int kind, const double* Mcol, double cutoff, int lcell, const double* x,
+                                 int n, double* worst) {
+  auto run = [&](auto tag) -> int {
+    constexpr int N = decltype(tag)::value;
+    HostList<double, N> L;
+    const int st = build_host<double, N>(kind, Mcol, cutoff, lcell, x, n, L);
+    if (st) return st;
+    const clm::DevGeom<double>& g = L.d;
+    clm::Geometry<double> geo;  // the bound needs the cell sides and lcell only
+    geo.dim = N;
+    geo.lcell = g.lcell;
+    for (int k = 0; k < 3; k++) geo.cs[k] = k < N ? g.cs[k] : 0.0;
+    const double bound = clm::split_distance_error(geo);
+    const std::vector<float4> fo = fp32_offsets(L);
+    const int w = 2 * g.lcell + 1, nst = (N == 3) ? w * w * w : w * w;  // entry 0: the cell itself
+    *worst = 0.0;
+    for (int ci_lin = 0; ci_lin < g.ncells; ci_lin++) {
+      if (!L.flags[(size_t)ci_lin]) continue;
+      int ci[3];
+      clm::cart_of(ci_lin, g.nc, N, ci);
+      for (int s = 0; s < nst; s++) {
+        int o[3] = {0, 0, 0};
+        if (s > 0) clm::stencil_offset(false, g.lcell, N, s - 1, o);
+        const int cj[3] = {ci[0] + o[0], ci[1] + o[1], N == 3 ? ci[2] + o[2] : 1};
+        bool inside = true;
+        for (int k = 0; k < N; k++) inside = inside && cj[k] >= 1 && cj[k] <= g.nc[k];
+        if (!inside) continue;
+        const int cj_lin = (N == 3) ? (cj[0] - 1) + g.nc[0] * ((cj[1] - 1) + g.nc[1] * (cj[2] - 1))
+                                    : (cj[0] - 1) + g.nc[0] * (cj[1] - 1);
+        for (int a = L.start[(size_t)ci_lin]; a < L.start[(size_t)ci_lin + 1]; a++) {
+          if (L.code[(size_t)a] < 0) continue;
+          for (int b = L.start[(size_t)cj_lin]; b < L.start[(size_t)cj_lin + 1]; b++) {
+            double d2 = 0.0;
+            for (int k = 0; k < N; k++) d2 += (L.x(a, k) - L.x(b, k)) * (L.x(a, k) - L.x(b, k));
+            if (d2 > g.cutoff_sqr || b == a) continue;
+            for (int fused = 0; fused < 2; fused++) {
+              float e = 0.f;
+              for (int k = 0; k < N; k++) {
+                const float pa = k == 0 ? fo[(size_t)a].x : (k == 1 ? fo[(size_t)a].y : fo[(size_t)a].z);
+                const float pb = k == 0 ? fo[(size_t)b].x : (k == 1 ? fo[(size_t)b].y : fo[(size_t)b].z);
+                const float q = fused ? std::fmaf(g.csf[k], (float)o[k], pb) : pb + g.csf[k] * (float)o[k];
+                const float dk = pa - q;
+                e = std::fmaf(dk, dk, e);
+              }
+              const double err = std::fabs((double)std::sqrt(e) - std::sqrt(d2));
+              *worst = std::max(*worst, err / bound);
+            }
+          }
+        }
+      }
+    }
+    return 0;
+  };
+  return dim == 3 ? run(std::integral_constant<int, 3>()) : run(std::integral_constant<int, 2>());
+}
+
+// The library's guard for split-form histograms: 1 when every positive edge is above the split form's
+// distance error window (split_bins_exact); *rmin receives that smallest safe edge.
+extern "C" int split_bins_probe(int dim, int kind, const double* Mcol, double cutoff, int lcell, const double* edges,
+                                int nedges, double* rmin) {
+  double M[3][3] = {};
+  for (int i = 0; i < dim; i++)
+    for (int j = 0; j < dim; j++) M[i][j] = (kind == clm::ORTHO && i != j) ? 0.0 : Mcol[j * dim + i];
+  clm::Geometry<double> g;
+  const int st = clm::make_geometry<double>(g, dim, kind, M, cutoff, lcell, nullptr);
+  if (st) return -st;
+  *rmin = clm::split_distance_error(g) * 4096.0;
+  return clm::split_bins_exact(g, edges, nedges) ? 1 : 0;
+}

@@ -446,3 +446,45 @@ def test_emulated_cross_map_matches_oracle(probe, orc, case, dtype):
     np.testing.assert_array_equal(i[a], ref["i"][b])
     np.testing.assert_array_equal(j[a], ref["j"][b])
     np.testing.assert_array_equal(d[a], np.asarray(ref["d"][b], np.float64))
+
+
+SPLIT_CELLS = [
+    (3, [250.0, 250.0, 250.0], 25.0, 20000, 250.0, 0.0),
+    (3, [[20.0, 4.0, 2.0], [0.0, 20.0, 3.0], [0.0, 0.0, 20.0]], 2.0, 20000, 20.0, -3.0),
+    (2, [30.0, 30.0], 2.0, 5000, 30.0, 0.0),
+    (2, [[30.0, 12.0], [0.0, 28.0]], 2.0, 5000, 40.0, -5.0),
+]
+
+
+@pytest.mark.parametrize("lcell", [1, 2, 3])
+@pytest.mark.parametrize("cell", SPLIT_CELLS, ids=lambda c: f"{c[0]}d-{kind_of(c[1])}")
+def test_split_distance_error_within_bound(probe, cell, lcell):
+    # the FP32 distance of the split form (cell-relative FP32 offsets, cell shift fused or not) differs from
+    # the exact one by less than the library's bound split_distance_error, over every pair within the cutoff
+    dim, uc, cut, n, span, shift = cell
+    x = np.ascontiguousarray(np.random.default_rng(50 + lcell).random((n, dim)) * span + shift)
+    u = np.asarray(uc, np.float64)
+    Mc = np.ascontiguousarray((np.diag(u) if u.ndim == 1 else u).flatten(order="F"))
+    worst = C.c_double()
+    assert probe.split_error_probe(dim, KINDS[kind_of(uc)], Mc.ctypes.data_as(C.c_void_p), C.c_double(cut), lcell,
+                                   x.ctypes.data_as(C.c_void_p), n, C.byref(worst)) == 0
+    assert 0.0 < worst.value < 1.0
+
+
+def test_split_histogram_guard(probe):
+    # split-form histograms keep the exact bins only for edges above the FP32 distance error window; the
+    # library runs finer edges in the exact form.  The two-set 2 x 2M workload's edges (first 0.1, cutoff 25
+    # in a 250 box) stay in the split form.
+    M = np.ascontiguousarray(np.diag([250.0] * 3).flatten(order="F"))
+    rmin = C.c_double()
+
+    def guard(edges, lcell=1):
+        e = np.ascontiguousarray(edges, np.float64)
+        return probe.split_bins_probe(3, KINDS["ortho"], M.ctypes.data_as(C.c_void_p), C.c_double(25.0), lcell,
+                                      e.ctypes.data_as(C.c_void_p), len(e), C.byref(rmin))
+
+    bins = 10.0 ** np.linspace(np.log10(0.1), np.log10(25.0), 51)
+    assert guard(bins) == 1
+    assert rmin.value == pytest.approx(np.sqrt(3) * 8 * 25.0 * 2.0 ** -12) and rmin.value < 0.1
+    assert guard(np.concatenate([[0.05], bins])) == 0
+    assert guard(np.arange(0.0, 26.0)) == 1  # an edge at 0 separates only pairs at distance 0

@@ -14,7 +14,9 @@ the host's cores:
   * the two-set radial histogram on a subsample of x against all 2M points of y.
 and through size-independent properties at full size: Newton's third law on the forces (sum of F ~ 0),
 equal counts across operators and precision forms, histogram counts equal between the exact and FP32-split
-forms, the dropped pairs (r <= first edge) accounted for.
+forms, the dropped pairs (r <= first edge) accounted for.  Last, a split-form histogram with edges finer than
+the split form's FP32 distance error, which the library runs in the exact form: its counts equal the
+oracle's for pairs planted within 1e-9 of the edges.
 
 Bars as in the other suites: counts and sets exact; Float64 values within 1e-12 and Float32 (or split)
 values within 1e-5 of the stated scale.  Each check compares plain numpy results (`check_*`), so the same
@@ -213,3 +215,40 @@ def test_histogram_two_sets_full_size(clm, orc):
     s.close()
     r = orc.run("rhist", xs, y, unitcell=sides, cutoff=25.0, bins=bins, vel_x=vxs, vel_y=vy, nthreads=NT)
     check_hist_subsample({"count": hc, "sum": hs}, r, vxs, vy)
+
+
+# ------------------------------------------------------------------ split-form histogram with fine edges
+def fine_edge_points(rng, edges, per_edge=40, side=20.0):
+    """Pairs of points planted at distances within 1e-9 (relative) of the given edges, on both sides, in
+    random directions, plus a uniform background."""
+    pts = [rng.random((2000, 3)) * side]
+    for e in edges:
+        for sgn in (-1.0, 1.0):
+            p = rng.random((per_edge, 3)) * side
+            u = rng.normal(size=(per_edge, 3))
+            u /= np.linalg.norm(u, axis=1)[:, None]
+            pts += [p, p + u * e * (1.0 + sgn * 1e-9)]
+    return np.concatenate(pts)
+
+
+def check_hist_exact_counts(hc, r, dropped_gpu, dropped_ref):
+    np.testing.assert_array_equal(hc, r["hist_count"])
+    assert dropped_gpu == dropped_ref
+
+
+def test_split_histogram_fine_edges(clm, orc):
+    # edges finer than the split form's FP32 distance error (1e-4, 1e-3 with cell side 2): the library runs
+    # such histograms in the exact form, so the counts equal the oracle's even for pairs within 1e-9 of an
+    # edge, and the pairs at or below the first edge are dropped as in the reference
+    rng = np.random.default_rng(17)
+    edges = [1e-4, 1e-3, 1e-2]
+    x = fine_edge_points(rng, edges)
+    v = rng.normal(0.0, 1.0, x.shape)
+    bins = np.array(edges + [0.1, 0.5, 1.0, 2.0])
+    s = clm.ParticleSystem(xpositions=x, unitcell=[20.0] * 3, cutoff=2.0, precision="split")
+    hc, hs = clm.pairwise(clm.RadialHistogram(bins, v), s)
+    n_gpu = clm.pairwise(clm.Count(), s)
+    s.close()
+    r = orc.run("rhist", x, unitcell=[20.0] * 3, cutoff=2.0, bins=bins, vel_x=v, nthreads=NT)
+    n_ref = orc.run("count", x, unitcell=[20.0] * 3, cutoff=2.0, nthreads=NT)["count"]
+    check_hist_exact_counts(hc, r, n_gpu - int(hc.sum()), n_ref - int(r["hist_count"].sum()))
