@@ -100,6 +100,72 @@ int build_host(int kind, const double* Mcol, double cutoff, int lcell, const dou
   return 0;
 }
 
+// FP32 prefilter coordinates of a cell list's copies for Float64 handles, as the gather writes them: the
+// FP32 offset of each copy from its cell origin, in float pairs.
+template <class T, int N> std::vector<float4> fp32_offsets(const HostList<T, N>& L) {
+  const clm::DevGeom<T>& g = L.d;
+  std::vector<float4> foff((size_t)L.total + 1);
+  if (sizeof(T) == 8) {
+    for (int t = 0; t < L.total; t++) {
+      int c[3];
+      clm::cart_of((int)L.skeys[(size_t)t], g.nc, N, c);
+      float o[3] = {0.f, 0.f, 0.f};
+      for (int d = 0; d < N; d++) {
+        float oh, ol;
+        clm::origin_ff(g.cbf_hi[d], g.cbf_lo[d], g.csf[d], g.csf_lo[d], c[d] - 1, oh, ol);
+        const float qh = (float)L.x(t, d);
+        const float ql = (float)(L.x(t, d) - (T)qh);
+        o[d] = (qh - oh) + (ql - ol);
+      }
+      foff[(size_t)t] = make_float4(o[0], o[1], o[2], 0.f);
+    }
+  }
+  return foff;
+}
+
+// The FP32 distance pass of the kernel for copy a of list La against copy b of list Lb in a cell displaced
+// by o: true when it keeps the pair (d2 - thr_hi < 0) with the displacement shift of the offsets both
+// fused and unfused.
+template <class T, int N>
+bool fp32_keeps(const HostList<T, N>& La, const std::vector<float4>& fa, int a, const HostList<T, N>& Lb,
+                const std::vector<float4>& fb, int b, const int* o) {
+  const clm::DevGeom<T>& g = La.d;
+  for (int fused = 0; fused < 2; fused++) {
+    float p[3] = {0.f, 0.f, 0.f}, q[3] = {0.f, 0.f, 0.f};
+    for (int k = 0; k < N; k++) {
+      if (sizeof(T) == 4) {
+        p[k] = (float)La.x(a, k);
+        q[k] = (float)Lb.x(b, k);
+      } else {
+        const float offk = k == 0 ? fb[(size_t)b].x : (k == 1 ? fb[(size_t)b].y : fb[(size_t)b].z);
+        const float sh = (float)o[k];
+        q[k] = fused ? std::fmaf(g.csf[k], sh, offk) : offk + g.csf[k] * sh;
+        p[k] = k == 0 ? fa[(size_t)a].x : (k == 1 ? fa[(size_t)a].y : fa[(size_t)a].z);
+      }
+    }
+    const float fx = p[0] - q[0], fy = p[1] - q[1], fz = p[2] - q[2];
+    const float ef = std::fmaf(fz, fz, std::fmaf(fy, fy, std::fmaf(fx, fx, -g.thr_hi)));
+    if (!(ef < 0.f)) return false;
+  }
+  return true;
+}
+
+// The split form's FP32 squared distance (Float64 handles) of copy a against copy b in a cell displaced by o,
+// with the displacement shift of the candidate's offset fused or not.
+template <class T, int N>
+float fp32_d2(const std::vector<float4>& fa, int a, const std::vector<float4>& fb, int b, const float* csf,
+              const int* o, bool fused) {
+  float e = 0.f;
+  for (int k = 0; k < N; k++) {
+    const float pa = k == 0 ? fa[(size_t)a].x : (k == 1 ? fa[(size_t)a].y : fa[(size_t)a].z);
+    const float pb = k == 0 ? fb[(size_t)b].x : (k == 1 ? fb[(size_t)b].y : fb[(size_t)b].z);
+    const float q = fused ? std::fmaf(csf[k], (float)o[k], pb) : pb + csf[k] * (float)o[k];
+    const float dk = pa - q;
+    e = std::fmaf(dk, dk, e);
+  }
+  return e;
+}
+
 template <class T, int N>
 int run(int kind, const double* Mcol, double cutoff, int lcell, const double* xin, int n, int64_t cap,
         int64_t* n_copies, int64_t* n_real_cells, int64_t* cell, int64_t* idx, int8_t* real, double* coords,
@@ -136,6 +202,7 @@ int band(int kind, const double* Mcol, double cutoff, int lcell, const double* x
   if (st) return st;
   const clm::DevGeom<T>& g = L.d;
   const T thr = (T)g.thr_lo;
+  const std::vector<float4> fo = fp32_offsets(L);
   const int w = 2 * g.lcell + 1;
   const int nst = (N == 3) ? w * w * w - 1 : w * w - 1;
   for (int k = 0; k < 5; k++) out[k] = 0;
@@ -169,6 +236,11 @@ int band(int kind, const double* Mcol, double cutoff, int lcell, const double* x
           T d2 = clm::xmul(dx[0], dx[0]);  // the exact d2, in the reference's order
           for (int k = 1; k < N; k++) d2 = clm::xadd(d2, clm::xmul(dx[k], dx[k]));
           bool shortcut = d2 <= thr;
+          if constexpr (sizeof(T) == 8) {
+            // the split form accepts a pair whose FP32 offset distance is below thr_lo (either rounding)
+            for (int fused = 0; fused < 2; fused++)
+              if (fp32_d2<T, N>(fo, a, fo, b, g.csf, o, fused != 0) <= g.thr_lo) shortcut = true;
+          }
           if constexpr (sizeof(T) == 4) {
             const float fx = xa[0] - xb[0], fy = xa[1] - xb[1], fz = (N == 3) ? xa[N - 1] - xb[N - 1] : 0.f;
             const float d2f = std::fmaf(fz, fz, std::fmaf(fy, fy, fx * fx));
@@ -240,56 +312,6 @@ extern "C" int cell_probe(int dim, int kind, const double* Mcol, double cutoff, 
 }
 
 namespace {
-// FP32 prefilter coordinates of a cell list's copies for Float64 handles, as the gather writes them: the
-// FP32 offset of each copy from its cell origin, in float pairs.
-template <class T, int N> std::vector<float4> fp32_offsets(const HostList<T, N>& L) {
-  const clm::DevGeom<T>& g = L.d;
-  std::vector<float4> foff((size_t)L.total + 1);
-  if (sizeof(T) == 8) {
-    for (int t = 0; t < L.total; t++) {
-      int c[3];
-      clm::cart_of((int)L.skeys[(size_t)t], g.nc, N, c);
-      float o[3] = {0.f, 0.f, 0.f};
-      for (int d = 0; d < N; d++) {
-        float oh, ol;
-        clm::origin_ff(g.cbf_hi[d], g.cbf_lo[d], g.csf[d], g.csf_lo[d], c[d] - 1, oh, ol);
-        const float qh = (float)L.x(t, d);
-        const float ql = (float)(L.x(t, d) - (T)qh);
-        o[d] = (qh - oh) + (ql - ol);
-      }
-      foff[(size_t)t] = make_float4(o[0], o[1], o[2], 0.f);
-    }
-  }
-  return foff;
-}
-
-// The FP32 distance pass of the kernel for copy a of list La against copy b of list Lb in a cell displaced
-// by o: true when it keeps the pair (d2 - thr_hi < 0) with the displacement shift of the offsets both
-// fused and unfused.
-template <class T, int N>
-bool fp32_keeps(const HostList<T, N>& La, const std::vector<float4>& fa, int a, const HostList<T, N>& Lb,
-                const std::vector<float4>& fb, int b, const int* o) {
-  const clm::DevGeom<T>& g = La.d;
-  for (int fused = 0; fused < 2; fused++) {
-    float p[3] = {0.f, 0.f, 0.f}, q[3] = {0.f, 0.f, 0.f};
-    for (int k = 0; k < N; k++) {
-      if (sizeof(T) == 4) {
-        p[k] = (float)La.x(a, k);
-        q[k] = (float)Lb.x(b, k);
-      } else {
-        const float offk = k == 0 ? fb[(size_t)b].x : (k == 1 ? fb[(size_t)b].y : fb[(size_t)b].z);
-        const float sh = (float)o[k];
-        q[k] = fused ? std::fmaf(g.csf[k], sh, offk) : offk + g.csf[k] * sh;
-        p[k] = k == 0 ? fa[(size_t)a].x : (k == 1 ? fa[(size_t)a].y : fa[(size_t)a].z);
-      }
-    }
-    const float fx = p[0] - q[0], fy = p[1] - q[1], fz = p[2] - q[2];
-    const float ef = std::fmaf(fz, fz, std::fmaf(fy, fy, std::fmaf(fx, fx, -g.thr_hi)));
-    if (!(ef < 0.f)) return false;
-  }
-  return true;
-}
-
 // The self-pair map of the pair kernel, emulated on the host from the library's own pieces: the cells with
 // real particles, every copy of such a cell as the particle side (real copies only in triclinic cells),
 // stencil entry 0 (the cell itself) then the forward half stencil (orthorhombic, non-periodic) or all
@@ -511,14 +533,7 @@ extern "C" int split_error_probe(int dim, int kind, const double* Mcol, double c
             for (int k = 0; k < N; k++) d2 += (L.x(a, k) - L.x(b, k)) * (L.x(a, k) - L.x(b, k));
             if (d2 > g.cutoff_sqr || b == a) continue;
             for (int fused = 0; fused < 2; fused++) {
-              float e = 0.f;
-              for (int k = 0; k < N; k++) {
-                const float pa = k == 0 ? fo[(size_t)a].x : (k == 1 ? fo[(size_t)a].y : fo[(size_t)a].z);
-                const float pb = k == 0 ? fo[(size_t)b].x : (k == 1 ? fo[(size_t)b].y : fo[(size_t)b].z);
-                const float q = fused ? std::fmaf(g.csf[k], (float)o[k], pb) : pb + g.csf[k] * (float)o[k];
-                const float dk = pa - q;
-                e = std::fmaf(dk, dk, e);
-              }
+              const float e = fp32_d2<double, N>(fo, a, fo, b, g.csf, o, fused != 0);
               const double err = std::fabs((double)std::sqrt(e) - std::sqrt(d2));
               *worst = std::max(*worst, err / bound);
             }

@@ -288,8 +288,8 @@ BAND_CELLS = [
 @pytest.mark.parametrize("cell", BAND_CELLS, ids=lambda c: f"{c[0]}d-{kind_of(c[1])}")
 def test_projection_filter_passes_inside_the_band(probe, cell, lcell, dtype):
     # The pair kernel evaluates the reference's projection filter (vicinal_cells.jl:4-75) only for pairs with
-    # d2 > rc^2 (1 - 2^-13) (and, for Float32 handles, accepts a pair whose FP32 fma distance test is below
-    # that bound).  The filter keeps every pair well inside the cutoff: |(x_j - x_i).u| <= d < rc, and the
+    # d2 > rc^2 (1 - 2^-13) (and accepts a pair whose FP32 distance is below that bound: the fma test on the
+    # coordinates for Float32 handles, on the cell-relative offsets in the split form for Float64 handles).  The filter keeps every pair well inside the cutoff: |(x_j - x_i).u| <= d < rc, and the
     # particle's projection on the cell-pair axis is at most half the centre distance (lcell 1) or
     # rc sqrt(N)/2 (lcell > 1), inside the margins.  Checked over every pair of the full stencil.
     dim, uc = cell
