@@ -145,7 +145,10 @@ int32_t clm_set_positions(clm_handle h, int32_t set, const void* xyz, int64_t n,
  * 1180-1204; non-periodic: src/internals/NonPeriodicCells.jl:93-251. */
 int32_t clm_build(clm_handle h);
 
-/* Select the precision form of clm_run (CLM_PREC_EXACT or CLM_PREC_SPLIT). */
+/* Select the precision form of clm_run (CLM_PREC_EXACT or CLM_PREC_SPLIT).  In the split form pair sets,
+ * counts and histogram bins stay those of the exact form; a Float64 radial histogram whose positive bin edges
+ * come closer to 0 than the split form's FP32 distance error window (about sqrt(dim) (3 lcell + 5) cell side
+ * 2^-12) runs in the exact form. */
 int32_t clm_set_precision(clm_handle h, int32_t precision);
 
 /* _pairwise!(op, output, box, cl) — src/internals/self.jl:28-184,
