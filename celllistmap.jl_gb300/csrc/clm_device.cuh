@@ -260,6 +260,26 @@ __host__ __device__ bool projection_pass(const DevGeom<T>& g, const T* cf, const
   return xabs(xsub(pt, pf)) <= g.cutoff;
 }
 
+// Radial histogram bins (test/examples/pairwise_velocities.jl:17-24): the index of the first of the
+// nbins + 1 ascending edges that is >= r (searchsortedfirst - 1 gives the bin: r on an edge goes to the
+// lower bin, r <= edges[0] to none, r > edges[nbins] to none).
+template <class E> __host__ __device__ __forceinline__ int first_edge_at_or_above(const E* edges, int nbins, E r) {
+  int lo = 0, hi = nbins + 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (edges[mid] >= r) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo;
+}
+
+// FP32 distance rf within 2^-12 (relative) of one of the two edges around it (lo from
+// first_edge_at_or_above): the split form then decides the bin from the exact distance.
+__host__ __device__ __forceinline__ bool near_edge(const float* edges, int nbins, int lo, float rf) {
+  const float tol = rf * 2.44140625e-4f;
+  return (lo <= nbins && xabs(edges[lo] - rf) <= tol) || (lo >= 1 && xabs(edges[lo - 1] - rf) <= tol);
+}
+
 // Device error bits (OR-ed into the handle's error word).
 enum DevError : int {
   DERR_NAN = 1,

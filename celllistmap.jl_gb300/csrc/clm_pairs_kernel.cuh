@@ -731,16 +731,9 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                 int b = -1;
                 if (sure) {
                   float rf = sqrtf(d2f);
-                  int lo = 0, hi = A.nbins + 1;
-                  while (lo < hi) {
-                    int mid = (lo + hi) >> 1;
-                    if (s_binf[mid] >= rf) hi = mid;
-                    else lo = mid + 1;
-                  }
+                  const int lo = first_edge_at_or_above(s_binf, A.nbins, rf);
                   b = lo - 1;
-                  const float tol = rf * 2.44140625e-4f;  // an edge within 2^-12: decide exactly
-                  if ((lo <= A.nbins && fabsf(s_binf[lo] - rf) <= tol) || (lo >= 1 && fabsf(s_binf[lo - 1] - rf) <= tol))
-                    exact_r = true;
+                  if (near_edge(s_binf, A.nbins, lo, rf)) exact_r = true;  // an edge within 2^-12: decide exactly
                   rfl = rf;
                   if constexpr (!std::is_same<FA, float>::value) r = (T)rf;
                 }
@@ -758,13 +751,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                   }
                   r = xsqrt(e2);
                   rfl = (float)r;
-                  int lo = 0, hi = A.nbins + 1;
-                  while (lo < hi) {
-                    int mid = (lo + hi) >> 1;
-                    if (s_bins[mid] >= r) hi = mid;
-                    else lo = mid + 1;
-                  }
-                  b = lo - 1;
+                  b = first_edge_at_or_above(s_bins, A.nbins, r) - 1;
                 }
                 if (b >= 0 && b < A.nbins) {
                   FA dv[3] = {0, 0, 0};

@@ -559,3 +559,13 @@ extern "C" int split_bins_probe(int dim, int kind, const double* Mcol, double cu
   *rmin = clm::split_distance_error(g) * 4096.0;
   return clm::split_bins_exact(g, edges, nedges) ? 1 : 0;
 }
+
+// The pair kernel's histogram bin search (first_edge_at_or_above, on Float64 edges) and the split form's
+// exact re-decision window (near_edge, on FP32 edges).
+extern "C" int bin_probe(const double* edges, int nbins, double r) {
+  return clm::first_edge_at_or_above(edges, nbins, r);
+}
+extern "C" int near_edge_probe(const float* edges, int nbins, float rf, int* lo) {
+  *lo = clm::first_edge_at_or_above(edges, nbins, rf);
+  return clm::near_edge(edges, nbins, *lo, rf) ? 1 : 0;
+}

@@ -488,3 +488,39 @@ def test_split_histogram_guard(probe):
     assert rmin.value == pytest.approx(np.sqrt(3) * 8 * 25.0 * 2.0 ** -12) and rmin.value < 0.1
     assert guard(np.concatenate([[0.05], bins])) == 0
     assert guard(np.arange(0.0, 26.0)) == 1  # an edge at 0 separates only pairs at distance 0
+
+
+def test_histogram_bin_search(probe):
+    # the kernel's bin of a distance r: searchsortedfirst(edges, r) - 1 (test/examples/pairwise_velocities.jl:
+    # 17-24): an r on an edge goes to the lower bin, r <= edges[0] and r > edges[-1] to none
+    probe.bin_probe.argtypes = [C.c_void_p, C.c_int, C.c_double]
+    edges = np.ascontiguousarray(10.0 ** np.linspace(-1, np.log10(25.0), 51))
+    rng = np.random.default_rng(3)
+    rs = np.concatenate([edges, np.nextafter(edges, 0), np.nextafter(edges, 30), rng.uniform(0, 30, 2000), [0.0]])
+    for r in rs:
+        lo = probe.bin_probe(edges.ctypes.data, 50, float(r))
+        assert lo == np.searchsorted(edges, r, side="left"), r
+
+
+def test_split_bin_window_covers_the_error(probe):
+    # an FP32 distance within the split form's error bound of the exact one: whenever it falls in another
+    # bin than the exact distance, the window sends the pair to the exact decision (edges above the guard's
+    # bound; the 2 x 2M workload: cutoff 25 in a 250 box, lcell 1)
+    probe.bin_probe.argtypes = [C.c_void_p, C.c_int, C.c_double]
+    probe.near_edge_probe.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_void_p]
+    edges = np.ascontiguousarray(10.0 ** np.linspace(-1, np.log10(25.0), 51))
+    ef = np.ascontiguousarray(edges.astype(np.float32))
+    err = np.sqrt(3) * 8 * 25.0 * 2.0 ** -24  # split_distance_error of that geometry
+    assert edges[0] > err * 4096
+    rng = np.random.default_rng(4)
+    lo = C.c_int()
+    flagged = 0
+    for e in edges:
+        for r in e + rng.uniform(-3 * err, 3 * err, 200):
+            b_exact = probe.bin_probe(edges.ctypes.data, 50, float(r)) - 1
+            for rf in (np.float32(r + err), np.float32(r - err), np.float32(r)):
+                near = probe.near_edge_probe(ef.ctypes.data, 50, float(rf), C.byref(lo))
+                if lo.value - 1 != b_exact:
+                    assert near == 1, (e, r, rf)
+                flagged += near
+    assert flagged > 0
