@@ -29,16 +29,18 @@ template <class T, int N> struct HostList {
 // Geometry and cell list of one set, as clm_set_box + clm_build make them; returns a clm status (or 9x for a
 // broken cell-start table).
 template <class T, int N>
-int build_host(int kind, const double* Mcol, double cutoff, int lcell, const double* xin, int n, HostList<T, N>& L) {
+int build_host(int kind, const double* Mcol, double cutoff, int lcell, const double* xin, int n, HostList<T, N>& L,
+               const double* other = nullptr, int n_other = 0) {
   std::vector<T> x((size_t)n * N), wrapped((size_t)n * N);
   for (size_t k = 0; k < x.size(); k++) x[k] = (T)xin[k];
   T M[3][3] = {}, origin[3] = {0, 0, 0};
   if (kind == clm::NONPERIODIC) {
-    // the limits box of the particles, as the library's set_limits + nonperiodic_cell make it
+    // the limits box of the particles (of both sets for x-y pairs: `other`), as the library's set_limits +
+    // nonperiodic_cell make it
     T lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-    for (int i = 0; i < n; i++)
+    for (int i = 0; i < n + n_other; i++)
       for (int k = 0; k < N; k++) {
-        const T v = x[(size_t)i * N + k];
+        const T v = i < n ? x[(size_t)i * N + k] : (T)other[(size_t)(i - n) * N + k];
         lo[k] = i ? clm::geo::jmin(lo[k], v) : v;
         hi[k] = i ? clm::geo::jmax(hi[k], v) : v;
       }
@@ -404,7 +406,7 @@ extern "C" int64_t map_nl_probe(int f64, int dim, int kind, const double* Mcol, 
 }
 
 namespace {
-// The x-y (cross) map of the pair kernel emulated on the host, periodic cells: the cells with real x
+// The x-y (cross) map of the pair kernel emulated on the host: the cells with real x
 // particles, every x copy of such a cell as the particle side (real copies only in triclinic cells), the y
 // copies of the cell itself and of all its neighbours as candidates, the kernel's pair rule, the exact test,
 // the band and the projection filter; the FP32 pass is checked as for self pairs.
@@ -412,11 +414,9 @@ template <class T, int N>
 int64_t map_cross(int kind, const double* Mcol, double cutoff, int lcell, const double* xin, int nx,
                   const double* yin, int ny, int64_t cap, int64_t* pi_out, int64_t* pj_out, double* d_out,
                   int64_t* lost, int* st_out) {
-  *st_out = (kind == clm::NONPERIODIC) ? 77 : 0;  // non-periodic cross boxes span both sets: not emulated
-  if (*st_out) return -1;
-  HostList<T, N> X, Y;
-  *st_out = build_host<T, N>(kind, Mcol, cutoff, lcell, xin, nx, X);
-  if (!*st_out) *st_out = build_host<T, N>(kind, Mcol, cutoff, lcell, yin, ny, Y);
+  HostList<T, N> X, Y;  // one geometry for both sets (non-periodic: the limits of both)
+  *st_out = build_host<T, N>(kind, Mcol, cutoff, lcell, xin, nx, X, yin, ny);
+  if (!*st_out) *st_out = build_host<T, N>(kind, Mcol, cutoff, lcell, yin, ny, Y, xin, nx);
   if (*st_out) return -1;
   const clm::DevGeom<T>& g = X.d;
   const bool tri = g.kind == clm::TRICLINIC;
@@ -458,7 +458,8 @@ int64_t map_cross(int kind, const double* Mcol, double cutoff, int lcell, const 
           const int code_j = Y.code[(size_t)b];
           const bool real_j = code_j >= 0;
           const int idx_j = real_j ? code_j : -code_j - 1;
-          if (!clm::pair_rule(true, tri, false, e == 0, jj, ii, real_i, real_j, idx_i, idx_j)) continue;
+          if (!clm::pair_rule(true, tri, g.kind == clm::NONPERIODIC, e == 0, jj, ii, real_i, real_j, idx_i, idx_j))
+            continue;
           T xb[3], dx[3];
           for (int k = 0; k < N; k++) {
             xb[k] = Y.x(b, k);

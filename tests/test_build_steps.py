@@ -415,7 +415,7 @@ def test_emulated_map_pathological_and_random_cells(probe, orc):
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
-@pytest.mark.parametrize("case", [c for c in CASES if c[1] is not None], ids=case_id)
+@pytest.mark.parametrize("case", CASES, ids=case_id)
 def test_emulated_cross_map_matches_oracle(probe, orc, case, dtype):
     # the kernel's x-y pair logic emulated on the host (tests/build_probe.cpp map_cross) against the oracle's
     # two-set neighbour list (src/internals/cross.jl:8-129): same (i, j) pairs, bit-identical distances
@@ -423,8 +423,11 @@ def test_emulated_cross_map_matches_oracle(probe, orc, case, dtype):
     rng = np.random.default_rng(31 + lcell + dim)
     x = (rng.random((n, dim)) * span + shift).astype(dtype)
     y = (rng.random((n // 2 + 7, dim)) * span + shift).astype(dtype)
-    u = np.asarray(uc, np.float64)
-    Mc = np.ascontiguousarray((np.diag(u) if u.ndim == 1 else u).flatten(order="F"))
+    if uc is None:
+        Mc = np.zeros(dim * dim)
+    else:
+        u = np.asarray(uc, np.float64)
+        Mc = np.ascontiguousarray((np.diag(u) if u.ndim == 1 else u).flatten(order="F"))
     xd, yd = (np.ascontiguousarray(a.astype(np.float64)) for a in (x, y))
     probe.map_cross_probe.restype = C.c_int64
     lost, st = C.c_int64(0), C.c_int(0)
