@@ -1,11 +1,17 @@
-// Test infrastructure: runs the cell-list build steps of the library (csrc/clm_build_steps.cuh: the geometry
-// copy the kernels receive, K1 wrap_count_at, K2 emit_at, K4 gather_at) on the host, one particle or copy at a
-// time, so that the CPU tests can compare the copies, their cells and their coordinates with the oracle's
-// serial cell list without a GPU.  The exclusive scan and the radix sort between the steps are replaced by
-// their contracts (copy offsets in particle order; a stable sort of the copies by cell).  It also exposes the
-// pair kernel's stencil enumeration and checks, over every pair of a host-built cell list, the condition under
-// which the pair kernel skips the projection filter.  Built by tests/test_build_steps.py with g++
-// -ffp-contract=off, as the library's host code is.
+// Test infrastructure: runs the library's device-code decisions on the host, so that the CPU tests can
+// compare them with the oracle without a GPU (built by tests/test_build_steps.py with g++
+// -ffp-contract=off, as the library's host code is):
+//   build_probe        the cell-list build steps (csrc/clm_build_steps.cuh: the geometry copy the kernels
+//                      receive, K1 wrap_count_at, K2 emit_at, K4 gather_at) one particle or copy at a time,
+//                      with the scan and the radix sort replaced by their contracts (copy offsets in particle
+//                      order; a stable sort of the copies by cell);
+//   stencil_probe      the pair kernel's stencil enumeration; cell_probe its cell index (border case);
+//   band_probe         the condition under which the pair kernel skips the projection filter;
+//   map_nl_probe,      the self and x-y pair maps emulated from the kernel's pieces (stencil, pair_rule,
+//   map_cross_probe    exact test, band, projection filter, FP32 distance pass);
+//   split_error_probe, the split form's FP32 distance error against its bound, the histogram guard, the
+//   split_bins_probe,  bin search and the exact re-decision window.
+//   bin_probe, near_edge_probe
 #include <algorithm>
 #include <cmath>
 #include <cstdint>

@@ -6,10 +6,14 @@ each copy, the gather of the copy coordinates in cell order) for the host and dr
 time.  The copies, their cells (with the border-case shift of real particles), their in-cell order, realness
 and coordinates must equal the oracle's (src/internals/CellLists.jl:727-1057, Box.jl:499-566) bit for bit, in
 Float64 and Float32, for orthorhombic, triclinic and non-periodic boxes in 2D and 3D, and over the
-reference's pathological coordinates and random cells (test/modules/Testing.jl:36-60, 162-257).  The pair
-kernel's stencil enumeration (csrc/clm_device.cuh stencil_offset) must list the reference's forward and full
-neighbour cells in the reference's order.  These run without a GPU; the GPU tests check the same lists built
-by the kernels themselves.
+reference's pathological coordinates and random cells (test/modules/Testing.jl:36-60, 162-257).
+
+The pair kernel's decisions are checked the same way (csrc/clm_device.cuh): its stencil lists the
+reference's forward and full neighbour cells in the reference's order; its shortcut around the projection
+filter keeps only pairs the filter keeps; the self and x-y maps emulated from its pieces give the oracle's
+neighbour lists with bit-identical distances; the split form's FP32 distance error stays within the bound
+its histogram guard uses, and the bin search and re-decision window decide the bins exactly.  These run
+without a GPU; the GPU tests check the kernels themselves.
 """
 import ctypes as C
 import os
