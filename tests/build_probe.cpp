@@ -10,8 +10,9 @@
 //   map_nl_probe,      the self and x-y pair maps emulated from the kernel's pieces (stencil, pair_rule,
 //   map_cross_probe    exact test, band, projection filter, FP32 distance pass);
 //   split_error_probe, the split form's FP32 distance error against its bound, the histogram guard, the
-//   split_bins_probe,  bin search and the exact re-decision window.
-//   bin_probe, near_edge_probe
+//   split_bins_probe,  bin search and the exact re-decision window, and the split form's histogram
+//   bin_probe,         counts composed over every x-y pair.
+//   near_edge_probe, split_hist_probe
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -575,4 +576,79 @@ extern "C" int bin_probe(const double* edges, int nbins, double r) {
 extern "C" int near_edge_probe(const float* edges, int nbins, float rf, int* lo) {
   *lo = clm::first_edge_at_or_above(edges, nbins, rf);
   return clm::near_edge(edges, nbins, *lo, rf) ? 1 : 0;
+}
+
+// Histogram counts of the x-y pairs the way the split form bins them (Float64 handles): a pair the FP32
+// pass accepts outright (FP32 distance below the band) takes its bin from that FP32 distance unless the
+// re-decision window applies; every other pair (and windowed ones) from the exact distance.  counts has
+// nbins entries; returns the number of binned pairs, or -1 with *st set.
+extern "C" int64_t split_hist_probe(int dim, int kind, const double* Mcol, double cutoff, int lcell, const double* x,
+                                    int nx, const double* y, int ny, const double* edges, int nbins, int64_t* counts,
+                                    int* st) {
+  auto run = [&](auto tag) -> int64_t {
+    constexpr int N = decltype(tag)::value;
+    HostList<double, N> X, Y;
+    *st = build_host<double, N>(kind, Mcol, cutoff, lcell, x, nx, X, y, ny);
+    if (!*st) *st = build_host<double, N>(kind, Mcol, cutoff, lcell, y, ny, Y, x, nx);
+    if (*st) return -1;
+    const clm::DevGeom<double>& g = X.d;
+    std::vector<float> ef((size_t)nbins + 1);
+    for (int k = 0; k <= nbins; k++) ef[(size_t)k] = (float)edges[k];
+    const std::vector<float4> fx = fp32_offsets(X), fy = fp32_offsets(Y);
+    const bool tri = g.kind == clm::TRICLINIC, nonper = g.kind == clm::NONPERIODIC;
+    const int w = 2 * g.lcell + 1, nent = (N == 3) ? w * w * w : w * w;
+    for (int k = 0; k < nbins; k++) counts[k] = 0;
+    int64_t binned = 0;
+    for (int ci_lin = 0; ci_lin < g.ncells; ci_lin++) {
+      if (!X.flags[(size_t)ci_lin]) continue;
+      int ci[3];
+      clm::cart_of(ci_lin, g.nc, N, ci);
+      double ctr_i[3] = {0, 0, 0};
+      clm::cell_center<double, N>(g, ci, ctr_i);
+      for (int a = X.start[(size_t)ci_lin]; a < X.start[(size_t)ci_lin + 1]; a++) {
+        const int ii = a - X.start[(size_t)ci_lin];
+        const int code_i = X.code[(size_t)a];
+        const bool real_i = code_i >= 0;
+        if (tri && !real_i) continue;
+        double xa[3];
+        for (int k = 0; k < N; k++) xa[k] = X.x(a, k);
+        for (int e = 0; e < nent; e++) {
+          int o[3] = {0, 0, 0};
+          if (e > 0) clm::stencil_offset(false, g.lcell, N, e - 1, o);
+          const int cj[3] = {ci[0] + o[0], ci[1] + o[1], N == 3 ? ci[2] + o[2] : 1};
+          bool inside = true;
+          for (int k = 0; k < N; k++) inside = inside && cj[k] >= 1 && cj[k] <= g.nc[k];
+          if (!inside) continue;
+          const int cj_lin = (N == 3) ? (cj[0] - 1) + g.nc[0] * ((cj[1] - 1) + g.nc[1] * (cj[2] - 1))
+                                      : (cj[0] - 1) + g.nc[0] * (cj[1] - 1);
+          double ctr_j[3] = {0, 0, 0};
+          if (e > 0) clm::cell_center<double, N>(g, cj, ctr_j);
+          for (int b = Y.start[(size_t)cj_lin]; b < Y.start[(size_t)cj_lin + 1]; b++) {
+            const int jj = b - Y.start[(size_t)cj_lin];
+            const int code_j = Y.code[(size_t)b];
+            if (!clm::pair_rule(true, tri, nonper, e == 0, jj, ii, real_i, code_j >= 0, 0, 0)) continue;
+            double xb[3], d2 = 0.0;
+            for (int k = 0; k < N; k++) xb[k] = Y.x(b, k);
+            for (int k = 0; k < N; k++) d2 = clm::xadd(d2, clm::xmul(clm::xsub(xa[k], xb[k]), clm::xsub(xa[k], xb[k])));
+            const float d2f = fp32_d2<double, N>(fx, a, fy, b, g.csf, o, true);
+            const bool sure = d2f <= g.thr_lo;
+            bool hit = sure || d2 <= g.cutoff_sqr;
+            if (hit && !sure && d2 > (double)g.thr_lo && e > 0) hit = clm::projection_pass<double, N>(g, ctr_i, ctr_j, xa, xb);
+            if (!hit) continue;
+            int bin;
+            const float rf = std::sqrt(d2f);
+            const int lo = clm::first_edge_at_or_above(ef.data(), nbins, rf);
+            if (sure && !clm::near_edge(ef.data(), nbins, lo, rf)) bin = lo - 1;
+            else bin = clm::first_edge_at_or_above(edges, nbins, clm::xsqrt(d2)) - 1;
+            if (bin >= 0 && bin < nbins) {
+              counts[bin]++;
+              binned++;
+            }
+          }
+        }
+      }
+    }
+    return binned;
+  };
+  return dim == 3 ? run(std::integral_constant<int, 3>()) : run(std::integral_constant<int, 2>());
 }

@@ -531,3 +531,26 @@ def test_split_bin_window_covers_the_error(probe):
                     assert near == 1, (e, r, rf)
                 flagged += near
     assert flagged > 0
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_emulated_split_histogram_counts(probe, orc, dim):
+    # the split form's binning composed over every x-y pair of a sample with the two-set workload's geometry
+    # (box 250, cutoff 25, 50 log-spaced edges from 0.1): the same counts as the oracle's exact histogram
+    rng = np.random.default_rng(12 + dim)
+    n = 20000 if dim == 3 else 4000
+    x = np.ascontiguousarray(rng.random((n, dim)) * 250.0)
+    y = np.ascontiguousarray(rng.random((n, dim)) * 250.0)
+    edges = np.ascontiguousarray(10.0 ** np.linspace(-1, np.log10(25.0), 51))
+    Mc = np.ascontiguousarray(np.diag([250.0] * dim).flatten(order="F"))
+    counts = np.zeros(50, np.int64)
+    st = C.c_int()
+    probe.split_hist_probe.restype = C.c_int64
+    vp = C.c_void_p
+    m = probe.split_hist_probe(dim, KINDS["ortho"], Mc.ctypes.data_as(vp), C.c_double(25.0), 1, x.ctypes.data_as(vp),
+                               n, y.ctypes.data_as(vp), n, edges.ctypes.data_as(vp), 50, counts.ctypes.data_as(vp),
+                               C.byref(st))
+    assert st.value == 0 and m == counts.sum() > 0
+    r = orc.run("rhist", x, y, dim=dim, unitcell=[250.0] * dim, cutoff=25.0, bins=edges, vel_x=np.zeros_like(x),
+                vel_y=np.zeros_like(y))
+    np.testing.assert_array_equal(counts, r["hist_count"])
