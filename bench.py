@@ -32,7 +32,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "within-cutoff pairs/s (cell-list build + pair map, LJ energy+forces)"
-NCU_TRAFFIC_BYTES = 56_836_352 + 319_232  # DRAM bytes per launch of the headline pair kernel (ncu)
+# DRAM bytes per launch of the headline pair kernel, from the ncu capture recorded beside its summary
+TRAFFIC_RECORD = os.path.join(ROOT, "profiles", "k_pairs_lj_forces_f32_fcc1M_triclinic.json")
 WORKLOAD = "fcc1M_f32_triclinic_lj_rc2.5"
 CUTOFF = 2.5
 
@@ -233,6 +234,15 @@ def measure_forms(pkg, L, A, dev, stream, flush, peaks, which, steps, warmup):
         roof = roofline_pairs(F, peak, bpp, hbm)
         return {"pairs_per_s": v, "kernel_ms": ms, "roofline_pairs_per_s": roof, "frac": v / roof}
 
+    def form_entry(pairs, ms, F, split, bpp=0.0):
+        """A Float64 form against the pipe that does its distance work: the FP32 pipe for the split form,
+        the FP64 pipe for the exact form (the other fraction beside it)."""
+        e = frac_entry(pairs, ms, F, p32 if split else p64, bpp)
+        e["pipe"] = "fp32" if split else "fp64"
+        other = roofline_pairs(F, p64 if split else p32, bpp, hbm)
+        e["frac_of_fp64_roofline" if split else "frac_of_fp32_roofline"] = e["pairs_per_s"] / other
+        return e
+
     if "cfg1" in which:
         log("cfg1")
         x, side = W.cfg1()
@@ -252,9 +262,8 @@ def measure_forms(pkg, L, A, dev, stream, flush, peaks, which, steps, warmup):
                 L.clm_set_precision(P.h, prec)
                 st_ms, k_ms, b_ms = P.timed([xd], A.OP[opname], p, o, steps, warmup, flush)
                 F = 8 * R + F_OP[opname]
-                e = frac_entry(pairs, k_ms, F, p64, 16.0 if opname == "nl" else 0.0)
-                e.update({"step_ms": st_ms, "build_ms": b_ms, "step_pairs_per_s": pairs / (st_ms * 1e-3),
-                          "frac_of_fp32_roofline": e["pairs_per_s"] / roofline_pairs(F, p32)})
+                e = form_entry(pairs, k_ms, F, tag == "split", 16.0 if opname == "nl" else 0.0)
+                e.update({"step_ms": st_ms, "build_ms": b_ms, "step_pairs_per_s": pairs / (st_ms * 1e-3)})
                 res[f"{opname}/{tag}"] = e
         P.close()
         out["cfg1"] = res
@@ -280,8 +289,8 @@ def measure_forms(pkg, L, A, dev, stream, flush, peaks, which, steps, warmup):
             L.clm_set_precision(P.h, prec)
             st_ms, k_ms, b_ms = P.timed([xd], A.OP["lj_forces"], p, o, steps, warmup, flush)
             F = 8 * R + F_OP["lj_forces"]
-            e = frac_entry(pairs, k_ms, F, p64)
-            e.update({"step_ms": st_ms, "build_ms": b_ms, "frac_of_fp32_roofline": e["pairs_per_s"] / roofline_pairs(F, p32)})
+            e = form_entry(pairs, k_ms, F, tag == "split")
+            e.update({"step_ms": st_ms, "build_ms": b_ms})
             res[tag] = e
         res["split_over_exact"] = res["exact"]["kernel_ms"] / res["split"]["kernel_ms"]
         P.close()
@@ -317,28 +326,33 @@ def measure_forms(pkg, L, A, dev, stream, flush, peaks, which, steps, warmup):
                 if k >= warmup:
                     ts.append(bs.last_step()["step_ms"])
             ms = statistics.median(ts)
-            e = frac_entry(pairs, ms, F, p64, 16.0)
+            e = form_entry(pairs, ms, F, tag == "split", 16.0)
             e.update({"graph_launches": bs.last_step()["launches"], "step_ms": ms})
             res[tag] = e
             bs.graph = False
-        # the plain path on the same systems: one handle, one system at a time (host loop)
+        # the plain path on the same systems, one system at a time: the sum of its device time per system
+        # (CUDA events around each build and map, the library's own timings), so that host overhead between
+        # the systems is not counted against it
         P = Plain(L, A, np.float64, 3, 1, stream)
         o = A.Outputs()
         p = A.OpParams()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for s in range(len(sides)):
-            if not valid[s]:
-                continue
-            P.box(np.diag([sides[s]] * 3), A.CLM_ORTHO, 6.0)
-            xs = xd[off[s]:off[s + 1]]
-            P.step([xs], A.OP["nl"], p, o)
-            P.step([xs], A.OP["soft_energy"], p, o)
-        torch.cuda.synchronize()
-        plain_ms = (time.perf_counter() - t0) * 1e3
+        dev_ms = {"exact": 0.0, "split": 0.0}
+        for tag, prec in (("exact", A.CLM_PREC_EXACT), ("split", A.CLM_PREC_SPLIT)):
+            L.clm_set_precision(P.h, prec)
+            for s in range(len(sides)):
+                if not valid[s]:
+                    continue
+                P.box(np.diag([sides[s]] * 3), A.CLM_ORTHO, 6.0)
+                xs = xd[off[s]:off[s + 1]]
+                for opname in ("nl", "soft_energy"):
+                    P.step([xs], A.OP[opname], p, o)
+                    bm, mm = C.c_float(), C.c_float()
+                    L.clm_last_timings(P.h, C.byref(bm), C.byref(mm))
+                    dev_ms[tag] += bm.value + mm.value
         P.close()
-        res["plain_loop"] = {"step_ms": plain_ms, "pairs_per_s": pairs / (plain_ms * 1e-3)}
-        res["batched_over_plain"] = {t: plain_ms / res[t]["step_ms"] for t in ("exact", "split")}
+        res["plain_per_system"] = {t: {"device_ms": dev_ms[t], "pairs_per_s": pairs / (dev_ms[t] * 1e-3)}
+                                   for t in dev_ms}
+        res["batched_over_plain"] = {t: dev_ms[t] / res[t]["step_ms"] for t in ("exact", "split")}
         bs.close()
         del xd
         out["cfg3"] = res
@@ -405,14 +419,35 @@ def measure_forms(pkg, L, A, dev, stream, flush, peaks, which, steps, warmup):
             if pairs is None:
                 pairs = int(hc.sum())  # pairs with r >= 0.1 that fall in a bin
                 res["pairs_in_bins"] = pairs
-            e = frac_entry(pairs, k_ms, 8 * R + F_OP["rhist"], p64)
-            e.update({"step_ms": st_ms, "build_ms": b_ms, "frac_of_fp32_roofline":
-                      e["pairs_per_s"] / roofline_pairs(8 * R + F_OP["rhist"], p32)})
+            e = form_entry(pairs, k_ms, 8 * R + F_OP["rhist"], tag == "split")
+            e.update({"step_ms": st_ms, "build_ms": b_ms})
             res[tag] = e
-            if key == "cfg5_2d":
-                break  # the exact FP64 form of the full 2D case takes ~10 s per map; measured on the small case
         P.close()
         out[key] = res
+    return out
+
+
+def forms_summary(forms, build_roof):
+    """Compact view of every measured form: name -> [pairs/s, fraction of its roofline, pipe]."""
+    out = {}
+
+    def add(name, e, pipe):
+        if isinstance(e, dict) and "pairs_per_s" in e:
+            out[name] = [float(f"{e['pairs_per_s']:.3g}"), float(f"{e.get('frac', float('nan')):.3g}"),
+                         e.get("pipe", pipe)]
+
+    for key, res in forms.items():
+        if key in ("exact", "split"):
+            out[f"headline/{key}"] = [float(f"{res['value']:.3g}"), None, "fp32"]
+            continue
+        if not isinstance(res, dict):
+            continue
+        for tag, e in res.items():
+            add(f"{key}/{tag}", e, "fp32" if key == "cfg4" else "fp64")
+        if "batched_over_plain" in res:
+            out[f"{key}/batched_over_plain"] = {t: float(f"{v:.3g}") for t, v in res["batched_over_plain"].items()}
+    if build_roof.get("frac") is not None:
+        out["build/hbm"] = [float(f"{build_roof['achieved']:.3g}"), float(f"{build_roof['frac']:.3g}"), "hbm GB/s"]
     return out
 
 
@@ -440,7 +475,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        pairs, dt = cpu_reference(x_host, M, args.steps, max(0, min(args.warmup, 1)), threads)
+        pairs, dt = cpu_reference(x_host, M, args.steps, args.warmup, threads)
         v = pairs * args.steps / dt
         line = {"metric": METRIC, "value": v, "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
@@ -587,9 +622,12 @@ def main():
                   "bytes_per_build": build_bytes, "copies": copies, "cells": ncells, "build_ms": build_ms,
                   "note": "cell-list build (K1-K4, sort, scans) as a whole; launch- and latency-bound at this size"}
     # dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel on this workload, from one
-    # ncu capture (profiles/k_pairs_lj_forces_f32_fcc1M_triclinic.md); a profiler cannot run inside the
-    # timed region, so the figure is recorded rather than measured here
-    traffic = NCU_TRAFFIC_BYTES
+    # ncu capture recorded beside its summary in profiles/; a profiler cannot run inside the timed region,
+    # so the figure is read from that record rather than measured here
+    traffic = None
+    if os.path.exists(TRAFFIC_RECORD):
+        rec = json.load(open(TRAFFIC_RECORD))
+        traffic = int(rec["dram_bytes_read"]) + int(rec["dram_bytes_write"])
 
     peaks.clm_peak_fp64_gflops.restype = C.c_double
     peaks.clm_peak_fp64_gflops.argtypes = [C.c_int]
@@ -614,28 +652,32 @@ def main():
         except Exception as ex:  # pragma: no cover
             cpu = {"value": None, "unit": "pairs/s", "cores": threads, "kind": "port", "sample": f"failed: {ex}"}
 
+    forms = {"exact": {"value": value, "kernel_ms": k_exact},
+             "split": {"value": split_value, "kernel_ms": k_split, "ms_per_step": t_split / args.steps},
+             **forms_other}
     line = {
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_exact / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fcc + Gaussian jitter)",
         "config": {"workload": WORKLOAD, "n_particles": n, "pairs_per_step": pairs, "cutoff": CUTOFF,
-                   "cell": "triclinic", "op": "lj_energy_forces", "l2": "flushed between steps (256 MiB write)",
-                   "parallelism": f"replicas x{world}", "energy": energy},
-        "forms": {"exact": {"value": value, "kernel_ms": k_exact},
-                  "split": {"value": split_value, "kernel_ms": k_split, "ms_per_step": t_split / args.steps},
-                  **forms_other},
+                   "cell": "triclinic", "op": "lj_energy_forces", "l2": "flushed between steps (256 MiB write)"},
+        "parallelism": f"replicas x{world}", "energy": energy,
+        "forms": forms,
         "peaks": {"fp32_tflops": fp32_peak, "fp64_tflops": fp64_peak, "hbm_gbs": hbm,
                   "source": "FMA-loop probes (libclm_peaks.so) in this run; HBM from MEASURED_PEAKS.json"},
+        "build_roofline": build_roof,
         "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": int(x_pin.numel() * 4),
                 "d2h_bytes_per_step": int(f_pin.numel() * 4 + 8)},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak if fp32_peak > 0 else None, "traffic": traffic,
                      "kernel": "k_pairs<float,3,FORCES,exact>", "flops_per_pair": fpp, "candidates_per_hit": R,
                      "peak_source": "measured FP32 FMA throughput (libclm_peaks.so, same run)"},
-        "build_roofline": build_roof,
         "cpu_baseline": cpu,
         "clocks": clk,
         "gpu_launches": launches,
+        # last, so that it survives a tail of the output: every form's pairs/s, the fraction of its roofline
+        # and the pipe it is measured against
+        "forms_summary": forms_summary(forms, build_roof),
     }
     if rank == 0:
         print(json.dumps(line))

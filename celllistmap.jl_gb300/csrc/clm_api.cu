@@ -126,6 +126,18 @@ int build_dispatch(Handle& h, bool sync = true) {
   return h.dtype == CLM_F64 ? build_all<double>(h, sync) : build_all<float>(h, sync);
 }
 
+// A build enqueued by clm_run is checked (copy totals, NaN and overflow bits of the error word) together
+// with the map's results.  When that run returned early (an invalid argument), the set is still pending
+// and its error bits unread: the next call rebuilds it instead of trusting it.
+void drop_unchecked_builds(Handle& h) {
+  for (int s = 0; s < h.nsets; s++) {
+    if (h.sets[s].pending) {
+      h.sets[s].pending = false;
+      h.sets[s].dirty = true;
+    }
+  }
+}
+
 }  // namespace
 
 struct clm_handle_s : public Handle {};
@@ -263,6 +275,7 @@ int32_t clm_set_precision(clm_handle h, int32_t precision) {
 int32_t clm_build(clm_handle h) {
   if (!h) return ERR_ARG;
   if (h->batch.on) return fail(h, ERR_STATE, "a batch handle takes clm_batched_set_systems / clm_batched_run");
+  drop_unchecked_builds(*h);
   cudaMemsetAsync(h->err.p, 0, 64, h->stream);
   return build_dispatch(*h);
 }
@@ -271,6 +284,7 @@ int32_t clm_run(clm_handle h, int32_t op_id, const clm_op_params* params, clm_ou
   if (!h || !out) return ERR_ARG;
   if (h->batch.on) return fail(h, ERR_STATE, "a batch handle takes clm_batched_set_systems / clm_batched_run");
   if (!h->box_set) return fail(h, ERR_STATE, "clm_set_box must be called before clm_run");
+  drop_unchecked_builds(*h);
   for (int attempt = 0; attempt < 3; attempt++) {
     bool need = false;
     for (int s = 0; s < h->nsets; s++) need = need || h->sets[s].dirty || !h->sets[s].built;

@@ -368,6 +368,7 @@ template <class T> int finish_step(Handle& h, int nops, const int* ops, clm_batc
     return OK;
   }
   if (h.pinned[40] & DERR_CELL_RANGE) return fail(&h, ERR_INTERNAL, "batch consistency check failed");
+  if (h.pinned[40] & DERR_STAGE) return fail(&h, ERR_INTERNAL, "pair map: a staging wait for bulk copies timed out");
   int nl_slot = -1;
   for (int k = 0; k < nops; k++)
     if (ops[k] == CLM_OP_NL) nl_slot = k;

@@ -209,18 +209,38 @@ __host__ __device__ __forceinline__ void stencil_offset(bool forward, int l_rt, 
   }
 }
 
+// Self pairs in triclinic cells, visited once per pair of cells.  The reference visits, from every cell
+// holding a real particle, all its neighbour cells, and keeps the pairs (i, j) with i real and
+// index_i < index_j (src/internals/self.jl:106-135,164-184, vicinal_cells.jl:48-75).  Here the pair of cells
+// (A, B) is visited once: from A when B lies in A's forward half stencil, or when B lies in A's backward half
+// and holds no real particle (no work item starts from B).  A visited pair of copies is then the reference's
+// pair exactly when the copy with the lower particle index is real: that copy is the reference's i, the other
+// its j.  Entry k (0-based) of the neighbour list of this visit: k < nf the forward half stencil in the
+// reference's order, nf <= k < 2 nf the same offsets negated (the backward half), nf = ((2 lcell + 1)^dim - 1)/2.
+template <int LC = 0>
+__host__ __device__ __forceinline__ void sym_stencil_offset(int l_rt, int dim, int nf, int k, int* o, bool* back) {
+  *back = k >= nf;
+  stencil_offset<LC>(true, l_rt, dim, *back ? k - nf : k, o);
+  if (*back) {
+    o[0] = -o[0];
+    o[1] = -o[1];
+    o[2] = -o[2];
+  }
+}
+
 // Which visits of a candidate pair the map keeps (src/internals/self.jl:143-184, cross.jl:111-129), for a
 // particle copy i (slot ii of its cell) and a candidate copy j (slot slot_j; `same`: the same cell).
 // Self pairs: orthorhombic cells keep a pair once (j after i in the same cell; any cell of the forward half
-// stencil) when one of the copies is real; triclinic cells keep index_i < index_j (i real, full stencil);
-// non-periodic systems have no images.  Cross pairs in orthorhombic cells: the particle copy must be real
-// for a candidate of its own cell, and one of the two copies for a candidate of another cell; triclinic and
-// non-periodic cross pairs keep every visit.
+// stencil) when one of the copies is real; triclinic cells (visited once per pair of cells, see
+// sym_stencil_offset) keep a pair once (j after i in the same cell) when the copy of the lower particle
+// index is real; non-periodic systems have no images.  Cross pairs in orthorhombic cells: the particle copy
+// must be real for a candidate of its own cell, and one of the two copies for a candidate of another cell;
+// triclinic and non-periodic cross pairs keep every visit.
 __host__ __device__ __forceinline__ bool pair_rule(bool cross, bool tri, bool nonper, bool same, int slot_j, int ii,
                                                    bool real_i, bool real_j, int idx_i, int idx_j) {
   bool cand = true;
   if (!cross) {
-    if (tri) cand = idx_i < idx_j;
+    if (tri) cand = (!same || slot_j > ii) && idx_i != idx_j && ((idx_i < idx_j) ? real_i : real_j);
     else if (same) cand = (slot_j > ii) && (nonper || real_i || real_j);
     else cand = nonper || real_i || real_j;
   } else {
@@ -287,6 +307,7 @@ enum DevError : int {
   DERR_COPY_OVERFLOW = 4,
   DERR_NL_OVERFLOW = 8,
   DERR_SCAN = 16,  // a single-pass scan gave up waiting for the prefix of an earlier tile
+  DERR_STAGE = 32, // the pair kernel gave up waiting for the bulk copies of a staging window
 };
 
 }  // namespace clm

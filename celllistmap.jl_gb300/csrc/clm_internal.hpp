@@ -185,6 +185,14 @@ int check_build_totals(Handle& h, bool* overflow);
 template <class T> int set_limits(Handle& h, T* lo, T* hi);
 template <class T> void fill_devgeom(const Geometry<T>& g, int precision, DevGeom<T>& d);
 
+// Per-block partial slots that a scratch area of `scratch_bytes` holds for the allocation-free scalar map
+// (the first 256 bytes hold the final result): an energy, a count, a minimum d2 in the handle dtype (tsize
+// bytes) and its pair of indices per block.  A launch of more blocks than this is refused.
+inline size_t noalloc_block_slots(size_t scratch_bytes, size_t tsize) {
+  const size_t slot = sizeof(double) + sizeof(unsigned long long) + tsize + 2 * sizeof(int);
+  return scratch_bytes > 256 ? (scratch_bytes - 256) / slot : 0;
+}
+
 // Map (clm_pairs.cu)
 struct OpRequest;
 template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const void* params, void* outputs);

@@ -1,12 +1,12 @@
 // clm_run_noalloc: pair-map reductions that allocate no device memory.
 //
 // Who needs it: callers that cannot call cudaMalloc at the point where they evaluate energies --
-// code running inside a CUDA stream capture (allocation calls synchronize the device and break the
-// capture), applications whose device memory is entirely owned by their own pool allocator (a Julia
-// CUDA.jl or PyTorch caching pool, an MD engine with a fixed arena), and real-time loops that must not
-// call into the CUDA allocator.  They build the cell lists once with the ordinary entry points (which do
-// allocate), then evaluate scalar reductions of the pair map any number of times through this entry
-// point.
+// applications whose device memory is entirely owned by their own pool allocator (a Julia CUDA.jl or
+// PyTorch caching pool, an MD engine with a fixed arena: a cudaMalloc behind the pool's back can fail or
+// fragment it), and real-time loops that must not call into the CUDA allocator (cudaMalloc and cudaFree
+// can block on the whole device).  They build the cell lists once with the ordinary entry points (which
+// do allocate), then evaluate scalar reductions of the pair map any number of times through this entry
+// point.  The call waits for its result on the handle's stream and reads it on the host.
 //
 // The per-block partial sums and the final result of the reduction live in one file-scope device array
 // of 128 KiB + 256 B (4096 per-block slots), which every GPU that loads this library holds until the
@@ -74,6 +74,11 @@ extern "C" int32_t clm_run_noalloc(clm_handle h, int32_t op_id, const clm_op_par
     return clm::ERR_STATE;
   }
   for (int s = 0; s < h->nsets; s++) {
+    if (h->sets[s].pending) {
+      // a build enqueued by a clm_run that returned early: its totals and error bits were never checked
+      h->sets[s].pending = false;
+      h->sets[s].dirty = true;
+    }
     if (h->sets[s].dirty || !h->sets[s].built) {
       h->last_error = "clm_run_noalloc does not build cell lists (building allocates): call clm_build first";
       return clm::ERR_STATE;

@@ -526,6 +526,10 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
     h.last_error = "pair map consistency check failed (stencil cell outside the grid)";
     return ERR_INTERNAL;
   }
+  if (h.pinned[40] & DERR_STAGE) {
+    h.last_error = "pair map: a staging wait for bulk copies timed out";
+    return ERR_INTERNAL;
+  }
   std::memcpy(&O->scalar, hostres, 8);
   unsigned long long cnt;
   std::memcpy(&cnt, hostres + 8, 8);
@@ -630,8 +634,7 @@ int run_pairs_scalar_scratch(Handle& h, const Geometry<T>& g, int op, const void
     set_params(A, pp);
   }
   // scratch layout: [results, 256 B][partial energy][partial count][partial min d2][partial min ij]
-  const size_t slot = sizeof(double) + sizeof(unsigned long long) + sizeof(T) + 2 * sizeof(int);
-  const size_t cap_blocks = scratch_bytes > 256 ? (scratch_bytes - 256) / slot : 0;
+  const size_t cap_blocks = noalloc_block_slots(scratch_bytes, sizeof(T));
   const int needed = pairs_scalar_blocks_needed(h, op);
   if (needed < 0 || (size_t)needed > cap_blocks) {
     h.last_error = "the pair map needs more per-block partial slots than the allocation-free scratch holds";
@@ -664,6 +667,10 @@ int run_pairs_scalar_scratch(Handle& h, const Geometry<T>& g, int op, const void
   CLM_CUDA_TRY(h, cudaStreamSynchronize(h.stream));
   if (h.pinned[4] & DERR_CELL_RANGE) {
     h.last_error = "pair map consistency check failed (stencil cell outside the grid)";
+    return ERR_INTERNAL;
+  }
+  if (h.pinned[4] & DERR_STAGE) {
+    h.last_error = "pair map: a staging wait for bulk copies timed out";
     return ERR_INTERNAL;
   }
   const char* hr = reinterpret_cast<const char*>(h.pinned + 8);

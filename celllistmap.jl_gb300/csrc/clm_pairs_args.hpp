@@ -22,6 +22,7 @@ template <class T> struct SetView {
   const float4* xq;   // Float32 handles: coordinates; .w = particle code
   const int* code;
   const int* cell_start;
+  const int* cell_real;  // per cell: 1 when it holds a real particle
 };
 
 template <class T> struct PairArgs {
@@ -135,6 +136,7 @@ template <class T> inline SetView<T> view_of(const SetData& S) {
   v.xq = S.xq.as<float4>();
   v.code = S.code.as<int>();
   v.cell_start = S.cell_start.as<int>();
+  v.cell_real = S.cell_flags.as<int>();
   return v;
 }
 

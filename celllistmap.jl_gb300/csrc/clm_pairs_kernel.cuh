@@ -167,6 +167,44 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// Bulk asynchronous copies (cp.async.bulk, the TMA unit's untiled form) from this GPU's global memory into
+// shared memory, completing on an mbarrier that counts the bytes (expect_tx / complete_tx).  Addresses are
+// 16-byte aligned and sizes multiples of 16 bytes (the candidate records are 16-byte float4).
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+// makes mbarrier initialisations visible to the asynchronous proxy
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+// orders this thread's earlier shared-memory accesses before later asynchronous-proxy writes
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Waits for the phase of the given parity to complete, giving up after about a second (2^31 cycles).
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (clock64() - t0 > (1ll << 31)) return false;
+  }
+  return true;
+}
+
 // Geometry of the cell being processed: the launch's own (one system) or that of the cell's system
 // (batches); `cb` returns the first global cell of that system.
 template <bool B, class T>
@@ -199,12 +237,15 @@ __device__ __forceinline__ void force_add(const PairArgs<T>& A, bool ys, int idx
 // triclinic cells); forces add -df to the particle's sums and +df to the partner's.
 //
 // Each warp takes one cell (or one part of a crowded cell); the cells of its stencil are concatenated
-// into one candidate stream, staged 32*G candidates per round into shared memory with asynchronous
-// 16-byte copies (the next round is copied while the current one is tested).  Phase A: every lane tests
-// its particle against 32 staged candidates with an FP32 distance (FMA) and records the candidates inside
-// cutoff^2 (1 + 2^-13) in a bit mask.  Phase B: the set bits of all lanes are compacted into a queue that
-// all lanes work through: the reference's pair rules, the re-test in the input dtype where needed, and
-// the operator epilogue.  The projection filter of the reference is
+// into one candidate stream, staged in windows of 128 candidates into shared memory by bulk copies: each
+// lane holds one stencil cell and copies that cell's part of the window (its records are contiguous in
+// the cell list) with one cp.async.bulk, completing on the warp's mbarrier; the next window is copied
+// while the current one is tested.  Triclinic self pairs visit each pair of cells once (the forward half
+// stencil, and the backward cells without real particles: sym_stencil_offset), as orthorhombic self pairs
+// do.  Phase A: every lane tests its particle against 32 staged candidates per round with an FP32
+// distance (FMA) and records the candidates inside cutoff^2 (1 + 2^-13) in a bit mask.  Phase B: the set
+// bits of all lanes are compacted into a queue that all lanes work through: the reference's pair rules,
+// the re-test in the input dtype where needed, and the operator epilogue.  The projection filter of the reference is
 // evaluated only for pairs with d2 > cutoff^2 (1 - 2^-13): any pair further inside passes it (the
 // projection of the separation on a unit vector cannot exceed the separation, and the margin covers the
 // half cell), so skipping it elsewhere leaves the pair set unchanged.
@@ -219,7 +260,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
   constexpr bool IS_F = (OPK == OPK_FORCES) || (OPK == OPK_ADJ);
   constexpr bool FP64 = std::is_same<T, double>::value;
   constexpr bool ABS_PF = !FP64 && !SPLIT;  // FP32 exact form: the prefilter uses the coordinates themselves
-  constexpr int JC = 128;                   // staging capacity: 32 candidates per lane group (G <= 4)
+  constexpr int JC = 128;                   // staging window: 32 candidates per lane group (G <= 4)
   const DevGeom<T>& g = A.g;
   const int op = OPC ? OPC : A.op;
   const int lane = threadIdx.x & 31;
@@ -229,10 +270,11 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
   __shared__ int s_st_start[kWarps][32];
   __shared__ int s_st_pref[kWarps][33];
   __shared__ int s_st_meta[kWarps][32];
-  // staged candidates, two rounds (the next one is copied while the current one is tested)
+  // staged candidates, two windows (the next one is copied while the current one is tested)
   __shared__ __align__(16) float4 s_pf[2][kWarps][JC];  // prefilter coordinates; .w carries the particle code
-  __shared__ int s_meta[2][kWarps][JC];                 // stencil offset and flags of the candidate's cell
+  __shared__ int s_meta[2][kWarps][ABS_PF ? 1 : JC];    // stencil offset and flags of the candidate's cell
   __shared__ int s_tj[2][kWarps][ABS_PF ? 1 : JC];       // position of the candidate in the cell list
+  __shared__ __align__(8) unsigned long long s_mbar[kWarps][2];  // completion of the bulk copies of a window
   __shared__ unsigned short s_q[kWarps][1024];  // compacted candidates: (particle slot << 8) | staged index
   __shared__ T s_ix[kWarps][3][32];              // particles of the current chunk of the cell
   __shared__ float s_ipf[kWarps][3][32];
@@ -254,13 +296,23 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
   constexpr int F_SAME = 1 << 24;
   const bool tri = (g.kind == TRICLINIC);
   const bool nonper = (g.kind == NONPERIODIC);
-  const bool full = tri || CROSS;
-  const bool idx_rule = tri && !CROSS;  // triclinic self pairs: index_i < index_j, applied in phase A
+  const bool sym = tri && !CROSS;  // triclinic self pairs: each pair of cells once (sym_stencil_offset)
   const int l = g.lcell;
   const int w = 2 * l + 1;
   const int wN = (N == 3) ? w * w * w : w * w;
-  const int nent = (full ? wN - 1 : (wN - 1) / 2) + 1;  // entry 0 is the cell itself
-  const T band = (T)g.thr_lo;                           // d2 above this: projection filter applies
+  const int nf = (wN - 1) / 2;
+  // entry 0 is the cell itself; then all neighbours (cross pairs), the forward and the backward half
+  // (triclinic self pairs) or the forward half
+  const int nent = CROSS ? wN : (sym ? 2 * nf + 1 : nf + 1);
+  const T band = (T)g.thr_lo;  // d2 above this: projection filter applies
+  if (lane == 0) {
+    mbar_init(&s_mbar[warp][0], 1);
+    mbar_init(&s_mbar[warp][1], 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  unsigned ph = 0u;  // bit b: parity of the next phase of s_mbar[warp][b] to complete
+  bool bad = false;  // a staging wait gave up (error reported): this warp stops
 
   if constexpr (OPK == OPK_HIST) {
     for (int b = threadIdx.x; b < A.nbins; b += kThreads) {
@@ -292,7 +344,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
   const int n_real = *A.n_real_dev;
   const int S = A.cell_split;  // the host keeps cells x parts below 2^31
   const int n_items = n_real * S;
-  for (int r = gw; r < n_items; r += nw) {
+  for (int r = gw; r < n_items && !bad; r += nw) {
     const int rcell = r / S;
     const int part = r - rcell * S;
     const int li = A.real_list[rcell];
@@ -309,7 +361,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
     const int grp = lane % G;  // the G lanes of one particle are adjacent: the hit queue is ordered by particle
     const int il = lane / G;
 
-    for (int ib = part * LP; ib < ni; ib += LP * S) {
+    for (int ib = part * LP; ib < ni && !bad; ib += LP * S) {
       const int ii = ib + il;
       const bool vi = ii < ni;
       const int ti = si + (vi ? ii : 0);
@@ -332,7 +384,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
       }
       const bool real_i = code_i >= 0;
       const int idx_i = real_i ? code_i : -code_i - 1;
-      const bool act_i = tri ? (vi && real_i) : vi;
+      const bool act_i = (tri && CROSS) ? (vi && real_i) : vi;
       if (grp == 0) {
 #pragma unroll
         for (int d = 0; d < 3; d++) {
@@ -344,16 +396,23 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
       }
       __syncwarp();
 
-      for (int k0 = 0; k0 < nent; k0 += 32) {
-        // ---- stencil table for entries k0 .. k0+31
+      for (int k0 = 0; k0 < nent && !bad; k0 += 32) {
+        // ---- stencil table for entries k0 .. k0+31: lane k holds entry k0 + k (first copy, copies, offset)
+        int e_start = 0, e_cnt = 0, e_pref = 0;
         {
           const int kk = k0 + lane;
-          int cnt = 0, start = 0, meta = 0;
+          int meta = 0;
           if (kk < nent) {
             int o[3] = {0, 0, 0};
+            bool back = false;
             if (kk > 0) {
-              if (l == 1) stencil_offset<1>(!full, l, N, kk - 1, o);
-              else stencil_offset(!full, l, N, kk - 1, o);
+              if (CROSS) {
+                if (l == 1) stencil_offset<1>(false, l, N, kk - 1, o);
+                else stencil_offset(false, l, N, kk - 1, o);
+              } else {
+                if (l == 1) sym_stencil_offset<1>(l, N, nf, kk - 1, o, &back);
+                else sym_stencil_offset(l, N, nf, kk - 1, o, &back);
+              }
             }
             int cj[3] = {1, 1, 1};
             bool inr = true;
@@ -368,479 +427,506 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
               int lj = cj[0] - 1 + cb;
               if (N == 3) lj += gc.nc[0] * ((cj[1] - 1) + gc.nc[1] * (cj[2] - 1));
               else lj += gc.nc[0] * (cj[1] - 1);
-              start = A.Y.cell_start[lj];
-              cnt = A.Y.cell_start[lj + 1] - start;
+              // a backward cell holding real particles is an item of its own, which visits this pair of cells
+              if (!back || !A.Y.cell_real[lj]) {
+                e_start = A.Y.cell_start[lj];
+                e_cnt = A.Y.cell_start[lj + 1] - e_start;
+              }
               meta = (o[0] + 128) | ((o[1] + 128) << 8) | ((o[2] + 128) << 16);
               if (kk == 0) meta |= F_SAME;
             }
           }
-          int incl = cnt;
+          int incl = e_cnt;
 #pragma unroll
           for (int o2 = 1; o2 < 32; o2 <<= 1) {
             int y = __shfl_up_sync(FULL, incl, o2);
             if (lane >= o2) incl += y;
           }
+          e_pref = incl - e_cnt;
           s_st_pref[warp][lane + 1] = incl;
           if (lane == 0) s_st_pref[warp][0] = 0;
-          s_st_start[warp][lane] = start;
+          s_st_start[warp][lane] = e_start;
           s_st_meta[warp][lane] = meta;
         }
         __syncwarp();
         const int total = s_st_pref[warp][32];
+        const int same_end = (k0 == 0) ? s_st_pref[warp][1] : 0;  // stream positions of the cell itself
 
         const int JR = 32 * G;  // candidates per round: each lane tests exactly 32
-        // ---- stage candidates rbx .. rbx+JR-1 of the stream into buffer bsel with asynchronous copies
-        // (cp.async, 16 B per candidate: coordinates or cell offsets with the particle code in .w);
-        // positions past the stream are padded with a far point (its FP32 d2 is finite and above every
-        // threshold)
-        auto stage = [&](int rbx, int bsel) {
-          const int cnt = min(JR, total - rbx);
-          for (int q = lane; q < JR; q += 32) {
-            if (q < cnt) {
-              const int e = rbx + q;
+        // ---- stage window wi (stream positions wi*JC .. +JC-1) into buffer wi & 1: each lane copies the part
+        // of its stencil cell inside the window with one bulk copy (16-byte records: coordinates or cell
+        // offsets, the particle code in .w); lane 0 registers the window's bytes on the buffer's mbarrier
+        const float4* rec = ABS_PF ? A.Y.xq : A.Y.off;
+        auto issue = [&](int wi) {
+          const int w0 = wi * JC, bsel = wi & 1;
+          const int wc = min(JC, total - w0);
+          fence_proxy_async_smem();  // earlier reads and writes of this buffer come before the copy's writes
+          if (lane == 0) mbar_arrive_expect_tx(&s_mbar[warp][bsel], (unsigned)wc * 16u);
+          __syncwarp();
+          const int lo = max(e_pref, w0), hi = min(e_pref + e_cnt, w0 + wc);
+          if (lo < hi)
+            bulk_g2s(&s_pf[bsel][warp][lo - w0], rec + e_start + (lo - e_pref), (unsigned)(hi - lo) * 16u,
+                     &s_mbar[warp][bsel]);
+        };
+        const int nwin = (total + JC - 1) / JC;
+        if (nwin > 0) issue(0);
+        for (int wi = 0; wi < nwin; wi++) {
+          const int bsel = wi & 1, w0 = wi * JC, wc = min(JC, total - w0);
+          if (wi + 1 < nwin) issue(wi + 1);  // the next window's copies overlap this window's tests
+          {
+            const bool ok = __all_sync(FULL, mbar_wait_bounded(&s_mbar[warp][bsel], (ph >> bsel) & 1u));
+            ph ^= 1u << bsel;
+            if (!ok) {
+              // report, let the copies of the other buffer land (bounded), and stop this warp
+              if (lane == 0) atomicOr(A.err, DERR_STAGE);
+              if (wi + 1 < nwin) mbar_wait_bounded(&s_mbar[warp][bsel ^ 1], (ph >> (bsel ^ 1)) & 1u);
+              bad = true;
+              break;
+            }
+          }
+          if constexpr (!ABS_PF) {
+            // shift the offsets by the cell displacement so that x_i - x_j ~ off_i - pf, and record each
+            // candidate's cell (stencil offset, same-cell flag) and position in the cell list
+            for (int q = lane; q < wc; q += 32) {
+              const int e = w0 + q;
               int lo = 0;  // last stencil entry whose prefix is <= e (that entry is not empty)
 #pragma unroll
               for (int st = 16; st > 0; st >>= 1)
                 if (s_st_pref[warp][lo + st] <= e) lo += st;
-              const int tj = s_st_start[warp][lo] + (e - s_st_pref[warp][lo]);
-              s_meta[bsel][warp][q] = s_st_meta[warp][lo];
-              if constexpr (ABS_PF) {
-                cp_async16(&s_pf[bsel][warp][q], &A.Y.xq[tj]);
-              } else {
-                cp_async16(&s_pf[bsel][warp][q], &A.Y.off[tj]);
-                s_tj[bsel][warp][q] = tj;
-              }
-            } else {
-              s_pf[bsel][warp][q] = make_float4(3e18f, 3e18f, 3e18f, 0.f);
-            }
-          }
-          cp_async_commit();
-        };
-        if (total > 0) stage(0, 0);
-        int buf = 0;
-        for (int rb = 0; rb < total; rb += JR, buf ^= 1) {
-          const int cntr = min(JR, total - rb);
-          cp_async_wait_all();
-          __syncwarp();
-          if (!ABS_PF || idx_rule) {
-            // own slots only (a lane sees its own asynchronous copies after the wait): shift the offsets by
-            // the cell displacement so that x_i - x_j ~ off_i - pf, and for triclinic self pairs replace
-            // the particle code by the particle index (the pair rules there need no realness)
-            for (int q = lane; q < cntr; q += 32) {
-              float4 v = s_pf[buf][warp][q];
-              if constexpr (!ABS_PF) {
-                const int meta = s_meta[buf][warp][q];
-                v.x += gc.csf[0] * (float)((meta & 255) - 128);
-                v.y += gc.csf[1] * (float)(((meta >> 8) & 255) - 128);
-                v.z += gc.csf[2] * (float)(((meta >> 16) & 255) - 128);
-              }
-              if (idx_rule) {
-                const int c = __float_as_int(v.w);
-                v.w = __int_as_float(c ^ (c >> 31));
-              }
-              s_pf[buf][warp][q] = v;
+              const int meta = s_st_meta[warp][lo];
+              float4 v = s_pf[bsel][warp][q];
+              v.x += gc.csf[0] * (float)((meta & 255) - 128);
+              v.y += gc.csf[1] * (float)(((meta >> 8) & 255) - 128);
+              v.z += gc.csf[2] * (float)(((meta >> 16) & 255) - 128);
+              s_pf[bsel][warp][q] = v;
+              s_meta[bsel][warp][q] = meta;
+              s_tj[bsel][warp][q] = s_st_start[warp][lo] + (e - s_st_pref[warp][lo]);
             }
             __syncwarp();
           }
-          if (rb + JR < total) stage(rb + JR, buf ^ 1);  // the next round's copies overlap this round
-          // ---- phase A: 32 FP32 distance tests per lane into a bit mask (with the index rule of
-          // triclinic self pairs, so that the mirrored visit of a pair never enters the queue).  A test
-          // passes when the sign bit of d2 - thr (and of index_i - index_j) is set; the sign bits are
-          // shifted into the mask, candidate b landing on bit b.  thr carries a 2^-13 relative margin, far
-          // above the FP32 rounding of dx^2 - thr + dy^2 + dz^2, so the strict comparison keeps every pair
-          // the exact test can accept.
-          unsigned mask = 0u;
-          {
-            const float thr = g.thr_hi;
-            // the lane's 32 candidates are grp, grp + G, ...: G fixed at compile time per variant, so that
-            // every record is read at a constant offset
-            auto test32 = [&](auto g_const) {
-              constexpr int GG = decltype(g_const)::value;
-              const float4* pp = &s_pf[buf][warp][grp];
-              if (idx_rule) {
+          for (int rb = 0; rb < wc; rb += JR) {
+            const int cntr = min(JR, wc - rb);
+            // ---- phase A: 32 FP32 distance tests per lane into a bit mask.  A test passes when the sign bit
+            // of d2 - thr is set (in triclinic self pairs, and that of the codes' AND clear: a pair of two
+            // images is never the reference's pair); the sign bits are shifted into the mask, candidate b
+            // landing on bit b.  thr carries a 2^-13 relative margin, far above the FP32 rounding of
+            // dx^2 - thr + dy^2 + dz^2, so the strict comparison keeps every pair the exact test can accept.
+            unsigned mask = 0u;
+            {
+              const float thr = g.thr_hi;
+              // the lane's 32 candidates are rb + grp, rb + grp + G, ...: G fixed at compile time per
+              // variant, so that every record is read at a constant offset
+              auto test32 = [&](auto g_const) {
+                constexpr int GG = decltype(g_const)::value;
+                const float4* pp = &s_pf[bsel][warp][rb + grp];
+                if (sym) {
 #pragma unroll
-                for (int b = 31; b >= 0; b--) {
-                  const float4 p = pp[b * GG];
-                  const float dx = pi[0] - p.x, dy = pi[1] - p.y, dz = (N == 3) ? pi[2] - p.z : 0.f;
-                  const float e = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, -thr)));  // d2 - thr
-                  const int v = __float_as_int(e) & (idx_i - __float_as_int(p.w));  // .w: index
-                  mask = __funnelshift_l((unsigned)v, mask, 1);  // (mask << 1) | sign bit of v
-                }
-              } else {
+                  for (int b = 31; b >= 0; b--) {
+                    const float4 p = pp[b * GG];
+                    const float dx = pi[0] - p.x, dy = pi[1] - p.y, dz = (N == 3) ? pi[2] - p.z : 0.f;
+                    const float e = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, -thr)));  // d2 - thr
+                    const int v = __float_as_int(e) & ~(code_i & __float_as_int(p.w));  // .w: particle code
+                    mask = __funnelshift_l((unsigned)v, mask, 1);  // (mask << 1) | sign bit of v
+                  }
+                } else {
 #pragma unroll
-                for (int b = 31; b >= 0; b--) {
-                  const float4 p = pp[b * GG];
-                  const float dx = pi[0] - p.x, dy = pi[1] - p.y, dz = (N == 3) ? pi[2] - p.z : 0.f;
-                  const float e = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, -thr)));  // d2 - thr
-                  mask = __funnelshift_l(__float_as_uint(e), mask, 1);
-                }
-              }
-            };
-            if (G == 2) test32(std::integral_constant<int, 2>());
-            else if (G == 1) test32(std::integral_constant<int, 1>());
-            else test32(std::integral_constant<int, 4>());
-          }
-          if (!act_i) mask = 0u;
-          // ---- phase B: compact the candidates of all lanes into a queue and process them with every lane
-          // busy; each lane takes a contiguous run of the queue (runs are grouped by particle, so force
-          // sums stay in registers and are flushed to shared memory only when the particle changes)
-          int H;
-          {
-            const int nh = __popc(mask);
-            int incl = nh;
-#pragma unroll
-            for (int o2 = 1; o2 < 32; o2 <<= 1) {
-              int y = __shfl_up_sync(FULL, incl, o2);
-              if (lane >= o2) incl += y;
-            }
-            H = __shfl_sync(FULL, incl, 31);
-            int pos = incl - nh;
-            unsigned m = mask;
-            while (m) {
-              const int b = __ffs(m) - 1;
-              m &= m - 1u;
-              s_q[warp][pos++] = (unsigned short)((il << 8) | (b * G + grp));
-            }
-          }
-          __syncwarp();
-          const int per = (H + 31) >> 5;
-          const int qbeg = lane * per;
-          int cur = -1;
-          FA acc[3] = {0, 0, 0};
-          for (int t = 0; t < per; t++) {
-            const int q = qbeg + t;
-            const bool has = q < H;
-            int j = 0, ie = 0;
-            if (has) {
-              const int ent = s_q[warp][q];
-              ie = ent >> 8;
-              j = ent & 255;
-            }
-            T xi[3];
-            float pi[3];
-#pragma unroll
-            for (int d = 0; d < 3; d++) {
-              xi[d] = s_ix[warp][d][ie];
-              pi[d] = ABS_PF ? (float)xi[d] : s_ipf[warp][d][ie];
-            }
-            const int code_i = s_icode[warp][ie];
-            const bool real_i = code_i >= 0;
-            const int idx_i = real_i ? code_i : -code_i - 1;
-            const int ii = ib + ie;
-            bool hit = false, sure = false;
-            int idx_j = 0;
-            float d2f = 0.f;
-            float dvf[3] = {0.f, 0.f, 0.f};
-            T d2 = 0;
-            T xj[3] = {0, 0, 0};
-            T dxs[3] = {0, 0, 0};  // x_i - x_j of the exact re-test, reused by the force epilogues
-            int tjj = 0;  // the candidate's position in the cell list (coordinates read only when needed)
-            auto load_xj = [&]() {
-              if constexpr (!ABS_PF) {
-#pragma unroll
-                for (int d = 0; d < N; d++) xj[d] = pos_of(A.Y, d, tjj);
-              }
-            };
-            if (has) {
-              const float4 p = s_pf[buf][warp][j];
-              const int code_j = __float_as_int(p.w);
-              const bool real_j = code_j >= 0;
-              idx_j = real_j ? code_j : -code_j - 1;
-              const int meta = s_meta[buf][warp][j];
-              if constexpr (!ABS_PF) tjj = s_tj[buf][warp][j];
-              const bool same = (meta & F_SAME) != 0;
-              const int slot_j = rb + j;  // position inside the cell when same
-              const bool cand = pair_rule(CROSS, tri, nonper, same, slot_j, ii, real_i, real_j, idx_i, idx_j);
-              if (cand) {
-                dvf[0] = pi[0] - p.x;
-                dvf[1] = pi[1] - p.y;
-                dvf[2] = (N == 3) ? pi[2] - p.z : 0.f;
-                d2f = fmaf(dvf[2], dvf[2], fmaf(dvf[1], dvf[1], dvf[0] * dvf[0]));
-                if (ABS_PF) {
-                  xj[0] = (T)p.x;
-                  xj[1] = (T)p.y;
-                  if (N == 3) xj[N - 1] = (T)p.z;
-                }
-                if (!FP64 || SPLIT) {
-                  // FP32 input or split form: well inside the cutoff the FP32 value decides
-                  if (d2f <= g.thr_lo) {
-                    hit = true;
-                    sure = true;
+                  for (int b = 31; b >= 0; b--) {
+                    const float4 p = pp[b * GG];
+                    const float dx = pi[0] - p.x, dy = pi[1] - p.y, dz = (N == 3) ? pi[2] - p.z : 0.f;
+                    const float e = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, -thr)));  // d2 - thr
+                    mask = __funnelshift_l(__float_as_uint(e), mask, 1);
                   }
                 }
-                if (!sure) {
-                  load_xj();
+              };
+              if (G == 2) test32(std::integral_constant<int, 2>());
+              else if (G == 1) test32(std::integral_constant<int, 1>());
+              else test32(std::integral_constant<int, 4>());
+            }
+            {
+              // candidates past the window's end (stale records) are dropped: candidate b is rb + grp + b G
+              const int nb = (cntr - grp + G - 1) / G;
+              if (!act_i || nb <= 0) mask = 0u;
+              else if (nb < 32) mask &= (1u << nb) - 1u;
+            }
+            // ---- phase B: compact the candidates of all lanes into a queue and process them with every lane
+            // busy; each lane takes a contiguous run of the queue (runs are grouped by particle, so force
+            // sums stay in registers and are flushed to shared memory only when the particle changes)
+            int H;
+            {
+              const int nh = __popc(mask);
+              int incl = nh;
 #pragma unroll
-                  for (int d = 0; d < N; d++) dxs[d] = xsub(xi[d], xj[d]);
-                  d2 = xmul(dxs[0], dxs[0]);
+              for (int o2 = 1; o2 < 32; o2 <<= 1) {
+                int y = __shfl_up_sync(FULL, incl, o2);
+                if (lane >= o2) incl += y;
+              }
+              H = __shfl_sync(FULL, incl, 31);
+              int pos = incl - nh;
+              unsigned m = mask;
+              while (m) {
+                const int b = __ffs(m) - 1;
+                m &= m - 1u;
+                s_q[warp][pos++] = (unsigned short)((il << 8) | (rb + b * G + grp));
+              }
+            }
+            __syncwarp();
+            const int per = (H + 31) >> 5;
+            const int qbeg = lane * per;
+            int cur = -1;
+            FA acc[3] = {0, 0, 0};
+            for (int t = 0; t < per; t++) {
+              const int q = qbeg + t;
+              const bool has = q < H;
+              int j = 0, ie = 0;
+              if (has) {
+                const int ent = s_q[warp][q];
+                ie = ent >> 8;
+                j = ent & 255;
+              }
+              T xi[3];
+              float pi[3];
 #pragma unroll
-                  for (int d = 1; d < N; d++) d2 = xadd(d2, xmul(dxs[d], dxs[d]));
-                  hit = d2 <= g.cutoff_sqr;
-                  if (hit && d2 > band) {
-                    if (!same) {
+              for (int d = 0; d < 3; d++) {
+                xi[d] = s_ix[warp][d][ie];
+                pi[d] = ABS_PF ? (float)xi[d] : s_ipf[warp][d][ie];
+              }
+              const int code_i = s_icode[warp][ie];
+              const bool real_i = code_i >= 0;
+              const int idx_i = real_i ? code_i : -code_i - 1;
+              const int ii = ib + ie;
+              bool hit = false, sure = false;
+              int idx_j = 0;
+              int oi = 0, oj = 0;  // the pair as the reference orients it (i, j)
+              float d2f = 0.f;
+              float dvf[3] = {0.f, 0.f, 0.f};
+              T d2 = 0;
+              T xj[3] = {0, 0, 0};
+              T dxs[3] = {0, 0, 0};  // x_i - x_j of the exact re-test, reused by the force epilogues
+              int tjj = 0;  // the candidate's position in the cell list (coordinates read only when needed)
+              auto load_xj = [&]() {
+                if constexpr (!ABS_PF) {
+#pragma unroll
+                  for (int d = 0; d < N; d++) xj[d] = pos_of(A.Y, d, tjj);
+                }
+              };
+              if (has) {
+                const float4 p = s_pf[bsel][warp][j];
+                const int code_j = __float_as_int(p.w);
+                const bool real_j = code_j >= 0;
+                idx_j = real_j ? code_j : -code_j - 1;
+                const int epos = w0 + j;  // position in the stream: inside the cell itself when same
+                int meta = 0;
+                bool same;
+                if constexpr (ABS_PF) {
+                  same = epos < same_end;
+                } else {
+                  meta = s_meta[bsel][warp][j];
+                  tjj = s_tj[bsel][warp][j];
+                  same = (meta & F_SAME) != 0;
+                }
+                const bool cand = pair_rule(CROSS, tri, nonper, same, epos, ii, real_i, real_j, idx_i, idx_j);
+                // triclinic self pairs: the copy of the lower index is the reference's i
+                const bool sw = sym && idx_j < idx_i;
+                oi = sw ? idx_j : idx_i;
+                oj = sw ? idx_i : idx_j;
+                if (cand) {
+                  dvf[0] = pi[0] - p.x;
+                  dvf[1] = pi[1] - p.y;
+                  dvf[2] = (N == 3) ? pi[2] - p.z : 0.f;
+                  d2f = fmaf(dvf[2], dvf[2], fmaf(dvf[1], dvf[1], dvf[0] * dvf[0]));
+                  if (ABS_PF) {
+                    xj[0] = (T)p.x;
+                    xj[1] = (T)p.y;
+                    if (N == 3) xj[N - 1] = (T)p.z;
+                  }
+                  if (!FP64 || SPLIT) {
+                    // FP32 input or split form: well inside the cutoff the FP32 value decides
+                    if (d2f <= g.thr_lo) {
+                      hit = true;
+                      sure = true;
+                    }
+                  }
+                  if (!sure) {
+                    load_xj();
+#pragma unroll
+                    for (int d = 0; d < N; d++) dxs[d] = xsub(xi[d], xj[d]);
+                    d2 = xmul(dxs[0], dxs[0]);
+#pragma unroll
+                    for (int d = 1; d < N; d++) d2 = xadd(d2, xmul(dxs[d], dxs[d]));
+                    hit = d2 <= g.cutoff_sqr;
+                    if (hit && d2 > band && !same) {
+                      // the reference's projection filter, seen from the cell of the reference's i
+                      if constexpr (ABS_PF) {
+                        int lo = 0;
+#pragma unroll
+                        for (int st = 16; st > 0; st >>= 1)
+                          if (s_st_pref[warp][lo + st] <= epos) lo += st;
+                        meta = s_st_meta[warp][lo];
+                      }
                       int cj[3] = {ci[0] + (meta & 255) - 128, ci[1] + ((meta >> 8) & 255) - 128,
                                    ci[2] + ((meta >> 16) & 255) - 128};
                       T ctr_j[3];
                       cell_center<T, N>(gc, cj, ctr_j);
-                      hit = projection_pass<T, N>(gc, ctr_i, ctr_j, xi, xj);
+                      hit = sw ? projection_pass<T, N>(gc, ctr_j, ctr_i, xj, xi)
+                               : projection_pass<T, N>(gc, ctr_i, ctr_j, xi, xj);
                     }
                   }
                 }
               }
-            }
-            // ---------------- operator epilogues
-            if constexpr (OPK == OPK_NL) {
-              if constexpr (BATCH) c_acc += hit ? 1ull : 0ull;  // pairs per system
-              unsigned bal = __ballot_sync(FULL, hit);
-              if (bal) {
-                unsigned long long base = 0;
-                int leader = __ffs(bal) - 1;
-                if (lane == leader) base = atomicAdd(A.nl_count, (unsigned long long)__popc(bal));
-                base = __shfl_sync(FULL, base, leader);
+              // ---------------- operator epilogues
+              if constexpr (OPK == OPK_NL) {
+                if constexpr (BATCH) c_acc += hit ? 1ull : 0ull;  // pairs per system
+                unsigned bal = __ballot_sync(FULL, hit);
+                if (bal) {
+                  unsigned long long base = 0;
+                  int leader = __ffs(bal) - 1;
+                  if (lane == leader) base = atomicAdd(A.nl_count, (unsigned long long)__popc(bal));
+                  base = __shfl_sync(FULL, base, leader);
+                  if (hit) {
+                    T dval;
+                    if (sure && ABS_PF) {
+                      T dx = xsub(xi[0], xj[0]);
+                      T e2 = xmul(dx, dx);
+#pragma unroll
+                      for (int d = 1; d < N; d++) {
+                        T dd = xsub(xi[d], xj[d]);
+                        e2 = xadd(e2, xmul(dd, dd));
+                      }
+                      dval = xsqrt(e2);
+                    } else {
+                      dval = sure ? (T)sqrtf(d2f) : xsqrt(d2);
+                    }
+                    unsigned long long pos = base + __popc(bal & ((1u << lane) - 1u));
+                    if ((long long)pos < A.nl_cap) {
+                      A.nl_i[pos] = oi;
+                      A.nl_j[pos] = oj;
+                      A.nl_d[pos] = dval;
+                    }
+                  }
+                }
+              } else if constexpr (OPK == OPK_SCALAR) {
                 if (hit) {
-                  T dval;
-                  if (sure && ABS_PF) {
-                    T dx = xsub(xi[0], xj[0]);
-                    T e2 = xmul(dx, dx);
-#pragma unroll
-                    for (int d = 1; d < N; d++) {
-                      T dd = xsub(xi[d], xj[d]);
-                      e2 = xadd(e2, xmul(dd, dd));
-                    }
-                    dval = xsqrt(e2);
+                  if (op == 2) {
+                    c_acc++;
+                  } else if (sure) {
+                    float uu, gg;
+                    pair_value<float, T>(A, op, d2f, oi, oj, uu, gg);
+                    e_part += (FA)uu;
                   } else {
-                    dval = sure ? (T)sqrtf(d2f) : xsqrt(d2);
-                  }
-                  unsigned long long pos = base + __popc(bal & ((1u << lane) - 1u));
-                  if ((long long)pos < A.nl_cap) {
-                    A.nl_i[pos] = idx_i;
-                    A.nl_j[pos] = idx_j;
-                    A.nl_d[pos] = dval;
+                    V uu, gg;
+                    pair_value<V, T>(A, op, (V)d2, oi, oj, uu, gg);
+                    e_part += (FA)uu;
                   }
                 }
-              }
-            } else if constexpr (OPK == OPK_SCALAR) {
-              if (hit) {
-                if (op == 2) {
-                  c_acc++;
-                } else if (sure) {
-                  float uu, gg;
-                  pair_value<float, T>(A, op, d2f, idx_i, idx_j, uu, gg);
-                  e_part += (FA)uu;
-                } else {
-                  V uu, gg;
-                  pair_value<V, T>(A, op, (V)d2, idx_i, idx_j, uu, gg);
-                  e_part += (FA)uu;
-                }
-              }
-            } else if constexpr (IS_F) {
-              // `cur` follows every queue entry (hit or not), so the lanes holding a particle are exactly
-              // the lanes whose runs cover its entries: adjacent, and only the last one moves past it inside
-              // its run; no other lane updates that particle's sums during the loop
-              if (has && ie != cur) {
-                if (cur >= 0) {
+              } else if constexpr (IS_F) {
+                // `cur` follows every queue entry (hit or not), so the lanes holding a particle are exactly
+                // the lanes whose runs cover its entries: adjacent, and only the last one moves past it inside
+                // its run; no other lane updates that particle's sums during the loop
+                if (has && ie != cur) {
+                  if (cur >= 0) {
 #pragma unroll
-                  for (int d = 0; d < N; d++) s_if[warp][d][cur] += acc[d];
-                }
-                cur = ie;
-#pragma unroll
-                for (int d = 0; d < N; d++) acc[d] = FA(0);
-              }
-              if (hit) {
-                FA uu, gg;
-                FA df[3] = {0, 0, 0};
-                FA dv[3] = {0, 0, 0};
-                if (sure) {
-                  float uf, gf;
-                  pair_value<float, T>(A, op, d2f, idx_i, idx_j, uf, gf);
-                  uu = (FA)uf;
-                  gg = (FA)gf;
-#pragma unroll
-                  for (int d = 0; d < N; d++) dv[d] = (FA)dvf[d];
-                } else {
-                  V uv, gv;
-                  pair_value<V, T>(A, op, (V)d2, idx_i, idx_j, uv, gv);
-                  uu = (FA)uv;
-                  gg = (FA)gv;
-#pragma unroll
-                  for (int d = 0; d < N; d++) dv[d] = (FA)dxs[d];
-                }
-#pragma unroll
-                for (int d = 0; d < N; d++) df[d] = gg * dv[d];
-                if constexpr (OPK == OPK_ADJ) {
-                  {
-                    // virial W += g dx dx^T (g = u'(r)/r), and the parameter derivatives of the LJ term
-                    adj[0] += gg * dv[0] * dv[0];
-                    adj[1] += gg * dv[1] * dv[1];
-                    adj[2] += gg * dv[2] * dv[2];
-                    adj[3] += gg * dv[0] * dv[1];
-                    adj[4] += gg * dv[0] * dv[2];
-                    adj[5] += gg * dv[1] * dv[2];
-                    FA eps = par<FA>(A, 0), sig = par<FA>(A, 1);
-                    int cls = 0;
-                    if (A.ntypes > 0) {
-                      const int ti = A.tx[idx_i], tj = A.tx[idx_j];
-                      eps = eps_tab<FA>(A, ti * A.ntypes + tj);
-                      sig = sig_tab<FA>(A, ti * A.ntypes + tj);
-                      cls = ti + tj;  // 2 types: AA = 0, AB = 1, BB = 2
-                    }
-                    const FA c12 = par<FA>(A, 2), c6 = par<FA>(A, 3);
-                    const FA dd2 = sure ? (FA)d2f : (FA)d2;
-                    const FA sr2 = sig * sig * vrcp(dd2);
-                    const FA sr6 = sr2 * sr2 * sr2;
-                    const FA sr12 = sr6 * sr6;
-                    const FA lj = c12 * sr12 - c6 * sr6;
-                    const FA dsg = eps * (FA(12) * c12 * sr12 - FA(6) * c6 * sr6) * vrcp(sig);
-#pragma unroll
-                    for (int k = 0; k < 3; k++) {
-                      adj[6 + k] += (cls == k) ? lj : FA(0);
-                      adj[9 + k] += (cls == k) ? dsg : FA(0);
-                    }
+                    for (int d = 0; d < N; d++) s_if[warp][d][cur] += acc[d];
                   }
-                }
+                  cur = ie;
 #pragma unroll
-                for (int d = 0; d < N; d++) acc[d] -= df[d];
-                e_part += uu;
-                force_add<T, N, FA>(A, CROSS, idx_j, df);  // the partner's share
-              }
-            } else if constexpr (OPK == OPK_MIN) {
-              if (hit) {
-                T dd2 = sure ? (T)d2f : d2;
-                if (sure && ABS_PF) {
-                  T dx = xsub(xi[0], xj[0]);
-                  dd2 = xmul(dx, dx);
-#pragma unroll
-                  for (int d = 1; d < N; d++) {
-                    T dd = xsub(xi[d], xj[d]);
-                    dd2 = xadd(dd2, xmul(dd, dd));
-                  }
+                  for (int d = 0; d < N; d++) acc[d] = FA(0);
                 }
-                if (dd2 < best_d2 || (dd2 == best_d2 && (idx_i < best_i || (idx_i == best_i && idx_j < best_j)))) {
-                  best_d2 = dd2;
-                  best_i = idx_i;
-                  best_j = idx_j;
-                }
-              }
-            } else if constexpr (OPK == OPK_HIST) {
-              int hb = -1;   // bin of this lane's pair (-1: none)
-              FA hv = 0;     // its accumulator term
-              if (hit) {
-                bool exact_r = !sure;
-                T r = 0;
-                float rfl = 0.f;  // the distance in FP32 for the FP32 pair value (no FP64 conversions)
-                int b = -1;
-                if (sure) {
-                  float rf = sqrtf(d2f);
-                  const int lo = first_edge_at_or_above(s_binf, A.nbins, rf);
-                  b = lo - 1;
-                  if (near_edge(s_binf, A.nbins, lo, rf)) exact_r = true;  // an edge within 2^-12: decide exactly
-                  rfl = rf;
-                  if constexpr (!std::is_same<FA, float>::value) r = (T)rf;
-                }
-                if (exact_r) {
-                  T e2 = d2;  // the exact re-test's d2 (not sure), or recomputed near a bin edge
-                  if (sure) {
-                    load_xj();
-                    T dx = xsub(xi[0], xj[0]);
-                    e2 = xmul(dx, dx);
-#pragma unroll
-                    for (int d = 1; d < N; d++) {
-                      T dd = xsub(xi[d], xj[d]);
-                      e2 = xadd(e2, xmul(dd, dd));
-                    }
-                  }
-                  r = xsqrt(e2);
-                  rfl = (float)r;
-                  b = first_edge_at_or_above(s_bins, A.nbins, r) - 1;
-                }
-                if (b >= 0 && b < A.nbins) {
+                if (hit) {
+                  FA uu, gg;
+                  FA df[3] = {0, 0, 0};
                   FA dv[3] = {0, 0, 0};
                   if (sure) {
+                    float uf, gf;
+                    pair_value<float, T>(A, op, d2f, oi, oj, uf, gf);
+                    uu = (FA)uf;
+                    gg = (FA)gf;
 #pragma unroll
                     for (int d = 0; d < N; d++) dv[d] = (FA)dvf[d];
                   } else {
+                    V uv, gv;
+                    pair_value<V, T>(A, op, (V)d2, oi, oj, uv, gv);
+                    uu = (FA)uv;
+                    gg = (FA)gv;
 #pragma unroll
                     for (int d = 0; d < N; d++) dv[d] = (FA)dxs[d];
                   }
-                  if (tri) {
-                    FA rv[3];
 #pragma unroll
-                    for (int a = 0; a < N; a++) {
-                      FA s = 0;
+                  for (int d = 0; d < N; d++) df[d] = gg * dv[d];
+                  if constexpr (OPK == OPK_ADJ) {
+                    {
+                      // virial W += g dx dx^T (g = u'(r)/r), and the parameter derivatives of the LJ term
+                      adj[0] += gg * dv[0] * dv[0];
+                      adj[1] += gg * dv[1] * dv[1];
+                      adj[2] += gg * dv[2] * dv[2];
+                      adj[3] += gg * dv[0] * dv[1];
+                      adj[4] += gg * dv[0] * dv[2];
+                      adj[5] += gg * dv[1] * dv[2];
+                      FA eps = par<FA>(A, 0), sig = par<FA>(A, 1);
+                      int cls = 0;
+                      if (A.ntypes > 0) {
+                        const int ti = A.tx[oi], tj = A.tx[oj];
+                        eps = eps_tab<FA>(A, ti * A.ntypes + tj);
+                        sig = sig_tab<FA>(A, ti * A.ntypes + tj);
+                        cls = ti + tj;  // 2 types: AA = 0, AB = 1, BB = 2
+                      }
+                      const FA c12 = par<FA>(A, 2), c6 = par<FA>(A, 3);
+                      const FA dd2 = sure ? (FA)d2f : (FA)d2;
+                      const FA sr2 = sig * sig * vrcp(dd2);
+                      const FA sr6 = sr2 * sr2 * sr2;
+                      const FA sr12 = sr6 * sr6;
+                      const FA lj = c12 * sr12 - c6 * sr6;
+                      const FA dsg = eps * (FA(12) * c12 * sr12 - FA(6) * c6 * sr6) * vrcp(sig);
 #pragma unroll
-                      for (int k = 0; k < N; k++) s += (FA)gc.Rinv[a][k] * dv[k];
-                      rv[a] = s;
+                      for (int k = 0; k < 3; k++) {
+                        adj[6 + k] += (cls == k) ? lj : FA(0);
+                        adj[9 + k] += (cls == k) ? dsg : FA(0);
+                      }
                     }
-#pragma unroll
-                    for (int a = 0; a < N; a++) dv[a] = rv[a];
                   }
-                  FA dot = 0;
-                  if constexpr (std::is_same<FA, float>::value) {
-                    // FP32 pair values: velocities converted once by the host code
-                    const float* vy = CROSS ? A.vyf : A.vxf;
 #pragma unroll
-                    for (int d = 0; d < N; d++)
-                      dot += (A.vxf[(int64_t)idx_i * N + d] - vy[(int64_t)idx_j * N + d]) * dv[d];
-                    hv = dot * vrcp(rfl);
-                  } else {
-                    const T* vy = CROSS ? A.vy : A.vx;
+                  for (int d = 0; d < N; d++) acc[d] -= df[d];
+                  e_part += uu;
+                  force_add<T, N, FA>(A, CROSS, idx_j, df);  // the partner's share
+                }
+              } else if constexpr (OPK == OPK_MIN) {
+                if (hit) {
+                  T dd2 = sure ? (T)d2f : d2;
+                  if (sure && ABS_PF) {
+                    T dx = xsub(xi[0], xj[0]);
+                    dd2 = xmul(dx, dx);
 #pragma unroll
-                    for (int d = 0; d < N; d++)
-                      dot += ((FA)A.vx[(int64_t)idx_i * N + d] - (FA)vy[(int64_t)idx_j * N + d]) * dv[d];
-                    hv = dot / (FA)r;
+                    for (int d = 1; d < N; d++) {
+                      T dd = xsub(xi[d], xj[d]);
+                      dd2 = xadd(dd2, xmul(dd, dd));
+                    }
                   }
-                  hb = b;
+                  if (dd2 < best_d2 || (dd2 == best_d2 && (oi < best_i || (oi == best_i && oj < best_j)))) {
+                    best_d2 = dd2;
+                    best_i = oi;
+                    best_j = oj;
+                  }
+                }
+              } else if constexpr (OPK == OPK_HIST) {
+                int hb = -1;   // bin of this lane's pair (-1: none)
+                FA hv = 0;     // its accumulator term
+                if (hit) {
+                  bool exact_r = !sure;
+                  T r = 0;
+                  float rfl = 0.f;  // the distance in FP32 for the FP32 pair value (no FP64 conversions)
+                  int b = -1;
+                  if (sure) {
+                    float rf = sqrtf(d2f);
+                    const int lo = first_edge_at_or_above(s_binf, A.nbins, rf);
+                    b = lo - 1;
+                    if (near_edge(s_binf, A.nbins, lo, rf)) exact_r = true;  // an edge within 2^-12: decide exactly
+                    rfl = rf;
+                    if constexpr (!std::is_same<FA, float>::value) r = (T)rf;
+                  }
+                  if (exact_r) {
+                    T e2 = d2;  // the exact re-test's d2 (not sure), or recomputed near a bin edge
+                    if (sure) {
+                      load_xj();
+                      T dx = xsub(xi[0], xj[0]);
+                      e2 = xmul(dx, dx);
+#pragma unroll
+                      for (int d = 1; d < N; d++) {
+                        T dd = xsub(xi[d], xj[d]);
+                        e2 = xadd(e2, xmul(dd, dd));
+                      }
+                    }
+                    r = xsqrt(e2);
+                    rfl = (float)r;
+                    b = first_edge_at_or_above(s_bins, A.nbins, r) - 1;
+                  }
+                  if (b >= 0 && b < A.nbins) {
+                    FA dv[3] = {0, 0, 0};
+                    if (sure) {
+#pragma unroll
+                      for (int d = 0; d < N; d++) dv[d] = (FA)dvf[d];
+                    } else {
+#pragma unroll
+                      for (int d = 0; d < N; d++) dv[d] = (FA)dxs[d];
+                    }
+                    if (tri) {
+                      FA rv[3];
+#pragma unroll
+                      for (int a = 0; a < N; a++) {
+                        FA s = 0;
+#pragma unroll
+                        for (int k = 0; k < N; k++) s += (FA)gc.Rinv[a][k] * dv[k];
+                        rv[a] = s;
+                      }
+#pragma unroll
+                      for (int a = 0; a < N; a++) dv[a] = rv[a];
+                    }
+                    FA dot = 0;
+                    if constexpr (std::is_same<FA, float>::value) {
+                      // FP32 pair values: velocities converted once by the host code
+                      const float* vy = CROSS ? A.vyf : A.vxf;
+#pragma unroll
+                      for (int d = 0; d < N; d++)
+                        dot += (A.vxf[(int64_t)idx_i * N + d] - vy[(int64_t)idx_j * N + d]) * dv[d];
+                      hv = dot * vrcp(rfl);
+                    } else {
+                      const T* vy = CROSS ? A.vy : A.vx;
+#pragma unroll
+                      for (int d = 0; d < N; d++)
+                        dot += ((FA)A.vx[(int64_t)idx_i * N + d] - (FA)vy[(int64_t)idx_j * N + d]) * dv[d];
+                      hv = dot / (FA)r;
+                    }
+                    hb = b;
+                  }
+                }
+                // lanes holding the same bin are summed by a tree over their group; the group's first lane
+                // then updates the warp's own bin (groups have distinct bins: no atomics)
+                if (__any_sync(FULL, hb >= 0)) {
+                  const unsigned peers = __match_any_sync(FULL, hb);
+                  const FA v = group_sum(peers, hv, lane);
+                  if (hb >= 0 && lane == __ffs(peers) - 1) {
+                    s_ws[hb] += v;
+                    s_wc[hb] += (unsigned)__popc(peers);
+                  }
                 }
               }
-              // lanes holding the same bin are summed by a tree over their group; the group's first lane
-              // then updates the warp's own bin (groups have distinct bins: no atomics)
-              if (__any_sync(FULL, hb >= 0)) {
-                const unsigned peers = __match_any_sync(FULL, hb);
-                const FA v = group_sum(peers, hv, lane);
-                if (hb >= 0 && lane == __ffs(peers) - 1) {
-                  s_ws[hb] += v;
-                  s_wc[hb] += (unsigned)__popc(peers);
+            }
+            if constexpr (IS_F) {
+              // lanes ending on the same particle are adjacent: sum each run of equal `cur` into its first
+              // lane, which alone adds it to the particle's sums
+              __syncwarp();
+#pragma unroll
+              for (int off = 1; off < 32; off <<= 1) {
+                const int co = __shfl_down_sync(FULL, cur, off);
+                FA t[3];
+#pragma unroll
+                for (int d = 0; d < N; d++) t[d] = __shfl_down_sync(FULL, acc[d], off);
+                if (lane + off < 32 && co == cur) {
+#pragma unroll
+                  for (int d = 0; d < N; d++) acc[d] += t[d];
+                }
+              }
+              const int cprev = __shfl_up_sync(FULL, cur, 1);
+              if (cur >= 0 && (lane == 0 || cprev != cur)) {
+#pragma unroll
+                for (int d = 0; d < N; d++) s_if[warp][d][cur] += acc[d];
+              }
+            }
+            if constexpr (OPK == OPK_HIST) {
+              // move the warp's bins (at most 1024 pairs of this round) into the block's FP64 bins
+              __syncwarp();
+              for (int b = lane; b < A.nbins; b += 32) {
+                const unsigned c = s_wc[b];
+                if (c) {
+                  atomicAdd(&s_hc[b], (unsigned long long)c);
+                  atomicAdd(&s_hs[b], (double)s_ws[b]);
+                  s_wc[b] = 0u;
+                  s_ws[b] = FA(0);
                 }
               }
             }
-          }
-          if constexpr (IS_F) {
-            // lanes ending on the same particle are adjacent: sum each run of equal `cur` into its first
-            // lane, which alone adds it to the particle's sums
             __syncwarp();
-#pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-              const int co = __shfl_down_sync(FULL, cur, off);
-              FA t[3];
-#pragma unroll
-              for (int d = 0; d < N; d++) t[d] = __shfl_down_sync(FULL, acc[d], off);
-              if (lane + off < 32 && co == cur) {
-#pragma unroll
-                for (int d = 0; d < N; d++) acc[d] += t[d];
-              }
-            }
-            const int cprev = __shfl_up_sync(FULL, cur, 1);
-            if (cur >= 0 && (lane == 0 || cprev != cur)) {
-#pragma unroll
-              for (int d = 0; d < N; d++) s_if[warp][d][cur] += acc[d];
-            }
-          }
-          if constexpr (OPK == OPK_HIST) {
-            // move the warp's bins (at most 1024 pairs of this round) into the block's FP64 bins
-            __syncwarp();
-            for (int b = lane; b < A.nbins; b += 32) {
-              const unsigned c = s_wc[b];
-              if (c) {
-                atomicAdd(&s_hc[b], (unsigned long long)c);
-                atomicAdd(&s_hs[b], (double)s_ws[b]);
-                s_wc[b] = 0u;
-                s_ws[b] = FA(0);
-              }
-            }
           }
           __syncwarp();
         }
-        __syncwarp();
       }
       e_tot += (double)e_part;
       e_part = 0;

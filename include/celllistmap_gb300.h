@@ -185,15 +185,15 @@ int32_t clm_fetch_celllist(clm_handle h, int32_t set, int64_t cap, int64_t* cell
 int32_t clm_last_timings(clm_handle h, float* build_ms, float* map_ms);
 
 /* Allocation-free pair reductions, for callers that cannot call cudaMalloc where they evaluate
- * (inside a CUDA stream capture, under an application-owned device pool, in a real-time loop).
- * No counterpart in the reference.  Supports CLM_OP_COUNT, CLM_OP_SUM_D2, CLM_OP_SUM_D,
+ * (under an application-owned device pool, in a real-time loop that must not enter the CUDA
+ * allocator).  No counterpart in the reference.  Supports CLM_OP_COUNT, CLM_OP_SUM_D2, CLM_OP_SUM_D,
  * CLM_OP_SUM_INV_D, CLM_OP_SOFT_ENERGY, CLM_OP_LJ_ENERGY (no type tables) and CLM_OP_MINDIST on a
  * handle whose cell lists are already built (clm_build; returns CLM_ERR_STATE otherwise, since
  * building allocates).  Per-block partials live in a static 128 KiB + 256 B device array (4096 block
  * slots, held by every GPU that loads the library until exit); a launch needing more slots returns
  * CLM_ERR_CAPACITY.  The first call on a device looks up the array's device address, so make it
  * before any stream capture.  Calls share the array: calls that overlap on the GPU race.  Call with
- * the handle's device current. */
+ * the handle's device current.  The call waits for its result (stream synchronization, host read). */
 int32_t clm_run_noalloc(clm_handle h, int32_t op_id, const clm_op_params* params, clm_outputs* out);
 
 /* LJ energy, forces and adjoint in one call: clm_run(h, CLM_OP_LJ_ADJOINT, params, out).  The

@@ -13,6 +13,8 @@
 //   split_bins_probe,  bin search and the exact re-decision window, and the split form's histogram
 //   bin_probe,         counts composed over every x-y pair.
 //   near_edge_probe, split_hist_probe
+//   map_nl_visits_probe the self-pair map's candidate visits that reach the hit queue, and its pairs;
+//   noalloc_slots_probe the per-block slots of the allocation-free entry point's scratch.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -20,6 +22,7 @@
 #include <vector>
 
 #include "clm_build_steps.cuh"
+#include "clm_internal.hpp"
 
 namespace {
 
@@ -322,15 +325,18 @@ extern "C" int cell_probe(int dim, int kind, const double* Mcol, double cutoff, 
 
 namespace {
 // The self-pair map of the pair kernel, emulated on the host from the library's own pieces: the cells with
-// real particles, every copy of such a cell as the particle side (real copies only in triclinic cells),
-// stencil entry 0 (the cell itself) then the forward half stencil (orthorhombic, non-periodic) or all
-// neighbours (triclinic), the kernel's pair rule, the exact test in the input dtype and, for pairs in the
-// band d2 > thr_lo of another cell, the projection filter.  The FP32 distance pass of the kernel is
-// evaluated too, with the cell-displacement shift of the offsets both fused and unfused: a pair the exact
-// test accepts but the FP32 pass would drop is counted in *lost.
+// real particles, every copy of such a cell as the particle side, stencil entry 0 (the cell itself) then
+// the forward half stencil (orthorhombic, non-periodic) or, in triclinic cells, the forward half and the
+// cells of the backward half that hold no real particle (sym_stencil_offset), the kernel's pair rule, the
+// exact test in the input dtype and, for pairs in the band d2 > thr_lo of another cell, the projection
+// filter seen from the cell of the reference's i (the copy of the lower index in triclinic cells).  The FP32
+// distance pass of the kernel is evaluated too, with the cell-displacement shift of the offsets both fused
+// and unfused: a pair the exact test accepts but the FP32 pass would drop is counted in *lost.  *visits
+// (when given) receives the number of candidate visits the FP32 pass could let through: copies pairs within
+// the cutoff before the pair rule, excluding pairs of two images (which the kernel drops in that pass).
 template <class T, int N>
 int64_t map_nl(int kind, const double* Mcol, double cutoff, int lcell, const double* xin, int n, int64_t cap,
-               int64_t* pi_out, int64_t* pj_out, double* d_out, int64_t* lost, int* st_out) {
+               int64_t* pi_out, int64_t* pj_out, double* d_out, int64_t* lost, int* st_out, int64_t* visits = nullptr) {
   HostList<T, N> L;
   *st_out = build_host<T, N>(kind, Mcol, cutoff, lcell, xin, n, L);
   if (*st_out) return -1;
@@ -338,11 +344,13 @@ int64_t map_nl(int kind, const double* Mcol, double cutoff, int lcell, const dou
   const bool tri = g.kind == clm::TRICLINIC, nonper = g.kind == clm::NONPERIODIC;
   const int w = 2 * g.lcell + 1;
   const int wN = (N == 3) ? w * w * w : w * w;
-  const int nent = (tri ? wN - 1 : (wN - 1) / 2) + 1;
+  const int nf = (wN - 1) / 2;
+  const int nent = nf * (tri ? 2 : 1) + 1;
   const T band = (T)g.thr_lo;
   const std::vector<float4> foff = fp32_offsets(L);
   int64_t np = 0;
   *lost = 0;
+  if (visits) *visits = 0;
   for (int ci_lin = 0; ci_lin < g.ncells; ci_lin++) {
     if (!L.flags[(size_t)ci_lin]) continue;
     int ci[3];
@@ -355,18 +363,19 @@ int64_t map_nl(int kind, const double* Mcol, double cutoff, int lcell, const dou
       const int code_i = L.code[(size_t)a];
       const bool real_i = code_i >= 0;
       const int idx_i = real_i ? code_i : -code_i - 1;
-      if (tri && !real_i) continue;
       T xa[3];
       for (int k = 0; k < N; k++) xa[k] = L.x(a, k);
       for (int e = 0; e < nent; e++) {
         int o[3] = {0, 0, 0};
-        if (e > 0) clm::stencil_offset(!tri, g.lcell, N, e - 1, o);
+        bool back = false;
+        if (e > 0) clm::sym_stencil_offset(g.lcell, N, nf, e - 1, o, &back);
         const int cj[3] = {ci[0] + o[0], ci[1] + o[1], N == 3 ? ci[2] + o[2] : 1};
         bool inside = true;
         for (int k = 0; k < N; k++) inside = inside && cj[k] >= 1 && cj[k] <= g.nc[k];
         if (!inside) continue;
         const int cj_lin = (N == 3) ? (cj[0] - 1) + g.nc[0] * ((cj[1] - 1) + g.nc[1] * (cj[2] - 1))
                                     : (cj[0] - 1) + g.nc[0] * (cj[1] - 1);
+        if (back && L.flags[(size_t)cj_lin]) continue;  // that pair of cells is visited from the other cell
         const int sj = L.start[(size_t)cj_lin], nj = L.start[(size_t)cj_lin + 1] - sj;
         T ctr_j[3] = {0, 0, 0};
         if (e > 0) clm::cell_center<T, N>(g, cj, ctr_j);
@@ -375,7 +384,6 @@ int64_t map_nl(int kind, const double* Mcol, double cutoff, int lcell, const dou
           const int code_j = L.code[(size_t)b];
           const bool real_j = code_j >= 0;
           const int idx_j = real_j ? code_j : -code_j - 1;
-          if (!clm::pair_rule(false, tri, nonper, e == 0, jj, ii, real_i, real_j, idx_i, idx_j)) continue;
           T xb[3], dx[3];
           for (int k = 0; k < N; k++) {
             xb[k] = L.x(b, k);
@@ -383,14 +391,19 @@ int64_t map_nl(int kind, const double* Mcol, double cutoff, int lcell, const dou
           }
           T d2 = clm::xmul(dx[0], dx[0]);
           for (int k = 1; k < N; k++) d2 = clm::xadd(d2, clm::xmul(dx[k], dx[k]));
+          if (visits && d2 <= g.cutoff_sqr && (e > 0 || jj > ii) && (real_i || real_j)) (*visits)++;
+          if (!clm::pair_rule(false, tri, nonper, e == 0, jj, ii, real_i, real_j, idx_i, idx_j)) continue;
+          // the reference's i: the particle copy, or in triclinic cells the copy of the lower index
+          const bool swap = tri && idx_j < idx_i;
           bool hit = d2 <= g.cutoff_sqr;
-          if (hit && d2 > band && e > 0) hit = clm::projection_pass<T, N>(g, ctr_i, ctr_j, xa, xb);
+          if (hit && d2 > band && e > 0)
+            hit = swap ? clm::projection_pass<T, N>(g, ctr_j, ctr_i, xb, xa) : clm::projection_pass<T, N>(g, ctr_i, ctr_j, xa, xb);
           if (!hit) continue;
           // the FP32 distance pass must keep this pair, whichever way the shift rounds
           if (!fp32_keeps(L, foff, a, L, foff, b, o)) (*lost)++;
           if (np < cap) {
-            pi_out[np] = idx_i;
-            pj_out[np] = idx_j;
+            pi_out[np] = swap ? idx_j : idx_i;
+            pj_out[np] = swap ? idx_i : idx_j;
             d_out[np] = (double)clm::xsqrt(d2);
           }
           np++;
@@ -651,4 +664,20 @@ extern "C" int64_t split_hist_probe(int dim, int kind, const double* Mcol, doubl
     return binned;
   };
   return dim == 3 ? run(std::integral_constant<int, 3>()) : run(std::integral_constant<int, 2>());
+}
+
+// The self-pair map's candidate visits that pass the FP32 pass's image test (see map_nl), and its pairs.
+extern "C" int64_t map_nl_visits_probe(int f64, int dim, int kind, const double* Mcol, double cutoff, int lcell,
+                                       const double* x, int n, int64_t* visits, int* st) {
+  int64_t lost = 0;
+  if (dim == 3)
+    return f64 ? map_nl<double, 3>(kind, Mcol, cutoff, lcell, x, n, 0, nullptr, nullptr, nullptr, &lost, st, visits)
+               : map_nl<float, 3>(kind, Mcol, cutoff, lcell, x, n, 0, nullptr, nullptr, nullptr, &lost, st, visits);
+  return f64 ? map_nl<double, 2>(kind, Mcol, cutoff, lcell, x, n, 0, nullptr, nullptr, nullptr, &lost, st, visits)
+             : map_nl<float, 2>(kind, Mcol, cutoff, lcell, x, n, 0, nullptr, nullptr, nullptr, &lost, st, visits);
+}
+
+// Per-block slots of the allocation-free entry point's scratch (clm_internal.hpp noalloc_block_slots).
+extern "C" long long noalloc_slots_probe(long long scratch_bytes, int tsize) {
+  return (long long)clm::noalloc_block_slots((size_t)scratch_bytes, (size_t)tsize);
 }

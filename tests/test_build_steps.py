@@ -554,3 +554,17 @@ def test_emulated_split_histogram_counts(probe, orc, dim):
     r = orc.run("rhist", x, y, dim=dim, unitcell=[250.0] * dim, cutoff=25.0, bins=edges, vel_x=np.zeros_like(x),
                 vel_y=np.zeros_like(y))
     np.testing.assert_array_equal(counts, r["hist_count"])
+
+
+def test_noalloc_scratch_slots(probe):
+    # the allocation-free entry point's static scratch (128 KiB + 256 B: a 256-byte result area, then one
+    # slot per block of an energy, a count, a minimum d2 in the handle dtype and its pair of indices) holds
+    # 4096 blocks for Float64 handles and 4681 for Float32 ones; a launch of more blocks is refused
+    # (CLM_ERR_CAPACITY), which a GB300 never needs (at most 6 blocks per SM x 152 SMs)
+    probe.noalloc_slots_probe.restype = C.c_longlong
+    probe.noalloc_slots_probe.argtypes = [C.c_longlong, C.c_int]
+    assert probe.noalloc_slots_probe(128 * 1024 + 256, 8) == 4096
+    assert probe.noalloc_slots_probe(128 * 1024 + 256, 4) == 4681
+    assert probe.noalloc_slots_probe(256, 8) == 0
+    assert probe.noalloc_slots_probe(100, 8) == 0
+    assert probe.noalloc_slots_probe(256 + 31, 8) == 0 and probe.noalloc_slots_probe(256 + 32, 8) == 1

@@ -1,5 +1,6 @@
 """clm_run_noalloc: pair-map reductions for callers that cannot allocate device memory where they
-evaluate (inside a CUDA stream capture, under an application-owned device pool, in a real-time loop).
+evaluate (under an application-owned device pool, or in a real-time loop that must not enter the CUDA
+allocator).
 
 The entry point is checked through the C ABI against clm_run on the same built handle, on two calls in
 a row (the calls share a static scratch array, which keeps the previous call's contents), and the
@@ -89,4 +90,31 @@ def test_noalloc_refuses_what_would_allocate(clm):
     assert L.clm_run_noalloc(h, A.OP["soft_energy"], C.byref(_params(A, ())), C.byref(o)) == 7
     s.build()
     assert L.clm_run_noalloc(h, A.OP["soft_energy"], C.byref(_params(A, ())), C.byref(o)) == 0
+    # per-type LJ tables are staged in handle buffers: refused with CLM_ERR_ARG
+    p = _params(A, (1.0, 1.0, 4.0, 4.0))
+    t = np.zeros(s.n_x, np.int32)
+    tab = np.ones(1)
+    p.ntypes, p.types_x, p.eps_table, p.sig_table = 1, t.ctypes.data, tab.ctypes.data, tab.ctypes.data
+    assert L.clm_run_noalloc(h, A.OP["lj_energy"], C.byref(p), C.byref(o)) == 1
+    s.close()
+
+
+def test_noalloc_refuses_a_build_nobody_checked(clm):
+    # clm_run enqueues the rebuild of updated positions and checks its totals and error bits with the map's
+    # results; when it returns early (an unknown operator), the rebuilt set was never checked, so the
+    # allocation-free entry point refuses it (CLM_ERR_STATE) until clm_build has checked a build again
+    A = clm._abi
+    L = A.load()
+    s = _built_system(clm, np.float64, False)
+    h = s._handle.h
+    o = A.Outputs()
+    x2 = np.asarray(s.xpositions) + 0.05
+    s.update(xpositions=x2)
+    assert L.clm_run(h, 999, C.byref(_params(A, ())), C.byref(o)) == 1
+    assert L.clm_run_noalloc(h, A.OP["soft_energy"], C.byref(_params(A, ())), C.byref(o)) == 7
+    s.build()
+    assert L.clm_run_noalloc(h, A.OP["soft_energy"], C.byref(_params(A, ())), C.byref(o)) == 0
+    ref = A.Outputs()
+    assert L.clm_run(h, A.OP["soft_energy"], C.byref(_params(A, ())), C.byref(ref)) == 0
+    assert abs(o.scalar - ref.scalar) <= 1e-12 * abs(ref.scalar)
     s.close()

@@ -11,7 +11,7 @@ the host's cores:
     dU/dsigma);
   * the 4096 batched systems (14.2M particles): every system's status, and counts and energies of a
     sample of systems;
-  * the two-set radial histogram on a subsample of x against all 2M points of y.
+  * the two-set radial histogram, 3D and 2D, on a subsample of x against all 2M points of y.
 and through size-independent properties at full size: Newton's third law on the forces (sum of F ~ 0),
 equal counts across operators and precision forms, histogram counts equal between the exact and FP32-split
 forms, the dropped pairs (r <= first edge) accounted for.  Last, a split-form histogram with edges finer than
@@ -192,8 +192,10 @@ def check_hist_forms(g, vx, vy):
     assert g["count_exact"] - int(g["exact"][0].sum()) == g["below_first_edge"]
 
 
-def test_histogram_two_sets_full_size(clm, orc):
-    x, y, vx, vy, sides = clm.workloads.cfg5()  # 2 x 2,000,000 Float64 points, side 250, cutoff 25
+@pytest.mark.parametrize("dim", [3, 2])
+def test_histogram_two_sets_full_size(clm, orc, dim):
+    # 2 x 2,000,000 Float64 points, side 250, cutoff 25 (3D: 1.7e10 pairs in bins; 2D: 1.3e11)
+    x, y, vx, vy, sides = clm.workloads.cfg5(dim=dim)
     bins = clm.workloads.cfg5_bins()
     g = {}
     s = clm.ParticleSystem(xpositions=x, ypositions=y, unitcell=sides, cutoff=25.0)
@@ -203,7 +205,8 @@ def test_histogram_two_sets_full_size(clm, orc):
     g["split"] = clm.pairwise(clm.RadialHistogram(bins, vx, vy), s)
     g["count_split"] = clm.pairwise(clm.Count(), s)
     s.close()
-    # pairs with r <= 0.1 (1108 here; 4e12 * (4/3 pi 0.1^3) / 250^3 ~ 1072 expected for uniform points)
+    # pairs with r <= 0.1 (3D: 1108 here, 4e12 (4/3 pi 0.1^3) / 250^3 ~ 1072 expected for uniform points;
+    # 2D: ~ 4e12 pi 0.1^2 / 250^2 ~ 2.0e6)
     kd = pytest.importorskip("scipy.spatial")
     g["below_first_edge"] = int(kd.cKDTree(x, boxsize=sides[0]).count_neighbors(kd.cKDTree(y, boxsize=sides[0]),
                                                                                 bins[0]))
@@ -213,7 +216,7 @@ def test_histogram_two_sets_full_size(clm, orc):
     s = clm.ParticleSystem(xpositions=xs, ypositions=y, unitcell=sides, cutoff=25.0)
     hc, hs = clm.pairwise(clm.RadialHistogram(bins, vxs, vy), s)
     s.close()
-    r = orc.run("rhist", xs, y, unitcell=sides, cutoff=25.0, bins=bins, vel_x=vxs, vel_y=vy, nthreads=NT)
+    r = orc.run("rhist", xs, y, dim=dim, unitcell=sides, cutoff=25.0, bins=bins, vel_x=vxs, vel_y=vy, nthreads=NT)
     check_hist_subsample({"count": hc, "sum": hs}, r, vxs, vy)
 
 
