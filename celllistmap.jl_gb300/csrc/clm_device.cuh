@@ -249,6 +249,28 @@ __host__ __device__ __forceinline__ bool pair_rule(bool cross, bool tri, bool no
   return cand;
 }
 
+// pair_rule as the pair kernel applies it, in three parts.  In the FP32 distance pass: a pair of two images
+// is dropped (the AND of the two particle codes, image = negative code, is negative), and in the cell itself
+// the slots same_cell_dropped names are masked out per round.  In the hit queue: a triclinic self pair of a
+// real copy and an image is kept when the copy of the lower index is real (sym_mixed_keeps).  Together
+// these equal pair_rule (checked over every case by the CPU tests).
+__host__ __device__ __forceinline__ bool same_cell_dropped(bool cross, bool tri, bool nonper, int slot_j, int ii,
+                                                           bool real_i) {
+  if (!cross) return slot_j <= ii;  // self pairs: each pair of the cell once, from its earlier slot
+  return !tri && !nonper && !real_i;  // cross pairs, orthorhombic: the particle copy must be real
+}
+__host__ __device__ __forceinline__ bool sym_mixed_keeps(int code_i, int code_j) {
+  const int idx_i = code_i >= 0 ? code_i : ~code_i, idx_j = code_j >= 0 ? code_j : ~code_j;
+  return (idx_i < idx_j) ? code_i >= 0 : code_j >= 0;
+}
+__host__ __device__ __forceinline__ bool pair_rule_parts(bool cross, bool tri, bool nonper, bool same, int slot_j,
+                                                         int ii, int code_i, int code_j) {
+  if ((code_i & code_j) < 0) return false;
+  if (same && same_cell_dropped(cross, tri, nonper, slot_j, ii, code_i >= 0)) return false;
+  if (!cross && tri && (code_i ^ code_j) < 0) return sym_mixed_keeps(code_i, code_j);
+  return true;
+}
+
 template <class T, int N>
 __host__ __device__ __forceinline__ T exact_dot_rel(const T* x, const T* c, const T* u) {
   T s = xmul(xsub(x[0], c[0]), u[0]);

@@ -276,9 +276,10 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
   __shared__ int s_tj[2][kWarps][ABS_PF ? 1 : JC];       // position of the candidate in the cell list
   __shared__ __align__(8) unsigned long long s_mbar[kWarps][2];  // completion of the bulk copies of a window
   __shared__ unsigned short s_q[kWarps][1024];  // compacted candidates: (particle slot << 8) | staged index
-  __shared__ T s_ix[kWarps][3][32];              // particles of the current chunk of the cell
-  __shared__ float s_ipf[kWarps][3][32];
-  __shared__ int s_icode[kWarps][32];
+  // particles of the current chunk of the cell: prefilter coordinates with the particle code in .w, and
+  // (Float64 handles) the coordinates in the handle dtype for the exact re-test
+  __shared__ __align__(16) float4 s_i4[kWarps][32];
+  __shared__ T s_ix[kWarps][3][ABS_PF ? 1 : 32];
   __shared__ FA s_if[kWarps][3][IS_F ? 32 : 1];  // force sums of those particles
   // radial histogram (dynamic shared memory, layout in hist_smem): block bins in FP64, bin edges, and
   // per-warp bins that the warp updates without atomics
@@ -386,13 +387,12 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
       const int idx_i = real_i ? code_i : -code_i - 1;
       const bool act_i = (tri && CROSS) ? (vi && real_i) : vi;
       if (grp == 0) {
+        s_i4[warp][il] = make_float4(pi[0], pi[1], pi[2], __int_as_float(code_i));
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-          s_ix[warp][d][il] = xi[d];
-          s_ipf[warp][d][il] = pi[d];
+          if constexpr (!ABS_PF) s_ix[warp][d][il] = xi[d];
           if constexpr (IS_F) s_if[warp][d][il] = FA(0);
         }
-        s_icode[warp][il] = code_i;
       }
       __syncwarp();
 
@@ -507,10 +507,10 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
           for (int rb = 0; rb < wc; rb += JR) {
             const int cntr = min(JR, wc - rb);
             // ---- phase A: 32 FP32 distance tests per lane into a bit mask.  A test passes when the sign bit
-            // of d2 - thr is set (in triclinic self pairs, and that of the codes' AND clear: a pair of two
-            // images is never the reference's pair); the sign bits are shifted into the mask, candidate b
-            // landing on bit b.  thr carries a 2^-13 relative margin, far above the FP32 rounding of
-            // dx^2 - thr + dy^2 + dz^2, so the strict comparison keeps every pair the exact test can accept.
+            // of d2 - thr is set and that of the AND of the two particle codes is clear (a pair of two images is
+            // never the reference's pair); the sign bits are shifted into the mask, candidate b landing on bit
+            // b.  thr carries a 2^-13 relative margin, far above the FP32 rounding of dx^2 - thr + dy^2 + dz^2,
+            // so the strict comparison keeps every pair the exact test can accept.
             unsigned mask = 0u;
             {
               const float thr = g.thr_hi;
@@ -519,23 +519,13 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
               auto test32 = [&](auto g_const) {
                 constexpr int GG = decltype(g_const)::value;
                 const float4* pp = &s_pf[bsel][warp][rb + grp];
-                if (sym) {
 #pragma unroll
-                  for (int b = 31; b >= 0; b--) {
-                    const float4 p = pp[b * GG];
-                    const float dx = pi[0] - p.x, dy = pi[1] - p.y, dz = (N == 3) ? pi[2] - p.z : 0.f;
-                    const float e = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, -thr)));  // d2 - thr
-                    const int v = __float_as_int(e) & ~(code_i & __float_as_int(p.w));  // .w: particle code
-                    mask = __funnelshift_l((unsigned)v, mask, 1);  // (mask << 1) | sign bit of v
-                  }
-                } else {
-#pragma unroll
-                  for (int b = 31; b >= 0; b--) {
-                    const float4 p = pp[b * GG];
-                    const float dx = pi[0] - p.x, dy = pi[1] - p.y, dz = (N == 3) ? pi[2] - p.z : 0.f;
-                    const float e = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, -thr)));  // d2 - thr
-                    mask = __funnelshift_l(__float_as_uint(e), mask, 1);
-                  }
+                for (int b = 31; b >= 0; b--) {
+                  const float4 p = pp[b * GG];
+                  const float dx = pi[0] - p.x, dy = pi[1] - p.y, dz = (N == 3) ? pi[2] - p.z : 0.f;
+                  const float e = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, -thr)));  // d2 - thr
+                  const int v = __float_as_int(e) & ~(code_i & __float_as_int(p.w));  // .w: particle code
+                  mask = __funnelshift_l((unsigned)v, mask, 1);  // (mask << 1) | sign bit of v
                 }
               };
               if (G == 2) test32(std::integral_constant<int, 2>());
@@ -543,10 +533,22 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
               else test32(std::integral_constant<int, 4>());
             }
             {
-              // candidates past the window's end (stale records) are dropped: candidate b is rb + grp + b G
+              // bit b is stream position base + b G.  Dropped: positions past the window's end (stale
+              // records), and in the cell itself the pairs the reference does not visit from this copy: the
+              // earlier slots for self pairs (each pair of the cell once), every slot for an image copy in
+              // cross pairs of orthorhombic cells (the particle copy must be real there).  What remains of
+              // the pair rules is in phase B (triclinic self pairs of a real copy and an image).
+              const int base = w0 + rb + grp;
               const int nb = (cntr - grp + G - 1) / G;
               if (!act_i || nb <= 0) mask = 0u;
               else if (nb < 32) mask &= (1u << nb) - 1u;
+              int lim = -1;  // last dropped position of the cell itself
+              if (!CROSS) lim = min(ii, same_end - 1);
+              else if (!tri && !nonper && code_i < 0) lim = same_end - 1;
+              if (lim >= base) {
+                const int nr = (lim - base) / G + 1;
+                mask &= (nr >= 32) ? 0u : ~((1u << nr) - 1u);
+              }
             }
             // ---- phase B: compact the candidates of all lanes into a queue and process them with every lane
             // busy; each lane takes a contiguous run of the queue (runs are grouped by particle, so force
@@ -572,28 +574,49 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
             __syncwarp();
             const int per = (H + 31) >> 5;
             const int qbeg = lane * per;
-            int cur = -1;
+            int cur = -1;  // the particle slot of this lane's run (its data below, its force sums in acc)
+            float4 xi4 = make_float4(0.f, 0.f, 0.f, 0.f);
             FA acc[3] = {0, 0, 0};
             for (int t = 0; t < per; t++) {
               const int q = qbeg + t;
               const bool has = q < H;
-              int j = 0, ie = 0;
+              int j = 0, ie = (cur < 0) ? 0 : cur;
               if (has) {
                 const int ent = s_q[warp][q];
                 ie = ent >> 8;
                 j = ent & 255;
               }
-              T xi[3];
-              float pi[3];
+              // `cur` follows every queue entry (hit or not), so the lanes holding a particle are exactly the
+              // lanes whose runs cover its entries: adjacent, and only the last one moves past it inside its
+              // run; no other lane updates that particle's sums during the loop
+              if (has && ie != cur) {
+                if constexpr (IS_F) {
+                  if (cur >= 0) {
 #pragma unroll
-              for (int d = 0; d < 3; d++) {
-                xi[d] = s_ix[warp][d][ie];
-                pi[d] = ABS_PF ? (float)xi[d] : s_ipf[warp][d][ie];
+                    for (int d = 0; d < N; d++) s_if[warp][d][cur] += acc[d];
+                  }
+#pragma unroll
+                  for (int d = 0; d < N; d++) acc[d] = FA(0);
+                }
+                cur = ie;
+                xi4 = s_i4[warp][ie];
               }
-              const int code_i = s_icode[warp][ie];
+              const float pi[3] = {xi4.x, xi4.y, xi4.z};
+              T xi[3] = {0, 0, 0};
+              if constexpr (ABS_PF) {
+                xi[0] = xi4.x;
+                xi[1] = xi4.y;
+                xi[2] = xi4.z;
+              }
+              auto load_xi = [&]() {
+                if constexpr (!ABS_PF) {
+#pragma unroll
+                  for (int d = 0; d < 3; d++) xi[d] = s_ix[warp][d][ie];
+                }
+              };
+              const int code_i = __float_as_int(xi4.w);
               const bool real_i = code_i >= 0;
-              const int idx_i = real_i ? code_i : -code_i - 1;
-              const int ii = ib + ie;
+              const int idx_i = real_i ? code_i : ~code_i;
               bool hit = false, sure = false;
               int idx_j = 0;
               int oi = 0, oj = 0;  // the pair as the reference orients it (i, j)
@@ -612,20 +635,11 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
               if (has) {
                 const float4 p = s_pf[bsel][warp][j];
                 const int code_j = __float_as_int(p.w);
-                const bool real_j = code_j >= 0;
-                idx_j = real_j ? code_j : -code_j - 1;
-                const int epos = w0 + j;  // position in the stream: inside the cell itself when same
-                int meta = 0;
-                bool same;
-                if constexpr (ABS_PF) {
-                  same = epos < same_end;
-                } else {
-                  meta = s_meta[bsel][warp][j];
-                  tjj = s_tj[bsel][warp][j];
-                  same = (meta & F_SAME) != 0;
-                }
-                const bool cand = pair_rule(CROSS, tri, nonper, same, epos, ii, real_i, real_j, idx_i, idx_j);
-                // triclinic self pairs: the copy of the lower index is the reference's i
+                idx_j = code_j >= 0 ? code_j : ~code_j;
+                // the rest of the pair rules: in triclinic self pairs of a real copy and an image, the copy of
+                // the lower index is the reference's i and must be real
+                bool cand = true;
+                if (sym && (code_i ^ code_j) < 0) cand = sym_mixed_keeps(code_i, code_j);
                 const bool sw = sym && idx_j < idx_i;
                 oi = sw ? idx_j : idx_i;
                 oj = sw ? idx_i : idx_j;
@@ -647,6 +661,12 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                     }
                   }
                   if (!sure) {
+                    load_xi();
+                    int meta = 0;
+                    if constexpr (!ABS_PF) {
+                      meta = s_meta[bsel][warp][j];
+                      tjj = s_tj[bsel][warp][j];
+                    }
                     load_xj();
 #pragma unroll
                     for (int d = 0; d < N; d++) dxs[d] = xsub(xi[d], xj[d]);
@@ -654,7 +674,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
 #pragma unroll
                     for (int d = 1; d < N; d++) d2 = xadd(d2, xmul(dxs[d], dxs[d]));
                     hit = d2 <= g.cutoff_sqr;
-                    if (hit && d2 > band && !same) {
+                    const int epos = w0 + j;  // position in the stream
+                    if (hit && d2 > band && epos >= same_end) {
                       // the reference's projection filter, seen from the cell of the reference's i
                       if constexpr (ABS_PF) {
                         int lo = 0;
@@ -719,18 +740,6 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                   }
                 }
               } else if constexpr (IS_F) {
-                // `cur` follows every queue entry (hit or not), so the lanes holding a particle are exactly
-                // the lanes whose runs cover its entries: adjacent, and only the last one moves past it inside
-                // its run; no other lane updates that particle's sums during the loop
-                if (has && ie != cur) {
-                  if (cur >= 0) {
-#pragma unroll
-                    for (int d = 0; d < N; d++) s_if[warp][d][cur] += acc[d];
-                  }
-                  cur = ie;
-#pragma unroll
-                  for (int d = 0; d < N; d++) acc[d] = FA(0);
-                }
                 if (hit) {
                   FA uu, gg;
                   FA df[3] = {0, 0, 0};
@@ -825,6 +834,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                   if (exact_r) {
                     T e2 = d2;  // the exact re-test's d2 (not sure), or recomputed near a bin edge
                     if (sure) {
+                      load_xi();
+                      if constexpr (!ABS_PF) tjj = s_tj[bsel][warp][j];
                       load_xj();
                       T dx = xsub(xi[0], xj[0]);
                       e2 = xmul(dx, dx);

@@ -681,3 +681,14 @@ extern "C" int64_t map_nl_visits_probe(int f64, int dim, int kind, const double*
 extern "C" long long noalloc_slots_probe(long long scratch_bytes, int tsize) {
   return (long long)clm::noalloc_block_slots((size_t)scratch_bytes, (size_t)tsize);
 }
+
+// pair_rule and its three parts as the pair kernel applies them (clm_device.cuh), for one case.
+extern "C" int pair_rule_probe(int cross, int tri, int nonper, int same, int slot_j, int ii, int code_i, int code_j,
+                               int* parts) {
+  const int idx_i = code_i >= 0 ? code_i : ~code_i, idx_j = code_j >= 0 ? code_j : ~code_j;
+  *parts = clm::pair_rule_parts(cross != 0, tri != 0, nonper != 0, same != 0, slot_j, ii, code_i, code_j) ? 1 : 0;
+  return clm::pair_rule(cross != 0, tri != 0, nonper != 0, same != 0, slot_j, ii, code_i >= 0, code_j >= 0, idx_i,
+                        idx_j)
+             ? 1
+             : 0;
+}

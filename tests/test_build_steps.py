@@ -568,3 +568,35 @@ def test_noalloc_scratch_slots(probe):
     assert probe.noalloc_slots_probe(256, 8) == 0
     assert probe.noalloc_slots_probe(100, 8) == 0
     assert probe.noalloc_slots_probe(256 + 31, 8) == 0 and probe.noalloc_slots_probe(256 + 32, 8) == 1
+
+
+def test_pair_rule_parts_equal_pair_rule(probe):
+    # the pair kernel applies the reference's pair rules (pair_rule) in three parts: pairs of two images
+    # dropped in the FP32 distance pass, same-cell slots masked per round, and in the hit queue the
+    # lower-index rule of triclinic self pairs of a real copy and an image.  Over every case the parts keep
+    # exactly the pairs pair_rule keeps, for the visits the kernel makes (the particle copy is real in
+    # triclinic cross pairs; two copies of one particle are never both visited within the cutoff, since
+    # the unit-cell check keeps images more than twice the cutoff apart)
+    probe.pair_rule_probe.restype = C.c_int
+    parts = C.c_int(0)
+    n = 0
+    codes = [0, 1, 2, 5, ~0, ~1, ~2, ~5]
+    for cross in (0, 1):
+        for kind in ("ortho", "tri", "nonper"):
+            tri, nonper = int(kind == "tri"), int(kind == "nonper")
+            for same in (0, 1):
+                for slot_j in range(4):
+                    for ii in range(4):
+                        for ci in codes:
+                            for cj in codes:
+                                if nonper and (ci < 0 or cj < 0):
+                                    continue  # no images without periodic boundaries
+                                if (ci if ci >= 0 else ~ci) == (cj if cj >= 0 else ~cj):
+                                    continue
+                                if cross and tri and ci < 0:
+                                    continue  # triclinic cross pairs visit real particle copies only
+                                ref = probe.pair_rule_probe(cross, tri, nonper, same, slot_j, ii, ci, cj,
+                                                            C.byref(parts))
+                                assert parts.value == ref, (cross, kind, same, slot_j, ii, ci, cj)
+                                n += 1
+    assert n > 3000
