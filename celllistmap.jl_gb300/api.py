@@ -328,7 +328,7 @@ class RadialHistogram(Operator):
 
 
 class NeighborList(Operator):
-    """push_pair!: list of (i, j, d) (src/internals/neighborlist.jl:253-262); unordered."""
+    """push_pair!: list of (i, j, d) (src/internals/neighborlist.jl:67-76); unordered."""
     op = "nl"
 
     def __init__(self, index_base: int = 0):
@@ -385,7 +385,7 @@ def _as_positions(x, dim, dtype):
 
 
 def _get_dim(unitcell, x, y=None):
-    """get_dim (src/internals/auxiliary_functions.jl:83-112)."""
+    """get_dim (src/internals/auxiliary_functions.jl:8-37)."""
     ds = [np.asarray(unitcell).shape[0] if unitcell is not None else 0]
     for p in (x, y):
         if p is None:

@@ -281,7 +281,7 @@ __host__ __device__ __forceinline__ T exact_dot_rel(const T* x, const T* c, cons
 
 // The reference's projection filter for a pair seen from cell `from` (center cf) towards cell `to`
 // (center ct): the particle of `to` must satisfy |proj| <= margin and |proj_to - proj_from| <= cutoff
-// (src/internals/vicinal_cells.jl:4-75, auxiliary_functions.jl:166-186).
+// (src/internals/vicinal_cells.jl:4-75, auxiliary_functions.jl:66-111).
 template <class T, int N>
 __host__ __device__ bool projection_pass(const DevGeom<T>& g, const T* cf, const T* ct, const T* x_from,
                                          const T* x_to) {

@@ -1,9 +1,9 @@
 // Cell-pair map on the GPU, host side: operator staging, launches, reductions and results.
 //
 // Replaces _pairwise! and its inner loops:
-//   self  src/internals/self.jl:106-184      cross src/internals/cross.jl:265-313
+//   self  src/internals/self.jl:106-184      cross src/internals/cross.jl:81-129
 //   vicinal cells with projection culling    src/internals/vicinal_cells.jl:4-75,
-//                                            src/internals/auxiliary_functions.jl:166-186
+//                                            src/internals/auxiliary_functions.jl:66-111
 //   non-periodic inner loops                 src/internals/NonPeriodicCells.jl:281-352
 // and the per-batch output copies + reduce_output! with on-chip reductions.
 //
@@ -162,7 +162,7 @@ __global__ void k_forces_out(const FA* __restrict__ facc, int64_t n, DevGeom<T> 
 
 }  // namespace
 
-// Estimated number of pairs assuming uniform density (src/internals/neighborlist.jl:229-241)
+// Estimated number of pairs assuming uniform density (src/internals/neighborlist.jl:43-58)
 static double estimated_pairs(const Handle& h, double vol) {
   const double pi = 3.14159265358979323846;
   double sph = (h.dim == 2 ? pi : 4.0 * pi / 3.0) * std::pow(h.cutoff, h.dim);

@@ -2,9 +2,9 @@
 // that instantiate it.
 //
 // Replaces _pairwise! and its inner loops:
-//   self  src/internals/self.jl:106-184      cross src/internals/cross.jl:265-313
+//   self  src/internals/self.jl:106-184      cross src/internals/cross.jl:81-129
 //   vicinal cells with projection culling    src/internals/vicinal_cells.jl:4-75,
-//                                            src/internals/auxiliary_functions.jl:166-186
+//                                            src/internals/auxiliary_functions.jl:66-111
 //   non-periodic inner loops                 src/internals/NonPeriodicCells.jl:281-352
 // and the per-batch output copies + reduce_output! with on-chip reductions.
 #pragma once

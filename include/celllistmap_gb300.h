@@ -55,7 +55,7 @@ enum clm_cell_kind { CLM_ORTHO = 0, CLM_TRICLINIC = 1, CLM_NONPERIODIC = 2 };
 /* Built-in pair operators.  Each reproduces one closure pattern of the
  * reference (file:line of the pattern in the comments). */
 enum clm_op_id {
-  CLM_OP_NL = 1,             /* push_pair!: (i, j, d), src/internals/neighborlist.jl:253-262 */
+  CLM_OP_NL = 1,             /* push_pair!: (i, j, d), src/internals/neighborlist.jl:67-76 */
   CLM_OP_COUNT = 2,          /* number of pairs, test/modules/Testing.jl:135-141 */
   CLM_OP_SUM_D2 = 3,         /* output += d2, src/API/ParticleSystem.jl:110-118 */
   CLM_OP_SUM_D = 4,          /* output += d, test/modules/Testing.jl:22 */
@@ -153,7 +153,7 @@ int32_t clm_set_precision(clm_handle h, int32_t precision);
 
 /* _pairwise!(op, output, box, cl) — src/internals/self.jl:28-184,
  * src/internals/cross.jl:8-129 — for one built-in operator.  Builds first if a
- * set is dirty (UpdateParticleSystem!, src/internals/ParticleSystem.jl:379-445). */
+ * set is dirty (UpdateParticleSystem!, src/internals/ParticleSystem.jl:129-224). */
 int32_t clm_run(clm_handle h, int32_t op_id, const clm_op_params* params, clm_outputs* out);
 
 /* Neighbour list of the last CLM_OP_NL run: the number of pairs, then the

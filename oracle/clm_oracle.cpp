@@ -17,11 +17,11 @@
 //   self map          src/internals/self.jl:50-63, 106-184
 //   cross map         src/internals/cross.jl:30-129
 //   projection cull   src/internals/vicinal_cells.jl:4-75,
-//                     src/internals/auxiliary_functions.jl:141-186
+//                     src/internals/auxiliary_functions.jl:66-111
 //   naive oracle      test/modules/Testing.jl:62-104 (wrap_relative_to,
 //                     CellOperations.jl:102-127)
 // Operator semantics follow the reference's examples:
-//   neighbour list    src/internals/neighborlist.jl:253-262
+//   neighbour list    src/internals/neighborlist.jl:67-76
 //   forces            test/examples/gravitational_force.jl:37-44
 //   min distance      test/examples/nearest_neighbor.jl:9-16,43
 //   radial histogram  test/examples/pairwise_velocities.jl:17-24
@@ -969,7 +969,7 @@ template <class T, int N> struct Mapper {
     for (int k = 0; k < N; k++) dc[k] = ctr_j[k] - ctr_i[k];
     T dcn = snorm<T, N>(dc);
     for (int k = 0; k < N; k++) dc[k] = dc[k] / dcn;
-    // project_particles! (auxiliary_functions.jl:166-186)
+    // project_particles! (auxiliary_functions.jl:66-111)
     double margin_d;
     T margin_T;
     bool margin_is_T = (B.lcell == 1);

@@ -27,9 +27,10 @@ def test_library_exports_every_declared_symbol(clm):
 
 
 def test_julia_binding_covers_every_declared_symbol():
-    # the reference-side binding (ccall stubs of a Julia package extension) names every entry point
-    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    bound = set(re.findall(r"ccall\(\(:(clm_[a-z_0-9]+)\s*,", doc))
+    # the reference-side binding (the ccall stubs of a CellListMap.jl package extension) names every entry
+    # point of the header
+    src = open(os.path.join(ROOT, "celllistmap.jl_gb300", "julia", "CellListMapGB300Ext.jl")).read()
+    bound = set(re.findall(r"ccall\(\(:(clm_[a-z_0-9]+)\s*,", src))
     assert sorted(bound) == declared_symbols()
 
 

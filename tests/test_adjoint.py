@@ -6,7 +6,8 @@ The reference obtains these gradients by running its map with ForwardDiff dual n
 CPU: the oracle's adjoint against central finite differences of its own energy (rel 1e-6) and against
 a numpy restatement from its neighbour list (rel 1e-12).
 GPU: the CUDA path against the oracle.  Bar: Float64 rel 1e-12, Float32 rel 1e-5, each relative to
-the sum of absolute pair contributions of that quantity (computed from the oracle's neighbour list).
+the sum of absolute pair contributions of that quantity (computed from the oracle's neighbour list); and the
+GPU adjoint against central finite differences of the GPU's own energy (rel 1e-6).
 """
 import numpy as np
 import pytest
@@ -240,3 +241,63 @@ def test_autograd_lj_energy(orc, clm, kind):
             m = p["cls"] == k
             assert abs(et.grad[a, b].item() - f * ref["deps"][k]) <= tol * np.abs(p["u_over_eps"][m]).sum()
             assert abs(st.grad[a, b].item() - f * ref["dsig"][k]) <= tol * np.abs(p["du_dsig"][m]).sum()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cell", ["cubic", "triclinic"])
+def test_gpu_adjoint_finite_differences(clm, cell):
+    """The GPU adjoint against FP64 central differences of the GPU's own LJ energy (the library
+    differentiated, not the oracle): dU/dx = -F at a few particles, dU/dM (cubic: dU/dL = tr W / L), and
+    dU/deps, dU/dsigma per type pair; 2,000-particle Float64 mixture, relative bar 1e-6 (1e-5 for the
+    position derivatives, whose differences cancel more), as in the oracle's own finite-difference test.
+    The reference checks its ForwardDiff gradients the same way (test/examples/generic_types.jl:10-20,102)."""
+    x, L, t, eps, sig = mixture(clm, n=2000, seed=7)
+    M = np.diag([L] * 3) if cell == "cubic" else tri_cell(L)
+    if cell == "triclinic":
+        x = x / L @ M.T
+    uc = np.diag(M) if cell == "cubic" else M
+
+    def energy(xx, MM, e_tab, s_tab):
+        s = clm.ParticleSystem(positions=xx, unitcell=np.diag(MM) if cell == "cubic" else MM, cutoff=CUT,
+                               dtype=np.float64)
+        u = clm.pairwise(clm.LennardJones(c12=C12, c6=C6, types_x=t, eps_table=e_tab, sig_table=s_tab), s)
+        s.close()
+        return u
+
+    s = clm.ParticleSystem(positions=x, unitcell=uc, cutoff=CUT, dtype=np.float64)
+    a = clm.pairwise(clm.LennardJonesAdjoint(c12=C12, c6=C6, types_x=t, eps_table=eps, sig_table=sig), s)
+    s.close()
+    assert abs(a.energy - energy(x, M, eps, sig)) <= 1e-12 * abs(a.energy)
+    h = 1e-6
+    for p in range(2):
+        for q in range(p, 2):
+            for table, got in ((eps, a.dU_deps), (sig, a.dU_dsigma)):
+                tp, tm = table.copy(), table.copy()
+                tp[p, q] += h
+                tp[q, p] = tp[p, q]
+                tm[p, q] -= h
+                tm[q, p] = tm[p, q]
+                if table is eps:
+                    fd = (energy(x, M, tp, sig) - energy(x, M, tm, sig)) / (2 * h)
+                else:
+                    fd = (energy(x, M, eps, tp) - energy(x, M, eps, tm)) / (2 * h)
+                assert abs(got[p, q] - fd) <= 1e-6 * max(1.0, abs(fd)), (p, q, got[p, q], fd)
+    # the cell, positions following it (scaled coordinates fixed)
+    Minv = np.linalg.inv(M)
+    entries = [(0, 0), (1, 1), (2, 2)] if cell == "cubic" else [(0, 0), (0, 1), (1, 2), (2, 2), (0, 2)]
+    for r, c in entries:
+        E = np.zeros((3, 3))
+        E[r, c] = h
+        fd = (energy(x @ ((M + E) @ Minv).T, M + E, eps, sig) - energy(x @ ((M - E) @ Minv).T, M - E, eps, sig)) / (2 * h)
+        assert abs(a.dU_dcell[r, c] - fd) <= 1e-6 * max(1.0, abs(fd)), (r, c, a.dU_dcell[r, c], fd)
+    if cell == "cubic":
+        fd = (energy(x * (L + h) / L, np.diag([L + h] * 3), eps, sig)
+              - energy(x * (L - h) / L, np.diag([L - h] * 3), eps, sig)) / (2 * h)
+        assert abs(np.trace(a.virial) / L - fd) <= 1e-6 * abs(fd)
+    for i in (0, 11, len(x) - 5):
+        for c in range(3):
+            xp, xm = x.copy(), x.copy()
+            xp[i, c] += h
+            xm[i, c] -= h
+            fd = (energy(xp, M, eps, sig) - energy(xm, M, eps, sig)) / (2 * h)
+            assert abs(-a.forces[i, c] - fd) <= 1e-5 * max(1.0, abs(fd)), (i, c, a.forces[i, c], fd)

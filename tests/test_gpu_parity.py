@@ -5,6 +5,14 @@ Bar (stated here):
   * counts and histogram counts: exact;
   * energies: relative 1e-12 (Float64) / 1e-5 (Float32) of the FP64 oracle, relative to sum|u|;
   * forces: max-abs error <= 1e-12 (Float64) / 1e-5 (Float32) times max|F_oracle|.
+Two per-result bars are looser, on purpose:
+  * LJ forces with per-type tables (test_lennard_jones_types): 10x the force bar (1e-11 / 1e-4 times
+    max|F_oracle|).  Each term carries (sigma/d)^12 from the hardware reciprocal estimate (a few ulp, times
+    12 through the power) and the per-particle sums cancel large repulsive and attractive terms, so the
+    error relative to the largest force is about ten times that of the untyped LJ forces;
+  * split-form forces (test_split_form_keeps_sets_exact): 1e-4 times max|F_oracle|.  The split form
+    computes each pair term in FP32 from cell-relative offsets whose distances carry an absolute error of
+    about cell size x 2^-22; its energy keeps the 1e-5 bar.
 """
 import numpy as np
 import pytest

@@ -56,7 +56,7 @@ def test_argon_neighborlists(orc, argon):
 
 
 def test_argon_min_distance(orc, argon):
-    # src/API/parallel_custom.jl:279-289
+    # src/API/parallel_custom.jl:174-192
     r = orc.run("mindist", argon, unitcell=ARGON_SIDES, cutoff=8.0)
     assert r["min"][2] == 2.1991993997816563  # bit-exact with Float64 coordinates
 
