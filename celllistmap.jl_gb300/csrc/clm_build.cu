@@ -49,23 +49,64 @@ constexpr int SCAN_TILE = kBlock * SCAN_IPT;
 constexpr unsigned long long kScanAgg = 1ull << 32, kScanPrefix = 2ull << 32;
 constexpr int kScanSpinLimit = 1 << 20;
 
-__global__ void __launch_bounds__(kBlock) k_scan_1pass(const int* in, int* out, int64_t m, int* __restrict__ total,
-                                                       unsigned long long* __restrict__ status,
-                                                       unsigned* __restrict__ ticket, int64_t ntiles,
-                                                       int* __restrict__ err) {
-  __shared__ int wsum[kBlock / 32];
-  __shared__ int s_tile, s_excl;
-  if (threadIdx.x == 0) s_tile = (int)atomicAdd(ticket, 1u);
-  __syncthreads();
-  const int tile = s_tile;
+// Decoupled look-back of tile `tile` (called by warp 0 of the tile's block): publishes the tile's aggregate,
+// sums the published words of earlier tiles back to the nearest inclusive prefix, publishes the tile's own
+// inclusive prefix and returns its exclusive prefix (in every lane).
+__device__ __forceinline__ int lookback(int tile, int agg, unsigned long long* __restrict__ status,
+                                        int* __restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  int excl = 0;
+  if (tile == 0) {
+    if (lane == 0) atomicExch(&status[0], kScanPrefix | (unsigned)agg);
+    return 0;
+  }
+  if (lane == 0) atomicExch(&status[tile], kScanAgg | (unsigned)agg);
+  // look back over windows of 32 earlier tiles (lane k reads tile top - k; below tile 0 reads as a zero
+  // prefix) until a window holds an inclusive prefix with every nearer tile published
+  int top = tile - 1;
+  int spins = 0;
+  bool gave_up = false;
+  while (true) {
+    const int jj = top - lane;
+    unsigned long long wd = 2ull << 32;  // a zero inclusive prefix below tile 0
+    if (jj >= 0) wd = *(volatile unsigned long long*)&status[jj];
+    const unsigned long long state = wd & ~0xffffffffull;
+    const unsigned pend = __ballot_sync(0xffffffffu, state == 0ull);
+    const unsigned pref = __ballot_sync(0xffffffffu, state == kScanPrefix);
+    const int first = pref ? __ffs(pref) - 1 : 31;  // nearest prefix, or the whole window
+    const unsigned need = (first == 31) ? 0xffffffffu : ((2u << first) - 1u);
+    if (pend & need) {
+      if (++spins > kScanSpinLimit) {
+        gave_up = true;
+        break;
+      }
+      __nanosleep(32);
+      continue;
+    }
+    int val = (lane <= first) ? (int)(unsigned)(wd & 0xffffffffull) : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+    excl += val;
+    if (pref & need) break;
+    top -= 32;
+  }
+  if (lane == 0) {
+    if (gave_up) atomicOr(err, DERR_SCAN);
+    atomicExch(&status[tile], kScanPrefix | (unsigned)(excl + agg));
+  }
+  return excl;
+}
+
+// Exclusive scan of the block's kBlock x IPT values v (thread-major), in place; returns the block aggregate
+// to every thread and leaves in `thread_off` the exclusive prefix of this thread's first value.  wsum holds
+// kBlock / 32 + 1 ints.
+template <int IPT>
+__device__ __forceinline__ int block_scan(int (&v)[IPT], int& thread_off, int* wsum) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t base = (int64_t)tile * SCAN_TILE + (int64_t)threadIdx.x * SCAN_IPT;
-  int v[SCAN_IPT];
   int s = 0;
 #pragma unroll
-  for (int k = 0; k < SCAN_IPT; k++) {
-    int64_t idx = base + k;
-    int t = (idx < m) ? in[idx] : 0;
+  for (int k = 0; k < IPT; k++) {
+    const int t = v[k];
     v[k] = s;
     s += t;
   }
@@ -77,6 +118,7 @@ __global__ void __launch_bounds__(kBlock) k_scan_1pass(const int* in, int* out, 
   }
   if (lane == 31) wsum[warp] = incl;
   __syncthreads();
+  int agg = 0;
   if (warp == 0) {
     int w = (lane < kBlock / 32) ? wsum[lane] : 0;
     int wi = w;
@@ -86,53 +128,42 @@ __global__ void __launch_bounds__(kBlock) k_scan_1pass(const int* in, int* out, 
       if (lane >= o) wi += y;
     }
     if (lane < kBlock / 32) wsum[lane] = wi - w;
-    const int agg = __shfl_sync(0xffffffffu, wi, kBlock / 32 - 1);  // the block aggregate
-    int excl = 0;
-    if (tile == 0) {
-      if (lane == 0) atomicExch(&status[0], kScanPrefix | (unsigned)agg);
-    } else {
-      if (lane == 0) atomicExch(&status[tile], kScanAgg | (unsigned)agg);
-      // look back over windows of 32 earlier tiles (lane k reads tile top - k; below tile 0 reads as a
-      // zero prefix) until a window holds an inclusive prefix with every nearer tile published
-      int top = tile - 1;
-      int spins = 0;
-      bool gave_up = false;
-      while (true) {
-        const int jj = top - lane;
-        unsigned long long wd = 2ull << 32;  // a zero inclusive prefix below tile 0
-        if (jj >= 0) wd = *(volatile unsigned long long*)&status[jj];
-        const unsigned long long state = wd & ~0xffffffffull;
-        const unsigned pend = __ballot_sync(0xffffffffu, state == 0ull);
-        const unsigned pref = __ballot_sync(0xffffffffu, state == kScanPrefix);
-        const int first = pref ? __ffs(pref) - 1 : 31;          // nearest prefix, or the whole window
-        const unsigned need = (first == 31) ? 0xffffffffu : ((2u << first) - 1u);
-        if (pend & need) {
-          if (++spins > kScanSpinLimit) {
-            gave_up = true;
-            break;
-          }
-          __nanosleep(32);
-          continue;
-        }
-        int val = (lane <= first) ? (int)(unsigned)(wd & 0xffffffffull) : 0;
+    const int a = __shfl_sync(0xffffffffu, wi, kBlock / 32 - 1);
+    if (lane == 0) wsum[kBlock / 32] = a;
+  }
+  __syncthreads();
+  agg = wsum[kBlock / 32];
+  thread_off = (incl - s) + wsum[warp];
+  return agg;
+}
+
+__global__ void __launch_bounds__(kBlock) k_scan_1pass(const int* in, int* out, int64_t m, int* __restrict__ total,
+                                                       unsigned long long* __restrict__ status,
+                                                       unsigned* __restrict__ ticket, int64_t ntiles,
+                                                       int* __restrict__ err) {
+  __shared__ int wsum[kBlock / 32 + 1];
+  __shared__ int s_tile, s_excl;
+  if (threadIdx.x == 0) s_tile = (int)atomicAdd(ticket, 1u);
+  __syncthreads();
+  const int tile = s_tile;
+  const int64_t base = (int64_t)tile * SCAN_TILE + (int64_t)threadIdx.x * SCAN_IPT;
+  int v[SCAN_IPT];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
-        excl += val;
-        if (pref & need) break;
-        top -= 32;
-      }
-      if (lane == 0) {
-        if (gave_up) atomicOr(err, DERR_SCAN);
-        atomicExch(&status[tile], kScanPrefix | (unsigned)(excl + agg));
-      }
-    }
-    if (lane == 0) {
+  for (int k = 0; k < SCAN_IPT; k++) {
+    int64_t idx = base + k;
+    v[k] = (idx < m) ? in[idx] : 0;
+  }
+  int off = 0;
+  const int agg = block_scan<SCAN_IPT>(v, off, wsum);
+  if (threadIdx.x < 32) {
+    const int excl = lookback(tile, agg, status, err);
+    if (threadIdx.x == 0) {
       s_excl = excl;
       if (total && tile == ntiles - 1) *total = excl + agg;
     }
   }
   __syncthreads();
-  const int off = (incl - s) + wsum[warp] + s_excl;
+  off += s_excl;
 #pragma unroll
   for (int k = 0; k < SCAN_IPT; k++) {
     int64_t idx = base + k;
@@ -319,6 +350,98 @@ __global__ void __launch_bounds__(kBlock) k_emit_b(const DevGeom<T>* __restrict_
   if (i >= n) return;
   const int s = psys[i];
   emit_at<T, N>(gtab[s], cbase[s], wrapped, mask, ncopy, copy_off, i, cap, keys, vals, err);
+}
+
+// ------------------------------------------------------------------ K1 + scan + K2 in one pass (one system)
+// Each tile of WE_TILE particles wraps its particles and tests their images (wrap_count_at), scans the copy
+// counts in particle order, takes the copy offset of its first particle by decoupled look-back, and writes
+// the key and value of every copy (emit_copies): the same copies at the same positions as K1, the scan and
+// K2 in turn.  The last tile writes the total number of copies.
+constexpr int WE_PPT = 1;
+constexpr int WE_TILE = kBlock * WE_PPT;
+
+template <class T, int N>
+__global__ void __launch_bounds__(kBlock) k_wrap_emit(DevGeom<T> g, const T* __restrict__ x, int n,
+                                                      T* __restrict__ wrapped, uint32_t* __restrict__ mask,
+                                                      int* __restrict__ ncopy, int cap, uint32_t* __restrict__ keys,
+                                                      uint32_t* __restrict__ vals, int* __restrict__ total,
+                                                      unsigned long long* __restrict__ status,
+                                                      unsigned* __restrict__ ticket, int ntiles, int* __restrict__ err) {
+  __shared__ int wsum[kBlock / 32 + 1];
+  __shared__ int s_tile, s_excl;
+  if (threadIdx.x == 0) s_tile = (int)atomicAdd(ticket, 1u);
+  __syncthreads();
+  const int tile = s_tile;
+  const int i0 = tile * WE_TILE + threadIdx.x * WE_PPT;  // this thread's particles i0 .. i0 + WE_PPT - 1
+  int v[WE_PPT];
+#pragma unroll
+  for (int k = 0; k < WE_PPT; k++) {
+    const int i = i0 + k;
+    v[k] = 0;
+    if (i < n) {
+      if (!wrap_count_at<T, N>(g, x, i, wrapped, mask, ncopy)) atomicOr(err, DERR_NAN);
+      v[k] = ncopy[i];
+    }
+  }
+  int cnt[WE_PPT];
+#pragma unroll
+  for (int k = 0; k < WE_PPT; k++) cnt[k] = v[k];
+  int off = 0;
+  const int agg = block_scan<WE_PPT>(v, off, wsum);
+  if (threadIdx.x < 32) {
+    const int excl = lookback(tile, agg, status, err);
+    if (threadIdx.x == 0) {
+      s_excl = excl;
+      if (tile == ntiles - 1) *total = excl + agg;
+    }
+  }
+  __syncthreads();
+  off += s_excl;
+#pragma unroll
+  for (int k = 0; k < WE_PPT; k++) {
+    const int i = i0 + k;
+    if (i < n && cnt[k] > 0) {
+      T p[N];
+#pragma unroll
+      for (int d = 0; d < N; d++) p[d] = wrapped[(int64_t)i * N + d];
+      emit_copies<T, N>(g, 0, p, mask[i], cnt[k], i, v[k] + off, cap, keys, vals, err);
+    }
+  }
+}
+
+// The cells with real particles, in linear order, in one pass: each tile scans its cells' flags, takes its
+// first slot by decoupled look-back, and lists its flagged cells; the last tile writes their number.
+__global__ void __launch_bounds__(kBlock) k_compact_1pass(const int* __restrict__ flags, int ncells,
+                                                          int* __restrict__ list, int* __restrict__ total,
+                                                          unsigned long long* __restrict__ status,
+                                                          unsigned* __restrict__ ticket, int ntiles,
+                                                          int* __restrict__ err) {
+  __shared__ int wsum[kBlock / 32 + 1];
+  __shared__ int s_tile, s_excl;
+  if (threadIdx.x == 0) s_tile = (int)atomicAdd(ticket, 1u);
+  __syncthreads();
+  const int tile = s_tile;
+  const int c0 = tile * SCAN_TILE + threadIdx.x * SCAN_IPT;
+  int v[SCAN_IPT], f[SCAN_IPT];
+#pragma unroll
+  for (int k = 0; k < SCAN_IPT; k++) {
+    f[k] = (c0 + k < ncells && flags[c0 + k]) ? 1 : 0;
+    v[k] = f[k];
+  }
+  int off = 0;
+  const int agg = block_scan<SCAN_IPT>(v, off, wsum);
+  if (threadIdx.x < 32) {
+    const int excl = lookback(tile, agg, status, err);
+    if (threadIdx.x == 0) {
+      s_excl = excl;
+      if (tile == ntiles - 1) *total = excl + agg;
+    }
+  }
+  __syncthreads();
+  off += s_excl;
+#pragma unroll
+  for (int k = 0; k < SCAN_IPT; k++)
+    if (f[k]) list[v[k] + off] = c0 + k;
 }
 
 // ------------------------------------------------------------------ K4: gather in cell order
@@ -583,6 +706,8 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
   const DevGeom<T>* gtab = h.batch.gtab.as<DevGeom<T>>();
   const int* psys = h.batch.psys.as<int>();
   const int* cbase = h.batch.cbase_d.as<int>();
+  int* n_dev = S.copy_off.as<int>() + n;  // total number of copies, on the device
+  int st = OK;
   if (batch) {
     if (N == 3)
       k_wrap_count_b<T, 3><<<gn, kBlock, 0, h.stream>>>(gtab, psys, S.x.as<T>(), (int)n, S.wrapped.as<T>(),
@@ -590,18 +715,10 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
     else
       k_wrap_count_b<T, 2><<<gn, kBlock, 0, h.stream>>>(gtab, psys, S.x.as<T>(), (int)n, S.wrapped.as<T>(),
                                                        S.mask.as<uint32_t>(), S.ncopy.as<int>(), h.batch.sys_err.as<int>());
-  } else if (N == 3)
-    k_wrap_count<T, 3><<<gn, kBlock, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
-                                                   S.ncopy.as<int>(), err);
-  else
-    k_wrap_count<T, 2><<<gn, kBlock, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
-                                                   S.ncopy.as<int>(), err);
-  CLM_CUDA_TRY(h, cudaGetLastError());
-  h.launches++;
-  int* n_dev = S.copy_off.as<int>() + n;  // total number of copies, on the device
-  int st = scan_exclusive(h, S.ncopy.as<int>(), S.copy_off.as<int>(), n, n_dev);
-  if (st) return st;
-  if (batch) {
+    CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+    st = scan_exclusive(h, S.ncopy.as<int>(), S.copy_off.as<int>(), n, n_dev);
+    if (st) return st;
     if (N == 3)
       k_emit_b<T, 3><<<gn, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
                                                  S.ncopy.as<int>(), S.copy_off.as<int>(), (int)n, (int)cap,
@@ -612,16 +729,29 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
                                                  S.ncopy.as<int>(), S.copy_off.as<int>(), (int)n, (int)cap,
                                                  S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
                                                  err);
-  } else if (N == 3)
-    k_emit<T, 3><<<gn, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(),
-                                             S.copy_off.as<int>(), (int)n, (int)cap, S.keys[0].as<uint32_t>(),
-                                             S.vals[0].as<uint32_t>(), err);
-  else
-    k_emit<T, 2><<<gn, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(),
-                                             S.copy_off.as<int>(), (int)n, (int)cap, S.keys[0].as<uint32_t>(),
-                                             S.vals[0].as<uint32_t>(), err);
-  CLM_CUDA_TRY(h, cudaGetLastError());
-  h.launches++;
+    CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+  } else {
+    // wrap, images, copy offsets and keys in one launch (tile status words and ticket zeroed first)
+    const int we_tiles = (int)((n + WE_TILE - 1) / WE_TILE);
+    DevBuf& sb = h.scan.level[0];
+    if (!sb.reserve((size_t)(we_tiles + 2) * sizeof(unsigned long long))) return ERR_NOMEM;
+    unsigned long long* status = sb.as<unsigned long long>();
+    CLM_CUDA_TRY(h, cudaMemsetAsync(status, 0, (size_t)(we_tiles + 1) * sizeof(unsigned long long), h.stream));
+    unsigned* ticket = reinterpret_cast<unsigned*>(status + we_tiles);
+    if (N == 3)
+      k_wrap_emit<T, 3><<<we_tiles, kBlock, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(),
+                                                          S.mask.as<uint32_t>(), S.ncopy.as<int>(), (int)cap,
+                                                          S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev,
+                                                          status, ticket, we_tiles, err);
+    else
+      k_wrap_emit<T, 2><<<we_tiles, kBlock, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(),
+                                                          S.mask.as<uint32_t>(), S.ncopy.as<int>(), (int)cap,
+                                                          S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev,
+                                                          status, ticket, we_tiles, err);
+    CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+  }
   // stable LSD radix sort by cell: the fewest passes of at most 10-bit digits, digits as small as that allows
   int bits = 1;
   while (((int64_t)1 << bits) < ncells) bits++;
@@ -671,10 +801,22 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
   // cells with real particles, in linear order; their number stays on the device (real_scan[ncells])
-  st = scan_exclusive(h, S.cell_flags.as<int>(), S.real_scan.as<int>(), ncells, S.real_scan.as<int>() + ncells);
-  if (st) return st;
-  k_compact<<<grid_for(ncells), kBlock, 0, h.stream>>>(S.cell_flags.as<int>(), S.real_scan.as<int>(), (int)ncells,
-                                                       S.real_list.as<int>());
+  if (batch) {
+    // batches also read the per-cell scan (the items of each system)
+    st = scan_exclusive(h, S.cell_flags.as<int>(), S.real_scan.as<int>(), ncells, S.real_scan.as<int>() + ncells);
+    if (st) return st;
+    k_compact<<<grid_for(ncells), kBlock, 0, h.stream>>>(S.cell_flags.as<int>(), S.real_scan.as<int>(), (int)ncells,
+                                                         S.real_list.as<int>());
+  } else {
+    const int ct = (int)((ncells + SCAN_TILE - 1) / SCAN_TILE);
+    DevBuf& sb = h.scan.level[0];
+    if (!sb.reserve((size_t)(ct + 2) * sizeof(unsigned long long))) return ERR_NOMEM;
+    unsigned long long* status = sb.as<unsigned long long>();
+    CLM_CUDA_TRY(h, cudaMemsetAsync(status, 0, (size_t)(ct + 1) * sizeof(unsigned long long), h.stream));
+    k_compact_1pass<<<ct, kBlock, 0, h.stream>>>(S.cell_flags.as<int>(), (int)ncells, S.real_list.as<int>(),
+                                                 S.real_scan.as<int>() + ncells, status,
+                                                 reinterpret_cast<unsigned*>(status + ct), ct, err);
+  }
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
   return OK;

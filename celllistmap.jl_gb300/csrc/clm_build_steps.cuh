@@ -186,22 +186,20 @@ __host__ __device__ __forceinline__ bool wrap_count_at(const DevGeom<T>& g, cons
   return true;
 }
 
-// ------------------------------------------------------------------ K2: keys, histogram, real flags
-// `cb` is the first global cell of the particle's system (0 for one system).
+// ------------------------------------------------------------------ K2: keys of every copy
+// The copies of particle i (wrapped position p, image mask m, ncp copies) at copy positions base .. base+ncp-1:
+// the key is the copy's cell (the real copy first, with the border-case shift, then the images in
+// increasing image code), the value (i << 5) | image code.  `cb` is the first global cell of the particle's
+// system (0 for one system).
 template <class T, int N>
-__host__ __device__ __forceinline__ void emit_at(const DevGeom<T>& g, int cb, const T* __restrict__ wrapped,
-                                        const uint32_t* __restrict__ mask, const int* __restrict__ ncopy,
-                                        const int* __restrict__ copy_off, int i, int cap, uint32_t* __restrict__ keys,
-                                        uint32_t* __restrict__ vals, int* __restrict__ err) {
-  if (ncopy[i] == 0) return;
-  int base = copy_off[i];
-  if (base < 0 || base + ncopy[i] > cap) {
+__host__ __device__ __forceinline__ void emit_copies(const DevGeom<T>& g, int cb, const T* p, uint32_t m, int ncp,
+                                                     int i, int base, int cap, uint32_t* __restrict__ keys,
+                                                     uint32_t* __restrict__ vals, int* __restrict__ err) {
+  if (ncp == 0) return;
+  if (base < 0 || base + ncp > cap) {
     flag_error(err, DERR_COPY_OVERFLOW);
     return;
   }
-  T p[N];
-#pragma unroll
-  for (int k = 0; k < N; k++) p[k] = wrapped[(int64_t)i * N + k];
   int li = cell_of<T, N>(g, p, true);
   if (li < 0) {
     flag_error(err, DERR_CELL_RANGE);
@@ -211,7 +209,6 @@ __host__ __device__ __forceinline__ void emit_at(const DevGeom<T>& g, int cb, co
   keys[base] = (uint32_t)li;
   vals[base] = ((uint32_t)i << 5) | (uint32_t)g.zero_code;
   int t = 1;
-  uint32_t m = mask[i];
   while (m) {
     int k = lowest_bit(m);
     m &= m - 1;
@@ -228,6 +225,19 @@ __host__ __device__ __forceinline__ void emit_at(const DevGeom<T>& g, int cb, co
     vals[base + t] = ((uint32_t)i << 5) | (uint32_t)k;
     t++;
   }
+}
+
+// The same from the arrays the wrap step wrote and the scanned copy offsets.
+template <class T, int N>
+__host__ __device__ __forceinline__ void emit_at(const DevGeom<T>& g, int cb, const T* __restrict__ wrapped,
+                                        const uint32_t* __restrict__ mask, const int* __restrict__ ncopy,
+                                        const int* __restrict__ copy_off, int i, int cap, uint32_t* __restrict__ keys,
+                                        uint32_t* __restrict__ vals, int* __restrict__ err) {
+  if (ncopy[i] == 0) return;
+  T p[N];
+#pragma unroll
+  for (int k = 0; k < N; k++) p[k] = wrapped[(int64_t)i * N + k];
+  emit_copies<T, N>(g, cb, p, mask[i], ncopy[i], i, copy_off[i], cap, keys, vals, err);
 }
 
 // ------------------------------------------------------------------ K4: gather in cell order
