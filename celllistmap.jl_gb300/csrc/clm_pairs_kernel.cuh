@@ -251,10 +251,13 @@ __device__ __forceinline__ void force_add(const PairArgs<T>& A, bool ys, int idx
 // half cell), so skipping it elsewhere leaves the pair set unchanged.
 // Resident blocks per SM (6 for Float32, 3 for Float64: at most 85 / 170 registers per thread; the
 // kernels use 64-80 / 113-152) were picked by timing 4..8 and 3..4 on GB300; fewer registers spill in the
-// pair epilogues.
+// pair epilogues.  The split-form histogram of Float64 handles runs 5 blocks (at most 102 registers, small
+// spills): timed at 3..6 blocks on the two-set workload, 5 gave 1.37x (3D) and 1.2x (2D) over 3; the exact
+// histogram keeps 3 (its FP64 pipe is the bound at any of these).
 // OPC: the operator id when fixed at compile time (the LJ force loop), 0 = read from the arguments.
 template <class T, int N, int OPK, bool SPLIT, bool CROSS, bool BATCH, int OPC = 0>
-__global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(const PairArgs<T> A) {
+__global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : ((OPK == OPK_HIST && SPLIT) ? 5 : 3))
+    k_pairs(const PairArgs<T> A) {
   using V = T;
   using FA = typename std::conditional<std::is_same<T, double>::value && !SPLIT, double, float>::type;
   constexpr bool IS_F = (OPK == OPK_FORCES) || (OPK == OPK_ADJ);
@@ -822,8 +825,21 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
                   bool exact_r = !sure;
                   T r = 0;
                   float rfl = 0.f;  // the distance in FP32 for the FP32 pair value (no FP64 conversions)
+                  double rinv = 0.0;  // exact form of Float64 handles: 1/r of the accumulator term
                   int b = -1;
-                  if (sure) {
+                  if constexpr (std::is_same<FA, double>::value) {
+                    // exact form (the d2 of the exact re-test): the bin from the FP32 distance, decided again
+                    // from the IEEE distance when an edge lies within 2^-12 of it (as in the split form; the
+                    // FP32 distance of the exact d2 is within 2^-23 of the IEEE one); the term's 1/r from the
+                    // FP64 rsqrt estimate refined by two Newton steps, to FP64 rounding, without an IEEE sqrt
+                    // and divide per pair
+                    const float rf = sqrtf((float)d2);
+                    const int lo = first_edge_at_or_above(s_binf, A.nbins, rf);
+                    b = lo - 1;
+                    if (near_edge(s_binf, A.nbins, lo, rf)) b = first_edge_at_or_above(s_bins, A.nbins, xsqrt(d2)) - 1;
+                    rinv = vrsqrt((double)d2);
+                    exact_r = false;
+                  } else if (sure) {
                     float rf = sqrtf(d2f);
                     const int lo = first_edge_at_or_above(s_binf, A.nbins, rf);
                     b = lo - 1;
@@ -883,7 +899,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : 3) k_pairs(co
 #pragma unroll
                       for (int d = 0; d < N; d++)
                         dot += ((FA)A.vx[(int64_t)idx_i * N + d] - (FA)vy[(int64_t)idx_j * N + d]) * dv[d];
-                      hv = dot / (FA)r;
+                      hv = dot * (FA)rinv;
                     }
                     hb = b;
                   }
