@@ -577,17 +577,27 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : ((OPK == OPK_
             __syncwarp();
             const int per = (H + 31) >> 5;
             const int qbeg = lane * per;
+            // Where the FP32 value decides the pairs well inside the cutoff (Float32 inputs, the split form),
+            // the first sweep of the queue only marks the others (a band of 2^-13 around the cutoff, for the
+            // exact re-test and the projection filter), and a second sweep over the same runs, made only when
+            // a lane marked one, evaluates them: the main loop carries no exact path.
+            constexpr bool DEFER = !FP64 || SPLIT;
+            bool marked = false;
+            auto sweep = [&](auto rare_c) {
+            constexpr bool RARE = decltype(rare_c)::value;
             int cur = -1;  // the particle slot of this lane's run (its data below, its force sums in acc)
             float4 xi4 = make_float4(0.f, 0.f, 0.f, 0.f);
             FA acc[3] = {0, 0, 0};
             for (int t = 0; t < per; t++) {
               const int q = qbeg + t;
               const bool has = q < H;
+              bool live = has;  // the entry is evaluated in this sweep
               int j = 0, ie = (cur < 0) ? 0 : cur;
               if (has) {
                 const int ent = s_q[warp][q];
-                ie = ent >> 8;
+                ie = (ent >> 8) & 31;
                 j = ent & 255;
+                if constexpr (RARE) live = (ent & 0x8000) != 0;
               }
               // `cur` follows every queue entry (hit or not), so the lanes holding a particle are exactly the
               // lanes whose runs cover its entries: adjacent, and only the last one moves past it inside its
@@ -635,7 +645,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : ((OPK == OPK_
                   for (int d = 0; d < N; d++) xj[d] = pos_of(A.Y, d, tjj);
                 }
               };
-              if (has) {
+              if (live) {
                 const float4 p = s_pf[bsel][warp][j];
                 const int code_j = __float_as_int(p.w);
                 idx_j = code_j >= 0 ? code_j : ~code_j;
@@ -656,14 +666,18 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : ((OPK == OPK_
                     xj[1] = (T)p.y;
                     if (N == 3) xj[N - 1] = (T)p.z;
                   }
-                  if (!FP64 || SPLIT) {
-                    // FP32 input or split form: well inside the cutoff the FP32 value decides
+                  if (DEFER && !RARE) {
+                    // FP32 input or split form: well inside the cutoff the FP32 value decides; the others are
+                    // marked for the second sweep
                     if (d2f <= g.thr_lo) {
                       hit = true;
                       sure = true;
+                    } else {
+                      s_q[warp][q] = (unsigned short)(s_q[warp][q] | 0x8000u);
+                      marked = true;
                     }
                   }
-                  if (!sure) {
+                  if constexpr (!DEFER || RARE) {
                     load_xi();
                     int meta = 0;
                     if constexpr (!ABS_PF) {
@@ -936,6 +950,12 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : ((OPK == OPK_
 #pragma unroll
                 for (int d = 0; d < N; d++) s_if[warp][d][cur] += acc[d];
               }
+            }
+            };
+            sweep(std::false_type());
+            if (DEFER && __any_sync(FULL, marked)) {
+              __syncwarp();
+              sweep(std::true_type());
             }
             if constexpr (OPK == OPK_HIST) {
               // move the warp's bins (at most 1024 pairs of this round) into the block's FP64 bins
