@@ -2,20 +2,23 @@
 //
 // Replaces UpdateCellList! (src/internals/CellLists.jl:727-927, serial order
 // of add_particles! 940-950 and add_particle_to_celllist! 983-1057) and the
-// non-periodic build (src/internals/NonPeriodicCells.jl:93-251):
+// non-periodic build (src/internals/NonPeriodicCells.jl:93-251).
 //
-//   K1 k_wrap_count  wrap into the first cell (wrap_to_first, CellOperations.jl:91-94),
-//                    rotate, test the 3^N-1 translation images against the computing
-//                    box (replicate_particle!, Box.jl:556-566) -> copies per particle
-//   scan             exclusive prefix sum of copies per particle
-//   K2 k_emit        one (cell, particle<<5|image) key/value per copy, cell histogram,
-//                    real-cell flags (particle_cell + real_particle_border_case)
-//   K3 radix sort    stable LSD radix sort of the keys by cell: inside a cell the
-//                    copies keep particle-index order, which is the reference's serial
-//                    order (a particle has at most one copy per cell)
-//   K4 k_gather      coordinates of each copy in cell order (SoA), particle codes,
-//                    FP32 cell-relative offsets for the pair prefilter
-//   compaction       list of cells that contain real particles, in linear order
+// One system (counting build, four launches after one memset):
+//   k_wrap_emit     wrap into the first cell (wrap_to_first, CellOperations.jl:91-94),
+//                   rotate, test the 3^N-1 translation images against the computing
+//                   box (replicate_particle!, Box.jl:556-566), scan the copies per
+//                   particle (decoupled look-back), write one (cell, particle<<5|image)
+//                   key/value per copy (particle_cell + real_particle_border_case), and
+//                   take each copy's arrival slot in its cell with an atomic counter
+//   k_cell_scan     cell starts and the list of cells that contain real particles
+//   k_cell_scatter  copies to their cells' slots in arrival order
+//   k_rank_gather   each copy to its rank by value inside its cell (particle-index
+//                   order, the reference's serial order), with its coordinates (SoA),
+//                   particle code and 16-byte candidate record
+// Batches (global cell index over all systems): K1 k_wrap_count_b, a scan of the
+// copies, K2 k_emit_b, a stable LSD radix sort of the keys by cell, K4 k_gather_b,
+// and the real-cell scan and compaction.
 //
 // Every kernel bounds-checks its indices; inconsistencies set bits of the
 // handle's device error word instead of faulting.
@@ -49,7 +52,7 @@ constexpr int SCAN_TILE = kBlock * SCAN_IPT;
 constexpr unsigned long long kScanAgg = 1ull << 32, kScanPrefix = 2ull << 32;
 constexpr int kScanSpinLimit = 1 << 20;
 
-// Decoupled look-back of tile `tile` (called by warp 0 of the tile's block): publishes the tile's aggregate,
+// Decoupled look-back of tile `tile` (called by one whole warp of the tile's block): publishes the tile's aggregate,
 // sums the published words of earlier tiles back to the nearest inclusive prefix, publishes the tile's own
 // inclusive prefix and returns its exclusive prefix (in every lane).
 __device__ __forceinline__ int lookback(int tile, int agg, unsigned long long* __restrict__ status,
@@ -355,8 +358,10 @@ __global__ void __launch_bounds__(kBlock) k_emit_b(const DevGeom<T>* __restrict_
 // ------------------------------------------------------------------ K1 + scan + K2 in one pass (one system)
 // Each tile of WE_TILE particles wraps its particles and tests their images (wrap_count_at), scans the copy
 // counts in particle order, takes the copy offset of its first particle by decoupled look-back, and writes
-// the key and value of every copy (emit_copies): the same copies at the same positions as K1, the scan and
-// K2 in turn.  The last tile writes the total number of copies.
+// the key and value of every copy (the cells of copy_cell, in emit_copies' order): the same copies at the
+// same positions as K1, the scan and K2 in turn.  The last tile writes the total number of copies.  Every
+// copy also takes the next slot of its cell's counter (its arrival rank, in `ranks`), and the real copy
+// marks its cell: cell_cf holds {copies, holds a real particle} per cell, zeroed before the launch.
 constexpr int WE_PPT = 1;
 constexpr int WE_TILE = kBlock * WE_PPT;
 
@@ -366,7 +371,9 @@ __global__ void __launch_bounds__(kBlock) k_wrap_emit(DevGeom<T> g, const T* __r
                                                       int* __restrict__ ncopy, int cap, uint32_t* __restrict__ keys,
                                                       uint32_t* __restrict__ vals, int* __restrict__ total,
                                                       unsigned long long* __restrict__ status,
-                                                      unsigned* __restrict__ ticket, int ntiles, int* __restrict__ err) {
+                                                      unsigned* __restrict__ ticket, int ntiles,
+                                                      int* __restrict__ cell_cf, uint32_t* __restrict__ ranks,
+                                                      int* __restrict__ err) {
   __shared__ int wsum[kBlock / 32 + 1];
   __shared__ int s_tile, s_excl;
   if (threadIdx.x == 0) s_tile = (int)atomicAdd(ticket, 1u);
@@ -397,80 +404,167 @@ __global__ void __launch_bounds__(kBlock) k_wrap_emit(DevGeom<T> g, const T* __r
   }
   __syncthreads();
   off += s_excl;
+  // the copies of the particle (the real copy, then the images in increasing image code), walked by the
+  // lanes of a warp together: in each round the lanes whose copies fall in the same cell take consecutive
+  // slots of that cell's counter with one atomic (match_any groups them)
+  static_assert(WE_PPT == 1, "one particle per thread");
+  const int i = i0;
+  const int base = v[0] + off;
+  int nc = (i < n) ? cnt[0] : 0;
+  if (nc > 0 && (base < 0 || base + nc > cap)) {
+    atomicOr(err, DERR_COPY_OVERFLOW);  // the build is repeated with the exact size
+    nc = 0;
+  }
+  T p[N];
+  uint32_t m = 0u;
+  if (nc > 0) {
 #pragma unroll
-  for (int k = 0; k < WE_PPT; k++) {
-    const int i = i0 + k;
-    if (i < n && cnt[k] > 0) {
-      T p[N];
-#pragma unroll
-      for (int d = 0; d < N; d++) p[d] = wrapped[(int64_t)i * N + d];
-      emit_copies<T, N>(g, 0, p, mask[i], cnt[k], i, v[k] + off, cap, keys, vals, err);
+    for (int d = 0; d < N; d++) p[d] = wrapped[(int64_t)i * N + d];
+    m = mask[i];
+  }
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const int rounds = __reduce_max_sync(0xffffffffu, nc);
+  for (int c = 0; c < rounds; c++) {
+    uint32_t key = 0xffffffffu;  // no copy in this round
+    if (c < nc) {
+      int k = g.zero_code;
+      if (c > 0) {
+        k = lowest_bit(m);
+        m &= m - 1u;
+      }
+      key = (uint32_t)copy_cell<T, N>(g, p, k, err);
+      keys[base + c] = key;
+      vals[base + c] = ((uint32_t)i << 5) | (uint32_t)k;
+      if (c == 0) cell_cf[2 * key + 1] = 1;  // the cell holds a real particle
     }
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(peers) - 1;
+    int first = 0;
+    if (lane == leader && key != 0xffffffffu) first = atomicAdd(&cell_cf[2 * key], __popc(peers));
+    first = __shfl_sync(0xffffffffu, first, leader);
+    if (key != 0xffffffffu) ranks[base + c] = (uint32_t)(first + __popc(peers & lt));
   }
 }
 
-// The cells with real particles, in linear order, in one pass: each tile scans its cells' flags, takes its
-// first slot by decoupled look-back, and lists its flagged cells; the last tile writes their number.
-__global__ void __launch_bounds__(kBlock) k_compact_1pass(const int* __restrict__ flags, int ncells,
-                                                          int* __restrict__ list, int* __restrict__ total,
-                                                          unsigned long long* __restrict__ status,
-                                                          unsigned* __restrict__ ticket, int ntiles,
-                                                          int* __restrict__ err) {
-  __shared__ int wsum[kBlock / 32 + 1];
-  __shared__ int s_tile, s_excl;
+// Cell starts and the list of cells with real particles, in one pass over cell_cf: each tile scans its
+// cells' copy counts and real flags, takes both prefixes by decoupled look-back (warp 0 the counts, warp 1
+// the flags; one ticket orders the tiles of both), and writes cell_start, the real flags the pair kernel
+// reads, and the real cells in linear order.  The last tile closes cell_start and writes the number of
+// real cells.
+__global__ void __launch_bounds__(kBlock) k_cell_scan(const int* __restrict__ cell_cf, int ncells,
+                                                      int* __restrict__ cell_start, int* __restrict__ cell_flags,
+                                                      int* __restrict__ real_list, int* __restrict__ n_real,
+                                                      unsigned long long* __restrict__ status_c,
+                                                      unsigned long long* __restrict__ status_f,
+                                                      unsigned* __restrict__ ticket, int ntiles,
+                                                      int* __restrict__ err) {
+  __shared__ int wsum_c[kBlock / 32 + 1], wsum_f[kBlock / 32 + 1];
+  __shared__ int s_tile, s_excl_c, s_excl_f;
   if (threadIdx.x == 0) s_tile = (int)atomicAdd(ticket, 1u);
   __syncthreads();
   const int tile = s_tile;
   const int c0 = tile * SCAN_TILE + threadIdx.x * SCAN_IPT;
-  int v[SCAN_IPT], f[SCAN_IPT];
+  int vc[SCAN_IPT], vf[SCAN_IPT], f[SCAN_IPT];
 #pragma unroll
   for (int k = 0; k < SCAN_IPT; k++) {
-    f[k] = (c0 + k < ncells && flags[c0 + k]) ? 1 : 0;
-    v[k] = f[k];
+    int2 cf = make_int2(0, 0);
+    if (c0 + k < ncells) cf = reinterpret_cast<const int2*>(cell_cf)[c0 + k];
+    vc[k] = cf.x;
+    f[k] = cf.y != 0;
+    vf[k] = f[k];
   }
-  int off = 0;
-  const int agg = block_scan<SCAN_IPT>(v, off, wsum);
-  if (threadIdx.x < 32) {
-    const int excl = lookback(tile, agg, status, err);
+  int off_c = 0, off_f = 0;
+  const int agg_c = block_scan<SCAN_IPT>(vc, off_c, wsum_c);
+  const int agg_f = block_scan<SCAN_IPT>(vf, off_f, wsum_f);
+  const int warp = threadIdx.x >> 5;
+  if (warp == 0) {
+    const int excl = lookback(tile, agg_c, status_c, err);
     if (threadIdx.x == 0) {
-      s_excl = excl;
-      if (tile == ntiles - 1) *total = excl + agg;
+      s_excl_c = excl;
+      if (tile == ntiles - 1) cell_start[ncells] = excl + agg_c;
+    }
+  } else if (warp == 1) {
+    const int excl = lookback(tile, agg_f, status_f, err);
+    if ((threadIdx.x & 31) == 0) {
+      s_excl_f = excl;
+      if (tile == ntiles - 1) *n_real = excl + agg_f;
     }
   }
   __syncthreads();
-  off += s_excl;
+  off_c += s_excl_c;
+  off_f += s_excl_f;
 #pragma unroll
-  for (int k = 0; k < SCAN_IPT; k++)
-    if (f[k]) list[v[k] + off] = c0 + k;
+  for (int k = 0; k < SCAN_IPT; k++) {
+    const int c = c0 + k;
+    if (c < ncells) {
+      cell_start[c] = vc[k] + off_c;
+      cell_flags[c] = f[k];
+      if (f[k]) real_list[vf[k] + off_f] = c;
+    }
+  }
+}
+
+// Every copy (particle order) to its cell's slots, at its arrival rank: sorted keys and values grouped by
+// cell, each cell's values still in arrival order.
+__global__ void __launch_bounds__(kBlock) k_cell_scatter(const uint32_t* __restrict__ keys,
+                                                         const uint32_t* __restrict__ vals,
+                                                         const uint32_t* __restrict__ ranks,
+                                                         const int* __restrict__ n_dev, int cap, int ncells,
+                                                         const int* __restrict__ cell_start,
+                                                         uint32_t* __restrict__ skeys, uint32_t* __restrict__ svals,
+                                                         int* __restrict__ err) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = min(*n_dev, cap);
+  if (t >= n) return;
+  const uint32_t li = keys[t];
+  if (li >= (uint32_t)ncells) {
+    atomicOr(err, DERR_CELL_RANGE);
+    return;
+  }
+  const int pos = cell_start[li] + (int)ranks[t];
+  if (pos < 0 || pos >= n || pos >= cell_start[li + 1]) {
+    atomicOr(err, DERR_CELL_RANGE);
+    return;
+  }
+  skeys[pos] = li;
+  svals[pos] = vals[t];
+}
+
+// K4 after the counting placement: slot q of the placed list holds a copy of cell li in arrival order; the
+// copy's final slot is the cell's start plus its rank by value in the cell (rank_in_cell), which puts
+// every cell in particle-index order.  The copy's coordinates, code and 16-byte record are written there.
+template <class T, int N>
+__global__ void __launch_bounds__(kBlock) k_rank_gather(DevGeom<T> g, const T* __restrict__ wrapped,
+                                                        const uint32_t* __restrict__ skeys,
+                                                        const uint32_t* __restrict__ svals,
+                                                        const int* __restrict__ cell_start, int ncells, int cap, int n,
+                                                        T* __restrict__ px, T* __restrict__ py, T* __restrict__ pz,
+                                                        float4* __restrict__ off, float4* __restrict__ xq,
+                                                        int* __restrict__ code, int* __restrict__ cell_flags,
+                                                        int* __restrict__ err) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tot = min(cell_start[ncells], cap);
+  if (q >= tot) return;
+  const uint32_t li = skeys[q];
+  const uint32_t v = svals[q];
+  if (li >= (uint32_t)ncells) {
+    atomicOr(err, DERR_CELL_RANGE);
+    return;
+  }
+  const int s = cell_start[li];
+  const int e = min(cell_start[li + 1], tot);
+  const int t = s + rank_in_cell(svals, s, e, v);
+  int p = (int)(v >> 5);
+  int k = (int)(v & 31u);
+  if (t < s || t >= e || p >= n || k >= g.nimg) {
+    atomicOr(err, DERR_CELL_RANGE);
+    return;
+  }
+  gather_at<T, N>(g, wrapped, t, p, k, (int)li, px, py, pz, off, xq, code, cell_flags, 0);
 }
 
 // ------------------------------------------------------------------ K4: gather in cell order
-template <class T, int N>
-__global__ void __launch_bounds__(kBlock) k_gather(DevGeom<T> g, const T* __restrict__ wrapped,
-                                                   const uint32_t* __restrict__ skeys,
-                                                   const uint32_t* __restrict__ svals, const int* __restrict__ n_dev,
-                                                   int cap, int n, T* __restrict__ px, T* __restrict__ py,
-                                                   T* __restrict__ pz, float4* __restrict__ off, float4* __restrict__ xq,
-                                                   int* __restrict__ code, int* __restrict__ cell_flags,
-                                                   int ncells, int* __restrict__ cell_start, int* __restrict__ err) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nc = min(*n_dev, cap);
-  if (t > nc) return;
-  cell_starts_at(skeys, t, nc, ncells, cell_start);
-  if (t == nc) return;
-  uint32_t v = svals[t];
-  int p = (int)(v >> 5);
-  int k = (int)(v & 31u);
-  int li = (int)skeys[t];
-  if (p >= n || k >= g.nimg || li < 0 || li >= g.ncells) {
-    atomicOr(err, DERR_CELL_RANGE);
-    p = 0;
-    k = g.zero_code;
-    li = 0;
-  }
-  gather_at<T, N>(g, wrapped, t, p, k, li, px, py, pz, off, xq, code, cell_flags, 0);
-}
-
 template <class T, int N>
 __global__ void __launch_bounds__(kBlock) k_gather_b(const DevGeom<T>* __restrict__ gtab, const int* __restrict__ psys,
                                                      const int* __restrict__ cbase, const T* __restrict__ wrapped,
@@ -643,6 +737,74 @@ template <class T> int64_t copy_capacity(const SetData& S, const Geometry<T>& g)
   return std::max<int64_t>(std::max<int64_t>(S.copy_cap, (int64_t)est), n + 64);
 }
 
+// One system: the counting build.  One zeroed region holds the look-back words of the two single-pass
+// scans and the per-cell {copies, real} counters; then four launches: wrap + copy offsets + keys + arrival
+// ranks (k_wrap_emit), cell starts + real-cell list (k_cell_scan), placement by arrival (k_cell_scatter),
+// and the gather at each copy's rank in its cell (k_rank_gather).
+template <class T>
+int build_counting(Handle& h, SetData& S, const DevGeom<T>& dg, int N, int64_t n, int64_t ncells, int64_t cap) {
+  int* err = h.err.as<int>();
+  const int64_t we_tiles = (n + WE_TILE - 1) / WE_TILE;
+  const int64_t ct = (ncells + SCAN_TILE - 1) / SCAN_TILE;
+  // 64-bit words: wrap-emit status + ticket, cell-scan count status + ticket, cell-scan flag status, then
+  // the per-cell counters (two ints per cell)
+  const int64_t w_we = we_tiles + 1, w_c = ct + 1, w_f = ct;
+  const size_t zero_bytes = sizeof(unsigned long long) * (size_t)(w_we + w_c + w_f + ncells + 1);
+  if (!S.cell_count.reserve(zero_bytes) || !S.wrapped.reserve(sizeof(T) * N * n) ||
+      !S.mask.reserve(sizeof(uint32_t) * n) || !S.ncopy.reserve(sizeof(int) * (n + 1)) ||
+      !S.keys[0].reserve(sizeof(uint32_t) * cap) || !S.keys[1].reserve(sizeof(uint32_t) * cap) ||
+      !S.vals[0].reserve(sizeof(uint32_t) * cap) || !S.vals[1].reserve(sizeof(uint32_t) * cap) ||
+      !S.rank.reserve(sizeof(uint32_t) * cap) || !S.px.reserve(sizeof(T) * cap) || !S.py.reserve(sizeof(T) * cap) ||
+      !S.pz.reserve(sizeof(T) * cap) || !S.off.reserve(std::is_same<T, float>::value ? 16 : sizeof(float4) * cap) ||
+      !S.code.reserve(sizeof(int) * cap) || !S.xq.reserve(std::is_same<T, float>::value ? sizeof(float4) * cap : 16))
+    return ERR_NOMEM;
+  unsigned long long* z = S.cell_count.as<unsigned long long>();
+  unsigned long long* st_we = z;
+  unsigned long long* st_c = z + w_we;
+  unsigned long long* st_f = st_c + w_c;
+  int* cell_cf = reinterpret_cast<int*>(st_f + w_f);
+  CLM_CUDA_TRY(h, cudaMemsetAsync(z, 0, zero_bytes, h.stream));
+  int* n_dev = S.copy_off.as<int>() + n;  // total number of copies, on the device
+  if (N == 3)
+    k_wrap_emit<T, 3><<<(unsigned)we_tiles, kBlock, 0, h.stream>>>(
+        dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(), (int)cap,
+        S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev, st_we, reinterpret_cast<unsigned*>(st_we + we_tiles),
+        (int)we_tiles, cell_cf, S.rank.as<uint32_t>(), err);
+  else
+    k_wrap_emit<T, 2><<<(unsigned)we_tiles, kBlock, 0, h.stream>>>(
+        dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(), (int)cap,
+        S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev, st_we, reinterpret_cast<unsigned*>(st_we + we_tiles),
+        (int)we_tiles, cell_cf, S.rank.as<uint32_t>(), err);
+  CLM_CUDA_TRY(h, cudaGetLastError());
+  h.launches++;
+  k_cell_scan<<<(unsigned)ct, kBlock, 0, h.stream>>>(cell_cf, (int)ncells, S.cell_start.as<int>(), S.cell_flags.as<int>(),
+                                                     S.real_list.as<int>(), S.real_scan.as<int>() + ncells, st_c, st_f,
+                                                     reinterpret_cast<unsigned*>(st_c + ct), (int)ct, err);
+  CLM_CUDA_TRY(h, cudaGetLastError());
+  h.launches++;
+  const int gc = grid_for(cap);
+  k_cell_scatter<<<gc, kBlock, 0, h.stream>>>(S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), S.rank.as<uint32_t>(),
+                                              n_dev, (int)cap, (int)ncells, S.cell_start.as<int>(),
+                                              S.keys[1].as<uint32_t>(), S.vals[1].as<uint32_t>(), err);
+  CLM_CUDA_TRY(h, cudaGetLastError());
+  h.launches++;
+  if (N == 3)
+    k_rank_gather<T, 3><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[1].as<uint32_t>(),
+                                                     S.vals[1].as<uint32_t>(), S.cell_start.as<int>(), (int)ncells,
+                                                     (int)cap, (int)n, S.px.as<T>(), S.py.as<T>(), S.pz.as<T>(),
+                                                     S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(),
+                                                     S.cell_flags.as<int>(), err);
+  else
+    k_rank_gather<T, 2><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[1].as<uint32_t>(),
+                                                     S.vals[1].as<uint32_t>(), S.cell_start.as<int>(), (int)ncells,
+                                                     (int)cap, (int)n, S.px.as<T>(), S.py.as<T>(), S.pz.as<T>(),
+                                                     S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(),
+                                                     S.cell_flags.as<int>(), err);
+  CLM_CUDA_TRY(h, cudaGetLastError());
+  h.launches++;
+  return OK;
+}
+
 template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
   SetData& S = h.sets[set];
   const int N = g.dim;
@@ -661,11 +823,12 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
   DevGeom<T> dg;
   fill_devgeom(g, h.precision, dg);
   int* err = h.err.as<int>();
-  if (!S.cell_count.reserve(sizeof(int) * (ncells + 1)) || !S.cell_start.reserve(sizeof(int) * (ncells + 1)) ||
-      !S.cell_flags.reserve(sizeof(int) * (ncells + 1)) || !S.real_scan.reserve(sizeof(int) * (ncells + 1)) ||
-      !S.real_list.reserve(sizeof(int) * (ncells + 1)) || !S.copy_off.reserve(sizeof(int) * (n + 1)))
+  if (!S.cell_start.reserve(sizeof(int) * (ncells + 1)) || !S.cell_flags.reserve(sizeof(int) * (ncells + 1)) ||
+      !S.real_scan.reserve(sizeof(int) * (ncells + 1)) || !S.real_list.reserve(sizeof(int) * (ncells + 1)) ||
+      !S.copy_off.reserve(sizeof(int) * (n + 1)))
     return ERR_NOMEM;
-  CLM_CUDA_TRY(h, cudaMemsetAsync(S.cell_flags.p, 0, sizeof(int) * (ncells + 1), h.stream));
+  // one system: the counting build writes every cell's flag; batches and empty sets start from zero flags
+  if (batch || n == 0) CLM_CUDA_TRY(h, cudaMemsetAsync(S.cell_flags.p, 0, sizeof(int) * (ncells + 1), h.stream));
   S.built = true;
   S.dirty = false;
   S.pending = true;
@@ -693,6 +856,7 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
     return ERR_ARG;
   }
   S.cap_used = cap;
+  if (!batch) return build_counting<T>(h, S, dg, N, n, ncells, cap);
   const int ntiles = (int)((cap + RS_TILE - 1) / RS_TILE);
   if (!S.wrapped.reserve(sizeof(T) * N * n) || !S.mask.reserve(sizeof(uint32_t) * n) ||
       !S.ncopy.reserve(sizeof(int) * (n + 1)) || !S.keys[0].reserve(sizeof(uint32_t) * cap) ||
@@ -708,51 +872,28 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
   const int* cbase = h.batch.cbase_d.as<int>();
   int* n_dev = S.copy_off.as<int>() + n;  // total number of copies, on the device
   int st = OK;
-  if (batch) {
-    if (N == 3)
-      k_wrap_count_b<T, 3><<<gn, kBlock, 0, h.stream>>>(gtab, psys, S.x.as<T>(), (int)n, S.wrapped.as<T>(),
-                                                       S.mask.as<uint32_t>(), S.ncopy.as<int>(), h.batch.sys_err.as<int>());
-    else
-      k_wrap_count_b<T, 2><<<gn, kBlock, 0, h.stream>>>(gtab, psys, S.x.as<T>(), (int)n, S.wrapped.as<T>(),
-                                                       S.mask.as<uint32_t>(), S.ncopy.as<int>(), h.batch.sys_err.as<int>());
-    CLM_CUDA_TRY(h, cudaGetLastError());
-    h.launches++;
-    st = scan_exclusive(h, S.ncopy.as<int>(), S.copy_off.as<int>(), n, n_dev);
-    if (st) return st;
-    if (N == 3)
-      k_emit_b<T, 3><<<gn, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
-                                                 S.ncopy.as<int>(), S.copy_off.as<int>(), (int)n, (int)cap,
-                                                 S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
-                                                 err);
-    else
-      k_emit_b<T, 2><<<gn, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
-                                                 S.ncopy.as<int>(), S.copy_off.as<int>(), (int)n, (int)cap,
-                                                 S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
-                                                 err);
-    CLM_CUDA_TRY(h, cudaGetLastError());
-    h.launches++;
-  } else {
-    // wrap, images, copy offsets and keys in one launch (tile status words and ticket zeroed first)
-    const int we_tiles = (int)((n + WE_TILE - 1) / WE_TILE);
-    DevBuf& sb = h.scan.level[0];
-    if (!sb.reserve((size_t)(we_tiles + 2) * sizeof(unsigned long long))) return ERR_NOMEM;
-    unsigned long long* status = sb.as<unsigned long long>();
-    CLM_CUDA_TRY(h, cudaMemsetAsync(status, 0, (size_t)(we_tiles + 1) * sizeof(unsigned long long), h.stream));
-    unsigned* ticket = reinterpret_cast<unsigned*>(status + we_tiles);
-    if (N == 3)
-      k_wrap_emit<T, 3><<<we_tiles, kBlock, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(),
-                                                          S.mask.as<uint32_t>(), S.ncopy.as<int>(), (int)cap,
-                                                          S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev,
-                                                          status, ticket, we_tiles, err);
-    else
-      k_wrap_emit<T, 2><<<we_tiles, kBlock, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(),
-                                                          S.mask.as<uint32_t>(), S.ncopy.as<int>(), (int)cap,
-                                                          S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev,
-                                                          status, ticket, we_tiles, err);
-    CLM_CUDA_TRY(h, cudaGetLastError());
-    h.launches++;
-  }
-  // stable LSD radix sort by cell: the fewest passes of at most 10-bit digits, digits as small as that allows
+  if (N == 3)
+    k_wrap_count_b<T, 3><<<gn, kBlock, 0, h.stream>>>(gtab, psys, S.x.as<T>(), (int)n, S.wrapped.as<T>(),
+                                                     S.mask.as<uint32_t>(), S.ncopy.as<int>(), h.batch.sys_err.as<int>());
+  else
+    k_wrap_count_b<T, 2><<<gn, kBlock, 0, h.stream>>>(gtab, psys, S.x.as<T>(), (int)n, S.wrapped.as<T>(),
+                                                     S.mask.as<uint32_t>(), S.ncopy.as<int>(), h.batch.sys_err.as<int>());
+  CLM_CUDA_TRY(h, cudaGetLastError());
+  h.launches++;
+  st = scan_exclusive(h, S.ncopy.as<int>(), S.copy_off.as<int>(), n, n_dev);
+  if (st) return st;
+  if (N == 3)
+    k_emit_b<T, 3><<<gn, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
+                                               S.ncopy.as<int>(), S.copy_off.as<int>(), (int)n, (int)cap,
+                                               S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), err);
+  else
+    k_emit_b<T, 2><<<gn, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
+                                               S.ncopy.as<int>(), S.copy_off.as<int>(), (int)n, (int)cap,
+                                               S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), err);
+  CLM_CUDA_TRY(h, cudaGetLastError());
+  h.launches++;
+  // stable LSD radix sort by global cell: the fewest passes of at most 10-bit digits, digits as small as that
+  // allows
   int bits = 1;
   while (((int64_t)1 << bits) < ncells) bits++;
   const int passes = (bits + 9) / 10;
@@ -777,46 +918,26 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
   }
   // gather coordinates in cell order; cell offsets from the sorted keys
   const int gc = grid_for(cap + 1);  // copies, plus one thread that closes cell_start
-  if (batch) {
-    if (N == 3)
-      k_gather_b<T, 3><<<gc, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
-                                                   S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
-                                                   S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), S.cell_flags.as<int>(), (int)ncells,
-                                                   S.cell_start.as<int>(), err);
-    else
-      k_gather_b<T, 2><<<gc, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
-                                                   S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
-                                                   S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), S.cell_flags.as<int>(), (int)ncells,
-                                                   S.cell_start.as<int>(), err);
-  } else if (N == 3)
-    k_gather<T, 3><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
-                                               S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
-                                               S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), S.cell_flags.as<int>(), (int)ncells,
-                                                   S.cell_start.as<int>(), err);
+  if (N == 3)
+    k_gather_b<T, 3><<<gc, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
+                                                 S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
+                                                 S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(),
+                                                 S.code.as<int>(), S.cell_flags.as<int>(), (int)ncells,
+                                                 S.cell_start.as<int>(), err);
   else
-    k_gather<T, 2><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
-                                               S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
-                                               S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(), S.cell_flags.as<int>(), (int)ncells,
-                                                   S.cell_start.as<int>(), err);
+    k_gather_b<T, 2><<<gc, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
+                                                 S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
+                                                 S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(),
+                                                 S.code.as<int>(), S.cell_flags.as<int>(), (int)ncells,
+                                                 S.cell_start.as<int>(), err);
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
-  // cells with real particles, in linear order; their number stays on the device (real_scan[ncells])
-  if (batch) {
-    // batches also read the per-cell scan (the items of each system)
-    st = scan_exclusive(h, S.cell_flags.as<int>(), S.real_scan.as<int>(), ncells, S.real_scan.as<int>() + ncells);
-    if (st) return st;
-    k_compact<<<grid_for(ncells), kBlock, 0, h.stream>>>(S.cell_flags.as<int>(), S.real_scan.as<int>(), (int)ncells,
-                                                         S.real_list.as<int>());
-  } else {
-    const int ct = (int)((ncells + SCAN_TILE - 1) / SCAN_TILE);
-    DevBuf& sb = h.scan.level[0];
-    if (!sb.reserve((size_t)(ct + 2) * sizeof(unsigned long long))) return ERR_NOMEM;
-    unsigned long long* status = sb.as<unsigned long long>();
-    CLM_CUDA_TRY(h, cudaMemsetAsync(status, 0, (size_t)(ct + 1) * sizeof(unsigned long long), h.stream));
-    k_compact_1pass<<<ct, kBlock, 0, h.stream>>>(S.cell_flags.as<int>(), (int)ncells, S.real_list.as<int>(),
-                                                 S.real_scan.as<int>() + ncells, status,
-                                                 reinterpret_cast<unsigned*>(status + ct), ct, err);
-  }
+  // cells with real particles, in linear order; batches also read the per-cell scan (the items of each
+  // system); their number stays on the device (real_scan[ncells])
+  st = scan_exclusive(h, S.cell_flags.as<int>(), S.real_scan.as<int>(), ncells, S.real_scan.as<int>() + ncells);
+  if (st) return st;
+  k_compact<<<grid_for(ncells), kBlock, 0, h.stream>>>(S.cell_flags.as<int>(), S.real_scan.as<int>(), (int)ncells,
+                                                       S.real_list.as<int>());
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
   return OK;

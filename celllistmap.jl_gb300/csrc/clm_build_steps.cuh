@@ -191,6 +191,26 @@ __host__ __device__ __forceinline__ bool wrap_count_at(const DevGeom<T>& g, cons
 // the key is the copy's cell (the real copy first, with the border-case shift, then the images in
 // increasing image code), the value (i << 5) | image code.  `cb` is the first global cell of the particle's
 // system (0 for one system).
+// The cell of image k of a particle at wrapped position p (k = zero_code: the real copy, with the border-case
+// shift); an out-of-range cell is flagged and mapped to cell 0.
+template <class T, int N>
+__host__ __device__ __forceinline__ int copy_cell(const DevGeom<T>& g, const T* p, int k, int* __restrict__ err) {
+  int li;
+  if (k == g.zero_code) {
+    li = cell_of<T, N>(g, p, true);
+  } else {
+    T q[N];
+#pragma unroll
+    for (int d = 0; d < N; d++) q[d] = xadd(p[d], g.shift[k][d]);
+    li = cell_of<T, N>(g, q, false);
+  }
+  if (li < 0) {
+    flag_error(err, DERR_CELL_RANGE);
+    li = 0;
+  }
+  return li;
+}
+
 template <class T, int N>
 __host__ __device__ __forceinline__ void emit_copies(const DevGeom<T>& g, int cb, const T* p, uint32_t m, int ncp,
                                                      int i, int base, int cap, uint32_t* __restrict__ keys,
@@ -200,28 +220,13 @@ __host__ __device__ __forceinline__ void emit_copies(const DevGeom<T>& g, int cb
     flag_error(err, DERR_COPY_OVERFLOW);
     return;
   }
-  int li = cell_of<T, N>(g, p, true);
-  if (li < 0) {
-    flag_error(err, DERR_CELL_RANGE);
-    li = 0;
-  }
-  li += cb;
-  keys[base] = (uint32_t)li;
+  keys[base] = (uint32_t)(copy_cell<T, N>(g, p, g.zero_code, err) + cb);
   vals[base] = ((uint32_t)i << 5) | (uint32_t)g.zero_code;
   int t = 1;
   while (m) {
     int k = lowest_bit(m);
     m &= m - 1;
-    T q[N];
-#pragma unroll
-    for (int d = 0; d < N; d++) q[d] = xadd(p[d], g.shift[k][d]);
-    int lk = cell_of<T, N>(g, q, false);
-    if (lk < 0) {
-      flag_error(err, DERR_CELL_RANGE);
-      lk = 0;
-    }
-    lk += cb;
-    keys[base + t] = (uint32_t)lk;
+    keys[base + t] = (uint32_t)(copy_cell<T, N>(g, p, k, err) + cb);
     vals[base + t] = ((uint32_t)i << 5) | (uint32_t)k;
     t++;
   }
@@ -253,6 +258,24 @@ __host__ __device__ __forceinline__ void origin_ff(float cb_hi, float cb_lo, flo
   const float se = (cb_hi - (s - bb)) + (p - bb);
   hi = s;
   lo = se + pe + cb_lo;
+}
+
+// Counting placement by cell: copies reach their cell's slots [s, e) in arrival order (per-cell atomic
+// counters), so a cell's values (particle << 5 | image) arrive permuted.  The final slot of value v is s plus
+// the number of smaller values of its cell: values are distinct (one per copy), so the slots are a
+// permutation of [s, e) and the cell ends up in increasing particle index, the reference's serial order
+// (a particle has at most one copy per cell) -- the order a stable sort by cell gives.
+__host__ __device__ __forceinline__ int rank_in_cell(const uint32_t* __restrict__ vals, int s, int e, uint32_t v) {
+  int r = 0;
+  int k = s;
+  for (; k + 4 <= e; k += 4) {
+    r += (vals[k] < v) ? 1 : 0;
+    r += (vals[k + 1] < v) ? 1 : 0;
+    r += (vals[k + 2] < v) ? 1 : 0;
+    r += (vals[k + 3] < v) ? 1 : 0;
+  }
+  for (; k < e; k++) r += (vals[k] < v) ? 1 : 0;
+  return r;
 }
 
 // cell_start from the keys sorted by cell: copy t writes the starts of the cells between the previous

@@ -68,8 +68,10 @@ struct SetData {
   DevBuf wrapped;           // wrapped (and rotated) positions, n x dim
   DevBuf mask;              // per particle: bit k set if image k lies in the computing box
   DevBuf ncopy, copy_off;   // copies per particle and their exclusive scan
-  DevBuf keys[2], vals[2];  // (cell, particle<<5 | image) pairs for the radix sort
-  DevBuf cell_count, cell_start, cell_flags;
+  DevBuf keys[2], vals[2];  // (cell, particle<<5 | image) pairs: particle order, then grouped by cell
+  DevBuf rank;              // one system: each copy's arrival rank in its cell
+  DevBuf cell_count;        // one system: scan words and per-cell {copies, real} counters (zeroed per build)
+  DevBuf cell_start, cell_flags;
   DevBuf real_list, real_scan;
   DevBuf px, py, pz;        // copies in cell order (SoA), handle dtype
   DevBuf off;               // FP32 cell-relative offsets (float4, .w = code) for the prefilter

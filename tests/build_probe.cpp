@@ -3,8 +3,9 @@
 // -ffp-contract=off, as the library's host code is):
 //   build_probe        the cell-list build steps (csrc/clm_build_steps.cuh: the geometry copy the kernels
 //                      receive, K1 wrap_count_at, K2 emit_at, K4 gather_at) one particle or copy at a time,
-//                      with the scan and the radix sort replaced by their contracts (copy offsets in particle
-//                      order; a stable sort of the copies by cell);
+//                      with the copy-offset scan replaced by its contract (offsets in particle order) and the
+//                      counting placement emulated (arrival ranks in a scrambled order, cell starts, each
+//                      copy's final slot from rank_in_cell), which must give the stable sort by cell;
 //   stencil_probe      the pair kernel's stencil enumeration; cell_probe its cell index (border case);
 //   band_probe         the condition under which the pair kernel skips the projection filter;
 //   map_nl_probe,      the self and x-y pair maps emulated from the kernel's pieces (stencil, pair_rule,
@@ -78,17 +79,40 @@ int build_host(int kind, const double* Mcol, double cutoff, int lcell, const dou
   for (int i = 0; i < n; i++)
     clm::emit_at<T, N>(d, 0, wrapped.data(), mask.data(), ncopy.data(), off.data(), i, total, keys.data(),
                        vals.data(), &L.err);
-  // the radix sort's contract: copies ordered by cell, stable (particle order inside a cell)
+  const int ncells = d.ncells;
+  // the counting build of one system: copies take their cell's slots in an arrival order the device leaves
+  // open (emulated by a fixed scramble of the copies), the cell starts are the scan of the counts, and each
+  // copy moves to its cell's start plus its rank by value in the cell (rank_in_cell)
+  std::vector<int> cnt((size_t)ncells + 1, 0), arrival((size_t)total), order((size_t)total);
+  std::iota(order.begin(), order.end(), 0);
+  uint64_t rs = 0x9e3779b97f4a7c15ull;
+  for (int t = total - 1; t > 0; t--) {
+    rs = rs * 6364136223846793005ull + 1442695040888963407ull;
+    std::swap(order[(size_t)t], order[(size_t)((rs >> 33) % (uint64_t)(t + 1))]);
+  }
+  for (int q : order) arrival[(size_t)q] = cnt[keys[(size_t)q]]++;
+  std::vector<int> cstart((size_t)ncells + 1, 0);
+  for (int c = 0; c < ncells; c++) cstart[(size_t)c + 1] = cstart[(size_t)c] + cnt[(size_t)c];
+  std::vector<uint32_t> pk((size_t)total), pv((size_t)total), svals((size_t)total);
+  for (int t = 0; t < total; t++) {
+    const int pos = cstart[keys[(size_t)t]] + arrival[(size_t)t];
+    pk[(size_t)pos] = keys[(size_t)t];
+    pv[(size_t)pos] = vals[(size_t)t];
+  }
+  L.skeys.resize((size_t)total);
+  for (int q = 0; q < total; q++) {
+    const uint32_t c = pk[(size_t)q];
+    const int t = cstart[c] + clm::rank_in_cell(pv.data(), cstart[c], cstart[c + 1], pv[(size_t)q]);
+    L.skeys[(size_t)t] = c;
+    svals[(size_t)t] = pv[(size_t)q];
+  }
+  // which is the contract of a stable sort by cell (particle order inside a cell)
   std::vector<int> perm((size_t)total);
   std::iota(perm.begin(), perm.end(), 0);
   std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return keys[(size_t)a] < keys[(size_t)b]; });
-  std::vector<uint32_t> svals((size_t)total);
-  L.skeys.resize((size_t)total);
-  for (int t = 0; t < total; t++) {
-    L.skeys[(size_t)t] = keys[(size_t)perm[(size_t)t]];
-    svals[(size_t)t] = vals[(size_t)perm[(size_t)t]];
-  }
-  const int ncells = d.ncells;
+  for (int t = 0; t < total; t++)
+    if (L.skeys[(size_t)t] != keys[(size_t)perm[(size_t)t]] || svals[(size_t)t] != vals[(size_t)perm[(size_t)t]])
+      return 97;
   L.total = total;
   L.px.assign((size_t)total + 1, T(0));
   L.py.assign((size_t)total + 1, T(0));
@@ -109,6 +133,8 @@ int build_host(int kind, const double* Mcol, double cutoff, int lcell, const dou
     if (L.start[(size_t)c] < 0 || L.start[(size_t)c] > L.start[(size_t)c + 1]) return 99;
   for (int t = 0; t < total; t++)
     if (L.start[L.skeys[(size_t)t]] > t || L.start[L.skeys[(size_t)t] + 1] <= t) return 98;
+  for (int c = 0; c <= ncells; c++)
+    if (L.start[(size_t)c] != cstart[(size_t)c]) return 96;  // the cell scan's starts
   return 0;
 }
 
