@@ -519,8 +519,10 @@ def main():
     o_dev.out_on_device = 1
 
     def step_device():
+        # new positions, then the map: clm_run rebuilds the updated cell list itself (as pairwise! after an
+        # update of the positions does) and checks the build's totals with the map's results, one host
+        # synchronization per step
         st = L.clm_set_positions(h, 0, C.c_void_p(x_dev.data_ptr()), n, 1)
-        st = st or L.clm_build(h)
         st = st or L.clm_run(h, A.OP["lj_forces"], C.byref(p), C.byref(o_dev))
         if st:
             buf = C.create_string_buffer(512)

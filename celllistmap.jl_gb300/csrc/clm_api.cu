@@ -160,8 +160,10 @@ int32_t clm_create(int32_t dtype, int32_t dim, int32_t nsets, clm_handle* out) {
     return ERR_CUDA;
   }
   h->own_stream = true;
-  if (cudaMallocHost((void**)&h->pinned, 256) != cudaSuccess || !h->err.reserve(64)) {
+  if (cudaMallocHost((void**)&h->pinned, 256) != cudaSuccess ||
+      cudaMallocHost((void**)&h->pres, clm::kResultBytes) != cudaSuccess || !h->err.reserve(64)) {
     if (h->pinned) cudaFreeHost(h->pinned);
+    if (h->pres) cudaFreeHost(h->pres);
     cudaStreamDestroy(h->stream);
     delete h;
     return ERR_CUDA;
@@ -178,6 +180,7 @@ int32_t clm_destroy(clm_handle h) {
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
   if (h->pinned) cudaFreeHost(h->pinned);
+  if (h->pres) cudaFreeHost(h->pres);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return OK;

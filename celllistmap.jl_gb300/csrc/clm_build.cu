@@ -506,15 +506,18 @@ __global__ void __launch_bounds__(kBlock) k_cell_scan(const int* __restrict__ ce
 }
 
 // Every copy (particle order) to its cell's slots, at its arrival rank: sorted keys and values grouped by
-// cell, each cell's values still in arrival order.
+// cell, each cell's values still in arrival order.  The scan words and per-cell counters, read for the last
+// time by k_cell_scan, are cleared for the next build (`zero`, `zwords` 64-bit words).
 __global__ void __launch_bounds__(kBlock) k_cell_scatter(const uint32_t* __restrict__ keys,
                                                          const uint32_t* __restrict__ vals,
                                                          const uint32_t* __restrict__ ranks,
                                                          const int* __restrict__ n_dev, int cap, int ncells,
                                                          const int* __restrict__ cell_start,
                                                          uint32_t* __restrict__ skeys, uint32_t* __restrict__ svals,
+                                                         unsigned long long* __restrict__ zero, int64_t zwords,
                                                          int* __restrict__ err) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int64_t w = t; w < zwords; w += (int64_t)gridDim.x * blockDim.x) zero[w] = 0ull;
   const int n = min(*n_dev, cap);
   if (t >= n) return;
   const uint32_t li = keys[t];
@@ -750,6 +753,7 @@ int build_counting(Handle& h, SetData& S, const DevGeom<T>& dg, int N, int64_t n
   // the per-cell counters (two ints per cell)
   const int64_t w_we = we_tiles + 1, w_c = ct + 1, w_f = ct;
   const size_t zero_bytes = sizeof(unsigned long long) * (size_t)(w_we + w_c + w_f + ncells + 1);
+  const void* zero_at = S.cell_count.p;
   if (!S.cell_count.reserve(zero_bytes) || !S.wrapped.reserve(sizeof(T) * N * n) ||
       !S.mask.reserve(sizeof(uint32_t) * n) || !S.ncopy.reserve(sizeof(int) * (n + 1)) ||
       !S.keys[0].reserve(sizeof(uint32_t) * cap) || !S.keys[1].reserve(sizeof(uint32_t) * cap) ||
@@ -758,12 +762,15 @@ int build_counting(Handle& h, SetData& S, const DevGeom<T>& dg, int N, int64_t n
       !S.pz.reserve(sizeof(T) * cap) || !S.off.reserve(std::is_same<T, float>::value ? 16 : sizeof(float4) * cap) ||
       !S.code.reserve(sizeof(int) * cap) || !S.xq.reserve(std::is_same<T, float>::value ? sizeof(float4) * cap : 16))
     return ERR_NOMEM;
+  if (S.cell_count.p != zero_at) S.cell_count_zero = 0;  // a new allocation holds no cleared words
   unsigned long long* z = S.cell_count.as<unsigned long long>();
   unsigned long long* st_we = z;
   unsigned long long* st_c = z + w_we;
   unsigned long long* st_f = st_c + w_c;
   int* cell_cf = reinterpret_cast<int*>(st_f + w_f);
-  CLM_CUDA_TRY(h, cudaMemsetAsync(z, 0, zero_bytes, h.stream));
+  // cleared by the previous build's scatter unless the region grew or moved
+  if (S.cell_count_zero < zero_bytes) CLM_CUDA_TRY(h, cudaMemsetAsync(z, 0, zero_bytes, h.stream));
+  S.cell_count_zero = 0;
   int* n_dev = S.copy_off.as<int>() + n;  // total number of copies, on the device
   if (N == 3)
     k_wrap_emit<T, 3><<<(unsigned)we_tiles, kBlock, 0, h.stream>>>(
@@ -785,9 +792,11 @@ int build_counting(Handle& h, SetData& S, const DevGeom<T>& dg, int N, int64_t n
   const int gc = grid_for(cap);
   k_cell_scatter<<<gc, kBlock, 0, h.stream>>>(S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), S.rank.as<uint32_t>(),
                                               n_dev, (int)cap, (int)ncells, S.cell_start.as<int>(),
-                                              S.keys[1].as<uint32_t>(), S.vals[1].as<uint32_t>(), err);
+                                              S.keys[1].as<uint32_t>(), S.vals[1].as<uint32_t>(), z,
+                                              (int64_t)(zero_bytes / sizeof(unsigned long long)), err);
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
+  S.cell_count_zero = zero_bytes;
   if (N == 3)
     k_rank_gather<T, 3><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[1].as<uint32_t>(),
                                                      S.vals[1].as<uint32_t>(), S.cell_start.as<int>(), (int)ncells,

@@ -71,6 +71,7 @@ struct SetData {
   DevBuf keys[2], vals[2];  // (cell, particle<<5 | image) pairs: particle order, then grouped by cell
   DevBuf rank;              // one system: each copy's arrival rank in its cell
   DevBuf cell_count;        // one system: scan words and per-cell {copies, real} counters (zeroed per build)
+  size_t cell_count_zero = 0;  // bytes of cell_count left cleared by the last build (0: clear before use)
   DevBuf cell_start, cell_flags;
   DevBuf real_list, real_scan;
   DevBuf px, py, pz;        // copies in cell order (SoA), handle dtype
@@ -160,6 +161,11 @@ struct Handle {
   DevBuf opbuf;      // operator parameter staging (types, tables, velocities, bins)
   DevBuf outbuf;     // device outputs staged before copying to the caller
   int* pinned = nullptr;       // small pinned host staging area (256 bytes)
+  unsigned char* pres = nullptr;  // pinned host copy of a map's results (kResultBytes)
+  // The force accumulators of h.outbuf read as zero up to acc_zero_bytes when acc_zero_ptr == outbuf.p: the
+  // force conversion clears the sums it reads, so the next map need not clear them again.
+  void* acc_zero_ptr = nullptr;
+  size_t acc_zero_bytes = 0;
   cudaEvent_t ev[4] = {};
   float build_ms = 0, map_ms = 0;
   bool build_timing_pending = false;
@@ -168,6 +174,10 @@ struct Handle {
   BatchState batch;
   bool capturing = false;      // a stream capture is open: no synchronization, no timing events
 };
+
+// Results of one map on the device: scalar, count, minimum and its pair (first 256 bytes), histogram counts
+// and sums (16 x 256 bytes), adjoint sums.
+constexpr size_t kResultBytes = 256 + 16 * 256 + 128;
 
 // Status helpers
 #define CLM_CUDA_TRY(h, call)                                                            \
