@@ -16,9 +16,12 @@
 //   k_rank_gather   each copy to its rank by value inside its cell (particle-index
 //                   order, the reference's serial order), with its coordinates (SoA),
 //                   particle code and 16-byte candidate record
+// One system with crowded cells (more than kCountingMaxPerCell copies per cell
+// expected): k_wrap_emit without the counters, a stable LSD radix sort of the keys by
+// cell, K4 k_gather (cell starts from the sorted keys) and k_compact_1pass.
 // Batches (global cell index over all systems): K1 k_wrap_count_b, a scan of the
-// copies, K2 k_emit_b, a stable LSD radix sort of the keys by cell, K4 k_gather_b,
-// and the real-cell scan and compaction.
+// copies, K2 k_emit_b, the radix sort, K4 k_gather_b, and the real-cell scan and
+// compaction.
 //
 // Every kernel bounds-checks its indices; inconsistencies set bits of the
 // handle's device error word instead of faulting.
@@ -363,9 +366,11 @@ __global__ void __launch_bounds__(kBlock) k_emit_b(const DevGeom<T>* __restrict_
 // copy also takes the next slot of its cell's counter (its arrival rank, in `ranks`), and the real copy
 // marks its cell: cell_cf holds {copies, holds a real particle} per cell, zeroed before the launch.
 constexpr int WE_PPT = 1;
+// One system: above this many expected copies per cell the build sorts by radix instead of counting.
+constexpr double kCountingMaxPerCell = 64.0;
 constexpr int WE_TILE = kBlock * WE_PPT;
 
-template <class T, int N>
+template <class T, int N, bool COUNT>
 __global__ void __launch_bounds__(kBlock) k_wrap_emit(DevGeom<T> g, const T* __restrict__ x, int n,
                                                       T* __restrict__ wrapped, uint32_t* __restrict__ mask,
                                                       int* __restrict__ ncopy, int cap, uint32_t* __restrict__ keys,
@@ -436,14 +441,16 @@ __global__ void __launch_bounds__(kBlock) k_wrap_emit(DevGeom<T> g, const T* __r
       key = (uint32_t)copy_cell<T, N>(g, p, k, err);
       keys[base + c] = key;
       vals[base + c] = ((uint32_t)i << 5) | (uint32_t)k;
-      if (c == 0) cell_cf[2 * key + 1] = 1;  // the cell holds a real particle
+      if (COUNT && c == 0) cell_cf[2 * key + 1] = 1;  // the cell holds a real particle
     }
-    const unsigned peers = __match_any_sync(0xffffffffu, key);
-    const int leader = __ffs(peers) - 1;
-    int first = 0;
-    if (lane == leader && key != 0xffffffffu) first = atomicAdd(&cell_cf[2 * key], __popc(peers));
-    first = __shfl_sync(0xffffffffu, first, leader);
-    if (key != 0xffffffffu) ranks[base + c] = (uint32_t)(first + __popc(peers & lt));
+    if constexpr (COUNT) {
+      const unsigned peers = __match_any_sync(0xffffffffu, key);
+      const int leader = __ffs(peers) - 1;
+      int first = 0;
+      if (lane == leader && key != 0xffffffffu) first = atomicAdd(&cell_cf[2 * key], __popc(peers));
+      first = __shfl_sync(0xffffffffu, first, leader);
+      if (key != 0xffffffffu) ranks[base + c] = (uint32_t)(first + __popc(peers & lt));
+    }
   }
 }
 
@@ -567,7 +574,70 @@ __global__ void __launch_bounds__(kBlock) k_rank_gather(DevGeom<T> g, const T* _
   gather_at<T, N>(g, wrapped, t, p, k, (int)li, px, py, pz, off, xq, code, cell_flags, 0);
 }
 
+// Crowded cells (radix path of one system): the cells with real particles, in linear order, in one pass:
+// each tile scans its cells' flags, takes its first slot by decoupled look-back, and lists its flagged
+// cells; the last tile writes their number.
+__global__ void __launch_bounds__(kBlock) k_compact_1pass(const int* __restrict__ flags, int ncells,
+                                                          int* __restrict__ list, int* __restrict__ total,
+                                                          unsigned long long* __restrict__ status,
+                                                          unsigned* __restrict__ ticket, int ntiles,
+                                                          int* __restrict__ err) {
+  __shared__ int wsum[kBlock / 32 + 1];
+  __shared__ int s_tile, s_excl;
+  if (threadIdx.x == 0) s_tile = (int)atomicAdd(ticket, 1u);
+  __syncthreads();
+  const int tile = s_tile;
+  const int c0 = tile * SCAN_TILE + threadIdx.x * SCAN_IPT;
+  int v[SCAN_IPT], f[SCAN_IPT];
+#pragma unroll
+  for (int k = 0; k < SCAN_IPT; k++) {
+    f[k] = (c0 + k < ncells && flags[c0 + k]) ? 1 : 0;
+    v[k] = f[k];
+  }
+  int off = 0;
+  const int agg = block_scan<SCAN_IPT>(v, off, wsum);
+  if (threadIdx.x < 32) {
+    const int excl = lookback(tile, agg, status, err);
+    if (threadIdx.x == 0) {
+      s_excl = excl;
+      if (tile == ntiles - 1) *total = excl + agg;
+    }
+  }
+  __syncthreads();
+  off += s_excl;
+#pragma unroll
+  for (int k = 0; k < SCAN_IPT; k++)
+    if (f[k]) list[v[k] + off] = c0 + k;
+}
+
 // ------------------------------------------------------------------ K4: gather in cell order
+// One system after the radix sort: copy t of the sorted keys
+template <class T, int N>
+__global__ void __launch_bounds__(kBlock) k_gather(DevGeom<T> g, const T* __restrict__ wrapped,
+                                                   const uint32_t* __restrict__ skeys,
+                                                   const uint32_t* __restrict__ svals, const int* __restrict__ n_dev,
+                                                   int cap, int n, T* __restrict__ px, T* __restrict__ py,
+                                                   T* __restrict__ pz, float4* __restrict__ off, float4* __restrict__ xq,
+                                                   int* __restrict__ code, int* __restrict__ cell_flags,
+                                                   int ncells, int* __restrict__ cell_start, int* __restrict__ err) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nc = min(*n_dev, cap);
+  if (t > nc) return;
+  cell_starts_at(skeys, t, nc, ncells, cell_start);
+  if (t == nc) return;
+  uint32_t v = svals[t];
+  int p = (int)(v >> 5);
+  int k = (int)(v & 31u);
+  int li = (int)skeys[t];
+  if (p >= n || k >= g.nimg || li < 0 || li >= g.ncells) {
+    atomicOr(err, DERR_CELL_RANGE);
+    p = 0;
+    k = g.zero_code;
+    li = 0;
+  }
+  gather_at<T, N>(g, wrapped, t, p, k, li, px, py, pz, off, xq, code, cell_flags, 0);
+}
+
 template <class T, int N>
 __global__ void __launch_bounds__(kBlock) k_gather_b(const DevGeom<T>* __restrict__ gtab, const int* __restrict__ psys,
                                                      const int* __restrict__ cbase, const T* __restrict__ wrapped,
@@ -773,12 +843,12 @@ int build_counting(Handle& h, SetData& S, const DevGeom<T>& dg, int N, int64_t n
   S.cell_count_zero = 0;
   int* n_dev = S.copy_off.as<int>() + n;  // total number of copies, on the device
   if (N == 3)
-    k_wrap_emit<T, 3><<<(unsigned)we_tiles, kBlock, 0, h.stream>>>(
+    k_wrap_emit<T, 3, true><<<(unsigned)we_tiles, kBlock, 0, h.stream>>>(
         dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(), (int)cap,
         S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev, st_we, reinterpret_cast<unsigned*>(st_we + we_tiles),
         (int)we_tiles, cell_cf, S.rank.as<uint32_t>(), err);
   else
-    k_wrap_emit<T, 2><<<(unsigned)we_tiles, kBlock, 0, h.stream>>>(
+    k_wrap_emit<T, 2, true><<<(unsigned)we_tiles, kBlock, 0, h.stream>>>(
         dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(), (int)cap,
         S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev, st_we, reinterpret_cast<unsigned*>(st_we + we_tiles),
         (int)we_tiles, cell_cf, S.rank.as<uint32_t>(), err);
@@ -836,8 +906,7 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
       !S.real_scan.reserve(sizeof(int) * (ncells + 1)) || !S.real_list.reserve(sizeof(int) * (ncells + 1)) ||
       !S.copy_off.reserve(sizeof(int) * (n + 1)))
     return ERR_NOMEM;
-  // one system: the counting build writes every cell's flag; batches and empty sets start from zero flags
-  if (batch || n == 0) CLM_CUDA_TRY(h, cudaMemsetAsync(S.cell_flags.p, 0, sizeof(int) * (ncells + 1), h.stream));
+  if (n == 0) CLM_CUDA_TRY(h, cudaMemsetAsync(S.cell_flags.p, 0, sizeof(int) * (ncells + 1), h.stream));
   S.built = true;
   S.dirty = false;
   S.pending = true;
@@ -865,7 +934,13 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
     return ERR_ARG;
   }
   S.cap_used = cap;
-  if (!batch) return build_counting<T>(h, S, dg, N, n, ncells, cap);
+  // One system: the counting build, unless the cells are expected to be crowded (copies per cell from the
+  // uniform-density capacity): its in-cell ranking takes a cell's size in steps per copy, where the radix
+  // sort's cost does not depend on it.  Either gives the same cell list.
+  const bool crowded = !batch && (double)cap > kCountingMaxPerCell * (double)ncells;
+  if (!batch && !crowded) return build_counting<T>(h, S, dg, N, n, ncells, cap);
+  // the radix path's gather sets the real flags of the cells it fills
+  CLM_CUDA_TRY(h, cudaMemsetAsync(S.cell_flags.p, 0, sizeof(int) * (ncells + 1), h.stream));
   const int ntiles = (int)((cap + RS_TILE - 1) / RS_TILE);
   if (!S.wrapped.reserve(sizeof(T) * N * n) || !S.mask.reserve(sizeof(uint32_t) * n) ||
       !S.ncopy.reserve(sizeof(int) * (n + 1)) || !S.keys[0].reserve(sizeof(uint32_t) * cap) ||
@@ -881,28 +956,48 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
   const int* cbase = h.batch.cbase_d.as<int>();
   int* n_dev = S.copy_off.as<int>() + n;  // total number of copies, on the device
   int st = OK;
-  if (N == 3)
-    k_wrap_count_b<T, 3><<<gn, kBlock, 0, h.stream>>>(gtab, psys, S.x.as<T>(), (int)n, S.wrapped.as<T>(),
-                                                     S.mask.as<uint32_t>(), S.ncopy.as<int>(), h.batch.sys_err.as<int>());
-  else
-    k_wrap_count_b<T, 2><<<gn, kBlock, 0, h.stream>>>(gtab, psys, S.x.as<T>(), (int)n, S.wrapped.as<T>(),
-                                                     S.mask.as<uint32_t>(), S.ncopy.as<int>(), h.batch.sys_err.as<int>());
-  CLM_CUDA_TRY(h, cudaGetLastError());
-  h.launches++;
-  st = scan_exclusive(h, S.ncopy.as<int>(), S.copy_off.as<int>(), n, n_dev);
-  if (st) return st;
-  if (N == 3)
-    k_emit_b<T, 3><<<gn, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
-                                               S.ncopy.as<int>(), S.copy_off.as<int>(), (int)n, (int)cap,
-                                               S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), err);
-  else
-    k_emit_b<T, 2><<<gn, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
-                                               S.ncopy.as<int>(), S.copy_off.as<int>(), (int)n, (int)cap,
-                                               S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), err);
-  CLM_CUDA_TRY(h, cudaGetLastError());
-  h.launches++;
-  // stable LSD radix sort by global cell: the fewest passes of at most 10-bit digits, digits as small as that
-  // allows
+  if (!batch) {
+    // wrap, images, copy offsets and keys in one launch (tile status words and ticket zeroed first)
+    const int we_tiles = (int)((n + WE_TILE - 1) / WE_TILE);
+    DevBuf& sb = h.scan.level[0];
+    if (!sb.reserve((size_t)(we_tiles + 2) * sizeof(unsigned long long))) return ERR_NOMEM;
+    unsigned long long* status = sb.as<unsigned long long>();
+    CLM_CUDA_TRY(h, cudaMemsetAsync(status, 0, (size_t)(we_tiles + 1) * sizeof(unsigned long long), h.stream));
+    unsigned* ticket = reinterpret_cast<unsigned*>(status + we_tiles);
+    if (N == 3)
+      k_wrap_emit<T, 3, false><<<we_tiles, kBlock, 0, h.stream>>>(
+          dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(), (int)cap,
+          S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev, status, ticket, we_tiles, nullptr, nullptr, err);
+    else
+      k_wrap_emit<T, 2, false><<<we_tiles, kBlock, 0, h.stream>>>(
+          dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(), (int)cap,
+          S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev, status, ticket, we_tiles, nullptr, nullptr, err);
+    CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+  } else {
+    if (N == 3)
+      k_wrap_count_b<T, 3><<<gn, kBlock, 0, h.stream>>>(gtab, psys, S.x.as<T>(), (int)n, S.wrapped.as<T>(),
+                                                       S.mask.as<uint32_t>(), S.ncopy.as<int>(), h.batch.sys_err.as<int>());
+    else
+      k_wrap_count_b<T, 2><<<gn, kBlock, 0, h.stream>>>(gtab, psys, S.x.as<T>(), (int)n, S.wrapped.as<T>(),
+                                                       S.mask.as<uint32_t>(), S.ncopy.as<int>(), h.batch.sys_err.as<int>());
+    CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+    st = scan_exclusive(h, S.ncopy.as<int>(), S.copy_off.as<int>(), n, n_dev);
+    if (st) return st;
+    if (N == 3)
+      k_emit_b<T, 3><<<gn, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
+                                                 S.ncopy.as<int>(), S.copy_off.as<int>(), (int)n, (int)cap,
+                                                 S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), err);
+    else
+      k_emit_b<T, 2><<<gn, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.mask.as<uint32_t>(),
+                                                 S.ncopy.as<int>(), S.copy_off.as<int>(), (int)n, (int)cap,
+                                                 S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), err);
+    CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+  }
+  // stable LSD radix sort by cell (the global cell for batches): the fewest passes of at most 10-bit digits,
+  // digits as small as that allows
   int bits = 1;
   while (((int64_t)1 << bits) < ncells) bits++;
   const int passes = (bits + 9) / 10;
@@ -927,6 +1022,34 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
   }
   // gather coordinates in cell order; cell offsets from the sorted keys
   const int gc = grid_for(cap + 1);  // copies, plus one thread that closes cell_start
+  if (!batch) {
+    if (N == 3)
+      k_gather<T, 3><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
+                                                 S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
+                                                 S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(),
+                                                 S.code.as<int>(), S.cell_flags.as<int>(), (int)ncells,
+                                                 S.cell_start.as<int>(), err);
+    else
+      k_gather<T, 2><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
+                                                 S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
+                                                 S.py.as<T>(), S.pz.as<T>(), S.off.as<float4>(), S.xq.as<float4>(),
+                                                 S.code.as<int>(), S.cell_flags.as<int>(), (int)ncells,
+                                                 S.cell_start.as<int>(), err);
+    CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+    // cells with real particles, in linear order; their number stays on the device (real_scan[ncells])
+    const int ct = (int)((ncells + SCAN_TILE - 1) / SCAN_TILE);
+    DevBuf& sb = h.scan.level[0];
+    if (!sb.reserve((size_t)(ct + 2) * sizeof(unsigned long long))) return ERR_NOMEM;
+    unsigned long long* status = sb.as<unsigned long long>();
+    CLM_CUDA_TRY(h, cudaMemsetAsync(status, 0, (size_t)(ct + 1) * sizeof(unsigned long long), h.stream));
+    k_compact_1pass<<<ct, kBlock, 0, h.stream>>>(S.cell_flags.as<int>(), (int)ncells, S.real_list.as<int>(),
+                                                 S.real_scan.as<int>() + ncells, status,
+                                                 reinterpret_cast<unsigned*>(status + ct), ct, err);
+    CLM_CUDA_TRY(h, cudaGetLastError());
+    h.launches++;
+    return OK;
+  }
   if (N == 3)
     k_gather_b<T, 3><<<gc, kBlock, 0, h.stream>>>(gtab, psys, cbase, S.wrapped.as<T>(), S.keys[cur].as<uint32_t>(),
                                                  S.vals[cur].as<uint32_t>(), n_dev, (int)cap, (int)n, S.px.as<T>(),
