@@ -64,6 +64,18 @@ __device__ __forceinline__ double vrsqrt_1nr(double x) {
   return fma(0.5 * y, e, y);
 }
 
+// a <= b and a < b for non-negative values (squared distances, the cutoff, +inf), decided on the bit
+// patterns, which are ordered like the values for non-negative IEEE numbers: for FP64 an integer compare,
+// which leaves the FP64 pipe (one warp instruction per 16 cycles on GB300) to arithmetic.
+template <class T> __device__ __forceinline__ bool nonneg_le(T a, T b) {
+  if constexpr (std::is_same<T, double>::value) return __double_as_longlong(a) <= __double_as_longlong(b);
+  else return a <= b;
+}
+template <class T> __device__ __forceinline__ bool nonneg_lt(T a, T b) {
+  if constexpr (std::is_same<T, double>::value) return __double_as_longlong(a) < __double_as_longlong(b);
+  else return a < b;
+}
+
 // Operator parameter k and the LJ type tables in the precision of the pair value (no conversions per pair).
 template <class V, class T> __device__ __forceinline__ V par(const PairArgs<T>& A, int k) {
   if constexpr (std::is_same<V, float>::value) return A.pf[k];
@@ -701,9 +713,9 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : ((OPK == OPK_
                     d2 = xmul(dxs[0], dxs[0]);
 #pragma unroll
                     for (int d = 1; d < N; d++) d2 = xadd(d2, xmul(dxs[d], dxs[d]));
-                    hit = d2 <= g.cutoff_sqr;
+                    hit = nonneg_le(d2, g.cutoff_sqr);
                     const int epos = w0 + j;  // position in the stream
-                    if (hit && d2 > band && epos >= same_end) {
+                    if (hit && nonneg_lt(band, d2) && epos >= same_end) {
                       // the reference's projection filter, seen from the cell of the reference's i
                       if constexpr (ABS_PF) {
                         int lo = 0;
@@ -837,7 +849,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4) ? 6 : ((OPK == OPK_
                       dd2 = xadd(dd2, xmul(dd, dd));
                     }
                   }
-                  if (dd2 < best_d2 || (dd2 == best_d2 && (oi < best_i || (oi == best_i && oj < best_j)))) {
+                  if (nonneg_lt(dd2, best_d2) ||
+                      (!nonneg_lt(best_d2, dd2) && (oi < best_i || (oi == best_i && oj < best_j)))) {
                     best_d2 = dd2;
                     best_i = oi;
                     best_j = oj;
