@@ -272,7 +272,6 @@ template <class T> int enqueue_op(Handle& h, int slot, int op, const clm_op_para
       return fail(&h, ERR_NOMEM, "device allocation failed (forces)");
     A.fx = h.outbuf.as<double>();
     A.f4x = h.outbuf.as<float4>();
-    h.acc_zero_ptr = nullptr;  // the batched step leaves its sums in the accumulators
     CLM_CUDA_TRY(h, cudaMemsetAsync(h.outbuf.p, 0, acc_bytes, h.stream));
   }
   if (opk == OPK_NL) {

@@ -10,9 +10,9 @@
 //                   box (replicate_particle!, Box.jl:556-566), scan the copies per
 //                   particle (decoupled look-back), write one (cell, particle<<5|image)
 //                   key/value per copy (particle_cell + real_particle_border_case), and
-//                   take each copy's arrival slot in its cell with an atomic counter
+//                   count the copies of every cell (atomic adds)
 //   k_cell_scan     cell starts and the list of cells that contain real particles
-//   k_cell_scatter  copies to their cells' slots in arrival order
+//   k_cell_scatter  copies to their cells' slots in arrival order (atomic cursors)
 //   k_rank_gather   each copy to its rank by value inside its cell (particle-index
 //                   order, the reference's serial order), with its coordinates (SoA),
 //                   particle code and 16-byte candidate record
@@ -359,12 +359,13 @@ __global__ void __launch_bounds__(kBlock) k_emit_b(const DevGeom<T>* __restrict_
 }
 
 // ------------------------------------------------------------------ K1 + scan + K2 in one pass (one system)
-// Each tile of WE_TILE particles wraps its particles and tests their images (wrap_count_at), scans the copy
-// counts in particle order, takes the copy offset of its first particle by decoupled look-back, and writes
-// the key and value of every copy (the cells of copy_cell, in emit_copies' order): the same copies at the
-// same positions as K1, the scan and K2 in turn.  The last tile writes the total number of copies.  Every
-// copy also takes the next slot of its cell's counter (its arrival rank, in `ranks`), and the real copy
-// marks its cell: cell_cf holds {copies, holds a real particle} per cell, zeroed before the launch.
+// Each tile of WE_TILE particles wraps its particles and tests their images (wrap_count_regs), scans the
+// copy counts in particle order, takes the copy offset of its first particle by decoupled look-back, and
+// writes the key and value of every copy (the cells of copy_cell, in emit_copies' order): the same copies at
+// the same positions as K1, the scan and K2 in turn.  The last tile writes the total number of copies.  With
+// COUNT, every copy also adds one to its cell's counter and the real copy marks its cell (cell_cf holds
+// {copies, holds a real particle} per cell, zeroed before the launch); the adds return nothing, so no thread
+// waits on them.  The wrapped positions are stored for the gather; the rest stays in registers.
 constexpr int WE_PPT = 1;
 // One system: above this many expected copies per cell the build sorts by radix instead of counting.
 constexpr double kCountingMaxPerCell = 64.0;
@@ -372,34 +373,29 @@ constexpr int WE_TILE = kBlock * WE_PPT;
 
 template <class T, int N, bool COUNT>
 __global__ void __launch_bounds__(kBlock) k_wrap_emit(DevGeom<T> g, const T* __restrict__ x, int n,
-                                                      T* __restrict__ wrapped, uint32_t* __restrict__ mask,
-                                                      int* __restrict__ ncopy, int cap, uint32_t* __restrict__ keys,
+                                                      T* __restrict__ wrapped, int cap, uint32_t* __restrict__ keys,
                                                       uint32_t* __restrict__ vals, int* __restrict__ total,
                                                       unsigned long long* __restrict__ status,
                                                       unsigned* __restrict__ ticket, int ntiles,
-                                                      int* __restrict__ cell_cf, uint32_t* __restrict__ ranks,
-                                                      int* __restrict__ err) {
+                                                      int* __restrict__ cell_cf, int* __restrict__ err) {
+  static_assert(WE_PPT == 1, "one particle per thread");
   __shared__ int wsum[kBlock / 32 + 1];
   __shared__ int s_tile, s_excl;
   if (threadIdx.x == 0) s_tile = (int)atomicAdd(ticket, 1u);
   __syncthreads();
   const int tile = s_tile;
-  const int i0 = tile * WE_TILE + threadIdx.x * WE_PPT;  // this thread's particles i0 .. i0 + WE_PPT - 1
-  int v[WE_PPT];
+  const int i = tile * WE_TILE + threadIdx.x;  // this thread's particle
+  T p[N];
+  uint32_t m = 0u;
+  int v[1] = {0};
+  if (i < n) {
+    if (!wrap_count_regs<T, N>(g, x, i, p, m, v[0])) atomicOr(err, DERR_NAN);
 #pragma unroll
-  for (int k = 0; k < WE_PPT; k++) {
-    const int i = i0 + k;
-    v[k] = 0;
-    if (i < n) {
-      if (!wrap_count_at<T, N>(g, x, i, wrapped, mask, ncopy)) atomicOr(err, DERR_NAN);
-      v[k] = ncopy[i];
-    }
+    for (int d = 0; d < N; d++) wrapped[(int64_t)i * N + d] = p[d];
   }
-  int cnt[WE_PPT];
-#pragma unroll
-  for (int k = 0; k < WE_PPT; k++) cnt[k] = v[k];
+  int nc = v[0];
   int off = 0;
-  const int agg = block_scan<WE_PPT>(v, off, wsum);
+  const int agg = block_scan<1>(v, off, wsum);
   if (threadIdx.x < 32) {
     const int excl = lookback(tile, agg, status, err);
     if (threadIdx.x == 0) {
@@ -408,27 +404,15 @@ __global__ void __launch_bounds__(kBlock) k_wrap_emit(DevGeom<T> g, const T* __r
     }
   }
   __syncthreads();
-  off += s_excl;
-  // the copies of the particle (the real copy, then the images in increasing image code), walked by the
-  // lanes of a warp together: in each round the lanes whose copies fall in the same cell take consecutive
-  // slots of that cell's counter with one atomic (match_any groups them)
-  static_assert(WE_PPT == 1, "one particle per thread");
-  const int i = i0;
-  const int base = v[0] + off;
-  int nc = (i < n) ? cnt[0] : 0;
+  const int base = v[0] + off + s_excl;
   if (nc > 0 && (base < 0 || base + nc > cap)) {
     atomicOr(err, DERR_COPY_OVERFLOW);  // the build is repeated with the exact size
     nc = 0;
   }
-  T p[N];
-  uint32_t m = 0u;
-  if (nc > 0) {
-#pragma unroll
-    for (int d = 0; d < N; d++) p[d] = wrapped[(int64_t)i * N + d];
-    m = mask[i];
-  }
+  // the copies of the particle (the real copy, then the images in increasing image code), walked by the
+  // lanes of a warp together: in each round the lanes whose copies fall in the same cell add to that cell's
+  // counter with one add (match_any groups them)
   const int lane = threadIdx.x & 31;
-  const unsigned lt = (1u << lane) - 1u;
   const int rounds = __reduce_max_sync(0xffffffffu, nc);
   for (int c = 0; c < rounds; c++) {
     uint32_t key = 0xffffffffu;  // no copy in this round
@@ -445,11 +429,7 @@ __global__ void __launch_bounds__(kBlock) k_wrap_emit(DevGeom<T> g, const T* __r
     }
     if constexpr (COUNT) {
       const unsigned peers = __match_any_sync(0xffffffffu, key);
-      const int leader = __ffs(peers) - 1;
-      int first = 0;
-      if (lane == leader && key != 0xffffffffu) first = atomicAdd(&cell_cf[2 * key], __popc(peers));
-      first = __shfl_sync(0xffffffffu, first, leader);
-      if (key != 0xffffffffu) ranks[base + c] = (uint32_t)(first + __popc(peers & lt));
+      if (key != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&cell_cf[2 * key], __popc(peers));
     }
   }
 }
@@ -458,8 +438,8 @@ __global__ void __launch_bounds__(kBlock) k_wrap_emit(DevGeom<T> g, const T* __r
 // cells' copy counts and real flags, takes both prefixes by decoupled look-back (warp 0 the counts, warp 1
 // the flags; one ticket orders the tiles of both), and writes cell_start, the real flags the pair kernel
 // reads, and the real cells in linear order.  The last tile closes cell_start and writes the number of
-// real cells.
-__global__ void __launch_bounds__(kBlock) k_cell_scan(const int* __restrict__ cell_cf, int ncells,
+// real cells.  Each cell's counters are cleared after reading: they are the scatter's cursors next.
+__global__ void __launch_bounds__(kBlock) k_cell_scan(int* __restrict__ cell_cf, int ncells,
                                                       int* __restrict__ cell_start, int* __restrict__ cell_flags,
                                                       int* __restrict__ real_list, int* __restrict__ n_real,
                                                       unsigned long long* __restrict__ status_c,
@@ -476,7 +456,10 @@ __global__ void __launch_bounds__(kBlock) k_cell_scan(const int* __restrict__ ce
 #pragma unroll
   for (int k = 0; k < SCAN_IPT; k++) {
     int2 cf = make_int2(0, 0);
-    if (c0 + k < ncells) cf = reinterpret_cast<const int2*>(cell_cf)[c0 + k];
+    if (c0 + k < ncells) {
+      cf = reinterpret_cast<const int2*>(cell_cf)[c0 + k];
+      reinterpret_cast<int2*>(cell_cf)[c0 + k] = make_int2(0, 0);
+    }
     vc[k] = cf.x;
     f[k] = cf.y != 0;
     vf[k] = f[k];
@@ -512,27 +495,33 @@ __global__ void __launch_bounds__(kBlock) k_cell_scan(const int* __restrict__ ce
   }
 }
 
-// Every copy (particle order) to its cell's slots, at its arrival rank: sorted keys and values grouped by
-// cell, each cell's values still in arrival order.  The scan words and per-cell counters, read for the last
-// time by k_cell_scan, are cleared for the next build (`zero`, `zwords` 64-bit words).
+// Every copy (particle order) to its cell's slots in arrival order: the copies of one warp that share a cell
+// take consecutive slots with one atomic on the cell's cursor (cleared by k_cell_scan).  The sorted keys and
+// values come out grouped by cell, each cell's values in arrival order.
 __global__ void __launch_bounds__(kBlock) k_cell_scatter(const uint32_t* __restrict__ keys,
                                                          const uint32_t* __restrict__ vals,
-                                                         const uint32_t* __restrict__ ranks,
                                                          const int* __restrict__ n_dev, int cap, int ncells,
-                                                         const int* __restrict__ cell_start,
+                                                         const int* __restrict__ cell_start, int* __restrict__ cursor,
                                                          uint32_t* __restrict__ skeys, uint32_t* __restrict__ svals,
-                                                         unsigned long long* __restrict__ zero, int64_t zwords,
                                                          int* __restrict__ err) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  for (int64_t w = t; w < zwords; w += (int64_t)gridDim.x * blockDim.x) zero[w] = 0ull;
   const int n = min(*n_dev, cap);
-  if (t >= n) return;
-  const uint32_t li = keys[t];
-  if (li >= (uint32_t)ncells) {
-    atomicOr(err, DERR_CELL_RANGE);
-    return;
+  uint32_t li = 0xffffffffu;  // no copy
+  if (t < n) {
+    li = keys[t];
+    if (li >= (uint32_t)ncells) {
+      atomicOr(err, DERR_CELL_RANGE);
+      li = 0xffffffffu;
+    }
   }
-  const int pos = cell_start[li] + (int)ranks[t];
+  const int lane = threadIdx.x & 31;
+  const unsigned peers = __match_any_sync(0xffffffffu, li);
+  const int leader = __ffs(peers) - 1;
+  int first = 0;
+  if (li != 0xffffffffu && lane == leader) first = atomicAdd(&cursor[2 * li], __popc(peers));
+  first = __shfl_sync(0xffffffffu, first, leader);
+  if (li == 0xffffffffu) return;
+  const int pos = cell_start[li] + first + __popc(peers & ((1u << lane) - 1u));
   if (pos < 0 || pos >= n || pos >= cell_start[li + 1]) {
     atomicOr(err, DERR_CELL_RANGE);
     return;
@@ -544,6 +533,8 @@ __global__ void __launch_bounds__(kBlock) k_cell_scatter(const uint32_t* __restr
 // K4 after the counting placement: slot q of the placed list holds a copy of cell li in arrival order; the
 // copy's final slot is the cell's start plus its rank by value in the cell (rank_in_cell), which puts
 // every cell in particle-index order.  The copy's coordinates, code and 16-byte record are written there.
+// The scan words and per-cell counters (`zero`, `zwords` 64-bit words), used for the last time by the
+// scatter, are cleared for the next build.
 template <class T, int N>
 __global__ void __launch_bounds__(kBlock) k_rank_gather(DevGeom<T> g, const T* __restrict__ wrapped,
                                                         const uint32_t* __restrict__ skeys,
@@ -552,8 +543,10 @@ __global__ void __launch_bounds__(kBlock) k_rank_gather(DevGeom<T> g, const T* _
                                                         T* __restrict__ px, T* __restrict__ py, T* __restrict__ pz,
                                                         float4* __restrict__ off, float4* __restrict__ xq,
                                                         int* __restrict__ code, int* __restrict__ cell_flags,
+                                                        unsigned long long* __restrict__ zero, int64_t zwords,
                                                         int* __restrict__ err) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int64_t w = q; w < zwords; w += (int64_t)gridDim.x * blockDim.x) zero[w] = 0ull;
   const int tot = min(cell_start[ncells], cap);
   if (q >= tot) return;
   const uint32_t li = skeys[q];
@@ -825,12 +818,11 @@ int build_counting(Handle& h, SetData& S, const DevGeom<T>& dg, int N, int64_t n
   const size_t zero_bytes = sizeof(unsigned long long) * (size_t)(w_we + w_c + w_f + ncells + 1);
   const void* zero_at = S.cell_count.p;
   if (!S.cell_count.reserve(zero_bytes) || !S.wrapped.reserve(sizeof(T) * N * n) ||
-      !S.mask.reserve(sizeof(uint32_t) * n) || !S.ncopy.reserve(sizeof(int) * (n + 1)) ||
       !S.keys[0].reserve(sizeof(uint32_t) * cap) || !S.keys[1].reserve(sizeof(uint32_t) * cap) ||
       !S.vals[0].reserve(sizeof(uint32_t) * cap) || !S.vals[1].reserve(sizeof(uint32_t) * cap) ||
-      !S.rank.reserve(sizeof(uint32_t) * cap) || !S.px.reserve(sizeof(T) * cap) || !S.py.reserve(sizeof(T) * cap) ||
-      !S.pz.reserve(sizeof(T) * cap) || !S.off.reserve(std::is_same<T, float>::value ? 16 : sizeof(float4) * cap) ||
-      !S.code.reserve(sizeof(int) * cap) || !S.xq.reserve(std::is_same<T, float>::value ? sizeof(float4) * cap : 16))
+      !S.px.reserve(sizeof(T) * cap) || !S.py.reserve(sizeof(T) * cap) || !S.pz.reserve(sizeof(T) * cap) ||
+      !S.off.reserve(std::is_same<T, float>::value ? 16 : sizeof(float4) * cap) || !S.code.reserve(sizeof(int) * cap) ||
+      !S.xq.reserve(std::is_same<T, float>::value ? sizeof(float4) * cap : 16))
     return ERR_NOMEM;
   if (S.cell_count.p != zero_at) S.cell_count_zero = 0;  // a new allocation holds no cleared words
   unsigned long long* z = S.cell_count.as<unsigned long long>();
@@ -838,20 +830,18 @@ int build_counting(Handle& h, SetData& S, const DevGeom<T>& dg, int N, int64_t n
   unsigned long long* st_c = z + w_we;
   unsigned long long* st_f = st_c + w_c;
   int* cell_cf = reinterpret_cast<int*>(st_f + w_f);
-  // cleared by the previous build's scatter unless the region grew or moved
+  // cleared by the previous build's gather unless the region grew or moved
   if (S.cell_count_zero < zero_bytes) CLM_CUDA_TRY(h, cudaMemsetAsync(z, 0, zero_bytes, h.stream));
   S.cell_count_zero = 0;
   int* n_dev = S.copy_off.as<int>() + n;  // total number of copies, on the device
   if (N == 3)
     k_wrap_emit<T, 3, true><<<(unsigned)we_tiles, kBlock, 0, h.stream>>>(
-        dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(), (int)cap,
-        S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev, st_we, reinterpret_cast<unsigned*>(st_we + we_tiles),
-        (int)we_tiles, cell_cf, S.rank.as<uint32_t>(), err);
+        dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), (int)cap, S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
+        n_dev, st_we, reinterpret_cast<unsigned*>(st_we + we_tiles), (int)we_tiles, cell_cf, err);
   else
     k_wrap_emit<T, 2, true><<<(unsigned)we_tiles, kBlock, 0, h.stream>>>(
-        dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(), (int)cap,
-        S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev, st_we, reinterpret_cast<unsigned*>(st_we + we_tiles),
-        (int)we_tiles, cell_cf, S.rank.as<uint32_t>(), err);
+        dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), (int)cap, S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
+        n_dev, st_we, reinterpret_cast<unsigned*>(st_we + we_tiles), (int)we_tiles, cell_cf, err);
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
   k_cell_scan<<<(unsigned)ct, kBlock, 0, h.stream>>>(cell_cf, (int)ncells, S.cell_start.as<int>(), S.cell_flags.as<int>(),
@@ -860,27 +850,27 @@ int build_counting(Handle& h, SetData& S, const DevGeom<T>& dg, int N, int64_t n
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
   const int gc = grid_for(cap);
-  k_cell_scatter<<<gc, kBlock, 0, h.stream>>>(S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), S.rank.as<uint32_t>(),
-                                              n_dev, (int)cap, (int)ncells, S.cell_start.as<int>(),
-                                              S.keys[1].as<uint32_t>(), S.vals[1].as<uint32_t>(), z,
-                                              (int64_t)(zero_bytes / sizeof(unsigned long long)), err);
+  k_cell_scatter<<<gc, kBlock, 0, h.stream>>>(S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev, (int)cap,
+                                              (int)ncells, S.cell_start.as<int>(), cell_cf, S.keys[1].as<uint32_t>(),
+                                              S.vals[1].as<uint32_t>(), err);
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
-  S.cell_count_zero = zero_bytes;
+  const int64_t zwords = (int64_t)(zero_bytes / sizeof(unsigned long long));
   if (N == 3)
     k_rank_gather<T, 3><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[1].as<uint32_t>(),
                                                      S.vals[1].as<uint32_t>(), S.cell_start.as<int>(), (int)ncells,
                                                      (int)cap, (int)n, S.px.as<T>(), S.py.as<T>(), S.pz.as<T>(),
                                                      S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(),
-                                                     S.cell_flags.as<int>(), err);
+                                                     S.cell_flags.as<int>(), z, zwords, err);
   else
     k_rank_gather<T, 2><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[1].as<uint32_t>(),
                                                      S.vals[1].as<uint32_t>(), S.cell_start.as<int>(), (int)ncells,
                                                      (int)cap, (int)n, S.px.as<T>(), S.py.as<T>(), S.pz.as<T>(),
                                                      S.off.as<float4>(), S.xq.as<float4>(), S.code.as<int>(),
-                                                     S.cell_flags.as<int>(), err);
+                                                     S.cell_flags.as<int>(), z, zwords, err);
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
+  S.cell_count_zero = zero_bytes;
   return OK;
 }
 
@@ -965,13 +955,13 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
     CLM_CUDA_TRY(h, cudaMemsetAsync(status, 0, (size_t)(we_tiles + 1) * sizeof(unsigned long long), h.stream));
     unsigned* ticket = reinterpret_cast<unsigned*>(status + we_tiles);
     if (N == 3)
-      k_wrap_emit<T, 3, false><<<we_tiles, kBlock, 0, h.stream>>>(
-          dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(), (int)cap,
-          S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev, status, ticket, we_tiles, nullptr, nullptr, err);
+      k_wrap_emit<T, 3, false><<<we_tiles, kBlock, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), (int)cap,
+                                                                  S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev,
+                                                                  status, ticket, we_tiles, nullptr, err);
     else
-      k_wrap_emit<T, 2, false><<<we_tiles, kBlock, 0, h.stream>>>(
-          dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), S.mask.as<uint32_t>(), S.ncopy.as<int>(), (int)cap,
-          S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev, status, ticket, we_tiles, nullptr, nullptr, err);
+      k_wrap_emit<T, 2, false><<<we_tiles, kBlock, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), (int)cap,
+                                                                  S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev,
+                                                                  status, ticket, we_tiles, nullptr, err);
     CLM_CUDA_TRY(h, cudaGetLastError());
     h.launches++;
   } else {

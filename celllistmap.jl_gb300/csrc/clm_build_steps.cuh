@@ -57,6 +57,7 @@ template <class T> void fill_devgeom(const Geometry<T>& g, int precision, DevGeo
     d.cbmin[i] = g.cbmin[i];
     d.cbmax[i] = g.cbmax[i];
     d.cs[i] = g.cs[i];
+    d.inv_cs[i] = T(1) / g.cs[i];
     d.csf[i] = (float)g.cs[i];
     d.csf_lo[i] = (float)((double)g.cs[i] - (double)d.csf[i]);
     d.cbf_hi[i] = (float)g.cbmin[i];
@@ -72,12 +73,18 @@ template <class T> void fill_devgeom(const Geometry<T>& g, int precision, DevGeo
   d.cutoff_sqr = g.cutoff_sqr;
   d.margin_wide = (double)g.cutoff * (1.0 + std::sqrt((double)g.dim) / 2.0);
   d.nimg = (g.dim == 3) ? 27 : 9;
-  // with exact zeros below the diagonal, component i of an image shift depends only on s_i..s_dim-1, so
-  // the image tests can run dimension by dimension from the last one (same values, fewer tests)
-  d.img_tree = 1;
+  // With exact zeros below the diagonal, component i of an image shift depends only on s_i..s_dim-1, so
+  // the image tests can run dimension by dimension from the last one (img_tree 2); with exact zeros in the
+  // last row only, the last component depends only on s_dim-1 and is tested once per value of it (1).
+  // Same values as testing every image, fewer tests.
+  bool upper = true, last_row = true;
   for (int i = 0; i < g.dim; i++)
     for (int j = 0; j < i; j++)
-      if (g.Mal[i][j] != T(0)) d.img_tree = 0;
+      if (g.Mal[i][j] != T(0)) {
+        upper = false;
+        if (i == g.dim - 1) last_row = false;
+      }
+  d.img_tree = upper ? 2 : (last_row ? 1 : 0);
   d.zero_code = (g.dim == 3) ? 13 : 4;
   // translation_image: x + Mal * s, s in {-1,0,1}^N with the first index fastest
   for (int k = 0; k < d.nimg; k++) {
@@ -100,11 +107,11 @@ template <class T> void fill_devgeom(const Geometry<T>& g, int precision, DevGeo
 }
 
 // ------------------------------------------------------------------ K1: wrap, images, copy count
-// Returns false if the particle has a NaN coordinate (it then gets no copy).
+// Particle i: its wrapped position p, the mask of its images inside the computing box and its number of
+// copies.  Returns false if the particle has a NaN coordinate (it then gets no copy: p = 0, m = 0, cnt = 0).
 template <class T, int N>
-__host__ __device__ __forceinline__ bool wrap_count_at(const DevGeom<T>& g, const T* __restrict__ x, int i,
-                                              T* __restrict__ wrapped, uint32_t* __restrict__ mask,
-                                              int* __restrict__ ncopy) {
+__host__ __device__ __forceinline__ bool wrap_count_regs(const DevGeom<T>& g, const T* __restrict__ x, int i, T* p,
+                                                         uint32_t& mask_out, int& cnt_out) {
   T xi[N];
   bool bad = false;
 #pragma unroll
@@ -114,23 +121,20 @@ __host__ __device__ __forceinline__ bool wrap_count_at(const DevGeom<T>& g, cons
   }
   if (bad) {
 #pragma unroll
-    for (int k = 0; k < N; k++) wrapped[(int64_t)i * N + k] = T(0);
-    mask[i] = 0;
-    ncopy[i] = 0;
+    for (int k = 0; k < N; k++) p[k] = T(0);
+    mask_out = 0;
+    cnt_out = 0;
     return false;
   }
-  T p[N];
   if (g.kind == NONPERIODIC) {
 #pragma unroll
     for (int k = 0; k < N; k++) p[k] = xi[k];
   } else {
     wrap_point<T, N>(g, xi, p);
   }
-#pragma unroll
-  for (int k = 0; k < N; k++) wrapped[(int64_t)i * N + k] = p[k];
   uint32_t m = 0;
   int cnt = 1;
-  if (g.kind != NONPERIODIC && g.img_tree) {
+  if (g.kind != NONPERIODIC && g.img_tree == 2) {
     // image k = (s0+1) + 3(s1+1) [+ 9(s2+1)]: the last component is tested once per s_last, the next
     // once per (s_mid, s_last), the first per image; each test uses the shift of the image itself
     // (equal, for the components tested early, across the images that share their s values)
@@ -169,6 +173,30 @@ __host__ __device__ __forceinline__ bool wrap_count_at(const DevGeom<T>& g, cons
         }
       }
     }
+  } else if (g.kind != NONPERIODIC && g.img_tree == 1) {
+    // the last component once per s_last (equal across the images that share it), then the other
+    // components of each of those images
+#pragma unroll
+    for (int sl = -1; sl <= 1; sl++) {
+      constexpr int NR = (N == 3) ? 9 : 3;  // images per value of s_last
+      const T ql = xadd(p[N - 1], g.shift[NR * (sl + 1)][N - 1]);
+      if (!(g.cbmin[N - 1] <= ql && ql < g.cbmax[N - 1])) continue;
+#pragma unroll
+      for (int r = 0; r < NR; r++) {
+        const int k = NR * (sl + 1) + r;
+        if (k == g.zero_code) continue;
+        bool in = true;
+#pragma unroll
+        for (int d = 0; d < N - 1; d++) {
+          const T q = xadd(p[d], g.shift[k][d]);
+          in = in && (g.cbmin[d] <= q) && (q < g.cbmax[d]);
+        }
+        if (in) {
+          m |= 1u << k;
+          cnt++;
+        }
+      }
+    }
   } else if (g.kind != NONPERIODIC) {
     for (int k = 0; k < g.nimg; k++) {
       if (k == g.zero_code) continue;
@@ -181,16 +209,28 @@ __host__ __device__ __forceinline__ bool wrap_count_at(const DevGeom<T>& g, cons
       }
     }
   }
-  mask[i] = m;
-  ncopy[i] = cnt;
+  mask_out = m;
+  cnt_out = cnt;
   return true;
 }
 
+// The same into the arrays of the build (wrapped positions, image masks, copy counts).
+template <class T, int N>
+__host__ __device__ __forceinline__ bool wrap_count_at(const DevGeom<T>& g, const T* __restrict__ x, int i,
+                                              T* __restrict__ wrapped, uint32_t* __restrict__ mask,
+                                              int* __restrict__ ncopy) {
+  T p[N];
+  uint32_t m = 0;
+  int cnt = 0;
+  const bool ok = wrap_count_regs<T, N>(g, x, i, p, m, cnt);
+#pragma unroll
+  for (int k = 0; k < N; k++) wrapped[(int64_t)i * N + k] = p[k];
+  mask[i] = m;
+  ncopy[i] = cnt;
+  return ok;
+}
+
 // ------------------------------------------------------------------ K2: keys of every copy
-// The copies of particle i (wrapped position p, image mask m, ncp copies) at copy positions base .. base+ncp-1:
-// the key is the copy's cell (the real copy first, with the border-case shift, then the images in
-// increasing image code), the value (i << 5) | image code.  `cb` is the first global cell of the particle's
-// system (0 for one system).
 // The cell of image k of a particle at wrapped position p (k = zero_code: the real copy, with the border-case
 // shift); an out-of-range cell is flagged and mapped to cell 0.
 template <class T, int N>
@@ -211,6 +251,10 @@ __host__ __device__ __forceinline__ int copy_cell(const DevGeom<T>& g, const T* 
   return li;
 }
 
+// The copies of particle i (wrapped position p, image mask m, ncp copies) at copy positions base .. base+ncp-1:
+// the key is the copy's cell (the real copy first, with the border-case shift, then the images in
+// increasing image code), the value (i << 5) | image code.  `cb` is the first global cell of the particle's
+// system (0 for one system).
 template <class T, int N>
 __host__ __device__ __forceinline__ void emit_copies(const DevGeom<T>& g, int cb, const T* p, uint32_t m, int ncp,
                                                      int i, int base, int cap, uint32_t* __restrict__ keys,

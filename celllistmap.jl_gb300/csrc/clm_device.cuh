@@ -56,6 +56,7 @@ template <class T> struct DevGeom {
   T Rinv[3][3];   // rotation back for pair coordinates
   T shift[27][3]; // aligned-cell translation of image code k (first index fastest)
   T cbmin[3], cbmax[3], cs[3];
+  T inv_cs[3];          // RN(1 / cs) in the handle dtype (cell_of's quotient screen)
   T cutoff, cutoff_sqr;
   double margin_wide;   // projection margin when lcell > 1 (computed in double, as the reference does)
   float csf[3];         // cell sizes in FP32 for the prefilter (high part)
@@ -64,7 +65,8 @@ template <class T> struct DevGeom {
   float thr_hi, thr_lo; // FP32 prefilter bounds on d2 (maybe-inside / surely-inside)
   int zero_code;        // image code of the zero shift (13 in 3D, 4 in 2D)
   int nimg;             // 3^dim
-  int img_tree;         // aligned cell exactly upper triangular: image tests can be pruned per dimension
+  int img_tree;         // image-test pruning: 2 aligned cell exactly upper triangular (per dimension), 1 last
+                        // row zero below the diagonal (per value of the last image index), 0 none
 };
 
 // StaticArrays solve (Cramer form), then fastmod1, boundary -> 0, then M*p and R*(.)
@@ -122,15 +124,28 @@ __host__ __device__ __forceinline__ bool in_box(const DevGeom<T>& g, const T* x)
 // floor((x - xmin)/cell_size) + 1 with the border-case shift for real particles
 // (src/internals/Box.jl:499-508, src/internals/CellLists.jl:956-967).  Returns
 // the 0-based linear cell index, or -1 if the cell is outside the grid.
+// Only floor(RN(a / cs)) is used, so it is taken from qa = RN(a * RN(1 / cs)) when qa is more than 4 units in
+// the last place (u = 2^-24 or 2^-53 relative) from an integer: qa is within (2u + u^2)|a/cs| of the real
+// quotient and RN(a / cs) within u of it, so no integer lies between qa and RN(a / cs) and both floors agree.
+// Nearer an integer (a chance of a few in 10^5 per coordinate) the IEEE division decides.  The fractional
+// parts qa - floor(qa) and floor(qa) + 1 - qa are exact or rounded by far less than the margin.
+template <class T> __host__ __device__ __forceinline__ T cell_floor(T a, T cs, T inv_cs) {
+  constexpr T u = std::is_same<T, double>::value ? T(1.1102230246251565e-16) : T(5.9604645e-08f);
+  const T qa = xmul(a, inv_cs);
+  const T fq = xfloor(qa);
+  const T m = T(4) * u * (qa < T(0) ? -qa : qa);
+  if (xsub(qa, fq) > m && xsub(xadd(fq, T(1)), qa) > m) return fq;
+  return xfloor(xdiv(a, cs));
+}
+
 template <class T, int N>
 __host__ __device__ __forceinline__ int cell_of(const DevGeom<T>& g, const T* x, bool real) {
   int li = 0;
 #pragma unroll
   for (int i = N - 1; i >= 0; i--) {
-    T q = xdiv(xsub(x[i], g.cbmin[i]), g.cs[i]);
     // floor in the handle dtype (exact; cell indices are far below 2^24), which keeps Float32 builds off
     // GB300's slow FP64 pipe
-    const T fq = xfloor(q);
+    const T fq = cell_floor<T>(xsub(x[i], g.cbmin[i]), g.cs[i], g.inv_cs[i]);
     if (!(fq >= T(-1) && fq < (T)g.nc[i])) return -1;
     int c = (int)fq + 1;
     if (real) {

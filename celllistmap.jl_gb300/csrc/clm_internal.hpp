@@ -69,7 +69,6 @@ struct SetData {
   DevBuf mask;              // per particle: bit k set if image k lies in the computing box
   DevBuf ncopy, copy_off;   // copies per particle and their exclusive scan
   DevBuf keys[2], vals[2];  // (cell, particle<<5 | image) pairs: particle order, then grouped by cell
-  DevBuf rank;              // one system: each copy's arrival rank in its cell
   DevBuf cell_count;        // one system: scan words and per-cell {copies, real} counters (zeroed per build)
   size_t cell_count_zero = 0;  // bytes of cell_count left cleared by the last build (0: clear before use)
   DevBuf cell_start, cell_flags;
@@ -162,10 +161,6 @@ struct Handle {
   DevBuf outbuf;     // device outputs staged before copying to the caller
   int* pinned = nullptr;       // small pinned host staging area (256 bytes)
   unsigned char* pres = nullptr;  // pinned host copy of a map's results (kResultBytes)
-  // The force accumulators of h.outbuf read as zero up to acc_zero_bytes when acc_zero_ptr == outbuf.p: the
-  // force conversion clears the sums it reads, so the next map need not clear them again.
-  void* acc_zero_ptr = nullptr;
-  size_t acc_zero_bytes = 0;
   cudaEvent_t ev[4] = {};
   float build_ms = 0, map_ms = 0;
   bool build_timing_pending = false;

@@ -128,25 +128,20 @@ __global__ void k_reduce_hist(const unsigned long long* __restrict__ pc, const d
 // forces: sums (rotated frame; 16-byte FP32 records or FP64 components) -> output dtype in the original
 // frame
 template <class T, int N, class FA>
-__global__ void k_forces_out(FA* __restrict__ facc, int64_t n, DevGeom<T> g, int rotate, T* __restrict__ out) {
+__global__ void k_forces_out(const FA* __restrict__ facc, int64_t n, DevGeom<T> g, int rotate, T* __restrict__ out) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  // FP32 sums are rotated in FP32 (the FP64 pipe is slow on this part); FP64 sums in FP64.  The sums read
-  // are cleared for the next map.
+  // FP32 sums are rotated in FP32 (the FP64 pipe is slow on this part); FP64 sums in FP64
   using R = typename std::conditional<std::is_same<FA, float4>::value, float, double>::type;
   R f[N];
   if constexpr (std::is_same<FA, float4>::value) {
     const float4 v = facc[i];
-    facc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     f[0] = v.x;
     f[1] = v.y;
     if (N == 3) f[N - 1] = v.z;
   } else {
 #pragma unroll
-    for (int d = 0; d < N; d++) {
-      f[d] = facc[i * N + d];
-      facc[i * N + d] = 0.0;
-    }
+    for (int d = 0; d < N; d++) f[d] = facc[i * N + d];
   }
   if (rotate) {
     R r[N];
@@ -436,10 +431,7 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
       dst_x = (T*)O->forces_x;
       dst_y = (T*)O->forces_y;
     }
-    // the previous map's conversion left the sums cleared (unless the buffer moved or was used otherwise)
-    const bool zeroed = h.acc_zero_ptr == h.outbuf.p && h.acc_zero_bytes >= acc_bytes;
-    h.acc_zero_ptr = nullptr;  // not cleared until this map's conversion has run
-    if (!zeroed) CLM_CUDA_TRY(h, cudaMemsetAsync(h.outbuf.p, 0, acc_bytes, h.stream));
+    CLM_CUDA_TRY(h, cudaMemsetAsync(h.outbuf.p, 0, acc_bytes, h.stream));
   }
   if (opk == OPK_NL) {
     double vol = std::fabs((double)g.det_in);
@@ -504,10 +496,6 @@ template <class T> int run_pairs(Handle& h, const Geometry<T>& g, int op, const 
     if (nx && dst_x) out(nx, 0, dst_x);
     if (ny && dst_y) out(ny, nx, dst_y);
     CLM_CUDA_TRY(h, cudaGetLastError());
-    if ((nx == 0 || dst_x) && (ny == 0 || dst_y)) {  // every sum was read, so every sum is cleared
-      h.acc_zero_ptr = h.outbuf.p;
-      h.acc_zero_bytes = acc_bytes;
-    }
     if (!O->out_on_device) {
       if (O->forces_x && nx)
         CLM_CUDA_TRY(h, cudaMemcpyAsync(O->forces_x, dst_x, sizeof(T) * nx * N, cudaMemcpyDeviceToHost, h.stream));

@@ -15,7 +15,8 @@
 //   bin_probe,         counts composed over every x-y pair.
 //   near_edge_probe, split_hist_probe
 //   map_nl_visits_probe the self-pair map's candidate visits that reach the hit queue, and its pairs;
-//   noalloc_slots_probe the per-block slots of the allocation-free entry point's scratch.
+//   noalloc_slots_probe the per-block slots of the allocation-free entry point's scratch;
+//   cell_floor_probe   the cell index's floor from the reciprocal product against the IEEE quotient's.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -717,4 +718,20 @@ extern "C" int pair_rule_probe(int cross, int tri, int nonper, int same, int slo
                         idx_j)
              ? 1
              : 0;
+}
+
+// cell_floor (the cell index's floor of (x - xmin) / cs from a product with RN(1 / cs), the IEEE division near
+// integers) against floor of the IEEE quotient, for n numerators; returns the number of disagreements.
+extern "C" int64_t cell_floor_probe(int f64, const double* a, int64_t n, double cs) {
+  int64_t bad = 0;
+  for (int64_t t = 0; t < n; t++) {
+    if (f64) {
+      const double c = cs, inv = 1.0 / c, x = a[t];
+      if (clm::cell_floor<double>(x, c, inv) != std::floor(x / c)) bad++;
+    } else {
+      const float c = (float)cs, inv = 1.0f / c, x = (float)a[t];
+      if (clm::cell_floor<float>(x, c, inv) != std::floor(x / c)) bad++;
+    }
+  }
+  return bad;
 }

@@ -105,6 +105,9 @@ CASES = [
     (3, [[10.0, 2.0, 1.0], [0.0, 11.0, 1.5], [0.0, 0.0, 12.0]], 1.5, 1, 3000, 12.0, -1.0),
     (3, [[10.0, 2.0, 1.0], [0.0, 11.0, 1.5], [0.0, 0.0, 12.0]], 1.5, 3, 2000, 12.0, -1.0),
     (3, [[9.0, 0.5, -1.0], [1.0, 11.0, 0.5], [-0.5, 1.5, 12.0]], 2.0, 2, 2000, 30.0, -15.0),
+    # the benchmark's cell shape: its aligned cell has zeros below the diagonal in the last row only, so the
+    # image tests take their per-s_last pruning (test_geometry.py::test_last_row_pruning_cell)
+    (3, [[10.0, 2.0, 1.0], [0.0, 10.0, 1.5], [0.0, 0.0, 10.0]], 1.5, 1, 3000, 12.0, -1.0),
     (3, None, 1.5, 1, 3000, 12.0, -1.0),
     (3, None, 1.5, 2, 2000, 12.0, -1.0),
     (2, [10.0, 12.0], 1.2, 1, 2000, 12.0, -1.0),
@@ -600,3 +603,28 @@ def test_pair_rule_parts_equal_pair_rule(probe):
                                 assert parts.value == ref, (cross, kind, same, slot_j, ii, ci, cj)
                                 n += 1
     assert n > 3000
+
+
+@pytest.mark.parametrize("f64", [0, 1])
+def test_cell_floor_screen_matches_division(probe, f64):
+    """The build's cell index takes floor((x - xmin) / cs) from the product with RN(1 / cs) unless that product
+    is within 4 ulp of an integer: it must equal the floor of the IEEE quotient everywhere, in particular for
+    numerators a few ulp around multiples of the cell size (where the product and the quotient can round to
+    different sides of an integer) and for random cell sizes."""
+    dt = np.float64 if f64 else np.float32
+    rng = np.random.default_rng(7)
+    lib = probe
+    lib.cell_floor_probe.restype = C.c_int64
+    for cs in [2.5, 0.1, 1.0 / 3.0, 7.77, 0.0123456, 1234.5] + list(rng.uniform(0.01, 100.0, 20)):
+        cs = float(dt(cs))
+        k = np.arange(-3, 200, dtype=np.float64)
+        base = (k * cs).astype(dt)
+        vals = [base]
+        up, dn = base.copy(), base.copy()
+        for _ in range(8):
+            up = np.nextafter(up, dt(np.inf))
+            dn = np.nextafter(dn, dt(-np.inf))
+            vals += [up.copy(), dn.copy()]
+        vals.append(rng.uniform(-3 * cs, 200 * cs, 5000).astype(dt))
+        a = np.ascontiguousarray(np.concatenate(vals).astype(np.float64))
+        assert lib.cell_floor_probe(f64, a.ctypes.data_as(C.c_void_p), a.size, C.c_double(cs)) == 0, cs

@@ -115,3 +115,16 @@ def test_host_geometry_random_sweep(probe, orc, f64, kind):
             np.testing.assert_array_equal(rot.reshape(dim, dim, order="F"), b["rotation"])
         accepted += 1
     assert accepted >= 50
+
+
+@pytest.mark.parametrize("f64", [False, True])
+def test_last_row_pruning_cell(probe, f64):
+    """The benchmark's triclinic cell shape aligns to a matrix with exact zeros below the diagonal in its last
+    row and a nonzero entry in the middle row: the build's image tests then prune on the last image index
+    only (the branch the build-step tests check with this cell)."""
+    M = np.array([[10.0, 2.0, 1.0], [0.0, 10.0, 1.5], [0.0, 0.0, 10.0]])
+    st, nc, arrs = product_box(probe, M, 3, "tri", 1.5, 1, f64)
+    assert st == 0
+    mal = arrs[3].reshape(3, 3, order="F")
+    assert mal[2, 0] == 0.0 and mal[2, 1] == 0.0
+    assert mal[1, 0] != 0.0
