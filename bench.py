@@ -622,7 +622,7 @@ def main():
     build_roof = {"bound": "hbm", "achieved": build_gbs, "peak": hbm_peak, "unit": "GB/s",
                   "frac": (build_gbs / hbm_peak) if (build_gbs and hbm_peak) else None,
                   "bytes_per_build": build_bytes, "copies": copies, "cells": ncells, "build_ms": build_ms,
-                  "note": "cell-list build (K1-K4, sort, scans) as a whole; launch- and latency-bound at this size"}
+                  "note": "cell-list build (wrap and images, cell scan, scatter, in-cell rank and gather) as a whole; latency-bound at this size"}
     # dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel on this workload, from one
     # ncu capture recorded beside its summary in profiles/; a profiler cannot run inside the timed region,
     # so the figure is read from that record rather than measured here
