@@ -26,8 +26,12 @@ template <class T> __device__ __forceinline__ T pos_of(const SetView<T>& S, int 
 // Reciprocal and reciprocal square root for pair VALUES (energies, forces), which are checked against
 // tolerances, never used for pair membership or neighbour-list distances.
 //  FP32: hardware approximations (rcp.approx / rsqrt.approx, a couple of ulp).
-//  FP64: the hardware FP64 estimate refined by two Newton-Raphson steps, each of which squares the
-//        relative error (y <- y + y(1 - x y) for 1/x; y <- y + y/2 (1 - x y^2) for 1/sqrt(x)).
+//  FP64: the hardware FP64 estimate y refined by the second-order terms of a series in its residual e,
+//        which cubes the relative error (from the estimate's ~2^-22 to far below FP64 rounding):
+//        1/x = y / (1 - e) = y (1 + e + e^2 + ...) with e = 1 - x y;
+//        1/sqrt(x) = y (1 - e)^(-1/2) = y (1 + e/2 + 3e^2/8 + ...) with e = 1 - x y^2.
+//        Three and five FP64 instructions, where two Newton-Raphson steps take four and eight: GB300's FP64
+//        pipe takes 16 cycles per warp instruction and bounds the FP64 pair kernels.
 __device__ __forceinline__ float vrcp(float x) {
   float y;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
@@ -38,19 +42,15 @@ __device__ __forceinline__ double vrcp(double x) {
   double y;
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
   double e = fma(-x, y, 1.0);
-  y = fma(y, e, y);
-  e = fma(-x, y, 1.0);
+  e = fma(e, e, e);  // e + e^2
   return fma(y, e, y);
 }
 __device__ __forceinline__ double vrsqrt(double x) {
   double y;
   asm("rsqrt.approx.f64 %0, %1;" : "=d"(y) : "d"(x));
-#pragma unroll
-  for (int k = 0; k < 2; k++) {
-    double e = fma(-x, y * y, 1.0);
-    y = fma(0.5 * y, e, y);
-  }
-  return y;
+  const double e = fma(-x, y * y, 1.0);
+  const double p = fma(0.375, e, 0.5);  // 1/2 + 3e/8
+  return fma(y * e, p, y);
 }
 
 // 1/sqrt(x) for the FP64 radial-histogram term: the hardware estimate refined by one Newton-Raphson step,
