@@ -103,10 +103,10 @@ __device__ __forceinline__ int lookback(int tile, int agg, unsigned long long* _
   return excl;
 }
 
-// Exclusive scan of the block's kBlock x IPT values v (thread-major), in place; returns the block aggregate
-// to every thread and leaves in `thread_off` the exclusive prefix of this thread's first value.  wsum holds
-// kBlock / 32 + 1 ints.
-template <int IPT>
+// Exclusive scan of the block's NT x IPT values v (thread-major), in place; returns the block aggregate to
+// every thread and leaves in `thread_off` the exclusive prefix of this thread's first value.  wsum holds
+// NT / 32 + 1 ints (NT <= 1024).
+template <int IPT, int NT = kBlock>
 __device__ __forceinline__ int block_scan(int (&v)[IPT], int& thread_off, int* wsum) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int s = 0;
@@ -126,19 +126,19 @@ __device__ __forceinline__ int block_scan(int (&v)[IPT], int& thread_off, int* w
   __syncthreads();
   int agg = 0;
   if (warp == 0) {
-    int w = (lane < kBlock / 32) ? wsum[lane] : 0;
+    int w = (lane < NT / 32) ? wsum[lane] : 0;
     int wi = w;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       int y = __shfl_up_sync(0xffffffffu, wi, o);
       if (lane >= o) wi += y;
     }
-    if (lane < kBlock / 32) wsum[lane] = wi - w;
-    const int a = __shfl_sync(0xffffffffu, wi, kBlock / 32 - 1);
-    if (lane == 0) wsum[kBlock / 32] = a;
+    if (lane < NT / 32) wsum[lane] = wi - w;
+    const int a = __shfl_sync(0xffffffffu, wi, NT / 32 - 1);
+    if (lane == 0) wsum[NT / 32] = a;
   }
   __syncthreads();
-  agg = wsum[kBlock / 32];
+  agg = wsum[NT / 32];
   thread_off = (incl - s) + wsum[warp];
   return agg;
 }
@@ -369,17 +369,18 @@ __global__ void __launch_bounds__(kBlock) k_emit_b(const DevGeom<T>* __restrict_
 constexpr int WE_PPT = 1;
 // One system: above this many expected copies per cell the build sorts by radix instead of counting.
 constexpr double kCountingMaxPerCell = 64.0;
-constexpr int WE_TILE = kBlock * WE_PPT;
+constexpr int WE_BLOCK = 256;  // threads (particles) per tile of the wrap kernel
+constexpr int WE_TILE = WE_BLOCK * WE_PPT;
 
 template <class T, int N, bool COUNT>
-__global__ void __launch_bounds__(kBlock) k_wrap_emit(DevGeom<T> g, const T* __restrict__ x, int n,
+__global__ void __launch_bounds__(WE_BLOCK) k_wrap_emit(DevGeom<T> g, const T* __restrict__ x, int n,
                                                       T* __restrict__ wrapped, int cap, uint32_t* __restrict__ keys,
                                                       uint32_t* __restrict__ vals, int* __restrict__ total,
                                                       unsigned long long* __restrict__ status,
                                                       unsigned* __restrict__ ticket, int ntiles,
                                                       int* __restrict__ cell_cf, int* __restrict__ err) {
   static_assert(WE_PPT == 1, "one particle per thread");
-  __shared__ int wsum[kBlock / 32 + 1];
+  __shared__ int wsum[WE_BLOCK / 32 + 1];
   __shared__ int s_tile, s_excl;
   if (threadIdx.x == 0) s_tile = (int)atomicAdd(ticket, 1u);
   __syncthreads();
@@ -395,7 +396,7 @@ __global__ void __launch_bounds__(kBlock) k_wrap_emit(DevGeom<T> g, const T* __r
   }
   int nc = v[0];
   int off = 0;
-  const int agg = block_scan<1>(v, off, wsum);
+  const int agg = block_scan<1, WE_BLOCK>(v, off, wsum);
   if (threadIdx.x < 32) {
     const int excl = lookback(tile, agg, status, err);
     if (threadIdx.x == 0) {
@@ -835,11 +836,11 @@ int build_counting(Handle& h, SetData& S, const DevGeom<T>& dg, int N, int64_t n
   S.cell_count_zero = 0;
   int* n_dev = S.copy_off.as<int>() + n;  // total number of copies, on the device
   if (N == 3)
-    k_wrap_emit<T, 3, true><<<(unsigned)we_tiles, kBlock, 0, h.stream>>>(
+    k_wrap_emit<T, 3, true><<<(unsigned)we_tiles, WE_BLOCK, 0, h.stream>>>(
         dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), (int)cap, S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
         n_dev, st_we, reinterpret_cast<unsigned*>(st_we + we_tiles), (int)we_tiles, cell_cf, err);
   else
-    k_wrap_emit<T, 2, true><<<(unsigned)we_tiles, kBlock, 0, h.stream>>>(
+    k_wrap_emit<T, 2, true><<<(unsigned)we_tiles, WE_BLOCK, 0, h.stream>>>(
         dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), (int)cap, S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
         n_dev, st_we, reinterpret_cast<unsigned*>(st_we + we_tiles), (int)we_tiles, cell_cf, err);
   CLM_CUDA_TRY(h, cudaGetLastError());
@@ -955,11 +956,11 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
     CLM_CUDA_TRY(h, cudaMemsetAsync(status, 0, (size_t)(we_tiles + 1) * sizeof(unsigned long long), h.stream));
     unsigned* ticket = reinterpret_cast<unsigned*>(status + we_tiles);
     if (N == 3)
-      k_wrap_emit<T, 3, false><<<we_tiles, kBlock, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), (int)cap,
+      k_wrap_emit<T, 3, false><<<we_tiles, WE_BLOCK, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), (int)cap,
                                                                   S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev,
                                                                   status, ticket, we_tiles, nullptr, err);
     else
-      k_wrap_emit<T, 2, false><<<we_tiles, kBlock, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), (int)cap,
+      k_wrap_emit<T, 2, false><<<we_tiles, WE_BLOCK, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), (int)cap,
                                                                   S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev,
                                                                   status, ticket, we_tiles, nullptr, err);
     CLM_CUDA_TRY(h, cudaGetLastError());
