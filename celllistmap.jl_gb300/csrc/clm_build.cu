@@ -367,8 +367,12 @@ __global__ void __launch_bounds__(kBlock) k_emit_b(const DevGeom<T>* __restrict_
 // {copies, holds a real particle} per cell, zeroed before the launch); the adds return nothing, so no thread
 // waits on them.  The wrapped positions are stored for the gather; the rest stays in registers.
 constexpr int WE_PPT = 1;
-// One system: above this many expected copies per cell the build sorts by radix instead of counting.
+// One system: above this many expected copies per cell the build sorts by radix instead of counting; a set
+// whose counting build met a cell of more than kRadixAbovePerCell copies (clustered particles, which the
+// uniform-density estimate misses) is built by radix from then on: the in-cell ranking costs a cell's size
+// per copy, the radix sort does not depend on it.
 constexpr double kCountingMaxPerCell = 64.0;
+constexpr int kRadixAbovePerCell = 1024;
 constexpr int WE_BLOCK = 256;  // threads (particles) per tile of the wrap kernel
 constexpr int WE_TILE = WE_BLOCK * WE_PPT;
 
@@ -386,6 +390,7 @@ __global__ void __launch_bounds__(WE_BLOCK) k_wrap_emit(DevGeom<T> g, const T* _
   __syncthreads();
   const int tile = s_tile;
   const int i = tile * WE_TILE + threadIdx.x;  // this thread's particle
+  if (COUNT && tile == 0 && threadIdx.x == 0) total[1] = 0;  // the largest cell, found by k_cell_scan
   T p[N];
   uint32_t m = 0u;
   int v[1] = {0};
@@ -443,6 +448,7 @@ __global__ void __launch_bounds__(WE_BLOCK) k_wrap_emit(DevGeom<T> g, const T* _
 __global__ void __launch_bounds__(kBlock) k_cell_scan(int* __restrict__ cell_cf, int ncells,
                                                       int* __restrict__ cell_start, int* __restrict__ cell_flags,
                                                       int* __restrict__ real_list, int* __restrict__ n_real,
+                                                      int* __restrict__ max_cell,
                                                       unsigned long long* __restrict__ status_c,
                                                       unsigned long long* __restrict__ status_f,
                                                       unsigned* __restrict__ ticket, int ntiles,
@@ -464,6 +470,13 @@ __global__ void __launch_bounds__(kBlock) k_cell_scan(int* __restrict__ cell_cf,
     vc[k] = cf.x;
     f[k] = cf.y != 0;
     vf[k] = f[k];
+  }
+  {
+    int m = 0;  // the largest cell of this thread's, then of the warp's
+#pragma unroll
+    for (int k = 0; k < SCAN_IPT; k++) m = max(m, vc[k]);
+    m = __reduce_max_sync(0xffffffffu, m);
+    if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(max_cell, m);
   }
   int off_c = 0, off_f = 0;
   const int agg_c = block_scan<SCAN_IPT>(vc, off_c, wsum_c);
@@ -846,7 +859,8 @@ int build_counting(Handle& h, SetData& S, const DevGeom<T>& dg, int N, int64_t n
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
   k_cell_scan<<<(unsigned)ct, kBlock, 0, h.stream>>>(cell_cf, (int)ncells, S.cell_start.as<int>(), S.cell_flags.as<int>(),
-                                                     S.real_list.as<int>(), S.real_scan.as<int>() + ncells, st_c, st_f,
+                                                     S.real_list.as<int>(), S.real_scan.as<int>() + ncells,
+                                                     S.copy_off.as<int>() + n + 1, st_c, st_f,
                                                      reinterpret_cast<unsigned*>(st_c + ct), (int)ct, err);
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
@@ -895,7 +909,7 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
   int* err = h.err.as<int>();
   if (!S.cell_start.reserve(sizeof(int) * (ncells + 1)) || !S.cell_flags.reserve(sizeof(int) * (ncells + 1)) ||
       !S.real_scan.reserve(sizeof(int) * (ncells + 1)) || !S.real_list.reserve(sizeof(int) * (ncells + 1)) ||
-      !S.copy_off.reserve(sizeof(int) * (n + 1)))
+      !S.copy_off.reserve(sizeof(int) * (n + 2)))  // copies per particle scan, total, largest cell
     return ERR_NOMEM;
   if (n == 0) CLM_CUDA_TRY(h, cudaMemsetAsync(S.cell_flags.p, 0, sizeof(int) * (ncells + 1), h.stream));
   S.built = true;
@@ -906,6 +920,7 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
     CLM_CUDA_TRY(h, cudaMemsetAsync(S.real_scan.p, 0, sizeof(int) * (ncells + 1), h.stream));
     CLM_CUDA_TRY(h, cudaMemsetAsync(S.copy_off.p, 0, sizeof(int), h.stream));
     S.cap_used = 0;
+    S.counted = false;
     return OK;
   }
   int64_t cap = 0;
@@ -928,8 +943,9 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
   // One system: the counting build, unless the cells are expected to be crowded (copies per cell from the
   // uniform-density capacity): its in-cell ranking takes a cell's size in steps per copy, where the radix
   // sort's cost does not depend on it.  Either gives the same cell list.
-  const bool crowded = !batch && (double)cap > kCountingMaxPerCell * (double)ncells;
-  if (!batch && !crowded) return build_counting<T>(h, S, dg, N, n, ncells, cap);
+  const bool crowded = !batch && (S.prefer_radix || (double)cap > kCountingMaxPerCell * (double)ncells);
+  S.counted = !batch && !crowded;
+  if (S.counted) return build_counting<T>(h, S, dg, N, n, ncells, cap);
   // the radix path's gather sets the real flags of the cells it fills
   CLM_CUDA_TRY(h, cudaMemsetAsync(S.cell_flags.p, 0, sizeof(int) * (ncells + 1), h.stream));
   const int ntiles = (int)((cap + RS_TILE - 1) / RS_TILE);
@@ -1076,6 +1092,9 @@ int enqueue_build_totals(Handle& h) {
                                     cudaMemcpyDeviceToHost, h.stream));
     CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 33 + 2 * s, S.real_scan.as<int>() + S.ncells, sizeof(int),
                                     cudaMemcpyDeviceToHost, h.stream));
+    if (S.counted)
+      CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 44 + s, S.copy_off.as<int>() + S.n + 1, sizeof(int),
+                                      cudaMemcpyDeviceToHost, h.stream));
   }
   CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 40, h.err.p, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
   return OK;
@@ -1100,6 +1119,7 @@ int check_build_totals(Handle& h, bool* overflow) {
     }
     S.n_copies = h.pinned[32 + 2 * s];
     S.n_real_cells = h.pinned[33 + 2 * s];
+    if (S.counted && h.pinned[44 + s] > kRadixAbovePerCell) S.prefer_radix = true;
     S.pending = false;
     if (S.n_copies > S.cap_used || (errw & DERR_COPY_OVERFLOW)) {
       S.copy_cap = S.n_copies + S.n_copies / 8 + 1024;

@@ -84,6 +84,8 @@ struct SetData {
   int64_t copy_cap = 0;      // capacity for copies learned from previous builds
   int64_t cap_used = 0;      // capacity used by the last build
   bool pending = false;      // the device totals of the last build were not read back yet
+  bool counted = false;      // the last build was the counting build (its largest cell is read back)
+  bool prefer_radix = false; // a counting build met a cell of more than kRadixAbovePerCell copies
   int64_t n_cells_with_particles = 0;
   int64_t ncells = 0;
 };

@@ -371,6 +371,50 @@ def test_copy_capacity_overflow_rebuilds(clm, orc, via_run):
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_clustered_cells_switch_to_the_radix_build(clm, orc, dtype):
+    """A blob of 3000 particles inside one or two cells of a large box: the uniform-density estimate picks the
+    counting build, which then finds cells of more than 1024 copies, and the set's later builds sort by
+    radix (more launches per build than the counting build of a uniform set of the same size).  Every
+    build's cell list (copy by copy) and neighbour list must equal the oracle's."""
+    import ctypes as C
+    L = clm._abi.load()
+
+    def launches(sys_):
+        v = C.c_int64()
+        assert L.clm_stats(sys_._handle.h, C.byref(v)) == 0
+        return v.value
+
+    def step_launches(sys_, xx):
+        sys_.update(xpositions=xx)  # the next map rebuilds
+        n0 = launches(sys_)
+        got = clm.pairwise(clm.NeighborList(), sys_)
+        return got, launches(sys_) - n0
+
+    rng = np.random.default_rng(21)
+    uc = [20.0, 20.0, 20.0]
+    kw = dict(unitcell=uc, cutoff=1.0, dtype=dtype)
+    u = (20.0 * rng.random((3000, 3))).astype(dtype)  # the same number of particles, uniform: counting build
+    su = clm.ParticleSystem(xpositions=u, unitcell=uc, cutoff=1.0, dtype=dtype)
+    _, counting = step_launches(su, u)
+    su.close()
+    x = (10.2 + 0.5 * rng.random((3000, 3))).astype(dtype)
+    s = clm.ParticleSystem(xpositions=x, unitcell=uc, cutoff=1.0, dtype=dtype)
+    per_step = []
+    for step in range(3):
+        x = (x + dtype(0.01)).astype(dtype)
+        got, nl = step_launches(s, x)
+        per_step.append(nl)
+        assert_same_pairs(orc, got, orc.run("nl", x, **kw))
+        cl = s.fetch_celllist(0)
+        oc = orc.celllist(x, **kw)
+        np.testing.assert_array_equal(cl["cell"], oc["cell"])
+        np.testing.assert_array_equal(cl["index"], oc["index"])
+        np.testing.assert_array_equal(cl["coords"].astype(np.float64), oc["coords"])
+    assert per_step[-1] > counting, (per_step, counting)
+    s.close()
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
 def test_many_scan_tiles(clm, orc, dtype):
     """~200k particles of the headline geometry: the build's scans run over ~100 tiles (copy offsets) and
     ~170 tiles x 512 digits (radix histograms), so the single-pass look-back is exercised across many
