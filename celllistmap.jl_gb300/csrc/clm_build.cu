@@ -1,4 +1,4 @@
-// Cell-list construction on the GPU (K1-K4).
+// Cell-list construction on the GPU.
 //
 // Replaces UpdateCellList! (src/internals/CellLists.jl:727-927, serial order
 // of add_particles! 940-950 and add_particle_to_celllist! 983-1057) and the
@@ -18,9 +18,9 @@
 //                   particle code and 16-byte candidate record
 // One system with crowded cells (more than kCountingMaxPerCell copies per cell
 // expected): k_wrap_emit without the counters, a stable LSD radix sort of the keys by
-// cell, K4 k_gather (cell starts from the sorted keys) and k_compact_1pass.
-// Batches (global cell index over all systems): K1 k_wrap_count_b, a scan of the
-// copies, K2 k_emit_b, the radix sort, K4 k_gather_b, and the real-cell scan and
+// cell, k_gather (cell starts from the sorted keys) and k_compact_1pass.
+// Batches (global cell index over all systems): k_wrap_count_b, a scan of the
+// copies, k_emit_b, the radix sort, k_gather_b, and the real-cell scan and
 // compaction.
 //
 // Every kernel bounds-checks its indices; inconsistencies set bits of the
@@ -301,18 +301,9 @@ __global__ void __launch_bounds__(kBlock) k_rs_scatter(const uint32_t* __restric
   }
 }
 
-// ------------------------------------------------------------------ K1: wrap, images, copy count
+// ------------------------------------------------------------------ batches: wrap, images, copy count
 // (the per-particle step, wrap_count_at, is in clm_build_steps.cuh)
-template <class T, int N>
-__global__ void __launch_bounds__(kBlock) k_wrap_count(DevGeom<T> g, const T* __restrict__ x, int n,
-                                                       T* __restrict__ wrapped, uint32_t* __restrict__ mask,
-                                                       int* __restrict__ ncopy, int* __restrict__ err) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  if (!wrap_count_at<T, N>(g, x, i, wrapped, mask, ncopy)) atomicOr(err, DERR_NAN);
-}
-
-// Batches: each particle uses its system's geometry; a NaN marks only its system; particles of systems
+// Each particle uses its system's geometry; a NaN marks only its system; particles of systems
 // that failed the unit-cell check get no copies.
 template <class T, int N>
 __global__ void __launch_bounds__(kBlock) k_wrap_count_b(const DevGeom<T>* __restrict__ gtab,
@@ -333,18 +324,7 @@ __global__ void __launch_bounds__(kBlock) k_wrap_count_b(const DevGeom<T>* __res
   if (!wrap_count_at<T, N>(g, x, i, wrapped, mask, ncopy)) atomicOr(&sys_err[s], DERR_NAN);
 }
 
-// ------------------------------------------------------------------ K2: keys, histogram, real flags
-template <class T, int N>
-__global__ void __launch_bounds__(kBlock) k_emit(DevGeom<T> g, const T* __restrict__ wrapped,
-                                                 const uint32_t* __restrict__ mask, const int* __restrict__ ncopy,
-                                                 const int* __restrict__ copy_off, int n, int cap,
-                                                 uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
-                                                 int* __restrict__ err) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  emit_at<T, N>(g, 0, wrapped, mask, ncopy, copy_off, i, cap, keys, vals, err);
-}
-
+// ------------------------------------------------------------------ batches: keys of every copy
 template <class T, int N>
 __global__ void __launch_bounds__(kBlock) k_emit_b(const DevGeom<T>* __restrict__ gtab, const int* __restrict__ psys,
                                                    const int* __restrict__ cbase, const T* __restrict__ wrapped,
@@ -358,11 +338,11 @@ __global__ void __launch_bounds__(kBlock) k_emit_b(const DevGeom<T>* __restrict_
   emit_at<T, N>(gtab[s], cbase[s], wrapped, mask, ncopy, copy_off, i, cap, keys, vals, err);
 }
 
-// ------------------------------------------------------------------ K1 + scan + K2 in one pass (one system)
+// ------------------------------------------------------------------ one system: wrap, scan and keys in one pass
 // Each tile of WE_TILE particles wraps its particles and tests their images (wrap_count_regs), scans the
 // copy counts in particle order, takes the copy offset of its first particle by decoupled look-back, and
 // writes the key and value of every copy (the cells of copy_cell, in emit_copies' order): the same copies at
-// the same positions as K1, the scan and K2 in turn.  The last tile writes the total number of copies.  With
+// the same positions as a separate wrap kernel, scan and key kernel would.  The last tile writes the total number of copies.  With
 // COUNT, every copy also adds one to its cell's counter and the real copy marks its cell (cell_cf holds
 // {copies, holds a real particle} per cell, zeroed before the launch); the adds return nothing, so no thread
 // waits on them.  The wrapped positions are stored for the gather; the rest stays in registers.
@@ -544,7 +524,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_scatter(const uint32_t* __restr
   svals[pos] = vals[t];
 }
 
-// K4 after the counting placement: slot q of the placed list holds a copy of cell li in arrival order; the
+// The gather after the counting placement: slot q of the placed list holds a copy of cell li in arrival order; the
 // copy's final slot is the cell's start plus its rank by value in the cell (rank_in_cell), which puts
 // every cell in particle-index order.  The copy's coordinates, code and 16-byte record are written there.
 // The scan words and per-cell counters (`zero`, `zwords` 64-bit words), used for the last time by the
@@ -617,8 +597,8 @@ __global__ void __launch_bounds__(kBlock) k_compact_1pass(const int* __restrict_
     if (f[k]) list[v[k] + off] = c0 + k;
 }
 
-// ------------------------------------------------------------------ K4: gather in cell order
-// One system after the radix sort: copy t of the sorted keys
+// ------------------------------------------------------------------ gather in cell order after the radix sort
+// One system: copy t of the sorted keys
 template <class T, int N>
 __global__ void __launch_bounds__(kBlock) k_gather(DevGeom<T> g, const T* __restrict__ wrapped,
                                                    const uint32_t* __restrict__ skeys,
@@ -804,7 +784,7 @@ template <class T> int set_limits(Handle& h, T* lo, T* hi) {
 
 // Capacity for the copies (reals + images) of a set: the largest of the previous build's count and the
 // uniform-density estimate (computing-box volume / unit-cell volume), with a margin.  The build never
-// waits for the device: if the copies exceed the capacity, k_emit flags it, the result is discarded at
+// waits for the device: if the copies exceed the capacity, the key kernel flags it, the result is discarded at
 // the next host synchronization and the build is repeated with the exact size.
 template <class T> int64_t copy_capacity(const SetData& S, const Geometry<T>& g) {
   const int64_t n = S.n;
@@ -818,8 +798,8 @@ template <class T> int64_t copy_capacity(const SetData& S, const Geometry<T>& g)
 }
 
 // One system: the counting build.  One zeroed region holds the look-back words of the two single-pass
-// scans and the per-cell {copies, real} counters; then four launches: wrap + copy offsets + keys + arrival
-// ranks (k_wrap_emit), cell starts + real-cell list (k_cell_scan), placement by arrival (k_cell_scatter),
+// scans and the per-cell {copies, real} counters; then four launches: wrap + copy offsets + keys + cell
+// counts (k_wrap_emit), cell starts + real-cell list (k_cell_scan), placement by arrival (k_cell_scatter),
 // and the gather at each copy's rank in its cell (k_rank_gather).
 template <class T>
 int build_counting(Handle& h, SetData& S, const DevGeom<T>& dg, int N, int64_t n, int64_t ncells, int64_t cap) {

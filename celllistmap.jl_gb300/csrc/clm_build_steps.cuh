@@ -1,4 +1,4 @@
-// Per-particle and per-copy steps of the cell-list build (K1 wrap and images, K2 keys, K4 gather) and the
+// Per-particle and per-copy steps of the cell-list build (wrap and images, keys, in-cell rank, gather) and the
 // device copy of the box geometry.  The build kernels (clm_build.cu) call them on the device; the CPU tests
 // compile the same functions for the host (g++ with -ffp-contract=off) and compare the copies, cells and
 // coordinates they give with the oracle's serial cell list, without a GPU.
@@ -106,7 +106,7 @@ template <class T> void fill_devgeom(const Geometry<T>& g, int precision, DevGeo
   d.thr_lo = std::nextafter((float)(c2 * (1.0 - std::ldexp(1.0, -13))), 0.0f);
 }
 
-// ------------------------------------------------------------------ K1: wrap, images, copy count
+// ------------------------------------------------------------------ wrap, images, copy count
 // Particle i: its wrapped position p, the mask of its images inside the computing box and its number of
 // copies.  Returns false if the particle has a NaN coordinate (it then gets no copy: p = 0, m = 0, cnt = 0).
 template <class T, int N>
@@ -230,7 +230,7 @@ __host__ __device__ __forceinline__ bool wrap_count_at(const DevGeom<T>& g, cons
   return ok;
 }
 
-// ------------------------------------------------------------------ K2: keys of every copy
+// ------------------------------------------------------------------ keys of every copy
 // The cell of image k of a particle at wrapped position p (k = zero_code: the real copy, with the border-case
 // shift); an out-of-range cell is flagged and mapped to cell 0.
 template <class T, int N>
@@ -289,7 +289,7 @@ __host__ __device__ __forceinline__ void emit_at(const DevGeom<T>& g, int cb, co
   emit_copies<T, N>(g, cb, p, mask[i], ncopy[i], i, copy_off[i], cap, keys, vals, err);
 }
 
-// ------------------------------------------------------------------ K4: gather in cell order
+// ------------------------------------------------------------------ gather in cell order
 // origin of cell c along one axis as an unevaluated float pair (hi + lo): cbmin + cs*(c-1) with the
 // product and the sum carried exactly (TwoProduct with an FMA, TwoSum)
 __host__ __device__ __forceinline__ void origin_ff(float cb_hi, float cb_lo, float cs_hi, float cs_lo, int c1, float& hi,
