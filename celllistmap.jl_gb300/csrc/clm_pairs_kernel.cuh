@@ -1,4 +1,4 @@
-// Cell-pair map kernel (K5 self, K6 cross, K7 operator epilogues), included by the translation units
+// Cell-pair map kernel (self and cross pairs, operator epilogues), included by the translation units
 // that instantiate it.
 //
 // Replaces _pairwise! and its inner loops:
