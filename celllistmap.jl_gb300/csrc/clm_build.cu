@@ -356,13 +356,13 @@ constexpr int kRadixAbovePerCell = 1024;
 constexpr int WE_BLOCK = 256;  // threads (particles) per tile of the wrap kernel
 constexpr int WE_TILE = WE_BLOCK * WE_PPT;
 
-template <class T, int N, bool COUNT>
+template <class T, int N>
 __global__ void __launch_bounds__(WE_BLOCK) k_wrap_emit(DevGeom<T> g, const T* __restrict__ x, int n,
                                                       T* __restrict__ wrapped, int cap, uint32_t* __restrict__ keys,
                                                       uint32_t* __restrict__ vals, int* __restrict__ total,
                                                       unsigned long long* __restrict__ status,
                                                       unsigned* __restrict__ ticket, int ntiles,
-                                                      int* __restrict__ cell_cf, int* __restrict__ err) {
+                                                      int* __restrict__ err) {
   static_assert(WE_PPT == 1, "one particle per thread");
   __shared__ int wsum[WE_BLOCK / 32 + 1];
   __shared__ int s_tile, s_excl;
@@ -370,7 +370,6 @@ __global__ void __launch_bounds__(WE_BLOCK) k_wrap_emit(DevGeom<T> g, const T* _
   __syncthreads();
   const int tile = s_tile;
   const int i = tile * WE_TILE + threadIdx.x;  // this thread's particle
-  if (COUNT && tile == 0 && threadIdx.x == 0) total[1] = 0;  // the largest cell, found by k_cell_scan
   T p[N];
   uint32_t m = 0u;
   int v[1] = {0};
@@ -395,6 +394,54 @@ __global__ void __launch_bounds__(WE_BLOCK) k_wrap_emit(DevGeom<T> g, const T* _
     atomicOr(err, DERR_COPY_OVERFLOW);  // the build is repeated with the exact size
     nc = 0;
   }
+  // the copies of the particle: the real copy, then the images in increasing image code
+  for (int c = 0; c < nc; c++) {
+    int k = g.zero_code;
+    if (c > 0) {
+      k = lowest_bit(m);
+      m &= m - 1u;
+    }
+    keys[base + c] = (uint32_t)copy_cell<T, N>(g, p, k, err);
+    vals[base + c] = ((uint32_t)i << 5) | (uint32_t)k;
+  }
+}
+
+// One system, counting build: the same wrap, image tests and keys, with the copies of each tile of
+// WE_BLOCK particles in the tile's own range of `slots` staging slots (the in-cell ranking orders a cell by
+// value, so the copies need no position in particle order, and no tile waits on an earlier one).  Each
+// tile writes its number of copies; a tile with more copies than slots writes none and flags
+// DERR_TILE_OVERFLOW (the build is repeated with more slots).  Every copy adds one to its cell's counter
+// (the lanes of a warp whose copies share a cell with one add) and the real copy marks its cell; cell_cf
+// holds {copies, holds a real particle} per cell, zeroed before the launch.  Tile 0 clears the word of
+// the largest cell that k_cell_scan finds.
+template <class T, int N>
+__global__ void __launch_bounds__(WE_BLOCK) k_wrap_stage(DevGeom<T> g, const T* __restrict__ x, int n,
+                                                       T* __restrict__ wrapped, int slots, uint32_t* __restrict__ keys,
+                                                       uint32_t* __restrict__ vals, int* __restrict__ tile_count,
+                                                       int* __restrict__ cell_cf, int* __restrict__ max_cell,
+                                                       int* __restrict__ err) {
+  static_assert(WE_PPT == 1, "one particle per thread");
+  __shared__ int wsum[WE_BLOCK / 32 + 1];
+  const int tile = blockIdx.x;
+  const int i = tile * WE_TILE + threadIdx.x;  // this thread's particle
+  if (tile == 0 && threadIdx.x == 0) *max_cell = 0;
+  T p[N];
+  uint32_t m = 0u;
+  int v[1] = {0};
+  if (i < n) {
+    if (!wrap_count_regs<T, N>(g, x, i, p, m, v[0])) atomicOr(err, DERR_NAN);
+#pragma unroll
+    for (int d = 0; d < N; d++) wrapped[(int64_t)i * N + d] = p[d];
+  }
+  int nc = v[0];
+  int off = 0;
+  const int agg = block_scan<1, WE_BLOCK>(v, off, wsum);
+  if (agg > slots) nc = 0;  // the whole tile (agg is the tile's)
+  if (threadIdx.x == 0) {
+    tile_count[tile] = (agg > slots) ? 0 : agg;
+    if (agg > slots) atomicOr(err, DERR_TILE_OVERFLOW);
+  }
+  const int64_t base = (int64_t)tile * slots + v[0] + off;
   // the copies of the particle (the real copy, then the images in increasing image code), walked by the
   // lanes of a warp together: in each round the lanes whose copies fall in the same cell add to that cell's
   // counter with one add (match_any groups them)
@@ -411,12 +458,10 @@ __global__ void __launch_bounds__(WE_BLOCK) k_wrap_emit(DevGeom<T> g, const T* _
       key = (uint32_t)copy_cell<T, N>(g, p, k, err);
       keys[base + c] = key;
       vals[base + c] = ((uint32_t)i << 5) | (uint32_t)k;
-      if (COUNT && c == 0) cell_cf[2 * key + 1] = 1;  // the cell holds a real particle
+      if (c == 0) cell_cf[2 * key + 1] = 1;  // the cell holds a real particle
     }
-    if constexpr (COUNT) {
-      const unsigned peers = __match_any_sync(0xffffffffu, key);
-      if (key != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&cell_cf[2 * key], __popc(peers));
-    }
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    if (key != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&cell_cf[2 * key], __popc(peers));
   }
 }
 
@@ -489,39 +534,47 @@ __global__ void __launch_bounds__(kBlock) k_cell_scan(int* __restrict__ cell_cf,
   }
 }
 
-// Every copy (particle order) to its cell's slots in arrival order: the copies of one warp that share a cell
-// take consecutive slots with one atomic on the cell's cursor (cleared by k_cell_scan).  The sorted keys and
-// values come out grouped by cell, each cell's values in arrival order.
+// Every staged copy to its cell's slots in arrival order: block b walks the tile_count[b] copies staged in
+// tile b's slots, 256 at a time.  The copies of one warp that share a cell take consecutive slots with one
+// atomic on the cell's cursor (cleared by k_cell_scan).  The sorted keys and values come out grouped by cell,
+// each cell's values in arrival order; a total beyond `cap` is flagged (the build is repeated larger).
 __global__ void __launch_bounds__(kBlock) k_cell_scatter(const uint32_t* __restrict__ keys,
                                                          const uint32_t* __restrict__ vals,
-                                                         const int* __restrict__ n_dev, int cap, int ncells,
-                                                         const int* __restrict__ cell_start, int* __restrict__ cursor,
-                                                         uint32_t* __restrict__ skeys, uint32_t* __restrict__ svals,
-                                                         int* __restrict__ err) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int n = min(*n_dev, cap);
-  uint32_t li = 0xffffffffu;  // no copy
-  if (t < n) {
-    li = keys[t];
-    if (li >= (uint32_t)ncells) {
-      atomicOr(err, DERR_CELL_RANGE);
-      li = 0xffffffffu;
-    }
-  }
+                                                         const int* __restrict__ tile_count, int slots, int cap,
+                                                         int ncells, const int* __restrict__ cell_start,
+                                                         int* __restrict__ cursor, uint32_t* __restrict__ skeys,
+                                                         uint32_t* __restrict__ svals, int* __restrict__ err) {
+  const int count = min(tile_count[blockIdx.x], slots);
+  const int64_t first_slot = (int64_t)blockIdx.x * slots;
   const int lane = threadIdx.x & 31;
-  const unsigned peers = __match_any_sync(0xffffffffu, li);
-  const int leader = __ffs(peers) - 1;
-  int first = 0;
-  if (li != 0xffffffffu && lane == leader) first = atomicAdd(&cursor[2 * li], __popc(peers));
-  first = __shfl_sync(0xffffffffu, first, leader);
-  if (li == 0xffffffffu) return;
-  const int pos = cell_start[li] + first + __popc(peers & ((1u << lane) - 1u));
-  if (pos < 0 || pos >= n || pos >= cell_start[li + 1]) {
-    atomicOr(err, DERR_CELL_RANGE);
-    return;
+  for (int at = 0; at < count; at += kBlock) {  // the same trip count in every thread
+    const int j = at + (int)threadIdx.x;
+    uint32_t li = 0xffffffffu;  // no copy
+    if (j < count) {
+      li = keys[first_slot + j];
+      if (li >= (uint32_t)ncells) {
+        atomicOr(err, DERR_CELL_RANGE);
+        li = 0xffffffffu;
+      }
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, li);
+    const int leader = __ffs(peers) - 1;
+    int first = 0;
+    if (li != 0xffffffffu && lane == leader) first = atomicAdd(&cursor[2 * li], __popc(peers));
+    first = __shfl_sync(0xffffffffu, first, leader);
+    if (li == 0xffffffffu) continue;
+    const int pos = cell_start[li] + first + __popc(peers & ((1u << lane) - 1u));
+    if (pos < 0 || pos >= cell_start[li + 1]) {
+      atomicOr(err, DERR_CELL_RANGE);
+      continue;
+    }
+    if (pos >= cap) {
+      atomicOr(err, DERR_COPY_OVERFLOW);
+      continue;
+    }
+    skeys[pos] = li;
+    svals[pos] = vals[first_slot + j];
   }
-  skeys[pos] = li;
-  svals[pos] = vals[t];
 }
 
 // The gather after the counting placement: slot q of the placed list holds a copy of cell li in arrival order; the
@@ -797,59 +850,65 @@ template <class T> int64_t copy_capacity(const SetData& S, const Geometry<T>& g)
   return std::max<int64_t>(std::max<int64_t>(S.copy_cap, (int64_t)est), n + 64);
 }
 
-// One system: the counting build.  One zeroed region holds the look-back words of the two single-pass
-// scans and the per-cell {copies, real} counters; then four launches: wrap + copy offsets + keys + cell
-// counts (k_wrap_emit), cell starts + real-cell list (k_cell_scan), placement by arrival (k_cell_scatter),
-// and the gather at each copy's rank in its cell (k_rank_gather).
+// One system: the counting build.  One zeroed region holds the look-back words of the cell scan and the
+// per-cell {copies, real} counters; then four launches: wrap + keys staged per tile + cell counts
+// (k_wrap_stage), cell starts + real-cell list (k_cell_scan), placement by arrival (k_cell_scatter), and the
+// gather at each copy's rank in its cell (k_rank_gather).  The number of copies is the last cell start.
 template <class T>
 int build_counting(Handle& h, SetData& S, const DevGeom<T>& dg, int N, int64_t n, int64_t ncells, int64_t cap) {
   int* err = h.err.as<int>();
-  const int64_t we_tiles = (n + WE_TILE - 1) / WE_TILE;
+  const int64_t tiles = (n + WE_TILE - 1) / WE_TILE;
   const int64_t ct = (ncells + SCAN_TILE - 1) / SCAN_TILE;
-  // 64-bit words: wrap-emit status + ticket, cell-scan count status + ticket, cell-scan flag status, then
-  // the per-cell counters (two ints per cell)
-  const int64_t w_we = we_tiles + 1, w_c = ct + 1, w_f = ct;
-  const size_t zero_bytes = sizeof(unsigned long long) * (size_t)(w_we + w_c + w_f + ncells + 1);
+  // staging slots per tile: a few per particle, from the capacity's copies per particle (more after a tile
+  // overflowed), a multiple of 32
+  if (S.tile_mult <= 0) S.tile_mult = (int)std::min<int64_t>(27, std::max<int64_t>(2, (cap * 5 / 4 + n - 1) / n + 1));
+  const int slots = WE_BLOCK * S.tile_mult;
+  const int64_t nslots = tiles * slots;
+  // 64-bit words: cell-scan count status + ticket, cell-scan flag status, then the per-cell counters (two ints
+  // per cell)
+  const int64_t w_c = ct + 1, w_f = ct;
+  const size_t zero_bytes = sizeof(unsigned long long) * (size_t)(w_c + w_f + ncells + 1);
   const void* zero_at = S.cell_count.p;
   if (!S.cell_count.reserve(zero_bytes) || !S.wrapped.reserve(sizeof(T) * N * n) ||
-      !S.keys[0].reserve(sizeof(uint32_t) * cap) || !S.keys[1].reserve(sizeof(uint32_t) * cap) ||
-      !S.vals[0].reserve(sizeof(uint32_t) * cap) || !S.vals[1].reserve(sizeof(uint32_t) * cap) ||
-      !S.px.reserve(sizeof(T) * cap) || !S.py.reserve(sizeof(T) * cap) || !S.pz.reserve(sizeof(T) * cap) ||
+      !S.ncopy.reserve(sizeof(int) * (tiles + 1)) || !S.keys[0].reserve(sizeof(uint32_t) * nslots) ||
+      !S.vals[0].reserve(sizeof(uint32_t) * nslots) || !S.keys[1].reserve(sizeof(uint32_t) * cap) ||
+      !S.vals[1].reserve(sizeof(uint32_t) * cap) || !S.px.reserve(sizeof(T) * cap) ||
+      !S.py.reserve(sizeof(T) * cap) || !S.pz.reserve(sizeof(T) * cap) ||
       !S.off.reserve(std::is_same<T, float>::value ? 16 : sizeof(float4) * cap) || !S.code.reserve(sizeof(int) * cap) ||
       !S.xq.reserve(std::is_same<T, float>::value ? sizeof(float4) * cap : 16))
     return ERR_NOMEM;
   if (S.cell_count.p != zero_at) S.cell_count_zero = 0;  // a new allocation holds no cleared words
   unsigned long long* z = S.cell_count.as<unsigned long long>();
-  unsigned long long* st_we = z;
-  unsigned long long* st_c = z + w_we;
+  unsigned long long* st_c = z;
   unsigned long long* st_f = st_c + w_c;
   int* cell_cf = reinterpret_cast<int*>(st_f + w_f);
   // cleared by the previous build's gather unless the region grew or moved
   if (S.cell_count_zero < zero_bytes) CLM_CUDA_TRY(h, cudaMemsetAsync(z, 0, zero_bytes, h.stream));
   S.cell_count_zero = 0;
-  int* n_dev = S.copy_off.as<int>() + n;  // total number of copies, on the device
+  int* tile_count = S.ncopy.as<int>();
+  int* max_cell = S.copy_off.as<int>() + n + 1;  // the largest cell
   if (N == 3)
-    k_wrap_emit<T, 3, true><<<(unsigned)we_tiles, WE_BLOCK, 0, h.stream>>>(
-        dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), (int)cap, S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
-        n_dev, st_we, reinterpret_cast<unsigned*>(st_we + we_tiles), (int)we_tiles, cell_cf, err);
+    k_wrap_stage<T, 3><<<(unsigned)tiles, WE_BLOCK, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), slots,
+                                                                  S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
+                                                                  tile_count, cell_cf, max_cell, err);
   else
-    k_wrap_emit<T, 2, true><<<(unsigned)we_tiles, WE_BLOCK, 0, h.stream>>>(
-        dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), (int)cap, S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
-        n_dev, st_we, reinterpret_cast<unsigned*>(st_we + we_tiles), (int)we_tiles, cell_cf, err);
+    k_wrap_stage<T, 2><<<(unsigned)tiles, WE_BLOCK, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), slots,
+                                                                  S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
+                                                                  tile_count, cell_cf, max_cell, err);
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
   k_cell_scan<<<(unsigned)ct, kBlock, 0, h.stream>>>(cell_cf, (int)ncells, S.cell_start.as<int>(), S.cell_flags.as<int>(),
-                                                     S.real_list.as<int>(), S.real_scan.as<int>() + ncells,
-                                                     S.copy_off.as<int>() + n + 1, st_c, st_f,
-                                                     reinterpret_cast<unsigned*>(st_c + ct), (int)ct, err);
+                                                     S.real_list.as<int>(), S.real_scan.as<int>() + ncells, max_cell,
+                                                     st_c, st_f, reinterpret_cast<unsigned*>(st_c + ct), (int)ct, err);
+  CLM_CUDA_TRY(h, cudaGetLastError());
+  h.launches++;
+  k_cell_scatter<<<(unsigned)tiles, kBlock, 0, h.stream>>>(S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
+                                                           tile_count, slots, (int)cap, (int)ncells,
+                                                           S.cell_start.as<int>(), cell_cf, S.keys[1].as<uint32_t>(),
+                                                           S.vals[1].as<uint32_t>(), err);
   CLM_CUDA_TRY(h, cudaGetLastError());
   h.launches++;
   const int gc = grid_for(cap);
-  k_cell_scatter<<<gc, kBlock, 0, h.stream>>>(S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev, (int)cap,
-                                              (int)ncells, S.cell_start.as<int>(), cell_cf, S.keys[1].as<uint32_t>(),
-                                              S.vals[1].as<uint32_t>(), err);
-  CLM_CUDA_TRY(h, cudaGetLastError());
-  h.launches++;
   const int64_t zwords = (int64_t)(zero_bytes / sizeof(unsigned long long));
   if (N == 3)
     k_rank_gather<T, 3><<<gc, kBlock, 0, h.stream>>>(dg, S.wrapped.as<T>(), S.keys[1].as<uint32_t>(),
@@ -952,13 +1011,13 @@ template <class T> int build_set(Handle& h, int set, const Geometry<T>& g) {
     CLM_CUDA_TRY(h, cudaMemsetAsync(status, 0, (size_t)(we_tiles + 1) * sizeof(unsigned long long), h.stream));
     unsigned* ticket = reinterpret_cast<unsigned*>(status + we_tiles);
     if (N == 3)
-      k_wrap_emit<T, 3, false><<<we_tiles, WE_BLOCK, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), (int)cap,
-                                                                  S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev,
-                                                                  status, ticket, we_tiles, nullptr, err);
+      k_wrap_emit<T, 3><<<we_tiles, WE_BLOCK, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), (int)cap,
+                                                            S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev,
+                                                            status, ticket, we_tiles, err);
     else
-      k_wrap_emit<T, 2, false><<<we_tiles, WE_BLOCK, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), (int)cap,
-                                                                  S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev,
-                                                                  status, ticket, we_tiles, nullptr, err);
+      k_wrap_emit<T, 2><<<we_tiles, WE_BLOCK, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), (int)cap,
+                                                            S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(), n_dev,
+                                                            status, ticket, we_tiles, err);
     CLM_CUDA_TRY(h, cudaGetLastError());
     h.launches++;
   } else {
@@ -1068,8 +1127,9 @@ int enqueue_build_totals(Handle& h) {
   for (int s = 0; s < h.nsets; s++) {
     SetData& S = h.sets[s];
     if (!S.pending) continue;
-    CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 32 + 2 * s, S.copy_off.as<int>() + S.n, sizeof(int),
-                                    cudaMemcpyDeviceToHost, h.stream));
+    // the number of copies: the copy-offset scan's total, or (counting build) the last cell start
+    const int* copies = S.counted ? S.cell_start.as<int>() + S.ncells : S.copy_off.as<int>() + S.n;
+    CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 32 + 2 * s, copies, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
     CLM_CUDA_TRY(h, cudaMemcpyAsync(h.pinned + 33 + 2 * s, S.real_scan.as<int>() + S.ncells, sizeof(int),
                                     cudaMemcpyDeviceToHost, h.stream));
     if (S.counted)
@@ -1100,6 +1160,12 @@ int check_build_totals(Handle& h, bool* overflow) {
     S.n_copies = h.pinned[32 + 2 * s];
     S.n_real_cells = h.pinned[33 + 2 * s];
     if (S.counted && h.pinned[44 + s] > kRadixAbovePerCell) S.prefer_radix = true;
+    if (S.counted && (errw & DERR_TILE_OVERFLOW)) {
+      // a tile had more copies than its staging slots: more slots per particle, and build again
+      S.tile_mult = std::min(27, 2 * S.tile_mult);
+      S.dirty = true;
+      *overflow = true;
+    }
     S.pending = false;
     if (S.n_copies > S.cap_used || (errw & DERR_COPY_OVERFLOW)) {
       S.copy_cap = S.n_copies + S.n_copies / 8 + 1024;

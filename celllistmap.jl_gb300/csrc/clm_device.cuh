@@ -345,6 +345,7 @@ enum DevError : int {
   DERR_NL_OVERFLOW = 8,
   DERR_SCAN = 16,  // a single-pass scan gave up waiting for the prefix of an earlier tile
   DERR_STAGE = 32, // the pair kernel gave up waiting for the bulk copies of a staging window
+  DERR_TILE_OVERFLOW = 64,  // a tile of the counting build had more copies than its staging slots
 };
 
 }  // namespace clm

@@ -86,6 +86,7 @@ struct SetData {
   bool pending = false;      // the device totals of the last build were not read back yet
   bool counted = false;      // the last build was the counting build (its largest cell is read back)
   bool prefer_radix = false; // a counting build met a cell of more than kRadixAbovePerCell copies
+  int tile_mult = 0;         // counting build: staging slots per particle of a tile (0: from the estimate)
   int64_t n_cells_with_particles = 0;
   int64_t ncells = 0;
 };
