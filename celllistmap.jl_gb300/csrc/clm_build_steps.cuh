@@ -3,9 +3,11 @@
 // compile the same functions for the host (g++ with -ffp-contract=off) and compare the copies, cells and
 // coordinates they give with the oracle's serial cell list, without a GPU.
 #pragma once
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <type_traits>
 
 #include "clm_device.cuh"
@@ -37,12 +39,45 @@ __host__ __device__ __forceinline__ float bits_as_float(int v) {
   return f;
 #endif
 }
-template <class T> __host__ __device__ __forceinline__ bool is_nan(T v) {
+// NaN test on the bit pattern (a magnitude above that of inf), on the integer pipe
+__host__ __device__ __forceinline__ bool is_nan(double v) {
+  return (unsigned long long)(dbits(v) & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000ULL;
+}
+__host__ __device__ __forceinline__ bool is_nan(float v) {
 #ifdef __CUDA_ARCH__
-  return isnan(v);
+  const unsigned b = __float_as_uint(v);
 #else
-  return std::isnan(v);
+  unsigned b;
+  std::memcpy(&b, &v, sizeof b);
 #endif
+  return (b & 0x7FFFFFFFu) > 0x7F800000u;
+}
+
+// The value with order key q (order_key is its own inverse on the bit pattern).
+template <class T> T from_order_key(typename OrderKey<T>::type q) {
+  const auto b = q ^ (decltype(q))((typename std::make_unsigned<decltype(q)>::type)(q >> (8 * sizeof(q) - 1)) >> 1);
+  T v;
+  std::memcpy(&v, &b, sizeof v);
+  return v;
+}
+
+// The smallest order key q with RN(value(q) + s) >= b.  RN(p + s) does not decrease as p grows, so the p that
+// pass the test `b <= p + s` are those with key(p) >= q.  Bisection over [key(-inf), key(+inf)] (+inf passes
+// for finite s and b), bracketed first within 4 keys of RN(b - s), where q almost always lies.
+template <class T> typename OrderKey<T>::type first_key_at_least(T s, T b) {
+  using K = typename OrderKey<T>::type;
+  const auto pass = [&](K q) { return from_order_key<T>(q) + s >= b; };
+  K lo = order_key(-std::numeric_limits<T>::infinity()), hi = order_key(std::numeric_limits<T>::infinity());
+  const K q = std::min(std::max(order_key((T)(b - s)), lo), hi);
+  const K a = q - 4 > lo ? q - 4 : lo, z = q + 4 < hi ? q + 4 : hi;
+  if (!pass(a)) lo = a;
+  if (pass(z)) hi = z;
+  while (lo + 1 < hi) {
+    const K mid = (lo >> 1) + (hi >> 1) + (lo & hi & 1);
+    if (pass(mid)) hi = mid;
+    else lo = mid;
+  }
+  return pass(lo) ? lo : hi;
 }
 
 template <class T> void fill_devgeom(const Geometry<T>& g, int precision, DevGeom<T>& d) {
@@ -69,6 +104,20 @@ template <class T> void fill_devgeom(const Geometry<T>& g, int precision, DevGeo
     }
   }
   d.det_in = g.det_in;
+  d.inv_det = T(1) / g.det_in;
+  {
+    // the cofactors of the 3D solve, separately rounded in the handle dtype (wrap_point)
+    const auto& a = g.Min;
+    const auto c = [](T p, T q, T r, T s) { return xsub(xmul(p, q), xmul(r, s)); };
+    const T cof[3][3] = {{c(a[1][1], a[2][2], a[1][2], a[2][1]), c(a[0][2], a[2][1], a[0][1], a[2][2]),
+                          c(a[0][1], a[1][2], a[0][2], a[1][1])},
+                         {c(a[1][2], a[2][0], a[1][0], a[2][2]), c(a[0][0], a[2][2], a[0][2], a[2][0]),
+                          c(a[0][2], a[1][0], a[0][0], a[1][2])},
+                         {c(a[1][0], a[2][1], a[1][1], a[2][0]), c(a[0][1], a[2][0], a[0][0], a[2][1]),
+                          c(a[0][0], a[1][1], a[0][1], a[1][0])}};
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) d.cof[i][j] = cof[i][j];
+  }
   d.cutoff = g.cutoff;
   d.cutoff_sqr = g.cutoff_sqr;
   d.margin_wide = (double)g.cutoff * (1.0 + std::sqrt((double)g.dim) / 2.0);
@@ -97,6 +146,8 @@ template <class T> void fill_devgeom(const Geometry<T>& g, int precision, DevGeo
       T acc = g.Mal[i][0] * T(s[0]);
       for (int j = 1; j < g.dim; j++) acc = acc + g.Mal[i][j] * T(s[j]);
       d.shift[k][i] = acc;
+      d.img_lo[k][i] = first_key_at_least<T>(acc, g.cbmin[i]);
+      d.img_hi[k][i] = first_key_at_least<T>(acc, g.cbmax[i]);
     }
   }
   // FP32 prefilter band around cutoff^2 (relative 2^-13, far above the FP32
@@ -134,6 +185,10 @@ __host__ __device__ __forceinline__ bool wrap_count_regs(const DevGeom<T>& g, co
   }
   uint32_t m = 0;
   int cnt = 1;
+  // image tests on the order keys of p (image_in): the same decisions as cbmin <= p + shift < cbmax
+  typename OrderKey<T>::type pk[N];
+#pragma unroll
+  for (int k = 0; k < N; k++) pk[k] = order_key(p[k]);
   if (g.kind != NONPERIODIC && g.img_tree == 2) {
     // image k = (s0+1) + 3(s1+1) [+ 9(s2+1)]: the last component is tested once per s_last, the next
     // once per (s_mid, s_last), the first per image; each test uses the shift of the image itself
@@ -141,20 +196,17 @@ __host__ __device__ __forceinline__ bool wrap_count_regs(const DevGeom<T>& g, co
 #pragma unroll
     for (int sl = -1; sl <= 1; sl++) {
       const int kl = (N == 3) ? 9 * (sl + 1) + 4 : 3 * (sl + 1) + 1;
-      const T ql = xadd(p[N - 1], g.shift[kl][N - 1]);
-      if (!(g.cbmin[N - 1] <= ql && ql < g.cbmax[N - 1])) continue;
+      if (!image_in(g, kl, N - 1, pk[N - 1])) continue;
       if (N == 3) {
 #pragma unroll
         for (int sm = -1; sm <= 1; sm++) {
           const int km = 9 * (sl + 1) + 3 * (sm + 1) + 1;
-          const T qm = xadd(p[1], g.shift[km][1]);
-          if (!(g.cbmin[1] <= qm && qm < g.cbmax[1])) continue;
+          if (!image_in(g, km, 1, pk[1])) continue;
 #pragma unroll
           for (int s0 = -1; s0 <= 1; s0++) {
             const int k = 9 * (sl + 1) + 3 * (sm + 1) + (s0 + 1);
             if (k == g.zero_code) continue;
-            const T q0 = xadd(p[0], g.shift[k][0]);
-            if (g.cbmin[0] <= q0 && q0 < g.cbmax[0]) {
+            if (image_in(g, k, 0, pk[0])) {
               m |= 1u << k;
               cnt++;
             }
@@ -165,8 +217,7 @@ __host__ __device__ __forceinline__ bool wrap_count_regs(const DevGeom<T>& g, co
         for (int s0 = -1; s0 <= 1; s0++) {
           const int k = 3 * (sl + 1) + (s0 + 1);
           if (k == g.zero_code) continue;
-          const T q0 = xadd(p[0], g.shift[k][0]);
-          if (g.cbmin[0] <= q0 && q0 < g.cbmax[0]) {
+          if (image_in(g, k, 0, pk[0])) {
             m |= 1u << k;
             cnt++;
           }
@@ -179,18 +230,14 @@ __host__ __device__ __forceinline__ bool wrap_count_regs(const DevGeom<T>& g, co
 #pragma unroll
     for (int sl = -1; sl <= 1; sl++) {
       constexpr int NR = (N == 3) ? 9 : 3;  // images per value of s_last
-      const T ql = xadd(p[N - 1], g.shift[NR * (sl + 1)][N - 1]);
-      if (!(g.cbmin[N - 1] <= ql && ql < g.cbmax[N - 1])) continue;
+      if (!image_in(g, NR * (sl + 1), N - 1, pk[N - 1])) continue;
 #pragma unroll
       for (int r = 0; r < NR; r++) {
         const int k = NR * (sl + 1) + r;
         if (k == g.zero_code) continue;
         bool in = true;
 #pragma unroll
-        for (int d = 0; d < N - 1; d++) {
-          const T q = xadd(p[d], g.shift[k][d]);
-          in = in && (g.cbmin[d] <= q) && (q < g.cbmax[d]);
-        }
+        for (int d = 0; d < N - 1; d++) in = in && image_in(g, k, d, pk[d]);
         if (in) {
           m |= 1u << k;
           cnt++;
@@ -200,10 +247,10 @@ __host__ __device__ __forceinline__ bool wrap_count_regs(const DevGeom<T>& g, co
   } else if (g.kind != NONPERIODIC) {
     for (int k = 0; k < g.nimg; k++) {
       if (k == g.zero_code) continue;
-      T q[N];
+      bool in = true;
 #pragma unroll
-      for (int d = 0; d < N; d++) q[d] = xadd(p[d], g.shift[k][d]);
-      if (in_box<T, N>(g, q)) {
+      for (int d = 0; d < N; d++) in = in && image_in(g, k, d, pk[d]);
+      if (in) {
         m |= 1u << k;
         cnt++;
       }

@@ -8,6 +8,7 @@
 #pragma once
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 namespace clm {
@@ -32,16 +33,97 @@ CLM_XOP(xmul, float, __fmul_rn(a, b), a * b)
 CLM_XOP(xdiv, float, __fdiv_rn(a, b), a / b)
 #undef CLM_XOP
 #ifdef __CUDA_ARCH__
+__host__ __device__ __forceinline__ double xfma(double a, double b, double c) { return __fma_rn(a, b, c); }
 __host__ __device__ __forceinline__ double xsqrt(double a) { return __dsqrt_rn(a); }
 __host__ __device__ __forceinline__ float xsqrt(float a) { return __fsqrt_rn(a); }
 template <class T> __host__ __device__ __forceinline__ T xfloor(T a) { return floor(a); }
 template <class T> __host__ __device__ __forceinline__ T xabs(T a) { return fabs(a); }
 #else
+__host__ __device__ __forceinline__ double xfma(double a, double b, double c) { return std::fma(a, b, c); }
 __host__ __device__ __forceinline__ double xsqrt(double a) { return std::sqrt(a); }
 __host__ __device__ __forceinline__ float xsqrt(float a) { return std::sqrt(a); }
 template <class T> __host__ __device__ __forceinline__ T xfloor(T a) { return std::floor(a); }
 template <class T> __host__ __device__ __forceinline__ T xabs(T a) { return std::fabs(a); }
 #endif
+
+// ---------------------------------------------------------------- order keys
+// The bit pattern of a float or double with the magnitude bits of negative values inverted, read as a signed
+// integer: a <= b as numbers implies key(a) <= key(b) (-0 sorts just below +0; a NaN lies outside
+// [key(-inf), key(+inf)]).  The image tests compare these keys on the integer pipe.
+template <class T> struct OrderKey;
+template <> struct OrderKey<double> { using type = long long; };
+template <> struct OrderKey<float> { using type = int; };
+
+__host__ __device__ __forceinline__ long long order_key(double v) {
+#ifdef __CUDA_ARCH__
+  const long long b = __double_as_longlong(v);
+#else
+  long long b;
+  std::memcpy(&b, &v, sizeof b);
+#endif
+  return b ^ (long long)((unsigned long long)(b >> 63) >> 1);
+}
+__host__ __device__ __forceinline__ int order_key(float v) {
+#ifdef __CUDA_ARCH__
+  const int b = __float_as_int(v);
+#else
+  int b;
+  std::memcpy(&b, &v, sizeof b);
+#endif
+  return b ^ (int)((unsigned)(b >> 31) >> 1);
+}
+
+// RN(a / b) in double from y = RN(1 / b): q = q0 + (a - q0 b) y with q0 = RN(a y) (Markstein's correction
+// step), accepted when its remainder r = RN(a - q b) proves it: r = 0 (a = q b exactly: with q and b normal and
+// |b| 2^(E(q) - 53) normal, a - q b is a multiple of 2^-1074 and cannot round to 0 unless it is 0), or q is not
+// a power of two and |r| < |b| 2^(E(q) - 53) (the exact |a - q b| is then below that bound, which is
+// representable, so |a / b - q| is less than half the spacing of the doubles around q; a quotient of two
+// doubles is never a midpoint).  Otherwise (powers of two, zero, subnormal or extreme exponents, inf or NaN)
+// the IEEE division decides.  Four FP64 operations and integer checks instead of the division sequence.
+__host__ __device__ __forceinline__ long long dbits(double v) {
+#ifdef __CUDA_ARCH__
+  return __double_as_longlong(v);
+#else
+  long long b;
+  std::memcpy(&b, &v, sizeof b);
+  return b;
+#endif
+}
+__host__ __device__ __forceinline__ bool quot_fast(double a, double b, double y, double& q) {
+  const double q0 = xmul(a, y);
+  q = xfma(xfma(-q0, b, a), y, q0);
+  const double r = xfma(-q, b, a);
+  constexpr long long kMag = 0x7FFFFFFFFFFFFFFFLL, kFrac = 0x000FFFFFFFFFFFFFLL;
+  const long long bq = dbits(q), bb = dbits(b) & kMag, br = dbits(r) & kMag;
+  const int eq = (int)((bq >> 52) & 0x7ff), eb = (int)(bb >> 52), es = eb + eq - (1023 + 53);
+  return eq > 0 && eq < 0x7ff && eb > 0 && es > 0 && es < 0x7ff &&
+         (br == 0 || ((bq & kFrac) != 0 && br < bb + (long long)(eq - (1023 + 53)) * (1LL << 52)));
+}
+#ifdef __CUDA_ARCH__
+// a call, so that the compiler cannot evaluate the division ahead of the branch in every warp
+__device__ __noinline__ double div_rn_call(double a, double b) { return __ddiv_rn(a, b); }
+#endif
+__host__ __device__ __forceinline__ bool same_bits(double a, double b) { return dbits(a) == dbits(b); }
+__host__ __device__ __forceinline__ bool same_bits(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(a) == __float_as_uint(b);
+#else
+  unsigned x, y;
+  std::memcpy(&x, &a, sizeof x);
+  std::memcpy(&y, &b, sizeof y);
+  return x == y;
+#endif
+}
+__host__ __device__ __forceinline__ double quot_rn(double a, double b, double y) {
+  double q;
+  if (quot_fast(a, b, y, q)) return q;
+#ifdef __CUDA_ARCH__
+  return div_rn_call(a, b);
+#else
+  return a / b;
+#endif
+}
+__host__ __device__ __forceinline__ float quot_rn(float a, float b, float) { return xdiv(a, b); }
 
 // ---------------------------------------------------------------- geometry on device
 constexpr int kMaxDim = 3;
@@ -52,6 +134,8 @@ template <class T> struct DevGeom {
   int ncells;
   T Min[3][3];    // input unit cell (wrap solve / product)
   T det_in;
+  T inv_det;      // RN(1 / det_in) (quot_rn)
+  T cof[3][3];    // cofactors of the 3D Cramer solve, p_i = RN((cof[i][0] x0 + cof[i][1] x1 + cof[i][2] x2) / det)
   T R[3][3];      // rotation after wrapping (identity unless triclinic)
   T Rinv[3][3];   // rotation back for pair coordinates
   T shift[27][3]; // aligned-cell translation of image code k (first index fastest)
@@ -67,7 +151,15 @@ template <class T> struct DevGeom {
   int nimg;             // 3^dim
   int img_tree;         // image-test pruning: 2 aligned cell exactly upper triangular (per dimension), 1 last
                         // row zero below the diagonal (per value of the last image index), 0 none
+  // image k of a wrapped position p lies in the computing box along axis d, cbmin[d] <= RN(p[d] + shift[k][d])
+  // < cbmax[d], exactly when img_lo[k][d] <= order_key(p[d]) < img_hi[k][d]
+  typename OrderKey<T>::type img_lo[27][3], img_hi[27][3];
 };
+
+template <class T>
+__host__ __device__ __forceinline__ bool image_in(const DevGeom<T>& g, int k, int d, typename OrderKey<T>::type pk) {
+  return g.img_lo[k][d] <= pk && pk < g.img_hi[k][d];
+}
 
 // StaticArrays solve (Cramer form), then fastmod1, boundary -> 0, then M*p and R*(.)
 template <class T, int N>
@@ -75,18 +167,11 @@ __host__ __device__ __forceinline__ void wrap_point(const DevGeom<T>& g, const T
   T p[N];
   const auto& a = g.Min;
   if constexpr (N == 3) {
-    p[0] = xdiv(xadd(xadd(xmul(xsub(xmul(a[1][1], a[2][2]), xmul(a[1][2], a[2][1])), x[0]),
-                          xmul(xsub(xmul(a[0][2], a[2][1]), xmul(a[0][1], a[2][2])), x[1])),
-                     xmul(xsub(xmul(a[0][1], a[1][2]), xmul(a[0][2], a[1][1])), x[2])),
-                g.det_in);
-    p[1] = xdiv(xadd(xadd(xmul(xsub(xmul(a[1][2], a[2][0]), xmul(a[1][0], a[2][2])), x[0]),
-                          xmul(xsub(xmul(a[0][0], a[2][2]), xmul(a[0][2], a[2][0])), x[1])),
-                     xmul(xsub(xmul(a[0][2], a[1][0]), xmul(a[0][0], a[1][2])), x[2])),
-                g.det_in);
-    p[2] = xdiv(xadd(xadd(xmul(xsub(xmul(a[1][0], a[2][1]), xmul(a[1][1], a[2][0])), x[0]),
-                          xmul(xsub(xmul(a[0][1], a[2][0]), xmul(a[0][0], a[2][1])), x[1])),
-                     xmul(xsub(xmul(a[0][0], a[1][1]), xmul(a[0][1], a[1][0])), x[2])),
-                g.det_in);
+    // the cofactors (each RN(RN(a b) - RN(c d)), as the solve rounds them) come precomputed with the geometry
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      p[i] = quot_rn(xadd(xadd(xmul(g.cof[i][0], x[0]), xmul(g.cof[i][1], x[1])), xmul(g.cof[i][2], x[2])),
+                     g.det_in, g.inv_det);
   } else {
     p[0] = xdiv(xsub(xmul(a[1][1], x[0]), xmul(a[0][1], x[1])), g.det_in);
     p[1] = xdiv(xsub(xmul(a[0][0], x[1]), xmul(a[1][0], x[0])), g.det_in);
@@ -94,7 +179,7 @@ __host__ __device__ __forceinline__ void wrap_point(const DevGeom<T>& g, const T
 #pragma unroll
   for (int i = 0; i < N; i++) {
     p[i] = xsub(p[i], xfloor(p[i]));
-    if (p[i] == T(1)) p[i] = T(0);
+    if (same_bits(p[i], T(1))) p[i] = T(0);  // p == 1 (the only value equal to 1 is 1), on the integer pipe
   }
   T w[N];
 #pragma unroll
@@ -111,14 +196,6 @@ __host__ __device__ __forceinline__ void wrap_point(const DevGeom<T>& g, const T
     for (int k = 1; k < N; k++) s = xadd(s, xmul(g.R[i][k], w[k]));
     out[i] = s;
   }
-}
-
-template <class T, int N>
-__host__ __device__ __forceinline__ bool in_box(const DevGeom<T>& g, const T* x) {
-  bool ok = true;
-#pragma unroll
-  for (int i = 0; i < N; i++) ok = ok && (g.cbmin[i] <= x[i]) && (x[i] < g.cbmax[i]);
-  return ok;
 }
 
 // floor((x - xmin)/cell_size) + 1 with the border-case shift for real particles
@@ -138,16 +215,67 @@ template <class T> __host__ __device__ __forceinline__ T cell_floor(T a, T cs, T
   return xfloor(xdiv(a, cs));
 }
 
+// floor(qa) from the bit pattern of qa = RN(a * RN(1 / cs)), when that is also floor(RN(a / cs)): qa in
+// (0, 2^31) and at least 5 units in the last place of qa from every integer (which is more than the 4u|qa|
+// margin of cell_floor: qa < 2^(e+1), so 4u|qa| < 4 ulp).  Returns false otherwise (qa <= 0, near an integer,
+// huge, inf or NaN); cell_floor then decides.  Integer operations only, off the FP64 pipe for doubles.
+template <class T> struct FloatBits;
+template <> struct FloatBits<double> {
+  using U = unsigned long long;
+  static constexpr int kMant = 52, kBias = 1023;
+};
+template <> struct FloatBits<float> {
+  using U = unsigned;
+  static constexpr int kMant = 23, kBias = 127;
+};
+template <class T> __host__ __device__ __forceinline__ bool floor_quot_bits(T qa, int& fq) {
+  using U = typename FloatBits<T>::U;
+  constexpr int M = FloatBits<T>::kMant;
+  U b;
+#ifdef __CUDA_ARCH__
+  if constexpr (sizeof(T) == 8) b = (U)__double_as_longlong(qa);
+  else b = (U)__float_as_uint(qa);
+#else
+  std::memcpy(&b, &qa, sizeof b);
+#endif
+  const int e = (int)(b >> M) - FloatBits<T>::kBias;  // the sign bit makes e > 30 for negative qa
+  if (e < -1) {  // 0 < qa < 1/2 (zero and -0 go to cell_floor)
+    fq = 0;
+    return b != 0 && (b >> (8 * sizeof(U) - 1)) == 0;
+  }
+  if (e > 30) return false;
+  const int sh = M - e;  // bits of the fraction, 1 .. M + 1
+  const U mant = (b & ((U(1) << M) - 1)) | (U(1) << M);
+  const U one = U(1) << sh, frac = mant & (one - 1);
+  fq = (int)(mant >> sh);
+  return frac > 4 && one - frac > 4;
+}
+
+// cell_floor and its range test for the values floor_quot_bits leaves (a call on the device, so that the
+// division it may take stays off the common path): floor(RN(a / cs)) if in [-1, nc), else INT_MIN.
+template <class T>
+#ifdef __CUDA_ARCH__
+__device__ __noinline__
+#else
+inline
+#endif
+int floor_quot_call(T a, T cs, T inv_cs, int nc) {
+  const T fq = cell_floor<T>(a, cs, inv_cs);
+  return (fq >= T(-1) && fq < (T)nc) ? (int)fq : INT32_MIN;
+}
+
 template <class T, int N>
 __host__ __device__ __forceinline__ int cell_of(const DevGeom<T>& g, const T* x, bool real) {
   int li = 0;
 #pragma unroll
   for (int i = N - 1; i >= 0; i--) {
-    // floor in the handle dtype (exact; cell indices are far below 2^24), which keeps Float32 builds off
-    // GB300's slow FP64 pipe
-    const T fq = cell_floor<T>(xsub(x[i], g.cbmin[i]), g.cs[i], g.inv_cs[i]);
-    if (!(fq >= T(-1) && fq < (T)g.nc[i])) return -1;
-    int c = (int)fq + 1;
+    // floor(RN(RN(x - cbmin) / cs)) from the bits of the reciprocal product where that decides it, else
+    // cell_floor in the handle dtype (exact; cell indices are far below 2^24)
+    const T a = xsub(x[i], g.cbmin[i]);
+    int fq;
+    if (!floor_quot_bits<T>(xmul(a, g.inv_cs[i]), fq)) fq = floor_quot_call<T>(a, g.cs[i], g.inv_cs[i], g.nc[i]);
+    if (fq < -1 || fq >= g.nc[i]) return -1;
+    int c = fq + 1;
     if (real) {
       if (c == g.lcell) c += 1;
       if (c == g.nc[i] - g.lcell + 1) c -= 1;

@@ -17,6 +17,9 @@
 //   map_nl_visits_probe the self-pair map's candidate visits that reach the hit queue, and its pairs;
 //   noalloc_slots_probe the per-block slots of the allocation-free entry point's scratch;
 //   cell_floor_probe   the cell index's floor from the reciprocal product against the IEEE quotient's.
+//   image_key_probe    the image tests on order keys against the sums and compares they stand for.
+//   quot_probe         the wrap solve's checked reciprocal quotient against the IEEE division.
+//   cell_index_probe   the cell index's floor from the bits of the reciprocal product, with its range test.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -734,4 +737,90 @@ extern "C" int64_t cell_floor_probe(int f64, const double* a, int64_t n, double 
     }
   }
   return bad;
+}
+
+namespace {
+// The image tests of one geometry on order keys (image_in) against the tests they stand for,
+// cbmin <= RN(v + shift) < cbmax, for every image and axis: at the n values given, at the 7 keys around each
+// of the two thresholds, and at +-0, +-inf and NaN.  Returns the number of disagreements, or -2 - status.
+template <class T>
+int64_t image_keys(int dim, int kind, const double* Mcol, double cutoff, int lcell, const double* v, int64_t n) {
+  T M[3][3] = {};
+  for (int i = 0; i < dim; i++)
+    for (int j = 0; j < dim; j++) M[i][j] = (kind == clm::ORTHO && i != j) ? T(0) : (T)Mcol[j * dim + i];
+  clm::Geometry<T> g;
+  const int st = clm::make_geometry<T>(g, dim, kind, M, (T)cutoff, lcell, nullptr);
+  if (st) return -2 - st;
+  clm::DevGeom<T> d;
+  clm::fill_devgeom<T>(g, 1, d);
+  using K = typename clm::OrderKey<T>::type;
+  const T inf = std::numeric_limits<T>::infinity();
+  int64_t bad = 0;
+  std::vector<T> vals;
+  for (int k = 0; k < d.nimg; k++)
+    for (int a = 0; a < dim; a++) {
+      vals.clear();
+      for (int64_t t = 0; t < n; t++) vals.push_back((T)v[t]);
+      for (const K th : {d.img_lo[k][a], d.img_hi[k][a]})
+        for (int j = -3; j <= 3; j++) vals.push_back(clm::from_order_key<T>(th + j));
+      for (const T s : {T(0), -T(0), inf, -inf, std::numeric_limits<T>::quiet_NaN()}) vals.push_back(s);
+      for (const T x : vals) {
+        const T q = x + d.shift[k][a];
+        const bool want = d.cbmin[a] <= q && q < d.cbmax[a];
+        if (clm::image_in<T>(d, k, a, clm::order_key(x)) != want) bad++;
+      }
+    }
+  return bad;
+}
+}  // namespace
+
+extern "C" int64_t image_key_probe(int f64, int dim, int kind, const double* Mcol, double cutoff, int lcell,
+                                   const double* v, int64_t n) {
+  return f64 ? image_keys<double>(dim, kind, Mcol, cutoff, lcell, v, n)
+             : image_keys<float>(dim, kind, Mcol, cutoff, lcell, v, n);
+}
+
+// quot_rn (the wrap solve's division from RN(1 / b) with a checked correction step) against the IEEE quotient
+// a / b, bit for bit (NaN against NaN), for n pairs; returns the number of disagreements and, in *fallbacks,
+// how many pairs took the IEEE division.
+extern "C" int64_t quot_probe(const double* a, const double* b, int64_t n, int64_t* fallbacks) {
+  int64_t bad = 0, fb = 0;
+  for (int64_t t = 0; t < n; t++) {
+    const double y = 1.0 / b[t], q = clm::quot_rn(a[t], b[t], y), want = a[t] / b[t];
+    if (std::isnan(want) ? !std::isnan(q) : clm::dbits(q) != clm::dbits(want)) bad++;
+    double qf;
+    if (!clm::quot_fast(a[t], b[t], y, qf)) fb++;
+  }
+  *fallbacks = fb;
+  return bad;
+}
+
+namespace {
+template <class T> int64_t cell_index_t(const double* av, int64_t n, double csd, int nc, int64_t* fast) {
+  const T cs = (T)csd, inv = T(1) / cs;
+  int64_t bad = 0, nf = 0;
+  for (int64_t t = 0; t < n; t++) {
+    const T a = (T)av[t];
+    const T q = std::floor(a / cs);
+    const int want = (q >= T(-1) && q < (T)nc) ? (int)q : INT32_MIN;
+    int fq;
+    const bool f = clm::floor_quot_bits<T>(a * inv, fq);
+    if (f) {
+      nf++;
+      if (fq >= nc) fq = INT32_MIN;
+    } else {
+      fq = clm::floor_quot_call<T>(a, cs, inv, nc);
+    }
+    if (fq != want) bad++;
+  }
+  *fast = nf;
+  return bad;
+}
+}  // namespace
+
+// The cell index's floor as cell_of takes it (floor_quot_bits on the reciprocal product, else
+// floor_quot_call) against the IEEE floor(a / cs) with its range test [-1, nc), for n numerators; returns
+// the number of disagreements and, in *fast, how many the bit screen decided.
+extern "C" int64_t cell_index_probe(int f64, const double* a, int64_t n, double cs, int nc, int64_t* fast) {
+  return f64 ? cell_index_t<double>(a, n, cs, nc, fast) : cell_index_t<float>(a, n, cs, nc, fast);
 }

@@ -628,3 +628,113 @@ def test_cell_floor_screen_matches_division(probe, f64):
         vals.append(rng.uniform(-3 * cs, 200 * cs, 5000).astype(dt))
         a = np.ascontiguousarray(np.concatenate(vals).astype(np.float64))
         assert lib.cell_floor_probe(f64, a.ctypes.data_as(C.c_void_p), a.size, C.c_double(cs)) == 0, cs
+
+
+@pytest.mark.parametrize("f64", [0, 1])
+def test_image_tests_on_order_keys(probe, f64):
+    """The build tests whether image k of a wrapped position lies in the computing box along each axis by
+    comparing the position's order key (its bit pattern, magnitude inverted for negative values) with two
+    thresholds found on the host, instead of the sum p + shift and two compares.  For every image and axis of
+    periodic cells (orthorhombic and triclinic, 2D and 3D, lcell 1 to 3, random triclinic cells) the key test
+    must agree with the sum and compares: at random positions across and around the box, at the keys around
+    each threshold, and at +-0, +-inf and NaN."""
+    dt = np.float64 if f64 else np.float32
+    rng = np.random.default_rng(11)
+    lib = probe
+    lib.image_key_probe.restype = C.c_int64
+    cells = [(dim, uc, cut, lcell) for dim, uc, cut, lcell, *_ in CASES if uc is not None]
+    for _ in range(12):
+        dim = int(rng.integers(2, 4))
+        M = np.diag(rng.uniform(5.0, 20.0, dim)) + np.triu(rng.uniform(-3.0, 3.0, (dim, dim)), 1)
+        if rng.random() < 0.5:
+            M += np.tril(rng.uniform(-1.0, 1.0, (dim, dim)), -1)
+        cells.append((dim, M.tolist(), float(rng.uniform(0.5, 2.5)), int(rng.integers(1, 4))))
+    n_checked = 0
+    for dim, uc, cut, lcell in cells:
+        u = np.asarray(uc, np.float64)
+        M = np.diag(u) if u.ndim == 1 else u.reshape(dim, dim)
+        kind = 0 if u.ndim == 1 else 1
+        Mc = np.ascontiguousarray(M.flatten(order="F"))
+        span = float(np.abs(M).sum(axis=1).max()) + 3 * cut
+        v = [rng.uniform(-span, span, 4000), rng.uniform(-cut, cut, 1000), rng.uniform(-1e-6, 1e-6, 200)]
+        v = np.ascontiguousarray(np.concatenate(v).astype(dt).astype(np.float64))
+        bad = lib.image_key_probe(f64, dim, kind, Mc.ctypes.data_as(C.c_void_p), C.c_double(cut), lcell,
+                                  v.ctypes.data_as(C.c_void_p), C.c_int64(v.size))
+        assert bad == 0, (dim, uc, cut, lcell, bad)
+        n_checked += 1
+    assert n_checked >= 20
+
+
+def test_wrap_quotient_matches_division(probe):
+    """The Float64 wrap solve divides by det(M) through quot_rn: RN(a / b) from y = RN(1 / b) with one
+    correction step, kept only when the remainder proves it is the rounded quotient.  It must equal the IEEE
+    quotient bit for bit: random quotients over many binades, exact multiples, powers of two (always left to
+    the division), numerators a few ulp from multiples of b, signed zeros, subnormals, huge values, inf and
+    NaN.  The fast path must also take the great majority of ordinary pairs."""
+    rng = np.random.default_rng(5)
+    lib = probe
+    lib.quot_probe.restype = C.c_int64
+    n = 200000
+    b = rng.uniform(1.0, 2.0, n) * np.exp2(rng.integers(-30, 30, n).astype(np.float64))
+    b *= np.where(rng.random(n) < 0.2, -1.0, 1.0)
+    a = rng.uniform(-1.0, 1.0, n) * np.exp2(rng.integers(-40, 40, n).astype(np.float64))
+    fb = C.c_int64(0)
+    vp = C.c_void_p
+    assert lib.quot_probe(a.ctypes.data_as(vp), b.ctypes.data_as(vp), n, C.byref(fb)) == 0
+    assert fb.value < n // 100, fb.value
+    # positions against a box determinant, as the solve sees them
+    det = np.array([1000.0, 1234.5678, 1.0 / 3.0, 8.0, 1e-3, 7.0e5, -512.25])
+    k = rng.integers(-50000, 50000, 20000).astype(np.float64)
+    cases_a, cases_b = [], []
+    for d in det:
+        base = k * d
+        for s in range(-3, 4):
+            cases_a.append(base + s * np.spacing(np.abs(base)))
+            cases_b.append(np.full(base.size, d))
+        cases_a.append(rng.uniform(-3 * abs(d), 3 * abs(d), 20000))
+        cases_b.append(np.full(20000, d))
+    sp = np.array([0.0, -0.0, 1.0, -1.0, 2.0, 0.5, 3.0, 5e-324, -5e-324, 2.2250738585072014e-308,
+                   1.7976931348623157e308, -1.7976931348623157e308, np.inf, -np.inf, np.nan, 1e-300, 1e300,
+                   0.1, 1.0 / 3.0, np.nextafter(1.0, 2.0), np.nextafter(1.0, 0.0)])
+    aa, bb = np.meshgrid(sp, sp)
+    cases_a.append(aa.ravel())
+    cases_b.append(bb.ravel())
+    a = np.ascontiguousarray(np.concatenate(cases_a))
+    b = np.ascontiguousarray(np.concatenate(cases_b))
+    assert lib.quot_probe(a.ctypes.data_as(vp), b.ctypes.data_as(vp), a.size, C.byref(fb)) == 0
+
+
+@pytest.mark.parametrize("f64", [0, 1])
+def test_cell_index_bits_match_division(probe, f64):
+    """cell_of takes floor(RN((x - xmin) / cs)) from the bit pattern of the product with RN(1 / cs) when that
+    product lies in (0, 2^31) and at least 5 ulp from every integer, else from cell_floor; with the range
+    test [-1, nc) it must equal the IEEE floor of the quotient everywhere: numerators a few ulp around
+    multiples of the cell size (the last cell, the half cell), zeros of both signs, negative, subnormal,
+    tiny, huge, inf and NaN numerators, and random ones.  The bit screen must decide nearly all of the
+    random numerators."""
+    dt = np.float64 if f64 else np.float32
+    rng = np.random.default_rng(13)
+    lib = probe
+    lib.cell_index_probe.restype = C.c_int64
+    fast = C.c_int64(0)
+    for cs in [2.5, 0.1, 1.0 / 3.0, 7.77, 0.0123456, 1234.5] + list(rng.uniform(0.01, 100.0, 12)):
+        cs = float(dt(cs))
+        nc = int(rng.integers(3, 400))
+        k = np.arange(-3, nc + 3, dtype=np.float64)
+        base = np.concatenate([(k * cs).astype(dt), ((k + 0.5) * cs).astype(dt)])
+        vals = [base]
+        up, dn = base.copy(), base.copy()
+        for _ in range(8):
+            up = np.nextafter(up, dt(np.inf))
+            dn = np.nextafter(dn, dt(-np.inf))
+            vals += [up.copy(), dn.copy()]
+        tiny = np.finfo(dt).smallest_subnormal
+        vals.append(np.array([0.0, -0.0, tiny, -tiny, 1e-30, -1e-30, np.inf, -np.inf, np.nan, 1e30, -1e30,
+                              float(np.finfo(dt).max)], dt))
+        a = np.ascontiguousarray(np.concatenate(vals).astype(np.float64))
+        assert lib.cell_index_probe(f64, a.ctypes.data_as(C.c_void_p), a.size, C.c_double(cs), nc,
+                                    C.byref(fast)) == 0, cs
+        r = np.ascontiguousarray(rng.uniform(0.0, nc * cs, 20000).astype(dt).astype(np.float64))
+        assert lib.cell_index_probe(f64, r.ctypes.data_as(C.c_void_p), r.size, C.c_double(cs), nc,
+                                    C.byref(fast)) == 0, cs
+        assert fast.value > 0.99 * r.size, (cs, fast.value)
