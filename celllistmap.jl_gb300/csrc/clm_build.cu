@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(WE_BLOCK) k_wrap_emit(DevGeom<T> g, const T* _
 // (the lanes of a warp whose copies share a cell with one add) and the real copy marks its cell; cell_cf
 // holds {copies, holds a real particle} per cell, zeroed before the launch.  Tile 0 clears the word of
 // the largest cell that k_cell_scan finds.
-template <class T, int N>
+template <class T, int N, int SH = kShapeGeneral>
 __global__ void __launch_bounds__(WE_BLOCK) k_wrap_stage(DevGeom<T> g, const T* __restrict__ x, int n,
                                                        T* __restrict__ wrapped, int slots, uint32_t* __restrict__ keys,
                                                        uint32_t* __restrict__ vals, int* __restrict__ tile_count,
@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(WE_BLOCK) k_wrap_stage(DevGeom<T> g, const T* 
   uint32_t m = 0u;
   int v[1] = {0};
   if (i < n) {
-    if (!wrap_count_regs<T, N>(g, x, i, p, m, v[0])) atomicOr(err, DERR_NAN);
+    if (!wrap_count_regs<T, N, SH>(g, x, i, p, m, v[0])) atomicOr(err, DERR_NAN);
 #pragma unroll
     for (int d = 0; d < N; d++) wrapped[(int64_t)i * N + d] = p[d];
   }
@@ -887,11 +887,26 @@ int build_counting(Handle& h, SetData& S, const DevGeom<T>& dg, int N, int64_t n
   S.cell_count_zero = 0;
   int* tile_count = S.ncopy.as<int>();
   int* max_cell = S.copy_off.as<int>() + n + 1;  // the largest cell
-  if (N == 3)
+  // Float64 3D cells whose input matrix has exact zeros take a wrap that skips them (wrap_point_shaped)
+  bool shaped = false;
+  if constexpr (std::is_same<T, double>::value) {
+    if (N == 3 && dg.shape == kShapeDiag) {
+      k_wrap_stage<T, 3, kShapeDiag><<<(unsigned)tiles, WE_BLOCK, 0, h.stream>>>(
+          dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), slots, S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
+          tile_count, cell_cf, max_cell, err);
+      shaped = true;
+    } else if (N == 3 && dg.shape == kShapeUpper) {
+      k_wrap_stage<T, 3, kShapeUpper><<<(unsigned)tiles, WE_BLOCK, 0, h.stream>>>(
+          dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), slots, S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
+          tile_count, cell_cf, max_cell, err);
+      shaped = true;
+    }
+  }
+  if (!shaped && N == 3)
     k_wrap_stage<T, 3><<<(unsigned)tiles, WE_BLOCK, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), slots,
                                                                   S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
                                                                   tile_count, cell_cf, max_cell, err);
-  else
+  else if (!shaped)
     k_wrap_stage<T, 2><<<(unsigned)tiles, WE_BLOCK, 0, h.stream>>>(dg, S.x.as<T>(), (int)n, S.wrapped.as<T>(), slots,
                                                                   S.keys[0].as<uint32_t>(), S.vals[0].as<uint32_t>(),
                                                                   tile_count, cell_cf, max_cell, err);

@@ -118,6 +118,17 @@ template <class T> void fill_devgeom(const Geometry<T>& g, int precision, DevGeo
     for (int i = 0; i < 3; i++)
       for (int j = 0; j < 3; j++) d.cof[i][j] = cof[i][j];
   }
+  d.shape = kShapeGeneral;
+  if (g.dim == 3 && g.kind != NONPERIODIC) {
+    bool lower = true, upper = true, rid = true;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) {
+        if (i > j && (g.Min[i][j] != T(0) || d.cof[i][j] != T(0))) lower = false;
+        if (i < j && (g.Min[i][j] != T(0) || d.cof[i][j] != T(0))) upper = false;
+        if (g.R[i][j] != (i == j ? T(1) : T(0))) rid = false;
+      }
+    if (lower) d.shape = (upper && rid) ? kShapeDiag : kShapeUpper;
+  }
   d.cutoff = g.cutoff;
   d.cutoff_sqr = g.cutoff_sqr;
   d.margin_wide = (double)g.cutoff * (1.0 + std::sqrt((double)g.dim) / 2.0);
@@ -160,7 +171,7 @@ template <class T> void fill_devgeom(const Geometry<T>& g, int precision, DevGeo
 // ------------------------------------------------------------------ wrap, images, copy count
 // Particle i: its wrapped position p, the mask of its images inside the computing box and its number of
 // copies.  Returns false if the particle has a NaN coordinate (it then gets no copy: p = 0, m = 0, cnt = 0).
-template <class T, int N>
+template <class T, int N, int SH = kShapeGeneral>
 __host__ __device__ __forceinline__ bool wrap_count_regs(const DevGeom<T>& g, const T* __restrict__ x, int i, T* p,
                                                          uint32_t& mask_out, int& cnt_out) {
   T xi[N];
@@ -181,7 +192,7 @@ __host__ __device__ __forceinline__ bool wrap_count_regs(const DevGeom<T>& g, co
 #pragma unroll
     for (int k = 0; k < N; k++) p[k] = xi[k];
   } else {
-    wrap_point<T, N>(g, xi, p);
+    wrap_point<T, N, SH>(g, xi, p);
   }
   uint32_t m = 0;
   int cnt = 1;
@@ -351,6 +362,51 @@ __host__ __device__ __forceinline__ void origin_ff(float cb_hi, float cb_lo, flo
   lo = se + pe + cb_lo;
 }
 
+// The float pair of a double: hi = (float)q and lo = (float)(q - (double)hi), both rounded to nearest even.
+// float_pair takes them from q's bit pattern with integer operations when 2^-74 <= |q| < 2^126 (q and both
+// parts normal): hi keeps the top 23 of q's 52 fraction bits, rounded by the 29 dropped ones (a carry runs
+// into the exponent), and the difference q - hi is exactly the dropped bits' signed remainder r (|r| <= 2^28)
+// times 2^(E - 52), E the exponent of q; converting r to float rounds it as converting the exact double
+// difference does, and the power-of-two scale is exact.  Other values take the conversions (a call on the
+// device, so that they stay off the common path).  Off the FP64 pipe: the gather's FP32 offsets need three
+// components per copy.
+#ifdef __CUDA_ARCH__
+__device__ __noinline__
+#else
+inline
+#endif
+float2 float_pair_call(double q) {
+  const float hi = (float)q;
+  return make_float2(hi, (float)(q - (double)hi));
+}
+__host__ __device__ __forceinline__ void float_pair(double q, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)dbits(q);
+  const int e = (int)((b >> 52) & 0x7ff);  // biased exponent
+  if (e < 1023 - 74 || e > 1023 + 125) {
+    const float2 r = float_pair_call(q);
+    hi = r.x;
+    lo = r.y;
+    return;
+  }
+  const unsigned rem = (unsigned)(b & 0x1FFFFFFFull);                  // the 29 dropped fraction bits
+  const unsigned top = (unsigned)((b >> 29) & 0x7FFFFFull);            // the 23 kept ones
+  const bool up = rem > 0x10000000u || (rem == 0x10000000u && (top & 1u));
+  const bool neg = (b >> 63) != 0;
+  const unsigned hb = ((neg ? 1u : 0u) << 31) | ((((unsigned)(e - (1023 - 127)) << 23) | top) + (up ? 1u : 0u));
+  int r = (int)rem - (up ? 0x20000000 : 0);
+  if (neg) r = -r;
+  const unsigned sb = (unsigned)(e - (1023 + 52 - 127)) << 23;         // 2^(E - 52) as a float
+#ifdef __CUDA_ARCH__
+  hi = __uint_as_float(hb);
+  lo = __int2float_rn(r) * __uint_as_float(sb);
+#else
+  float scale;
+  std::memcpy(&hi, &hb, sizeof hi);
+  std::memcpy(&scale, &sb, sizeof scale);
+  lo = (float)r * scale;
+#endif
+}
+
 // Counting placement by cell: copies reach their cell's slots [s, e) in arrival order (per-cell atomic
 // counters), so a cell's values (particle << 5 | image) arrive permuted.  The final slot of value v is s plus
 // the number of smaller values of its cell: values are distinct (one per copy), so the slots are a
@@ -404,10 +460,9 @@ __host__ __device__ __forceinline__ void gather_at(const DevGeom<T>& g, const T*
 #pragma unroll
     for (int d = 0; d < N; d++) {
       // FP32 offset of the copy from its cell origin, all in float pairs: (qh + ql) - (oh + ol)
-      float oh, ol;
+      float oh, ol, qh, ql;
       origin_ff(g.cbf_hi[d], g.cbf_lo[d], g.csf[d], g.csf_lo[d], c[d] - 1, oh, ol);
-      const float qh = (float)q[d];
-      const float ql = (float)(q[d] - (T)qh);
+      float_pair((double)q[d], qh, ql);
       o[d] = (qh - oh) + (ql - ol);
     }
     off[t] = make_float4(o[0], o[1], o[2], bits_as_float(pc));

@@ -149,6 +149,8 @@ template <class T> struct DevGeom {
   float thr_hi, thr_lo; // FP32 prefilter bounds on d2 (maybe-inside / surely-inside)
   int zero_code;        // image code of the zero shift (13 in 3D, 4 in 2D)
   int nimg;             // 3^dim
+  int shape;            // kShapeUpper: input cell and cofactors zero below the diagonal; kShapeDiag: both
+                        // diagonal and R the identity (3D periodic cells); else kShapeGeneral
   int img_tree;         // image-test pruning: 2 aligned cell exactly upper triangular (per dimension), 1 last
                         // row zero below the diagonal (per value of the last image index), 0 none
   // image k of a wrapped position p lies in the computing box along axis d, cbmin[d] <= RN(p[d] + shift[k][d])
@@ -161,9 +163,82 @@ __host__ __device__ __forceinline__ bool image_in(const DevGeom<T>& g, int k, in
   return g.img_lo[k][d] <= pk && pk < g.img_hi[k][d];
 }
 
-// StaticArrays solve (Cramer form), then fastmod1, boundary -> 0, then M*p and R*(.)
-template <class T, int N>
+__host__ __device__ __forceinline__ unsigned long long mag_bits(double v) {
+  return (unsigned long long)dbits(v) & 0x7FFFFFFFFFFFFFFFull;
+}
+__host__ __device__ __forceinline__ unsigned long long mag_bits(float v) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(v) & 0x7FFFFFFFu;
+#else
+  unsigned b;
+  std::memcpy(&b, &v, sizeof b);
+  return b & 0x7FFFFFFFu;
+#endif
+}
+template <class T> __host__ __device__ __forceinline__ bool is_zero_bits(T v) { return mag_bits(v) == 0; }
+template <class T> __host__ __device__ __forceinline__ bool is_finite_bits(T v) {
+  return mag_bits(v) < (sizeof(T) == 8 ? 0x7FF0000000000000ull : 0x7F800000ull);
+}
+
+// Cell shapes whose wrap skips exact-zero terms (DevGeom::shape; 3D only).  A left-to-right sum of separately
+// rounded products whose dropped terms are signed zeros (a zero coefficient times a finite value) equals the
+// sum of the other terms whenever that sum is not zero: a zero term leaves a nonzero partial sum as it is,
+// and can only change the sign of a zero one, after which the next nonzero term gives the same value either
+// way.  So the shaped wrap keeps its result when every input is finite and no shortened sum is zero, and
+// otherwise the particle takes the full sums.
+enum : int { kShapeGeneral = 0, kShapeUpper = 1, kShapeDiag = 2 };
+
+template <class T, int SH>
+__host__ __device__ __forceinline__ bool wrap_point_shaped(const DevGeom<T>& g, const T* x, T* out) {
+  if (!(is_finite_bits(x[0]) && is_finite_bits(x[1]) && is_finite_bits(x[2]))) return false;
+  const auto& c = g.cof;
+  const auto& a = g.Min;
+  T p[3];
+  if constexpr (SH == kShapeDiag) {
+    p[0] = xmul(c[0][0], x[0]);
+    p[1] = xmul(c[1][1], x[1]);
+    p[2] = xmul(c[2][2], x[2]);
+  } else {
+    p[0] = xadd(xadd(xmul(c[0][0], x[0]), xmul(c[0][1], x[1])), xmul(c[0][2], x[2]));
+    p[1] = xadd(xmul(c[1][1], x[1]), xmul(c[1][2], x[2]));
+    p[2] = xmul(c[2][2], x[2]);
+  }
+  if (is_zero_bits(p[0]) || is_zero_bits(p[1]) || is_zero_bits(p[2])) return false;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    p[i] = quot_rn(p[i], g.det_in, g.inv_det);
+    p[i] = xsub(p[i], xfloor(p[i]));
+    if (same_bits(p[i], T(1))) p[i] = T(0);
+  }
+  T w[3];
+  if constexpr (SH == kShapeDiag) {
+    w[0] = xmul(a[0][0], p[0]);
+    w[1] = xmul(a[1][1], p[1]);
+    w[2] = xmul(a[2][2], p[2]);
+  } else {
+    w[0] = xadd(xadd(xmul(a[0][0], p[0]), xmul(a[0][1], p[1])), xmul(a[0][2], p[2]));
+    w[1] = xadd(xmul(a[1][1], p[1]), xmul(a[1][2], p[2]));
+    w[2] = xmul(a[2][2], p[2]);
+  }
+  if (is_zero_bits(w[0]) || is_zero_bits(w[1]) || is_zero_bits(w[2])) return false;
+  if constexpr (SH == kShapeDiag) {
+    // R is the identity: 1 * w_i is w_i and the other two terms are zeros
+#pragma unroll
+    for (int i = 0; i < 3; i++) out[i] = w[i];
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; i++) out[i] = xadd(xadd(xmul(g.R[i][0], w[0]), xmul(g.R[i][1], w[1])), xmul(g.R[i][2], w[2]));
+  }
+  return true;
+}
+
+// StaticArrays solve (Cramer form), then fastmod1, boundary -> 0, then M*p and R*(.).  SH: the cell's shape
+// (kShapeUpper / kShapeDiag skip its exact-zero terms where that is exact, see wrap_point_shaped).
+template <class T, int N, int SH = kShapeGeneral>
 __host__ __device__ __forceinline__ void wrap_point(const DevGeom<T>& g, const T* x, T* out) {
+  if constexpr (N == 3 && SH != kShapeGeneral) {
+    if (wrap_point_shaped<T, SH>(g, x, out)) return;
+  }
   T p[N];
   const auto& a = g.Min;
   if constexpr (N == 3) {

@@ -20,6 +20,8 @@
 //   image_key_probe    the image tests on order keys against the sums and compares they stand for.
 //   quot_probe         the wrap solve's checked reciprocal quotient against the IEEE division.
 //   cell_index_probe   the cell index's floor from the bits of the reciprocal product, with its range test.
+//   float_pair_probe   the gather's float pair of a double from its bits against the two conversions.
+//   wrap_shape_probe   the wrap that skips a cell's exact-zero terms against the general wrap.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -823,4 +825,56 @@ template <class T> int64_t cell_index_t(const double* av, int64_t n, double csd,
 // the number of disagreements and, in *fast, how many the bit screen decided.
 extern "C" int64_t cell_index_probe(int f64, const double* a, int64_t n, double cs, int nc, int64_t* fast) {
   return f64 ? cell_index_t<double>(a, n, cs, nc, fast) : cell_index_t<float>(a, n, cs, nc, fast);
+}
+
+// float_pair (the gather's float pair of a double from its bits) against the two conversions it stands for,
+// hi = (float)q and lo = (float)(q - (double)hi), bit for bit (NaN against NaN), for n values; returns the
+// number of disagreements.
+extern "C" int64_t float_pair_probe(const double* q, int64_t n) {
+  int64_t bad = 0;
+  for (int64_t t = 0; t < n; t++) {
+    float hi, lo;
+    clm::float_pair(q[t], hi, lo);
+    const float wh = (float)q[t], wl = (float)(q[t] - (double)wh);
+    uint32_t a, b, c, d;
+    std::memcpy(&a, &hi, 4);
+    std::memcpy(&b, &wh, 4);
+    std::memcpy(&c, &lo, 4);
+    std::memcpy(&d, &wl, 4);
+    const bool ok_hi = std::isnan(wh) ? std::isnan(hi) : a == b;
+    const bool ok_lo = std::isnan(wl) ? std::isnan(lo) : c == d;
+    if (!ok_hi || !ok_lo) bad++;
+  }
+  return bad;
+}
+
+// The shaped wrap (wrap_point with the cell's shape: exact-zero terms skipped, the full sums where that might
+// not be exact) against the general wrap, bit for bit, for n points of one 3D periodic geometry; returns
+// the number of disagreements (NaN against NaN), -1 if the geometry has the general shape, or -2 - status.
+// *shape receives the geometry's shape.
+extern "C" int64_t wrap_shape_probe(int kind, const double* Mcol, double cutoff, const double* x, int64_t n,
+                                    int* shape) {
+  double M[3][3] = {};
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) M[i][j] = (kind == clm::ORTHO && i != j) ? 0.0 : Mcol[j * 3 + i];
+  clm::Geometry<double> g;
+  const int st = clm::make_geometry<double>(g, 3, kind, M, cutoff, 1, nullptr);
+  if (st) return -2 - st;
+  clm::DevGeom<double> d;
+  clm::fill_devgeom<double>(g, 1, d);
+  *shape = d.shape;
+  if (d.shape == clm::kShapeGeneral) return -1;
+  int64_t bad = 0;
+  for (int64_t t = 0; t < n; t++) {
+    double a[3], b[3];
+    clm::wrap_point<double, 3>(d, x + 3 * t, a);
+    if (d.shape == clm::kShapeDiag) clm::wrap_point<double, 3, clm::kShapeDiag>(d, x + 3 * t, b);
+    else clm::wrap_point<double, 3, clm::kShapeUpper>(d, x + 3 * t, b);
+    for (int k = 0; k < 3; k++)
+      if (std::isnan(a[k]) ? !std::isnan(b[k]) : clm::dbits(a[k]) != clm::dbits(b[k])) {
+        bad++;
+        break;
+      }
+  }
+  return bad;
 }

@@ -738,3 +738,81 @@ def test_cell_index_bits_match_division(probe, f64):
         assert lib.cell_index_probe(f64, r.ctypes.data_as(C.c_void_p), r.size, C.c_double(cs), nc,
                                     C.byref(fast)) == 0, cs
         assert fast.value > 0.99 * r.size, (cs, fast.value)
+
+
+def test_float_pair_from_bits(probe):
+    """The gather splits each Float64 copy coordinate into a float pair for the FP32 offsets: hi = (float)q,
+    lo = (float)(q - hi).  float_pair takes both from q's bit pattern with integer operations: it must equal
+    the conversions bit for bit on random values over every binade the fast path takes and beyond it, on
+    round-to-nearest-even ties (29 dropped bits exactly half, kept bits odd and even), on carries into the
+    exponent, on floats themselves, on the limits of the fast range, and on zeros, subnormals, huge values,
+    inf and NaN."""
+    rng = np.random.default_rng(17)
+    lib = probe
+    lib.float_pair_probe.restype = C.c_int64
+    n = 200000
+    q = rng.uniform(1.0, 2.0, n) * np.exp2(rng.integers(-140, 140, n).astype(np.float64))
+    q *= np.where(rng.random(n) < 0.5, -1.0, 1.0)
+    # bit patterns built to hit the rounding cases: the dropped 29 bits at, just below and just above half,
+    # all ones (a carry through the 23 kept bits into the exponent), kept bits odd or even
+    e = rng.integers(1023 - 80, 1023 + 130, 4000).astype(np.uint64)
+    top = rng.integers(0, 1 << 23, 4000).astype(np.uint64)
+    cases = []
+    for rem in (0x10000000, 0x0FFFFFFF, 0x10000001, 0x1FFFFFFF, 0, 1):
+        for t in (top, top | np.uint64(1), top & ~np.uint64(1), np.full(4000, (1 << 23) - 1, np.uint64)):
+            bits = (e << np.uint64(52)) | (t << np.uint64(29)) | np.uint64(rem)
+            cases.append(bits.view(np.float64))
+            cases.append((bits | np.uint64(1 << 63)).view(np.float64))
+    edges = [np.exp2(float(k)) for k in (-74, -75, -73, 125, 126, 127, -126, -149, -150)]
+    sp = np.array([0.0, -0.0, 5e-324, -5e-324, 2.2250738585072014e-308, 1.7976931348623157e308, np.inf,
+                   -np.inf, np.nan, 1e-30, 3.4028234663852886e38, 3.4028235677973366e38, 1.0, -1.0, 0.1, 109.4]
+                  + edges + [np.nextafter(x, 0.0) for x in edges] + [np.nextafter(x, np.inf) for x in edges])
+    fl = rng.uniform(-200, 200, 5000).astype(np.float32).astype(np.float64)
+    allq = np.ascontiguousarray(np.concatenate([q, sp, fl] + cases))
+    assert lib.float_pair_probe(allq.ctypes.data_as(C.c_void_p), allq.size) == 0
+
+
+def test_shaped_wrap_matches_general(probe):
+    """Float64 3D cells with exact zeros in the input matrix (orthorhombic: diagonal with R the identity;
+    upper-triangular triclinic cells such as the benchmark's) wrap with the zero terms skipped.  That is
+    exact when every input is finite and no shortened sum is zero, and otherwise the particle takes the full
+    sums.  The shaped wrap must equal the general one bit for bit, signed zeros included: random positions
+    inside and far outside the box, lattice points and box corners (zero fractional coordinates, the
+    fallback), signed zeros, points a few ulp off multiples of the cell vectors, huge and non-finite
+    coordinates."""
+    rng = np.random.default_rng(19)
+    lib = probe
+    lib.wrap_shape_probe.restype = C.c_int64
+    cells = [(0, [10.0, 12.0, 11.0]), (0, [109.43846059, 109.43846059, 109.43846059]),
+             (1, [[109.43846059, 21.88769212, 10.94384606], [0.0, 109.43846059, 16.41576909],
+                  [0.0, 0.0, 109.43846059]]),
+             (1, [[10.0, 2.0, 1.0], [0.0, 11.0, 1.5], [0.0, 0.0, 12.0]]),
+             (1, [[10.0, -2.0, 1.0], [0.0, 11.0, -1.5], [0.0, 0.0, 12.0]]),
+             (1, [[12.0, 0.0, 0.0], [0.0, 10.0, 0.0], [0.0, 0.0, 11.0]]),
+             # negative sides (a triclinic cell with a negative diagonal fails the cell check)
+             (0, [-10.0, 12.0, -11.0])]
+    for _ in range(6):
+        M = np.diag(rng.uniform(5.0, 20.0, 3)) + np.triu(rng.uniform(-3.0, 3.0, (3, 3)), 1)
+        cells.append((1, M.tolist()))
+        cells.append((0, list(rng.uniform(5.0, 30.0, 3))))
+    seen = set()
+    shape = C.c_int(0)
+    for kind, uc in cells:
+        u = np.asarray(uc, np.float64)
+        M = np.diag(u) if u.ndim == 1 else u
+        Mc = np.ascontiguousarray(M.flatten(order="F"))
+        pts = [rng.uniform(-2.0, 3.0, (20000, 3)) @ M.T, rng.uniform(-1e6, 1e6, (2000, 3)),
+               (rng.integers(-3, 4, (3000, 3)).astype(np.float64)) @ M.T,
+               (rng.integers(-3, 4, (2000, 3)).astype(np.float64) * 0.5) @ M.T]
+        lat = (rng.integers(-3, 4, (2000, 3)).astype(np.float64)) @ M.T
+        for s in (-2, -1, 1, 2):
+            pts.append(lat + s * np.spacing(np.abs(lat) + 1e-300))
+        sp = np.array([0.0, -0.0, 1e-300, -1e-300, 5e-324, 1e300, -1e300, np.inf, -np.inf])
+        g3 = np.array(np.meshgrid(sp, sp, sp)).reshape(3, -1).T
+        pts.append(g3)
+        x = np.ascontiguousarray(np.concatenate(pts))
+        bad = lib.wrap_shape_probe(kind, Mc.ctypes.data_as(C.c_void_p), C.c_double(1.5),
+                                   x.ctypes.data_as(C.c_void_p), x.shape[0], C.byref(shape))
+        assert bad == 0, (kind, uc, bad)
+        seen.add(shape.value)
+    assert seen == {1, 2}, seen
