@@ -371,7 +371,7 @@ __host__ __device__ __forceinline__ void origin_ff(float cb_hi, float cb_lo, flo
 // device, so that they stay off the common path).  Off the FP64 pipe: the gather's FP32 offsets need three
 // components per copy.
 #ifdef __CUDA_ARCH__
-__device__ __noinline__
+static __device__ __noinline__
 #else
 inline
 #endif

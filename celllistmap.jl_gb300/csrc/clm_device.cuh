@@ -73,13 +73,7 @@ __host__ __device__ __forceinline__ int order_key(float v) {
   return b ^ (int)((unsigned)(b >> 31) >> 1);
 }
 
-// RN(a / b) in double from y = RN(1 / b): q = q0 + (a - q0 b) y with q0 = RN(a y) (Markstein's correction
-// step), accepted when its remainder r = RN(a - q b) proves it: r = 0 (a = q b exactly: with q and b normal and
-// |b| 2^(E(q) - 53) normal, a - q b is a multiple of 2^-1074 and cannot round to 0 unless it is 0), or q is not
-// a power of two and |r| < |b| 2^(E(q) - 53) (the exact |a - q b| is then below that bound, which is
-// representable, so |a / b - q| is less than half the spacing of the doubles around q; a quotient of two
-// doubles is never a midpoint).  Otherwise (powers of two, zero, subnormal or extreme exponents, inf or NaN)
-// the IEEE division decides.  Four FP64 operations and integer checks instead of the division sequence.
+// The bit pattern of a double, and equality of bit patterns (on the integer pipe).
 __host__ __device__ __forceinline__ long long dbits(double v) {
 #ifdef __CUDA_ARCH__
   return __double_as_longlong(v);
@@ -89,6 +83,25 @@ __host__ __device__ __forceinline__ long long dbits(double v) {
   return b;
 #endif
 }
+__host__ __device__ __forceinline__ bool same_bits(double a, double b) { return dbits(a) == dbits(b); }
+__host__ __device__ __forceinline__ bool same_bits(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(a) == __float_as_uint(b);
+#else
+  unsigned x, y;
+  std::memcpy(&x, &a, sizeof x);
+  std::memcpy(&y, &b, sizeof y);
+  return x == y;
+#endif
+}
+
+// RN(a / b) in double from y = RN(1 / b): q = q0 + (a - q0 b) y with q0 = RN(a y) (Markstein's correction
+// step), accepted when its remainder r = RN(a - q b) proves it: r = 0 (a = q b exactly: with q and b normal and
+// |b| 2^(E(q) - 53) normal, a - q b is a multiple of 2^-1074 and cannot round to 0 unless it is 0), or q is not
+// a power of two and |r| < |b| 2^(E(q) - 53) (the exact |a - q b| is then below that bound, which is
+// representable, so |a / b - q| is less than half the spacing of the doubles around q; a quotient of two
+// doubles is never a midpoint).  Otherwise (powers of two, zero, subnormal or extreme exponents, inf or NaN)
+// the IEEE division decides.  Four FP64 operations and integer checks instead of the division sequence.
 __host__ __device__ __forceinline__ bool quot_fast(double a, double b, double y, double& q) {
   const double q0 = xmul(a, y);
   q = xfma(xfma(-q0, b, a), y, q0);
@@ -101,19 +114,8 @@ __host__ __device__ __forceinline__ bool quot_fast(double a, double b, double y,
 }
 #ifdef __CUDA_ARCH__
 // a call, so that the compiler cannot evaluate the division ahead of the branch in every warp
-__device__ __noinline__ double div_rn_call(double a, double b) { return __ddiv_rn(a, b); }
+static __device__ __noinline__ double div_rn_call(double a, double b) { return __ddiv_rn(a, b); }
 #endif
-__host__ __device__ __forceinline__ bool same_bits(double a, double b) { return dbits(a) == dbits(b); }
-__host__ __device__ __forceinline__ bool same_bits(float a, float b) {
-#ifdef __CUDA_ARCH__
-  return __float_as_uint(a) == __float_as_uint(b);
-#else
-  unsigned x, y;
-  std::memcpy(&x, &a, sizeof x);
-  std::memcpy(&y, &b, sizeof y);
-  return x == y;
-#endif
-}
 __host__ __device__ __forceinline__ double quot_rn(double a, double b, double y) {
   double q;
   if (quot_fast(a, b, y, q)) return q;
