@@ -18,6 +18,7 @@
 //   noalloc_slots_probe the per-block slots of the allocation-free entry point's scratch;
 //   cell_floor_probe   the cell index's floor from the reciprocal product against the IEEE quotient's.
 //   image_key_probe    the image tests on order keys against the sums and compares they stand for.
+//   first_key_probe    the image-test thresholds on arbitrary shifts and bounds.
 //   quot_probe         the wrap solve's checked reciprocal quotient against the IEEE division.
 //   cell_index_probe   the cell index's floor from the bits of the reciprocal product, with its range test.
 //   float_pair_probe   the gather's float pair of a double from its bits against the two conversions.
@@ -875,6 +876,31 @@ extern "C" int64_t wrap_shape_probe(int kind, const double* Mcol, double cutoff,
         bad++;
         break;
       }
+  }
+  return bad;
+}
+
+// first_key_at_least (the image tests' thresholds) on arbitrary (s, b): the returned key q must pass,
+// RN(value(q) + s) >= b, and the key below it must not (unless q is key(-inf)), in the handle dtype; returns
+// the number of violations.
+extern "C" int64_t first_key_probe(int f64, const double* s, const double* b, int64_t n) {
+  int64_t bad = 0;
+  for (int64_t t = 0; t < n; t++) {
+    if (f64) {
+      const double ss = s[t], bb = b[t];
+      const long long q = clm::first_key_at_least<double>(ss, bb);
+      const bool at = clm::from_order_key<double>(q) + ss >= bb;
+      const bool below = q > clm::order_key(-std::numeric_limits<double>::infinity()) &&
+                         clm::from_order_key<double>(q - 1) + ss >= bb;
+      if (!at || below) bad++;
+    } else {
+      const float ss = (float)s[t], bb = (float)b[t];
+      const int q = clm::first_key_at_least<float>(ss, bb);
+      const bool at = clm::from_order_key<float>(q) + ss >= bb;
+      const bool below = q > clm::order_key(-std::numeric_limits<float>::infinity()) &&
+                         clm::from_order_key<float>(q - 1) + ss >= bb;
+      if (!at || below) bad++;
+    }
   }
   return bad;
 }

@@ -816,3 +816,30 @@ def test_shaped_wrap_matches_general(probe):
         assert bad == 0, (kind, uc, bad)
         seen.add(shape.value)
     assert seen == {1, 2}, seen
+
+
+@pytest.mark.parametrize("f64", [0, 1])
+def test_image_threshold_search(probe, f64):
+    """The image tests' thresholds: the smallest order key q with RN(value(q) + s) >= b, found by bisection
+    after a bracket of 4 keys around RN(b - s).  On arbitrary shifts and bounds it must be exactly the first
+    passing key: ordinary values, b - s near zero where the threshold lies many keys from RN(b - s) (the
+    bracket fails and the full bisection runs), s much larger or smaller than b, equal values, signed
+    zeros and subnormals."""
+    rng = np.random.default_rng(23)
+    lib = probe
+    lib.first_key_probe.restype = C.c_int64
+    dt = np.float64 if f64 else np.float32
+    n = 20000
+    s = rng.uniform(-100, 100, n)
+    b = rng.uniform(-100, 100, n)
+    s2 = rng.uniform(-100, 100, n)
+    b2 = s2 + rng.uniform(-1e-6, 1e-6, n) * np.abs(s2)  # b - s near zero
+    s3 = rng.uniform(-1, 1, n) * np.exp2(rng.integers(-60, 60, n).astype(np.float64))
+    b3 = rng.uniform(-1, 1, n) * np.exp2(rng.integers(-60, 60, n).astype(np.float64))
+    tiny = float(np.finfo(dt).smallest_subnormal)
+    sp = np.array([0.0, -0.0, 1.0, -1.0, tiny, -tiny, 5.0, -5.0, 1e-30, 1e30, 1234.5678])
+    ss, bb = np.meshgrid(sp, sp)
+    S = np.concatenate([s, s2, s2, s3, ss.ravel()]).astype(dt).astype(np.float64)
+    B = np.concatenate([b, b2, s2, b3, bb.ravel()]).astype(dt).astype(np.float64)
+    S, B = np.ascontiguousarray(S), np.ascontiguousarray(B)
+    assert lib.first_key_probe(f64, S.ctypes.data_as(C.c_void_p), B.ctypes.data_as(C.c_void_p), S.size) == 0
